@@ -1,0 +1,222 @@
+/*
+ * sgmres.h -- C ABI of libsgmres.so, the GB300 (sm_103a) solve path of
+ * schwarz-gmres: restarted GMRES(m) / FGMRES preconditioned by Jacobi,
+ * ILU(0), one-level ASM/RAS and two-level Schwarz with ILU(0) subdomain
+ * solves, all resident on one GPU.
+ *
+ * Conventions
+ *  - Every entry point returns sg_status; on failure sg_last_error() returns a
+ *    thread-local message (the reference throws std::runtime_error instead:
+ *    src/gpu/cuda_common.h:13-40, src/precond/coarse_solve.h:31-32,
+ *    src/decomp/domain_decomp.h:54-55).
+ *  - Indices are 0-based int32, values FP64, CSR column indices ascending
+ *    within a row (as src/core/sparse_matrix.h:13-18 and every reference
+ *    generator produce them).
+ *  - Vectors passed with SG_MEM_HOST are host pointers (copied in/out inside
+ *    the call); with SG_MEM_DEVICE they are device pointers on the context's
+ *    device, used in place on the context's stream.
+ *  - No entry point falls back to the CPU: without a usable CUDA device the
+ *    calls that compute return SG_ERR_CUDA.
+ */
+#ifndef SGMRES_H
+#define SGMRES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SG_ABI_VERSION 1
+
+typedef enum sg_status {
+    SG_OK = 0,
+    SG_ERR_INVALID_ARG = 1, /* bad size, pointer, option or CSR structure */
+    SG_ERR_CUDA = 2,        /* CUDA runtime failure or no device */
+    SG_ERR_OOM = 3,         /* device allocation failed */
+    SG_ERR_SINGULAR = 4,    /* coarse matrix singular, missing ILU diagonal */
+    SG_ERR_NOT_SETUP = 5,   /* preconditioner used before sg_precond_setup */
+    SG_ERR_NONFINITE = 6,   /* NaN/Inf in the right-hand side or the iteration */
+    SG_ERR_DEVICE_TIMEOUT = 7, /* a bounded device wait gave up */
+    SG_ERR_UNSUPPORTED = 8, /* option combination not provided */
+    SG_ERR_INTERNAL = 9
+} sg_status;
+
+typedef enum sg_mem { SG_MEM_HOST = 0, SG_MEM_DEVICE = 1 } sg_mem;
+
+/* Preconditioners of the reference CLI (src/main.cpp:44, :190-208). */
+typedef enum sg_precond_kind {
+    SG_PC_NONE = 0,
+    SG_PC_JACOBI = 1,       /* src/precond/jacobi.h:10-27 */
+    SG_PC_ILU0 = 2,         /* src/precond/ilu0.h:11-93 */
+    SG_PC_ASM = 3,          /* src/precond/asm.h:13-71 */
+    SG_PC_RAS = 4,          /* src/precond/ras.h:16-82 */
+    SG_PC_TWOLEVEL_ASM = 5, /* src/precond/two_level_schwarz.h:23-75, FineLevelType::ASM */
+    SG_PC_TWOLEVEL_RAS = 6  /* src/precond/two_level_schwarz.h:23-75, FineLevelType::RAS */
+} sg_precond_kind;
+
+/* Arithmetic / storage types. */
+typedef enum sg_dtype { SG_FP64 = 0, SG_FP32 = 1, SG_BF16 = 2 } sg_dtype;
+
+typedef struct sg_precond_opts {
+    int nparts;        /* subdomains (reference default 4, src/main.cpp:75) */
+    int overlap;       /* overlap layers (reference default 1, src/main.cpp:74) */
+    int factor_dtype;  /* storage of ILU factors: SG_FP64, SG_FP32 or SG_BF16 */
+    int sweep_dtype;   /* triangular sweeps: SG_FP64 or SG_FP32 (FP32 accumulate) */
+    const int* partition; /* optional host array [n] of part ids in [0,nparts);
+                             NULL = built-in graph partitioner. Takes the place
+                             of METIS_PartGraphKway (src/decomp/domain_decomp.h:23-58) */
+    int reserved[8];
+} sg_precond_opts;
+
+typedef struct sg_ctx sg_ctx;
+typedef struct sg_csr sg_csr;
+typedef struct sg_precond sg_precond;
+
+/* ---- context / errors ------------------------------------------------- */
+int sg_abi_version(void);
+const char* sg_last_error(void);
+const char* sg_status_string(sg_status st);
+/* Replaces CudaHandles::init (src/gpu/cuda_common.h:48-56): a device, one
+ * stream, no library handles. */
+sg_status sg_ctx_create(int device, sg_ctx** out);
+sg_status sg_ctx_destroy(sg_ctx* ctx);
+/* Run all work of this context on an existing cudaStream_t (NULL = the
+ * context's own stream). */
+sg_status sg_ctx_set_stream(sg_ctx* ctx, void* cuda_stream);
+sg_status sg_ctx_get_stream(sg_ctx* ctx, void** cuda_stream);
+sg_status sg_ctx_synchronize(sg_ctx* ctx);
+/* Kernels launched through this context so far (a CUDA-graph launch adds
+ * the kernel nodes it replays).  No counterpart in the reference. */
+sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count);
+
+/* ---- matrix ----------------------------------------------------------- */
+/* Copies a CSR matrix to the device (CSRMatrix, src/core/sparse_matrix.h:13-28;
+ * DeviceCSRMatrix::upload, src/gpu/cuda_sparse.h:15-51). Arrays are host or
+ * device pointers per `mem`. */
+sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* row_ptr,
+                        const int* col_idx, const double* vals, sg_mem mem, sg_csr** out);
+sg_status sg_csr_destroy(sg_csr* A);
+/* y = A x (CSRMatrix::spmv, src/core/sparse_matrix.h:30-37; replaces
+ * DeviceCSRMatrix::spmv, src/gpu/cuda_sparse.h:53-74). FP64, same summation
+ * order as the reference row loop. */
+sg_status sg_csr_spmv(sg_csr* A, const double* x, double* y, sg_mem mem);
+
+/* ---- preconditioner plugin (src/precond/preconditioner.h:7-20) ------- */
+sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_opts* opts,
+                            sg_precond** out);
+/* Preconditioner::setup(const CSRMatrix&) */
+sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A);
+/* Preconditioner::apply(const double* x, double* y, int n) const:
+ * overwrites all of y with M^{-1} x. */
+sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg_mem mem);
+sg_status sg_precond_destroy(sg_precond* pc);
+
+/* Read back set-up data for parity checks (host arrays).
+ * which: 0 partition[n], 1 owned_ptr[P+1], 2 owned[n], 3 sub_ptr[P+1],
+ *        4 sub[sum n_s], 5 ownloc_ptr[P+1], 6 ownloc[n]
+ * (DomainDecomposition, src/decomp/domain_decomp.h:12-20; RASPrecond::
+ * owned_local_indices_, src/precond/ras.h:34-41).  Returns the length in
+ * *len; out may be NULL to query the length. */
+sg_status sg_precond_get_decomposition(sg_precond* pc, int which, int* out, int cap, int* len);
+/* ILU(0) factors of subdomain s as computed on the device, in the local CSR
+ * layout of ILU0Precond (src/precond/ilu0.h:81-85): row_ptr[n_s+1],
+ * col_idx[nnz_s], lu_vals[nnz_s] (FP64), diag_ptr[n_s]; plus the forward and
+ * backward sweep level of every local row.  Any array may be NULL. */
+sg_status sg_precond_get_factors(sg_precond* pc, int s, int* n_s, int* nnz_s, int* row_ptr,
+                                 int* col_idx, double* lu_vals, int* diag_ptr,
+                                 int* level_lower, int* level_upper);
+/* Coarse operator A0 (P x P, row-major) of a two-level preconditioner as
+ * built on the device (CoarseSpace::A0, src/precond/coarse_space.h:43-60). */
+sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc);
+
+/* ---- solvers ---------------------------------------------------------- */
+typedef enum sg_solver {
+    SG_GMRES = 0, /* left preconditioned, src/core/gmres.cpp:34-160 */
+    SG_FGMRES = 1 /* right preconditioned storing V and Z, src/core/fgmres.cpp:28-144 */
+} sg_solver;
+
+typedef enum sg_tol_kind {
+    /* the reference rule: stop when |g_{j+1}| < tol (the preconditioned
+     * residual for GMRES, src/core/gmres.cpp:318; unpreconditioned for FGMRES,
+     * src/core/fgmres.cpp:170), or when the cycle-start norm < tol */
+    SG_TOL_REF_ABS = 0,
+    /* FP64 true relative residual ||b-Ax||/||b|| <= tol, checked at every
+     * restart only (the cycle granularity of the oracle harness) */
+    SG_TOL_TRUE_REL_CYCLE = 1,
+    /* FP64 true relative residual <= tol; a cycle stops early once the
+     * Arnoldi estimate says so, and the restart recomputes b-Ax in FP64 */
+    SG_TOL_TRUE_REL = 2
+} sg_tol_kind;
+
+typedef struct sg_solve_params {
+    int restart;     /* m (GMRESParams::restart, default 30) */
+    int max_iter;    /* GMRESParams::max_iter (default 1000) */
+    double tol;      /* GMRESParams::tol (default 1e-10) */
+    int tol_kind;    /* sg_tol_kind */
+    int precision;   /* SG_FP64: all-FP64 Krylov; SG_FP32: FP32 inner Krylov
+                        with FP64 true residual, update and least squares
+                        (GMRES-IR); the preconditioner uses its own dtypes */
+    int use_graph;   /* 1: launch each restart cycle as a CUDA graph */
+    double* history; /* optional host array receiving |g_{j+1}| per iteration */
+    int history_cap;
+    int reserved[8];
+} sg_solve_params;
+
+typedef struct sg_solve_result {
+    int iterations;           /* GMRESResult::iterations */
+    int cycles;
+    int converged;            /* GMRESResult::converged */
+    int history_len;
+    double residual_norm;     /* GMRESResult::residual_norm (last |g_{j+1}|) */
+    double true_rel_residual; /* ||b - A x||_2 / ||b||_2 in FP64 at exit */
+    double time_solve_s;      /* GMRESResult::time_solve_s */
+    double reserved[4];
+} sg_solve_result;
+
+/* gmres()/fgmres() (src/core/gmres.h:28-33, src/core/fgmres.h:42-47).
+ * x holds x0 on entry and the solution on exit.  pc may be NULL. */
+sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* pc,
+                   const double* b, double* x, int n, sg_mem mem,
+                   const sg_solve_params* params, sg_solve_result* result);
+
+/* ---- problem generators and partitions (host side, deterministic) ----- */
+/* make_poisson_2d / make_poisson_3d (src/mesh/poisson.h:10-74).  Call with
+ * NULL arrays to get nnz, then with arrays of n+1 / nnz / nnz entries. */
+sg_status sg_gen_poisson2d(int nx, int ny, int* row_ptr, int* col_idx, double* vals, int* nnz);
+sg_status sg_gen_poisson3d(int nx, int ny, int nz, int* row_ptr, int* col_idx, double* vals,
+                           int* nnz);
+/* -div(k grad u) on an nx*ny*nz grid, 7-point, Dirichlet, k = exp(sigma*g)
+ * with g a unit-variance Gaussian random field of squared-exponential
+ * correlation length `corr_len` cells (white noise from SplitMix64(seed)
+ * convolved with a separable Gaussian kernel); face coefficients are the
+ * harmonic mean of the two cell values.  Same index order as
+ * make_poisson_3d. */
+sg_status sg_gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr_len,
+                           uint64_t seed, int* row_ptr, int* col_idx, double* vals, int* nnz);
+/* n values uniform in [lo,hi): u = (SplitMix64(seed) >> 11) * 2^-53. */
+sg_status sg_gen_uniform(uint64_t seed, int n, double lo, double hi, double* out);
+/* Built-in graph partitioner used when no partition is given: recursive
+ * bisection of the CSR graph by breadth-first level structures. */
+sg_status sg_partition_graph(int n, const int* row_ptr, const int* col_idx, int nparts,
+                             int* part);
+/* Boxes of an nx*ny*nz grid from recursive coordinate bisection with cut
+ * fractions drawn from [0.5-spread, 0.5+spread] (seeded): uneven parts. */
+sg_status sg_partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed,
+                             int* part);
+/* Host-only integer set-up of a Schwarz/ILU(0) preconditioner, exactly as
+ * sg_precond_setup computes it before any device work: decomposition
+ * (build_decomposition, src/decomp/domain_decomp.h:61-93), owned-local map
+ * (src/precond/ras.h:34-41), local CSR of A[dofs,dofs] (src/core/
+ * sparse_matrix.h:53-83), ILU(0) diagonal positions (src/precond/ilu0.h:
+ * 19-29) and sweep levels.  which: 0-6 as sg_precond_get_decomposition;
+ * 7 local row_ptr (n_s+1 per subdomain, concatenated), 8 local col_idx,
+ * 9 diag_ptr, 10 forward level, 11 backward level. */
+sg_status sg_schwarz_structure(int n, const int* row_ptr, const int* col_idx, const int* part,
+                               int nparts, int overlap, int which, int* out, int cap, int* len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,487 @@
+"""schwarz_gmres_dashboard_gb300 -- GB300 (sm_103a) solve path of schwarz-gmres.
+
+Python mirror of the reference's C++ interface (src/core/sparse_matrix.h,
+src/precond/*.h, src/core/gmres.h, src/core/fgmres.h) over the C ABI of
+libsgmres.so.  Same names, argument meaning and error behaviour:
+
+    A = make_poisson_2d(20, 20)
+    M = RASPrecond(4, 1); M.setup(A)
+    x = np.zeros(A.nrows)
+    res = gmres(A, b, x, M, GMRESParams(restart=30, tol=1e-10))
+
+Every numerical step runs on the GPU; there is no CPU fallback -- without the
+built library the import fails, without a device the calls raise.
+Vectors may be numpy arrays (host) or CUDA tensors / objects exposing
+``__cuda_array_interface__`` (used in place on the device).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import SgError
+
+_clib = L.load()
+
+__all__ = [
+    "SgError", "Context", "default_context", "CSRMatrix", "make_identity", "make_poisson_2d",
+    "make_poisson_3d", "make_varcoef_3d", "uniform", "partition_graph", "partition_boxes",
+    "schwarz_structure",
+    "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
+    "TwoLevelSchwarzPrecond", "FineLevelType", "GMRESParams", "GMRESResult", "gmres", "fgmres",
+    "FP64", "FP32", "BF16", "TOL_REF_ABS", "TOL_TRUE_REL_CYCLE", "TOL_TRUE_REL",
+]
+
+FP64, FP32, BF16 = L.FP64, L.FP32, L.BF16
+TOL_REF_ABS, TOL_TRUE_REL_CYCLE, TOL_TRUE_REL = L.TOL_REF_ABS, L.TOL_TRUE_REL_CYCLE, L.TOL_TRUE_REL
+
+
+def _check(st):
+    L.check(st)
+
+
+# ---------------------------------------------------------------- context
+class Context:
+    """One device and one stream (replaces CudaHandles, src/gpu/cuda_common.h:42-107)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(_clib.sg_ctx_create(int(device), C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _check(_clib.sg_ctx_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(_clib.sg_ctx_get_stream(self.handle, C.byref(s)))
+        return s.value or 0
+
+    def synchronize(self) -> None:
+        _check(_clib.sg_ctx_synchronize(self.handle))
+
+    @property
+    def launch_count(self) -> int:
+        """Kernels launched through this context so far."""
+        c = C.c_longlong(0)
+        _check(_clib.sg_ctx_get_launch_count(self.handle, C.byref(c)))
+        return int(c.value)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            _clib.sg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _vec(a, n: int, writable: bool = False):
+    """(pointer, mem, keepalive) for a host numpy array or a device array."""
+    cai = getattr(a, "__cuda_array_interface__", None)
+    if cai is not None:
+        ptr = cai["data"][0]
+        typestr = cai["typestr"]
+        if typestr not in ("<f8", "=f8"):
+            raise TypeError("device vectors must be float64")
+        if cai.get("strides") not in (None, (8,)):
+            raise TypeError("device vectors must be contiguous")
+        if int(np.prod(cai["shape"])) < n:
+            raise ValueError("device vector too short")
+        return C.c_void_p(ptr), L.MEM_DEVICE, a
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        if writable:
+            raise TypeError("output vectors must be contiguous float64 numpy arrays")
+        a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.size < n:
+        raise ValueError("vector too short")
+    return C.c_void_p(a.ctypes.data), L.MEM_HOST, a
+
+
+# ---------------------------------------------------------------- matrix
+class CSRMatrix:
+    """CSRMatrix of src/core/sparse_matrix.h:13-84: int32 row_ptr/col_idx,
+    float64 vals, 0-based.  The device copy is made on first use (or by
+    ``upload()``); call ``upload()`` again after changing the arrays."""
+
+    def __init__(self, nrows=0, ncols=0, row_ptr=None, col_idx=None, vals=None):
+        self.nrows = int(nrows)
+        self.ncols = int(ncols)
+        self.row_ptr = np.zeros(self.nrows + 1, np.int32) if row_ptr is None else \
+            np.ascontiguousarray(row_ptr, dtype=np.int32)
+        self.col_idx = np.zeros(0, np.int32) if col_idx is None else \
+            np.ascontiguousarray(col_idx, dtype=np.int32)
+        self.vals = np.zeros(0, np.float64) if vals is None else \
+            np.ascontiguousarray(vals, dtype=np.float64)
+        self._dev = None
+        self._ctx = None
+
+    def nnz(self) -> int:
+        return int(self.vals.size)
+
+    def upload(self, ctx: Context | None = None):
+        ctx = ctx or default_context()
+        self.release()
+        h = C.c_void_p()
+        _check(_clib.sg_csr_create(ctx.handle, self.nrows, self.ncols, self.nnz(),
+                                  self.row_ptr.ctypes.data, self.col_idx.ctypes.data,
+                                  self.vals.ctypes.data, L.MEM_HOST, C.byref(h)))
+        self._dev, self._ctx = h, ctx
+        return self
+
+    def device(self, ctx: Context | None = None):
+        if self._dev is None or (ctx is not None and ctx is not self._ctx):
+            self.upload(ctx)
+        return self._dev
+
+    def release(self):
+        if self._dev is not None:
+            _clib.sg_csr_destroy(self._dev)
+            self._dev = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def spmv(self, x, y=None):
+        """y = A x on the GPU (sparse_matrix.h:30-37), bit-identical to the
+        reference's row loop."""
+        dev = self.device()
+        if y is None:
+            y = np.empty(self.nrows, np.float64)
+        px, mx, _kx = _vec(x, self.ncols)
+        py, my, _ky = _vec(y, self.nrows, writable=True)
+        if mx != my:
+            raise TypeError("x and y must both be host or both be device arrays")
+        _check(_clib.sg_csr_spmv(dev, px, py, mx))
+        return y
+
+    def diagonal(self, i: int) -> float:
+        for e in range(self.row_ptr[i], self.row_ptr[i + 1]):
+            if self.col_idx[e] == i:
+                return float(self.vals[e])
+        return 0.0
+
+
+def make_identity(n: int) -> CSRMatrix:
+    """make_identity (src/core/sparse_matrix.h:86-96)"""
+    return CSRMatrix(n, n, np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32),
+                     np.ones(n))
+
+
+def _gen(fn, dims, n, *extra):
+    nnz = C.c_int(0)
+    _check(fn(*dims, *extra, None, None, None, C.byref(nnz)))
+    rp = np.empty(n + 1, np.int32)
+    ci = np.empty(nnz.value, np.int32)
+    v = np.empty(nnz.value, np.float64)
+    _check(fn(*dims, *extra, rp.ctypes.data, ci.ctypes.data, v.ctypes.data, C.byref(nnz)))
+    return CSRMatrix(n, n, rp, ci, v)
+
+
+def make_poisson_2d(nx: int, ny: int) -> CSRMatrix:
+    """5-point Laplacian, Dirichlet (src/mesh/poisson.h:10-38)."""
+    return _gen(_clib.sg_gen_poisson2d, (nx, ny), nx * ny)
+
+
+def make_poisson_3d(nx: int, ny: int, nz: int) -> CSRMatrix:
+    """7-point Laplacian, Dirichlet (src/mesh/poisson.h:41-74)."""
+    return _gen(_clib.sg_gen_poisson3d, (nx, ny, nz), nx * ny * nz)
+
+
+def make_varcoef_3d(nx: int, ny: int, nz: int, sigma: float = 1.0, corr_len: float = 8.0,
+                    seed: int = 0) -> CSRMatrix:
+    """-div(k grad u), 7-point, k = exp(sigma * g), g a seeded unit-variance
+    Gaussian random field with squared-exponential correlation length
+    `corr_len` cells; harmonic-mean face coefficients."""
+    return _gen(_clib.sg_gen_varcoef3d, (nx, ny, nz), nx * ny * nz,
+                C.c_double(sigma), C.c_double(corr_len), C.c_uint64(seed))
+
+
+def uniform(n: int, seed: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
+    """Seeded U[lo,hi) values from SplitMix64 ((x >> 11) * 2^-53)."""
+    out = np.empty(n, np.float64)
+    _check(_clib.sg_gen_uniform(C.c_uint64(seed), n, C.c_double(lo), C.c_double(hi),
+                               out.ctypes.data))
+    return out
+
+
+def partition_graph(A: CSRMatrix, nparts: int) -> np.ndarray:
+    """Built-in graph partitioner (takes METIS_PartGraphKway's place)."""
+    part = np.empty(A.nrows, np.int32)
+    _check(_clib.sg_partition_graph(A.nrows, A.row_ptr.ctypes.data, A.col_idx.ctypes.data,
+                                   nparts, part.ctypes.data))
+    return part
+
+
+def partition_boxes(nx: int, ny: int, nz: int, nparts: int, spread: float = 0.0,
+                    seed: int = 0) -> np.ndarray:
+    """Boxes of a grid from recursive coordinate bisection with seeded uneven cuts."""
+    part = np.empty(nx * ny * nz, np.int32)
+    _check(_clib.sg_partition_boxes(nx, ny, nz, nparts, C.c_double(spread), C.c_uint64(seed),
+                                   part.ctypes.data))
+    return part
+
+
+STRUCTURE_NAMES = ["partition", "owned_ptr", "owned", "sub_ptr", "sub", "ownloc_ptr", "ownloc",
+                   "local_row_ptr", "local_col_idx", "diag_ptr", "level_lower", "level_upper"]
+
+
+def schwarz_structure(A: CSRMatrix, part, nparts: int, overlap: int) -> dict:
+    """Host-side integer set-up of the Schwarz/ILU(0) preconditioners (the part
+    of setup() that runs before any device work); no GPU needed."""
+    part = np.ascontiguousarray(part, dtype=np.int32)
+    out = {}
+    for which, nm in enumerate(STRUCTURE_NAMES):
+        ln = C.c_int(0)
+        _check(_clib.sg_schwarz_structure(A.nrows, A.row_ptr.ctypes.data, A.col_idx.ctypes.data,
+                                         part.ctypes.data, nparts, overlap, which, None, 0,
+                                         C.byref(ln)))
+        arr = np.empty(max(ln.value, 1), np.int32)
+        _check(_clib.sg_schwarz_structure(A.nrows, A.row_ptr.ctypes.data, A.col_idx.ctypes.data,
+                                         part.ctypes.data, nparts, overlap, which,
+                                         arr.ctypes.data, arr.size, C.byref(ln)))
+        out[nm] = arr[: ln.value]
+    return out
+
+
+# ---------------------------------------------------------------- preconditioners
+class FineLevelType(enum.Enum):
+    """src/precond/two_level_schwarz.h:21"""
+    ASM = 0
+    RAS = 1
+
+
+class Preconditioner:
+    """Preconditioner plugin of src/precond/preconditioner.h:7-20:
+    setup(A) then apply(x) -> y = M^{-1} x (overwrites all of y)."""
+
+    kind = "none"
+
+    def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
+                 factor_dtype: int = FP64, sweep_dtype: int = FP64,
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.nparts = int(nparts)
+        self.overlap = int(overlap)
+        self.partition = None if partition is None else np.ascontiguousarray(partition, np.int32)
+        self.factor_dtype = factor_dtype
+        self.sweep_dtype = sweep_dtype
+        opts = L.PrecondOpts()
+        opts.nparts = self.nparts
+        opts.overlap = self.overlap
+        opts.factor_dtype = factor_dtype
+        opts.sweep_dtype = sweep_dtype
+        opts.partition = self.partition.ctypes.data if self.partition is not None else None
+        self._opts = opts
+        h = C.c_void_p()
+        _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),
+                                      C.byref(h)))
+        self.handle = h
+        self.n = 0
+
+    def setup(self, A: CSRMatrix) -> None:
+        _check(_clib.sg_precond_setup(self.handle, A.device(self.ctx)))
+        self.n = A.nrows
+
+    def apply(self, x, y=None):
+        if y is None:
+            y = np.empty(self.n, np.float64)
+        px, mx, _kx = _vec(x, self.n)
+        py, my, _ky = _vec(y, self.n, writable=True)
+        if mx != my:
+            raise TypeError("x and y must both be host or both be device arrays")
+        _check(_clib.sg_precond_apply(self.handle, px, py, self.n, mx))
+        return y
+
+    # ---- set-up read-back (parity checks)
+    def decomposition(self) -> dict:
+        names = ["partition", "owned_ptr", "owned", "sub_ptr", "sub", "ownloc_ptr", "ownloc"]
+        out = {}
+        for which, nm in enumerate(names):
+            ln = C.c_int(0)
+            _check(_clib.sg_precond_get_decomposition(self.handle, which, None, 0, C.byref(ln)))
+            arr = np.empty(max(ln.value, 1), np.int32)
+            _check(_clib.sg_precond_get_decomposition(self.handle, which, arr.ctypes.data,
+                                                     arr.size, C.byref(ln)))
+            out[nm] = arr[: ln.value]
+        return out
+
+    def factors(self, s: int = 0) -> dict:
+        ns, nz = C.c_int(0), C.c_int(0)
+        _check(_clib.sg_precond_get_factors(self.handle, s, C.byref(ns), C.byref(nz), None, None,
+                                           None, None, None, None))
+        rp = np.empty(ns.value + 1, np.int32)
+        ci = np.empty(max(nz.value, 1), np.int32)
+        lu = np.empty(max(nz.value, 1), np.float64)
+        dg = np.empty(max(ns.value, 1), np.int32)
+        lo = np.empty(max(ns.value, 1), np.int32)
+        up = np.empty(max(ns.value, 1), np.int32)
+        _check(_clib.sg_precond_get_factors(self.handle, s, C.byref(ns), C.byref(nz),
+                                           rp.ctypes.data, ci.ctypes.data, lu.ctypes.data,
+                                           dg.ctypes.data, lo.ctypes.data, up.ctypes.data))
+        k, z = ns.value, nz.value
+        return dict(row_ptr=rp, col_idx=ci[:z], lu_vals=lu[:z], diag_ptr=dg[:k],
+                    level_lower=lo[:k], level_upper=up[:k])
+
+    def coarse_a0(self) -> np.ndarray:
+        nc = C.c_int(0)
+        _check(_clib.sg_precond_get_coarse(self.handle, None, 0, C.byref(nc)))
+        a0 = np.empty(nc.value * nc.value, np.float64)
+        _check(_clib.sg_precond_get_coarse(self.handle, a0.ctypes.data, a0.size, C.byref(nc)))
+        return a0.reshape(nc.value, nc.value)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _clib.sg_precond_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class NoPrecond(Preconditioner):
+    kind = "none"
+
+
+class JacobiPrecond(Preconditioner):
+    """src/precond/jacobi.h:10-27"""
+    kind = "jacobi"
+
+    def __init__(self, sweep_dtype: int = FP64, ctx: Context | None = None):
+        super().__init__(1, 0, None, FP64 if sweep_dtype == FP64 else FP32, sweep_dtype, ctx)
+
+
+class ILU0Precond(Preconditioner):
+    """src/precond/ilu0.h:11-93"""
+    kind = "ilu0"
+
+    def __init__(self, factor_dtype: int = FP64, sweep_dtype: int = FP64,
+                 ctx: Context | None = None):
+        super().__init__(1, 0, None, factor_dtype, sweep_dtype, ctx)
+
+
+class ASMPrecond(Preconditioner):
+    """src/precond/asm.h:13-71"""
+    kind = "asm"
+
+    def __init__(self, nparts: int, overlap: int, partition=None, factor_dtype: int = FP64,
+                 sweep_dtype: int = FP64, ctx: Context | None = None):
+        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx)
+
+
+class RASPrecond(Preconditioner):
+    """src/precond/ras.h:16-82"""
+    kind = "ras"
+
+    def __init__(self, nparts: int, overlap: int, partition=None, factor_dtype: int = FP64,
+                 sweep_dtype: int = FP64, ctx: Context | None = None):
+        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx)
+
+
+class TwoLevelSchwarzPrecond(Preconditioner):
+    """src/precond/two_level_schwarz.h:23-75 (fine ASM or RAS + piecewise-constant
+    coarse space with an FP64 LU)."""
+
+    def __init__(self, nparts: int, overlap: int, fine_type: FineLevelType = FineLevelType.RAS,
+                 partition=None, factor_dtype: int = FP64, sweep_dtype: int = FP64,
+                 ctx: Context | None = None):
+        self.kind = "twolevel_asm" if fine_type == FineLevelType.ASM else "twolevel_ras"
+        self.fine_type = fine_type
+        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx)
+
+
+# ---------------------------------------------------------------- solvers
+@dataclass
+class GMRESParams:
+    """GMRESParams (src/core/gmres.h:20-24) plus the GPU options."""
+    restart: int = 30
+    max_iter: int = 1000
+    tol: float = 1e-10
+    tol_kind: int = TOL_REF_ABS
+    precision: int = FP64
+    use_graph: bool = True
+
+
+@dataclass
+class GMRESResult:
+    """GMRESResult (src/core/gmres.h:12-18) plus true_rel_residual / cycles."""
+    iterations: int = 0
+    residual_norm: float = 0.0
+    converged: bool = False
+    time_solve_s: float = 0.0
+    residual_history: List[float] = field(default_factory=list)
+    true_rel_residual: float = 0.0
+    cycles: int = 0
+
+
+def _solve(solver: int, A: CSRMatrix, b, x, M: Optional[Preconditioner],
+           params: Optional[GMRESParams], history: bool = True) -> GMRESResult:
+    params = params or GMRESParams()
+    ctx = M.ctx if M is not None else default_context()
+    dev = A.device(ctx)
+    n = A.nrows
+    pb, mb, _kb = _vec(b, n)
+    px, mx, _kx = _vec(x, n, writable=True)
+    if mb != mx:
+        raise TypeError("b and x must both be host or both be device arrays")
+    p = L.SolveParams()
+    p.restart = params.restart
+    p.max_iter = params.max_iter
+    p.tol = params.tol
+    p.tol_kind = params.tol_kind
+    p.precision = params.precision
+    p.use_graph = 1 if params.use_graph else 0
+    hist = None
+    if history:
+        cap = max(params.max_iter, 0) + params.restart + 1
+        hist = np.zeros(cap, np.float64)
+        p.history = hist.ctypes.data
+        p.history_cap = cap
+    r = L.SolveResult()
+    st = _clib.sg_solve(ctx.handle, solver, dev, M.handle if M is not None else None, pb, px, n,
+                       mx, C.byref(p), C.byref(r))
+    _check(st)
+    hl = min(r.history_len, hist.size) if hist is not None else 0
+    return GMRESResult(iterations=r.iterations, residual_norm=r.residual_norm,
+                       converged=bool(r.converged), time_solve_s=r.time_solve_s,
+                       residual_history=list(hist[:hl]) if hist is not None else [],
+                       true_rel_residual=r.true_rel_residual, cycles=r.cycles)
+
+
+def gmres(A: CSRMatrix, b, x, M: Optional[Preconditioner] = None,
+          params: Optional[GMRESParams] = None) -> GMRESResult:
+    """Restarted GMRES(m), left preconditioning (src/core/gmres.h:28-33).
+    x holds x0 on entry and the solution on exit."""
+    return _solve(L.GMRES, A, b, x, M, params)
+
+
+def fgmres(A: CSRMatrix, b, x, M: Optional[Preconditioner] = None,
+           params: Optional[GMRESParams] = None) -> GMRESResult:
+    """FGMRES(m), right preconditioning (src/core/fgmres.h:42-47)."""
+    return _solve(L.FGMRES, A, b, x, M, params)

@@ -1,0 +1,581 @@
+// api.cpp -- the C ABI of libsgmres (declared in include/sgmres.h).  Every
+// entry point validates its arguments, runs on the context's device and
+// stream, and turns internal failures into an sg_status plus a thread-local
+// message.
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+
+#include "kernels.h"
+#include "sg_internal.h"
+
+namespace sg {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+void fail(sg_status st, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Error{st, buf};
+}
+
+// defined in setup.cpp / solver.cu
+void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part, int nparts, int overlap);
+void partition_graph(int n, const int* rp, const int* ci, int nparts, int* part);
+void partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed, int* part);
+int gen_poisson2d(int nx, int ny, int* rp, int* ci, double* v);
+int gen_poisson3d(int nx, int ny, int nz, int* rp, int* ci, double* v);
+int gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t seed, int* rp, int* ci,
+                  double* v);
+void gen_uniform(uint64_t seed, int n, double lo, double hi, double* out);
+void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, const double* b,
+                  double* x, const sg_solve_params& prm, sg_solve_result* res);
+
+template <class F>
+static sg_status guard(F&& f) {
+    try {
+        f();
+        g_last_error.clear();
+        return SG_OK;
+    } catch (const Error& e) {
+        g_last_error = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return SG_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return SG_ERR_INTERNAL;
+    } catch (...) {
+        g_last_error = "unknown internal error";
+        return SG_ERR_INTERNAL;
+    }
+}
+
+static void use_device(const sg_ctx* ctx) { SG_CUDA(cudaSetDevice(ctx->device)); }
+
+}  // namespace sg
+
+using namespace sg;
+
+void sg_csr::ensure_fp32() {
+    if (val32.p) return;
+    std::vector<float> v32(h_val.size() + 16, 0.0f);
+    for (size_t i = 0; i < h_val.size(); ++i) v32[i] = (float)h_val[i];
+    val32.upload(v32, ctx->stream);
+    SG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+extern "C" {
+
+int sg_abi_version(void) { return SG_ABI_VERSION; }
+
+const char* sg_last_error(void) { return g_last_error.c_str(); }
+
+const char* sg_status_string(sg_status st) {
+    switch (st) {
+    case SG_OK: return "ok";
+    case SG_ERR_INVALID_ARG: return "invalid argument";
+    case SG_ERR_CUDA: return "CUDA error";
+    case SG_ERR_OOM: return "out of memory";
+    case SG_ERR_SINGULAR: return "singular";
+    case SG_ERR_NOT_SETUP: return "not set up";
+    case SG_ERR_NONFINITE: return "non-finite value";
+    case SG_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case SG_ERR_UNSUPPORTED: return "unsupported";
+    case SG_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+sg_status sg_ctx_create(int device, sg_ctx** out) {
+    return guard([&] {
+        SG_CHECK_ARG(out, "out is NULL");
+        *out = nullptr;
+        int count = 0;
+        cudaError_t e = cudaGetDeviceCount(&count);
+        if (e != cudaSuccess || count == 0)
+            fail(SG_ERR_CUDA, "no CUDA device available (%s)",
+                 e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        SG_CHECK_ARG(device >= 0 && device < count, "device %d out of range [0,%d)", device, count);
+        auto* ctx = new sg_ctx();
+        try {
+            ctx->device = device;
+            SG_CUDA(cudaSetDevice(device));
+            SG_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+            SG_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+            ctx->stream = ctx->own_stream;
+            ctx->partials.alloc((size_t)ctx->num_sms * 8 * 40);
+            ctx->counter.alloc(4);
+            ctx->counter.zero(ctx->stream);
+            SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        } catch (...) {
+            delete ctx;
+            throw;
+        }
+        *out = ctx;
+    });
+}
+
+sg_status sg_ctx_destroy(sg_ctx* ctx) {
+    return guard([&] {
+        if (!ctx) return;
+        cudaSetDevice(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        delete ctx->work;
+        ctx->work = nullptr;
+        ctx->partials.release();
+        ctx->counter.release();
+        ctx->hist.release();
+        if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+        delete ctx;
+    });
+}
+
+sg_status sg_ctx_set_stream(sg_ctx* ctx, void* stream) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx, "ctx is NULL");
+        use_device(ctx);
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    });
+}
+
+sg_status sg_ctx_get_stream(sg_ctx* ctx, void** stream) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && stream, "NULL argument");
+        *stream = ctx->stream;
+    });
+}
+
+sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && count, "NULL argument");
+        *count = ctx->launches;
+    });
+}
+
+sg_status sg_ctx_synchronize(sg_ctx* ctx) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx, "ctx is NULL");
+        use_device(ctx);
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+// ------------------------------------------------------------------ matrix
+sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* row_ptr,
+                        const int* col_idx, const double* vals, sg_mem mem, sg_csr** out) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && out, "NULL argument");
+        *out = nullptr;
+        SG_CHECK_ARG(nrows >= 0 && ncols >= 0 && nnz >= 0, "negative size");
+        SG_CHECK_ARG(row_ptr, "row_ptr is NULL");
+        SG_CHECK_ARG(nnz == 0 || (col_idx && vals), "col_idx/vals are NULL");
+        use_device(ctx);
+        auto* A = new sg_csr();
+        try {
+            A->ctx = ctx;
+            A->nrows = nrows;
+            A->ncols = ncols;
+            A->nnz = nnz;
+            A->h_rp.resize((size_t)nrows + 1);
+            A->h_ci.resize((size_t)nnz + 16, 0);
+            A->h_val.resize((size_t)nnz);
+            if (mem == SG_MEM_DEVICE) {
+                SG_CUDA(cudaMemcpy(A->h_rp.data(), row_ptr, sizeof(int) * (nrows + 1),
+                                   cudaMemcpyDeviceToHost));
+                if (nnz) {
+                    SG_CUDA(cudaMemcpy(A->h_ci.data(), col_idx, sizeof(int) * nnz,
+                                       cudaMemcpyDeviceToHost));
+                    SG_CUDA(cudaMemcpy(A->h_val.data(), vals, sizeof(double) * nnz,
+                                       cudaMemcpyDeviceToHost));
+                }
+            } else {
+                std::memcpy(A->h_rp.data(), row_ptr, sizeof(int) * (nrows + 1));
+                if (nnz) {
+                    std::memcpy(A->h_ci.data(), col_idx, sizeof(int) * nnz);
+                    std::memcpy(A->h_val.data(), vals, sizeof(double) * nnz);
+                }
+            }
+            SG_CHECK_ARG(A->h_rp[0] == 0, "row_ptr[0] must be 0");
+            SG_CHECK_ARG(A->h_rp[nrows] == nnz, "row_ptr[nrows] (%d) != nnz (%d)", A->h_rp[nrows],
+                         nnz);
+            for (int i = 0; i < nrows; ++i) {
+                SG_CHECK_ARG(A->h_rp[i + 1] >= A->h_rp[i], "row_ptr decreases at row %d", i);
+                for (int e = A->h_rp[i]; e < A->h_rp[i + 1]; ++e) {
+                    const int c = A->h_ci[e];
+                    SG_CHECK_ARG(c >= 0 && c < ncols, "col_idx[%d] = %d outside [0,%d)", e, c, ncols);
+                    if (e > A->h_rp[i] && c < A->h_ci[e - 1]) A->sorted = false;
+                }
+            }
+            std::vector<double> vpad(A->h_val);
+            vpad.resize((size_t)nnz + 16, 0.0);
+            A->rp.upload(A->h_rp, ctx->stream);
+            A->ci.upload(A->h_ci, ctx->stream);
+            A->val.upload(vpad, ctx->stream);
+            A->h_ci.resize(nnz);
+            SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        } catch (...) {
+            delete A;
+            throw;
+        }
+        *out = A;
+    });
+}
+
+sg_status sg_csr_destroy(sg_csr* A) {
+    return guard([&] {
+        if (!A) return;
+        cudaSetDevice(A->ctx->device);
+        delete A;
+    });
+}
+
+sg_status sg_csr_spmv(sg_csr* A, const double* x, double* y, sg_mem mem) {
+    return guard([&] {
+        SG_CHECK_ARG(A && x && y, "NULL argument");
+        sg_ctx* ctx = A->ctx;
+        use_device(ctx);
+        if (!ctx->work) ctx->work = new SolveWork();
+        const double* dx = x;
+        double* dy = y;
+        if (mem == SG_MEM_HOST) {
+            SolveWork* w = ctx->work;
+            w->x64.upload(x, A->ncols, ctx->stream);
+            if (w->b64.n < (size_t)std::max(A->nrows, 1)) w->b64.alloc(std::max(A->nrows, 1));
+            dx = w->x64.p;
+            dy = w->b64.p;
+        }
+        launch_spmv<double, double, double>(ctx, A->nrows, A->rp.p, A->ci.p, A->val.p, dx, dy,
+                                            nullptr, nullptr);
+        if (mem == SG_MEM_HOST)
+            SG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * A->nrows, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+// ------------------------------------------------------------------ preconditioner
+sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_opts* opts,
+                            sg_precond** out) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && out, "NULL argument");
+        *out = nullptr;
+        SG_CHECK_ARG(kind >= SG_PC_NONE && kind <= SG_PC_TWOLEVEL_RAS, "unknown kind %d", (int)kind);
+        auto* pc = new sg_precond();
+        pc->ctx = ctx;
+        pc->kind = kind;
+        if (opts) pc->opts = *opts;
+        else {
+            pc->opts.nparts = 4;
+            pc->opts.overlap = 1;
+            pc->opts.factor_dtype = SG_FP64;
+            pc->opts.sweep_dtype = SG_FP64;
+        }
+        const int sd = pc->opts.sweep_dtype, fd = pc->opts.factor_dtype;
+        const bool ok = (sd == SG_FP64 && fd == SG_FP64) ||
+                        (sd == SG_FP32 && (fd == SG_FP32 || fd == SG_BF16));
+        if (!ok) {
+            delete pc;
+            fail(SG_ERR_INVALID_ARG,
+                 "sweep/factor dtypes: FP64 sweeps need FP64 factors; FP32 sweeps take FP32 or "
+                 "BF16 factors");
+        }
+        *out = pc;
+    });
+}
+
+sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && A, "NULL argument");
+        SG_CHECK_ARG(A->ctx == pc->ctx, "matrix and preconditioner belong to different contexts");
+        use_device(pc->ctx);
+        pc->is_setup = false;
+        pc->n = A->nrows;
+        if (pc->kind == SG_PC_NONE) {
+            pc->is_setup = true;
+            return;
+        }
+        if (pc->kind == SG_PC_JACOBI) {
+            SG_CHECK_ARG(A->nrows <= A->ncols, "Jacobi needs nrows <= ncols");
+            precond_setup_device(pc, A);
+            pc->is_setup = true;
+            return;
+        }
+        std::vector<int> part(A->nrows, 0);
+        int nparts = 1, overlap = 0;
+        if (pc->kind != SG_PC_ILU0) {
+            nparts = pc->opts.nparts;
+            overlap = pc->opts.overlap;
+            SG_CHECK_ARG(nparts >= 1, "nparts must be >= 1");
+            SG_CHECK_ARG(nparts <= std::max(A->nrows, 1), "nparts exceeds rows");
+            SG_CHECK_ARG(nparts <= 4096 || (pc->kind != SG_PC_TWOLEVEL_ASM &&
+                                            pc->kind != SG_PC_TWOLEVEL_RAS),
+                         "two-level preconditioners support at most 4096 parts");
+            if (pc->opts.partition)
+                std::memcpy(part.data(), pc->opts.partition, sizeof(int) * A->nrows);
+            else if (nparts > 1)
+                partition_graph(A->nrows, A->h_rp.data(), A->h_ci.data(), nparts, part.data());
+        }
+        pc->overlap = overlap;
+        build_schwarz_host(pc, A, part.data(), nparts, overlap);
+        precond_setup_device(pc, A);
+        pc->is_setup = true;
+    });
+}
+
+sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg_mem mem) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && x && y, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        SG_CHECK_ARG(n == pc->n, "n (%d) does not match the set-up size (%d)", n, pc->n);
+        sg_ctx* ctx = pc->ctx;
+        use_device(ctx);
+        const double* dx = x;
+        double* dy = y;
+        if (mem == SG_MEM_HOST) {
+            pc->io_x.upload(x, n, ctx->stream);
+            if (pc->io_y.n < (size_t)std::max(n, 1)) pc->io_y.alloc(std::max(n, 1));
+            dx = pc->io_x.p;
+            dy = pc->io_y.p;
+        }
+        precond_apply_device<double, double>(pc, dx, dy, nullptr);
+        if (mem == SG_MEM_HOST)
+            SG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+sg_status sg_precond_destroy(sg_precond* pc) {
+    return guard([&] {
+        if (!pc) return;
+        cudaSetDevice(pc->ctx->device);
+        delete pc;
+    });
+}
+
+sg_status sg_precond_get_decomposition(sg_precond* pc, int which, int* out, int cap, int* len) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && len, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        const std::vector<int>* v = nullptr;
+        switch (which) {
+        case 0: v = &pc->part; break;
+        case 1: v = &pc->owned_ptr; break;
+        case 2: v = &pc->owned; break;
+        case 3: v = &pc->sub_ptr; break;
+        case 4: v = &pc->sub; break;
+        case 5: v = &pc->ownloc_ptr; break;
+        case 6: v = &pc->ownloc; break;
+        default: fail(SG_ERR_INVALID_ARG, "unknown decomposition array %d", which);
+        }
+        *len = (int)v->size();
+        if (out) {
+            SG_CHECK_ARG(cap >= (int)v->size(), "cap %d < length %d", cap, (int)v->size());
+            std::copy(v->begin(), v->end(), out);
+        }
+    });
+}
+
+sg_status sg_precond_get_factors(sg_precond* pc, int s, int* n_s, int* nnz_s, int* row_ptr,
+                                 int* col_idx, double* lu_vals, int* diag_ptr, int* level_lower,
+                                 int* level_upper) {
+    return guard([&] {
+        SG_CHECK_ARG(pc, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        SG_CHECK_ARG(pc->kind >= SG_PC_ILU0, "no ILU factors for this preconditioner kind");
+        SG_CHECK_ARG(s >= 0 && s < pc->nparts, "subdomain %d out of range", s);
+        const SubInfo& inf = pc->h_info[s];
+        const int* rp = pc->lrp.data() + inf.csr_row_off;
+        const int nnz = rp[inf.n];
+        if (n_s) *n_s = inf.n;
+        if (nnz_s) *nnz_s = nnz;
+        if (row_ptr) std::copy(rp, rp + inf.n + 1, row_ptr);
+        if (col_idx) std::copy(pc->lci.begin() + inf.csr_nz_off,
+                               pc->lci.begin() + inf.csr_nz_off + nnz, col_idx);
+        if (diag_ptr) std::copy(pc->ldiag.begin() + inf.row_off,
+                                pc->ldiag.begin() + inf.row_off + inf.n, diag_ptr);
+        if (level_lower) std::copy(pc->lev_lo.begin() + inf.row_off,
+                                   pc->lev_lo.begin() + inf.row_off + inf.n, level_lower);
+        if (level_upper) std::copy(pc->lev_up.begin() + inf.row_off,
+                                   pc->lev_up.begin() + inf.row_off + inf.n, level_upper);
+        if (lu_vals) {
+            use_device(pc->ctx);
+            precond_read_factors(pc, s, lu_vals);
+        }
+    });
+}
+
+sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && nc, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        SG_CHECK_ARG(pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS,
+                     "not a two-level preconditioner");
+        *nc = pc->nc;
+        if (a0) {
+            SG_CHECK_ARG(cap >= pc->nc * pc->nc, "cap too small");
+            use_device(pc->ctx);
+            precond_read_coarse(pc, a0);
+        }
+    });
+}
+
+// ------------------------------------------------------------------ solve
+sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* pc,
+                   const double* b, double* x, int n, sg_mem mem, const sg_solve_params* params,
+                   sg_solve_result* result) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && A && b && x, "NULL argument");
+        SG_CHECK_ARG(A->ctx == ctx, "matrix belongs to a different context");
+        SG_CHECK_ARG(A->nrows == A->ncols, "the solvers need a square matrix");
+        SG_CHECK_ARG(n == A->nrows, "n (%d) != matrix rows (%d)", n, A->nrows);
+        SG_CHECK_ARG(solver == SG_GMRES || solver == SG_FGMRES, "unknown solver %d", (int)solver);
+        if (pc) {
+            SG_CHECK_ARG(pc->ctx == ctx, "preconditioner belongs to a different context");
+            if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+            SG_CHECK_ARG(pc->n == n, "preconditioner was set up for n=%d", pc->n);
+        }
+        sg_solve_params prm{};
+        if (params) prm = *params;
+        else {
+            prm.restart = 30;
+            prm.max_iter = 1000;
+            prm.tol = 1e-10;
+            prm.tol_kind = SG_TOL_REF_ABS;
+            prm.precision = SG_FP64;
+            prm.use_graph = 1;
+        }
+        use_device(ctx);
+        if (!ctx->work) ctx->work = new SolveWork();
+        SolveWork* w = ctx->work;
+        const double* db = b;
+        double* dx = x;
+        if (mem == SG_MEM_HOST) {
+            w->b64.upload(b, n, ctx->stream);
+            w->x64.upload(x, n, ctx->stream);
+            db = w->b64.p;
+            dx = w->x64.p;
+        }
+        struct CopyBack {
+            sg_ctx* ctx;
+            double* host;
+            const double* dev;
+            int n;
+            bool on;
+            ~CopyBack() {
+                if (on) {
+                    cudaMemcpyAsync(host, dev, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+                    cudaStreamSynchronize(ctx->stream);
+                }
+            }
+        } cb{ctx, x, dx, n, mem == SG_MEM_HOST};
+        solve_device(ctx, solver, A, pc, db, dx, prm, result);
+    });
+}
+
+// ------------------------------------------------------------------ generators
+sg_status sg_gen_poisson2d(int nx, int ny, int* row_ptr, int* col_idx, double* vals, int* nnz) {
+    return guard([&] {
+        SG_CHECK_ARG(nx > 0 && ny > 0 && nnz, "bad arguments");
+        SG_CHECK_ARG((long long)nx * ny * 5 < (1ll << 31), "grid too large for int32 CSR");
+        *nnz = gen_poisson2d(nx, ny, row_ptr, row_ptr ? col_idx : nullptr, vals);
+    });
+}
+
+sg_status sg_gen_poisson3d(int nx, int ny, int nz, int* row_ptr, int* col_idx, double* vals,
+                           int* nnz) {
+    return guard([&] {
+        SG_CHECK_ARG(nx > 0 && ny > 0 && nz > 0 && nnz, "bad arguments");
+        SG_CHECK_ARG((long long)nx * ny * nz * 7 < (1ll << 31), "grid too large for int32 CSR");
+        *nnz = gen_poisson3d(nx, ny, nz, row_ptr, row_ptr ? col_idx : nullptr, vals);
+    });
+}
+
+sg_status sg_gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr_len, uint64_t seed,
+                           int* row_ptr, int* col_idx, double* vals, int* nnz) {
+    return guard([&] {
+        SG_CHECK_ARG(nx > 0 && ny > 0 && nz > 0 && nnz, "bad arguments");
+        SG_CHECK_ARG(corr_len > 0.0 && sigma >= 0.0, "bad field parameters");
+        SG_CHECK_ARG((long long)nx * ny * nz * 7 < (1ll << 31), "grid too large for int32 CSR");
+        *nnz = gen_varcoef3d(nx, ny, nz, sigma, corr_len, seed, row_ptr, col_idx, vals);
+    });
+}
+
+sg_status sg_gen_uniform(uint64_t seed, int n, double lo, double hi, double* out) {
+    return guard([&] {
+        SG_CHECK_ARG(n >= 0 && (n == 0 || out), "bad arguments");
+        gen_uniform(seed, n, lo, hi, out);
+    });
+}
+
+sg_status sg_partition_graph(int n, const int* row_ptr, const int* col_idx, int nparts,
+                             int* part) {
+    return guard([&] {
+        SG_CHECK_ARG(row_ptr && part && (n == 0 || col_idx), "NULL argument");
+        partition_graph(n, row_ptr, col_idx, nparts, part);
+    });
+}
+
+sg_status sg_partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed,
+                             int* part) {
+    return guard([&] {
+        SG_CHECK_ARG(part, "NULL argument");
+        partition_boxes(nx, ny, nz, nparts, spread, seed, part);
+    });
+}
+
+sg_status sg_schwarz_structure(int n, const int* row_ptr, const int* col_idx, const int* part,
+                               int nparts, int overlap, int which, int* out, int cap, int* len) {
+    return guard([&] {
+        SG_CHECK_ARG(n >= 0 && row_ptr && part && len, "NULL argument");
+        sg_csr A;
+        A.nrows = A.ncols = n;
+        A.nnz = row_ptr[n];
+        A.h_rp.assign(row_ptr, row_ptr + n + 1);
+        A.h_ci.assign(col_idx, col_idx + A.nnz);
+        for (int i = 0; i < n; ++i) {
+            SG_CHECK_ARG(row_ptr[i + 1] >= row_ptr[i], "row_ptr decreases at row %d", i);
+            for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+                SG_CHECK_ARG(col_idx[e] >= 0 && col_idx[e] < n, "col_idx out of range");
+                if (e > row_ptr[i] && col_idx[e] < col_idx[e - 1]) A.sorted = false;
+            }
+        }
+        sg_precond pc;
+        pc.opts.sweep_dtype = SG_FP64;
+        build_schwarz_host(&pc, &A, part, nparts, overlap);
+        std::vector<int> lrp_abs;
+        const std::vector<int>* v = nullptr;
+        switch (which) {
+        case 0: v = &pc.part; break;
+        case 1: v = &pc.owned_ptr; break;
+        case 2: v = &pc.owned; break;
+        case 3: v = &pc.sub_ptr; break;
+        case 4: v = &pc.sub; break;
+        case 5: v = &pc.ownloc_ptr; break;
+        case 6: v = &pc.ownloc; break;
+        case 7: v = &pc.lrp; break;
+        case 8: v = &pc.lci; break;
+        case 9: v = &pc.ldiag; break;
+        case 10: v = &pc.lev_lo; break;
+        case 11: v = &pc.lev_up; break;
+        default: fail(SG_ERR_INVALID_ARG, "unknown structure array %d", which);
+        }
+        *len = (int)v->size();
+        if (out) {
+            SG_CHECK_ARG(cap >= (int)v->size(), "cap %d < length %d", cap, (int)v->size());
+            std::copy(v->begin(), v->end(), out);
+        }
+    });
+}
+
+}  // extern "C"

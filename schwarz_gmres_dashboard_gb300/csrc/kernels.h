@@ -1,0 +1,51 @@
+// kernels.h -- host-side launchers of the CUDA kernels of libsgmres.
+#pragma once
+
+#include "sg_internal.h"
+
+namespace sg {
+
+// ---------------------------------------------------------------- spmv.cu
+// y = scale * (A x) (scale may be null = 1).  `exact` (FP64 only) keeps the
+// reference's product/sum rounding and order.  `active`: when non-null and
+// *active == 0 the kernel does nothing (finished solve inside a graph).
+template <class TV, class TX, class TY>
+void launch_spmv(sg_ctx* ctx, int n, const int* rp, const int* ci, const TV* val, const TX* x,
+                 TY* y, const double* scale, const int* active);
+// r = b - A x in FP64 with ||r||; the last block updates the solve state
+// (rnorm, true-residual convergence test).
+void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double* x, double* r,
+                     SolveState* st);
+// ||v|| of a FP64 vector into st->bnorm (solve start); flags non-finite input.
+void launch_bnorm(sg_ctx* ctx, const double* v, int n, SolveState* st);
+
+// ---------------------------------------------------------------- krylov.cu
+// Cycle start: beta = ||raw0||, g = beta e1, vscale[0] = 1/beta, reference
+// stopping test on beta.
+template <class TV>
+void launch_cycle_init(sg_ctx* ctx, const TV* raw0, int n, SolveState* st, int m, bool flexible);
+// One CGS2 Arnoldi step on raw[j+1] against raw[0..j] (with the Givens
+// update of the least-squares problem done by the last block).
+template <class TV>
+void launch_cgs2(sg_ctx* ctx, TV* raw, size_t ldv, int n, int j, int m, SolveState* st,
+                 bool flexible);
+// y = H^{-1} g (k x k upper triangle) by one thread.
+void launch_backsolve(sg_ctx* ctx, SolveState* st, int m);
+// x += sum_k y_k * vscale_k * basis_k  (k < st->kcount)
+template <class TV>
+void launch_update_x(sg_ctx* ctx, const TV* basis, size_t ldv, int n, double* x, SolveState* st);
+// y = x with type conversion (no preconditioner)
+template <class TI, class TO>
+void launch_copy(sg_ctx* ctx, const TI* x, TO* y, int n, const int* active);
+// cycle bookkeeping after the update: cycles++, out-of-iterations test
+void launch_cycle_end(sg_ctx* ctx, SolveState* st);
+
+// ---------------------------------------------------------------- schwarz.cu
+void precond_setup_device(sg_precond* pc, const sg_csr* A);
+template <class TI, class TO>
+void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active);
+// copy the FP64 factors of subdomain s back to the host
+void precond_read_factors(sg_precond* pc, int s, double* lu_out);
+void precond_read_coarse(sg_precond* pc, double* a0_out);
+
+}  // namespace sg

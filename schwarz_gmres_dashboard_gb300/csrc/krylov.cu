@@ -1,0 +1,459 @@
+// krylov.cu -- Arnoldi / least-squares kernels of restarted GMRES(m) and
+// FGMRES (src/core/gmres.cpp:34-160, src/core/fgmres.cpp:28-144; replaces the
+// host-driven cuBLAS loop of src/gpu/gmres_gpu.cu:10-138).
+//
+// Basis storage: raw_k (k <= m) are the columns of a (m+1) x ldv array; the
+// orthonormal vector is v_k = vscale[k] * raw_k, so a new vector never needs
+// a separate normalisation pass.
+//
+// One Arnoldi step orthogonalises w = raw_{j+1} against raw_0..raw_j by
+// classical Gram-Schmidt applied twice (CGS2), in three streaming passes:
+//   A  h1 = V^T w                          (dot products, one pass)
+//   B  w' = w - V h1 ; h2 = V^T w'          (update and second dots, one pass)
+//   C  w'' = w' - V h2 ; ||w''||           (update and norm, one pass)
+// Every pass reduces per block, and the last block to finish sums the block
+// partials in block order; after pass C it also writes the Hessenberg column,
+// applies the Givens rotations (same formulas as src/core/gmres.cpp:9-30)
+// and tests convergence, so no value travels to the host inside a cycle.
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+namespace {
+
+constexpr int KT = 256;  // threads of the Krylov kernels
+
+// Givens rotation of src/core/gmres.cpp:9-30
+__device__ void rot_compute(double& c, double& s, double a, double b) {
+    if (fabs(b) < 1e-30) {
+        c = 1.0;
+        s = 0.0;
+    } else if (fabs(b) > fabs(a)) {
+        const double t = -a / b;
+        s = 1.0 / sqrt(1.0 + t * t);
+        c = s * t;
+    } else {
+        const double t = -b / a;
+        c = 1.0 / sqrt(1.0 + t * t);
+        s = c * t;
+    }
+}
+__device__ void rot_apply(double c, double s, double& h1, double& h2) {
+    const double t1 = c * h1 - s * h2;
+    const double t2 = s * h1 + c * h2;
+    h1 = t1;
+    h2 = t2;
+}
+
+// Completes Arnoldi step j once ||w''||^2 is known (thread 0 of the last block).
+__device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double* hist,
+                                 int hist_cap) {
+    const int ld = m + 1;
+    const double nrm = sqrt(ss);
+    double* Hc = st->H + (size_t)j * ld;
+    for (int i = 0; i <= j; ++i) Hc[i] = st->hsum[i];
+    Hc[j + 1] = nrm;
+    if (!(nrm >= 1e-30)) {
+        // breakdown (src/core/gmres.cpp:297-300): this column is used as is
+        if (!isfinite(nrm)) {
+            st->nonfinite = 1;
+            st->done = 1;
+        }
+        st->breakdown = 1;
+        st->kcount = j + 1;
+        st->cycle_active = 0;
+        return;
+    }
+    st->vscale[j + 1] = 1.0 / nrm;
+    for (int i = 0; i < j; ++i) rot_apply(st->cs[i], st->sn[i], Hc[i], Hc[i + 1]);
+    rot_compute(st->cs[j], st->sn[j], Hc[j], Hc[j + 1]);
+    rot_apply(st->cs[j], st->sn[j], Hc[j], Hc[j + 1]);
+    rot_apply(st->cs[j], st->sn[j], st->g[j], st->g[j + 1]);
+    const double res = fabs(st->g[j + 1]);
+    if (hist && st->hist_len < hist_cap) hist[st->hist_len] = res;
+    st->hist_len++;
+    st->last_res = res;
+    st->total_iter++;
+    st->kcount = j + 1;
+    st->j = j + 1;
+    bool stop = false;
+    if (st->tol_kind == SG_TOL_REF_ABS) {
+        if (res < st->tol) {
+            st->converged = 1;
+            st->done = 1;
+            stop = true;
+        }
+    } else if (st->tol_kind == SG_TOL_TRUE_REL) {
+        // estimated true residual; the restart verifies it in FP64
+        if (res * st->est_scale <= 0.5 * st->tol * st->bnorm) stop = true;
+    }
+    if (!isfinite(res)) {
+        st->nonfinite = 1;
+        st->done = 1;
+        stop = true;
+    }
+    if (j + 1 >= m) stop = true;
+    if (stop) st->cycle_active = 0;
+}
+
+template <class T>
+struct Vec;
+template <>
+struct Vec<double> {
+    static constexpr int N = 2;
+    using V = double2;
+};
+template <>
+struct Vec<float> {
+    static constexpr int N = 4;
+    using V = float4;
+};
+
+template <class T>
+__device__ __forceinline__ void vload(const T* p, T (&o)[Vec<T>::N]);
+template <>
+__device__ __forceinline__ void vload<double>(const double* p, double (&o)[2]) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    o[0] = v.x; o[1] = v.y;
+}
+template <>
+__device__ __forceinline__ void vload<float>(const float* p, float (&o)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+template <class T>
+__device__ __forceinline__ void vstore(T* p, const T (&o)[Vec<T>::N]);
+template <>
+__device__ __forceinline__ void vstore<double>(double* p, const double (&o)[2]) {
+    *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
+}
+template <>
+__device__ __forceinline__ void vstore<float>(float* p, const float (&o)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// ---- pass A (and generic second dots): s_k = raw_{k0+k} . w for k < kc
+template <class TV, int KMAX>
+__global__ void __launch_bounds__(KT)
+k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* __restrict__ w,
+       SolveState* st, int second, double* partials, unsigned* counter) {
+    if (!st->cycle_active) return;
+    constexpr int VN = Vec<TV>::N;
+    TV acc[KMAX];
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) acc[k] = (TV)0;
+    const int nvec = n / VN;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nvec; q += gridDim.x * blockDim.x) {
+        TV wv[VN];
+        vload<TV>(w + (size_t)q * VN, wv);
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k) {
+            if (k < kc) {
+                TV vv[VN];
+                vload<TV>(raw + (size_t)(k0 + k) * ldv + (size_t)q * VN, vv);
+#pragma unroll
+                for (int e = 0; e < VN; ++e) acc[k] += vv[e] * wv[e];
+            }
+        }
+    }
+    for (int i = nvec * VN + blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const TV wi = w[i];
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k)
+            if (k < kc) acc[k] += raw[(size_t)(k0 + k) * ldv + i] * wi;
+    }
+    __shared__ double red[(KT / 32) * KMAX];
+    __shared__ double bs[KMAX], tot[KMAX];
+    block_sum_multi<KMAX>(acc, kc, red, bs);
+    if (last_block_reduce(partials, counter, bs, kc, tot)) {
+        for (int k = threadIdx.x; k < kc; k += blockDim.x) {
+            const double h = st->vscale[k0 + k] * tot[k];
+            st->h[k0 + k] = h;
+            st->hsum[k0 + k] = second ? st->hsum[k0 + k] + h : h;
+        }
+    }
+}
+
+// ---- pass B fused: w' = w - sum c_k raw_k ; s2_k = raw_k . w'   (nk <= KMAX)
+template <class TV, int KMAX>
+__global__ void __launch_bounds__(KT)
+k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict__ w,
+           SolveState* st, double* partials, unsigned* counter) {
+    if (!st->cycle_active) return;
+    __shared__ TV cf[KMAX];
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
+    __syncthreads();
+    TV acc[KMAX];
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) acc[k] = (TV)0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        TV v[KMAX];
+        TV wi = w[i];
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k)
+            if (k < nk) v[k] = raw[(size_t)k * ldv + i];
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k)
+            if (k < nk) wi -= cf[k] * v[k];
+        w[i] = wi;
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k)
+            if (k < nk) acc[k] += v[k] * wi;
+    }
+    __shared__ double red[(KT / 32) * KMAX];
+    __shared__ double bs[KMAX], tot[KMAX];
+    block_sum_multi<KMAX>(acc, nk, red, bs);
+    if (last_block_reduce(partials, counter, bs, nk, tot)) {
+        for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+            const double h = st->vscale[k] * tot[k];
+            st->h[k] = h;
+            st->hsum[k] += h;
+        }
+    }
+}
+
+// ---- generic update: w -= sum_k c_k raw_k (any nk)
+template <class TV>
+__global__ void __launch_bounds__(KT)
+k_upd(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict__ w,
+      SolveState* st) {
+    if (!st->cycle_active) return;
+    __shared__ TV cf[SG_MMAX + 1];
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        TV wi = w[i];
+        for (int k = 0; k < nk; ++k) wi -= cf[k] * raw[(size_t)k * ldv + i];
+        w[i] = wi;
+    }
+}
+
+// ---- pass C: w'' = w' - sum c_k raw_k ; ||w''||^2 -> Arnoldi finalize
+template <class TV>
+__global__ void __launch_bounds__(KT)
+k_upd_norm(const TV* __restrict__ raw, size_t ldv, int n, int j, int m, TV* __restrict__ w,
+           SolveState* st, double* partials, unsigned* counter, double* hist, int hist_cap) {
+    if (!st->cycle_active) return;
+    const int nk = j + 1;
+    __shared__ TV cf[SG_MMAX + 1];
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
+    __syncthreads();
+    double ss = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        TV wi = w[i];
+        for (int k = 0; k < nk; ++k) wi -= cf[k] * raw[(size_t)k * ldv + i];
+        w[i] = wi;
+        ss += (double)wi * (double)wi;
+    }
+    __shared__ double red[KT / 32];
+    __shared__ double bs[1], tot[1];
+    double v1[1] = {ss};
+    block_sum_multi<1>(v1, 1, red, bs);
+    if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0)
+        arnoldi_finalize(st, j, m, tot[0], hist, hist_cap);
+}
+
+// ---- cycle start: beta = ||raw0||
+template <class TV>
+__global__ void __launch_bounds__(KT)
+k_cycle_init(const TV* __restrict__ raw0, int n, SolveState* st, int m, int flexible,
+             double* partials, unsigned* counter) {
+    if (st->done) return;
+    double ss = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double t = (double)raw0[i];
+        ss += t * t;
+    }
+    __shared__ double red[KT / 32];
+    __shared__ double bs[1], tot[1];
+    double v1[1] = {ss};
+    block_sum_multi<1>(v1, 1, red, bs);
+    if (!last_block_reduce(partials, counter, bs, 1, tot)) return;
+    const int ld = m + 1;
+    for (int i = threadIdx.x; i < ld * m; i += blockDim.x) st->H[i] = 0.0;
+    for (int i = threadIdx.x; i <= m; i += blockDim.x) st->g[i] = 0.0;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double beta = sqrt(tot[0]);
+    st->beta = beta;
+    st->j = 0;
+    st->kcount = 0;
+    st->breakdown = 0;
+    if (!isfinite(beta)) {
+        st->nonfinite = 1;
+        st->done = 1;
+        st->cycle_active = 0;
+        return;
+    }
+    if (st->tol_kind == SG_TOL_REF_ABS && beta < st->tol) {
+        // src/core/gmres.cpp:264-269
+        st->converged = 1;
+        st->done = 1;
+        st->cycle_active = 0;
+        return;
+    }
+    if (!(beta > 0.0)) {
+        st->done = 1;
+        st->cycle_active = 0;
+        return;
+    }
+    st->vscale[0] = 1.0 / beta;
+    st->g[0] = beta;
+    st->est_scale = flexible ? 1.0 : st->rnorm / beta;
+    st->cycle_active = 1;
+}
+
+__global__ void k_backsolve(SolveState* st, int m) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int k = st->kcount;
+    const int ld = m + 1;
+    // src/core/gmres.cpp:131-137
+    for (int i = k - 1; i >= 0; --i) {
+        double yi = st->g[i];
+        for (int l = i + 1; l < k; ++l) yi -= st->H[i + l * ld] * st->y[l];
+        st->y[i] = yi / st->H[i + i * ld];
+    }
+}
+
+template <class TV>
+__global__ void __launch_bounds__(KT)
+k_update_x(const TV* __restrict__ basis, size_t ldv, int n, double* __restrict__ x,
+           SolveState* st) {
+    const int k = st->kcount;
+    if (k <= 0) return;
+    __shared__ double cf[SG_MMAX];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) cf[i] = st->y[i] * st->vscale[i];
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double xi = x[i];
+        for (int q = 0; q < k; ++q) xi += cf[q] * (double)basis[(size_t)q * ldv + i];
+        x[i] = xi;
+    }
+}
+
+template <class TI, class TO>
+__global__ void k_copy(const TI* __restrict__ x, TO* __restrict__ y, int n,
+                       const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = (TO)x[i];
+}
+
+__global__ void k_cycle_end(SolveState* st) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    st->cycles++;
+    st->cycle_active = 0;
+    if (!st->done && st->total_iter >= st->max_iter) st->done = 1;
+}
+
+int kgrid(sg_ctx* ctx, int n, int per_sm) {
+    long long need = ((long long)n + KT - 1) / KT;
+    long long cap = (long long)ctx->num_sms * per_sm;
+    if (need > cap) need = cap;
+    return need < 1 ? 1 : (int)need;
+}
+
+}  // namespace
+
+template <class TV>
+void launch_cycle_init(sg_ctx* ctx, const TV* raw0, int n, SolveState* st, int m, bool flexible) {
+    k_cycle_init<TV><<<kgrid(ctx, n, 2), KT, 0, ctx->stream>>>(raw0, n, st, m, flexible ? 1 : 0,
+                                                               ctx->partials.p, ctx->counter.p);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template <class TV, int KMAX>
+static void dots_launch(sg_ctx* ctx, const TV* raw, size_t ldv, int n, int k0, int kc,
+                        const TV* w, SolveState* st, int second) {
+    k_dots<TV, KMAX><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(raw, ldv, n, k0, kc, w, st, second,
+                                                                ctx->partials.p, ctx->counter.p);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template <class TV>
+static void dots_any(sg_ctx* ctx, const TV* raw, size_t ldv, int n, int nk, const TV* w,
+                     SolveState* st, int second) {
+    for (int k0 = 0; k0 < nk; k0 += 32) {
+        const int kc = nk - k0 < 32 ? nk - k0 : 32;
+        if (kc <= 8) dots_launch<TV, 8>(ctx, raw, ldv, n, k0, kc, w, st, second);
+        else if (kc <= 16) dots_launch<TV, 16>(ctx, raw, ldv, n, k0, kc, w, st, second);
+        else dots_launch<TV, 32>(ctx, raw, ldv, n, k0, kc, w, st, second);
+    }
+}
+
+template <class TV>
+void launch_cgs2(sg_ctx* ctx, TV* raw, size_t ldv, int n, int j, int m, SolveState* st,
+                 bool flexible) {
+    (void)flexible;
+    const int nk = j + 1;
+    TV* w = raw + (size_t)(j + 1) * ldv;
+    // pass A
+    dots_any<TV>(ctx, raw, ldv, n, nk, w, st, 0);
+    // pass B
+    const int gB = kgrid(ctx, n, 2);
+    if (nk <= 8) {
+        k_upd_dots<TV, 8><<<gB, KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st, ctx->partials.p,
+                                                      ctx->counter.p);
+    } else if (nk <= 16) {
+        k_upd_dots<TV, 16><<<gB, KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st, ctx->partials.p,
+                                                       ctx->counter.p);
+    } else if (nk <= 32) {
+        k_upd_dots<TV, 32><<<gB, KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st, ctx->partials.p,
+                                                       ctx->counter.p);
+    } else {
+        k_upd<TV><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        dots_any<TV>(ctx, raw, ldv, n, nk, w, st, 1);
+    }
+    SG_CUDA(cudaGetLastError());
+    if (nk <= 32) count_launch(ctx);
+    // pass C
+    k_upd_norm<TV><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(
+        raw, ldv, n, j, m, w, st, ctx->partials.p, ctx->counter.p, ctx->hist_d, ctx->hist_cap);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+void launch_backsolve(sg_ctx* ctx, SolveState* st, int m) {
+    k_backsolve<<<1, 32, 0, ctx->stream>>>(st, m);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template <class TV>
+void launch_update_x(sg_ctx* ctx, const TV* basis, size_t ldv, int n, double* x, SolveState* st) {
+    k_update_x<TV><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(basis, ldv, n, x, st);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template <class TI, class TO>
+void launch_copy(sg_ctx* ctx, const TI* x, TO* y, int n, const int* active) {
+    k_copy<TI, TO><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(x, y, n, active);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+void launch_cycle_end(sg_ctx* ctx, SolveState* st) {
+    k_cycle_end<<<1, 32, 0, ctx->stream>>>(st);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template void launch_cycle_init<double>(sg_ctx*, const double*, int, SolveState*, int, bool);
+template void launch_cycle_init<float>(sg_ctx*, const float*, int, SolveState*, int, bool);
+template void launch_cgs2<double>(sg_ctx*, double*, size_t, int, int, int, SolveState*, bool);
+template void launch_cgs2<float>(sg_ctx*, float*, size_t, int, int, int, SolveState*, bool);
+template void launch_update_x<double>(sg_ctx*, const double*, size_t, int, double*, SolveState*);
+template void launch_update_x<float>(sg_ctx*, const float*, size_t, int, double*, SolveState*);
+template void launch_copy<double, double>(sg_ctx*, const double*, double*, int, const int*);
+template void launch_copy<double, float>(sg_ctx*, const double*, float*, int, const int*);
+template void launch_copy<float, float>(sg_ctx*, const float*, float*, int, const int*);
+template void launch_copy<float, double>(sg_ctx*, const float*, double*, int, const int*);
+
+}  // namespace sg

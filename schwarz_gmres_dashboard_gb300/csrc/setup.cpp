@@ -1,0 +1,491 @@
+// setup.cpp -- host-side integer set-up of the Schwarz preconditioners:
+// decomposition (src/decomp/domain_decomp.h:61-93), owned-local map
+// (src/precond/ras.h:34-41), local CSR structure of A[dofs,dofs]
+// (src/core/sparse_matrix.h:53-83), ILU(0) diagonal positions
+// (src/precond/ilu0.h:19-29) and the level schedules of the two sweeps.
+// All of it is integer work; the floating-point set-up (value gather,
+// factorisation, coarse operator) runs on the device (schwarz.cu).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "sg_internal.h"
+
+namespace sg {
+
+// Level of every row of one local CSR for the forward sweep (reads columns
+// before the first column >= row, src/precond/ilu0.h:62-67) and for the
+// backward sweep (reads the entries after the diagonal, :70-76).
+static int levels_lower(int n, const int* rp, const int* ci, int* lev) {
+    int nlev = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int e = rp[i]; e < rp[i + 1]; ++e) {
+            const int c = ci[e];
+            if (c >= i) break;
+            l = std::max(l, lev[c] + 1);
+        }
+        lev[i] = l;
+        nlev = std::max(nlev, l + 1);
+    }
+    return nlev;
+}
+
+static int levels_upper(int n, const int* rp, const int* ci, const int* dg, int* lev) {
+    int nlev = 0;
+    for (int i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int e = dg[i] + 1; e < rp[i + 1]; ++e) l = std::max(l, lev[ci[e]] + 1);
+        lev[i] = l;
+        nlev = std::max(nlev, l + 1);
+    }
+    return nlev;
+}
+
+// rows sorted by level (stable): perm[p] = row, ptr[l] = first position of level l
+static void level_order(int n, const int* lev, int nlev, std::vector<int>& perm,
+                        std::vector<int>& ptr) {
+    ptr.assign(nlev + 1, 0);
+    for (int i = 0; i < n; ++i) ptr[lev[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    perm.resize(n);
+    for (int i = 0; i < n; ++i) perm[fill[lev[i]]++] = i;
+}
+
+void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int nparts,
+                        int overlap) {
+    const int n = A->nrows;
+    const int* rp = A->h_rp.data();
+    const int* ci = A->h_ci.data();
+    SG_CHECK_ARG(nparts >= 1, "nparts must be >= 1 (got %d)", nparts);
+    SG_CHECK_ARG(overlap >= 0, "overlap must be >= 0 (got %d)", overlap);
+    SG_CHECK_ARG(A->nrows == A->ncols, "Schwarz/ILU preconditioners need a square matrix");
+    SG_CHECK_ARG(A->sorted, "ILU(0) needs column indices sorted within each row");
+    pc->nparts = nparts;
+    pc->part.assign(part_in, part_in + n);
+    for (int i = 0; i < n; ++i)
+        SG_CHECK_ARG(pc->part[i] >= 0 && pc->part[i] < nparts,
+                     "partition[%d] = %d is outside [0,%d)", i, pc->part[i], nparts);
+
+    // owned_dofs[s], ascending (src/decomp/domain_decomp.h:64-66)
+    pc->owned_ptr.assign(nparts + 1, 0);
+    for (int i = 0; i < n; ++i) pc->owned_ptr[pc->part[i] + 1]++;
+    for (int s = 0; s < nparts; ++s) pc->owned_ptr[s + 1] += pc->owned_ptr[s];
+    pc->owned.resize(n);
+    {
+        std::vector<int> fill(pc->owned_ptr.begin(), pc->owned_ptr.end() - 1);
+        for (int i = 0; i < n; ++i) pc->owned[fill[pc->part[i]]++] = i;
+    }
+    for (int s = 0; s < nparts; ++s)
+        if (pc->owned_ptr[s + 1] == pc->owned_ptr[s])
+            fail(SG_ERR_INVALID_ARG, "subdomain %d owns no rows", s);
+
+    // overlap: vertices within `overlap` hops of the owned set, sorted
+    // (src/decomp/domain_decomp.h:68-90); owned-local map (ras.h:34-41)
+    pc->sub_ptr.assign(nparts + 1, 0);
+    pc->sub.clear();
+    pc->ownloc_ptr.assign(nparts + 1, 0);
+    pc->ownloc.clear();
+    std::vector<unsigned char> mark(n, 0);
+    std::vector<int> set;
+    set.reserve(1024);
+    for (int s = 0; s < nparts; ++s) {
+        set.assign(pc->owned.begin() + pc->owned_ptr[s], pc->owned.begin() + pc->owned_ptr[s + 1]);
+        for (int v : set) mark[v] = 1;
+        size_t lo = 0;
+        for (int layer = 0; layer < overlap; ++layer) {
+            const size_t hi = set.size();
+            for (size_t q = lo; q < hi; ++q) {
+                const int r = set[q];
+                for (int e = rp[r]; e < rp[r + 1]; ++e) {
+                    const int c = ci[e];
+                    if (!mark[c]) {
+                        mark[c] = 1;
+                        set.push_back(c);
+                    }
+                }
+            }
+            lo = hi;
+        }
+        std::sort(set.begin(), set.end());
+        for (size_t q = 0; q < set.size(); ++q) {
+            mark[set[q]] = 0;
+            if (pc->part[set[q]] == s) pc->ownloc.push_back((int)q);
+        }
+        pc->sub.insert(pc->sub.end(), set.begin(), set.end());
+        pc->sub_ptr[s + 1] = (int)pc->sub.size();
+        pc->ownloc_ptr[s + 1] = (int)pc->ownloc.size();
+    }
+
+    // local CSR A[dofs,dofs] in row order, entries in original order
+    // (src/core/sparse_matrix.h:53-83), plus the global entry of each local one
+    pc->lrp.clear();
+    pc->lci.clear();
+    pc->lmap.clear();
+    pc->ldiag.assign(pc->sub.size(), -1);
+    pc->lev_lo.assign(pc->sub.size(), 0);
+    pc->lev_up.assign(pc->sub.size(), 0);
+    pc->h_info.assign(nparts, SubInfo{});
+    pc->h_lev_ptr_f.clear();
+    pc->h_lev_ptr_b.clear();
+    std::vector<int> perm_f_all(pc->sub.size()), perm_b_all(pc->sub.size());
+    std::vector<int> loc(n, -1);
+    long long fl_total = 0, fu_total = 0;
+    int max_n = 0;
+    std::vector<int> perm, ptr;
+    for (int s = 0; s < nparts; ++s) {
+        const int off = pc->sub_ptr[s];
+        const int ns = pc->sub_ptr[s + 1] - off;
+        const int* dofs = pc->sub.data() + off;
+        for (int li = 0; li < ns; ++li) loc[dofs[li]] = li;
+        SubInfo inf{};
+        inf.n = ns;
+        inf.row_off = off;
+        inf.csr_row_off = (int)pc->lrp.size();
+        inf.csr_nz_off = (long long)pc->lci.size();
+        const size_t rbase = pc->lrp.size();
+        const long long zbase = (long long)pc->lci.size();
+        for (int li = 0; li < ns; ++li) {
+            const int gi = dofs[li];
+            pc->lrp.push_back((int)((long long)pc->lci.size() - zbase));
+            for (int e = rp[gi]; e < rp[gi + 1]; ++e) {
+                const int lj = loc[ci[e]];
+                if (lj >= 0) {
+                    if (lj == li && pc->ldiag[off + li] < 0)
+                        pc->ldiag[off + li] = (int)((long long)pc->lci.size() - zbase);
+                    pc->lci.push_back(lj);
+                    pc->lmap.push_back(e);
+                }
+            }
+        }
+        pc->lrp.push_back((int)((long long)pc->lci.size() - zbase));
+        for (int li = 0; li < ns; ++li) loc[dofs[li]] = -1;
+        const int* lrp = pc->lrp.data() + rbase;
+        const int* lci = pc->lci.data() + zbase;
+        for (int li = 0; li < ns; ++li)
+            if (pc->ldiag[off + li] < 0)
+                fail(SG_ERR_SINGULAR, "ILU(0): row %d has no diagonal entry", dofs[li]);
+        // widths
+        int wl = 0, wu = 0;
+        for (int li = 0; li < ns; ++li) {
+            int cl = 0;
+            for (int e = lrp[li]; e < lrp[li + 1] && lci[e] < li; ++e) ++cl;
+            wl = std::max(wl, cl);
+            wu = std::max(wu, lrp[li + 1] - (pc->ldiag[off + li] + 1));
+        }
+        inf.wl = wl;
+        inf.wu = wu;
+        // level schedules
+        int* lo = pc->lev_lo.data() + off;
+        int* up = pc->lev_up.data() + off;
+        const int nlf = levels_lower(ns, lrp, lci, lo);
+        const int nlb = levels_upper(ns, lrp, lci, pc->ldiag.data() + off, up);
+        inf.nlev_f = nlf;
+        inf.lev_off_f = (int)pc->h_lev_ptr_f.size();
+        level_order(ns, lo, nlf, perm, ptr);
+        std::copy(perm.begin(), perm.end(), perm_f_all.begin() + off);
+        pc->h_lev_ptr_f.insert(pc->h_lev_ptr_f.end(), ptr.begin(), ptr.end());
+        inf.nlev_b = nlb;
+        inf.lev_off_b = (int)pc->h_lev_ptr_b.size();
+        level_order(ns, up, nlb, perm, ptr);
+        std::copy(perm.begin(), perm.end(), perm_b_all.begin() + off);
+        pc->h_lev_ptr_b.insert(pc->h_lev_ptr_b.end(), ptr.begin(), ptr.end());
+        inf.fl_off = fl_total;
+        inf.fu_off = fu_total;
+        fl_total += (long long)wl * ns;
+        fu_total += (long long)wu * ns;
+        inf.own_off = pc->ownloc_ptr[s];
+        inf.n_own = pc->ownloc_ptr[s + 1] - pc->ownloc_ptr[s];
+        inf.cscale = 1.0 / std::sqrt((double)(pc->owned_ptr[s + 1] - pc->owned_ptr[s]));
+        pc->h_info[s] = inf;
+        max_n = std::max(max_n, ns);
+    }
+    pc->fl_total = fl_total > 0 ? fl_total : 1;
+    pc->fu_total = fu_total > 0 ? fu_total : 1;
+    pc->max_n = max_n;
+    pc->total_rows = (long long)pc->sub.size();
+    pc->wide_cols = max_n > 65534;
+    if (pc->wide_cols) {
+        pc->h_perm_f32 = perm_f_all;
+        pc->h_perm_b32 = perm_b_all;
+    } else {
+        pc->h_perm_f16.assign(perm_f_all.begin(), perm_f_all.end());
+        pc->h_perm_b16.assign(perm_b_all.begin(), perm_b_all.end());
+    }
+    const size_t elt = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
+    pc->use_smem = (size_t)(max_n + 1) * elt <= 220u * 1024u;
+    pc->h_cscale.resize(nparts);
+    for (int s = 0; s < nparts; ++s) pc->h_cscale[s] = pc->h_info[s].cscale;
+    // launch order: largest subdomains first
+    pc->h_order.resize(nparts);
+    std::iota(pc->h_order.begin(), pc->h_order.end(), 0);
+    std::stable_sort(pc->h_order.begin(), pc->h_order.end(), [&](int a, int b) {
+        const long long ca = (long long)pc->h_info[a].n * (pc->h_info[a].nlev_f + pc->h_info[a].nlev_b);
+        const long long cb = (long long)pc->h_info[b].n * (pc->h_info[b].nlev_f + pc->h_info[b].nlev_b);
+        return ca > cb;
+    });
+}
+
+// ---------------------------------------------------------------- partitioners
+// Recursive bisection by breadth-first level structure: each group of
+// vertices is ordered by BFS from a pseudo-peripheral vertex (two sweeps,
+// ties by lowest index) and cut at the size proportional to the parts asked
+// of each half.  Deterministic; disconnected groups continue from their
+// lowest unvisited vertex.
+void partition_graph(int n, const int* rp, const int* ci, int nparts, int* part) {
+    SG_CHECK_ARG(n >= 0 && nparts >= 1, "bad partition arguments");
+    if (nparts == 1 || n == 0) {
+        std::fill(part, part + n, 0);
+        return;
+    }
+    SG_CHECK_ARG(nparts <= n, "nparts (%d) exceeds the number of rows (%d)", nparts, n);
+    std::vector<int> group(n, 0);  // group id of each vertex during recursion
+    std::vector<int> visit(n, -1);
+    int stamp = 0;
+    struct Task {
+        std::vector<int> verts;  // ascending
+        int k, base, gid;
+    };
+    std::vector<Task> stack;
+    std::vector<int> all(n);
+    std::iota(all.begin(), all.end(), 0);
+    stack.push_back({std::move(all), nparts, 0, 0});
+    int next_gid = 1;
+    std::vector<int> order, queue;
+    auto bfs = [&](const std::vector<int>& verts, int gid, int start, std::vector<int>& out) {
+        // BFS restricted to group gid; continues over components in index order
+        ++stamp;
+        out.clear();
+        size_t scan = 0;
+        int src = start;
+        while (true) {
+            if (visit[src] != stamp) {
+                visit[src] = stamp;
+                size_t head = out.size();
+                out.push_back(src);
+                while (head < out.size()) {
+                    const int v = out[head++];
+                    for (int e = rp[v]; e < rp[v + 1]; ++e) {
+                        const int c = ci[e];
+                        if (c >= 0 && c < n && group[c] == gid && visit[c] != stamp) {
+                            visit[c] = stamp;
+                            out.push_back(c);
+                        }
+                    }
+                }
+            }
+            while (scan < verts.size() && visit[verts[scan]] == stamp) ++scan;
+            if (scan >= verts.size()) break;
+            src = verts[scan];
+        }
+    };
+    while (!stack.empty()) {
+        Task t = std::move(stack.back());
+        stack.pop_back();
+        if (t.k == 1) {
+            for (int v : t.verts) part[v] = t.base;
+            continue;
+        }
+        const int k1 = t.k / 2, k2 = t.k - k1;
+        bfs(t.verts, t.gid, t.verts.front(), order);
+        bfs(t.verts, t.gid, order.back(), order);
+        const size_t cut = (size_t)((long long)t.verts.size() * k1 / t.k);
+        const int g1 = next_gid++, g2 = next_gid++;
+        std::vector<int> a(order.begin(), order.begin() + cut), b(order.begin() + cut, order.end());
+        for (int v : a) group[v] = g1;
+        for (int v : b) group[v] = g2;
+        std::sort(a.begin(), a.end());
+        std::sort(b.begin(), b.end());
+        stack.push_back({std::move(b), k2, t.base + k1, g2});
+        stack.push_back({std::move(a), k1, t.base, g1});
+    }
+}
+
+static inline uint64_t splitmix64(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static inline double u01(uint64_t& s) { return (double)(splitmix64(s) >> 11) * 0x1.0p-53; }
+
+// Recursive coordinate bisection of a grid into boxes with seeded uneven cuts.
+void partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed,
+                     int* part) {
+    SG_CHECK_ARG(nx > 0 && ny > 0 && nz > 0 && nparts >= 1, "bad box partition arguments");
+    SG_CHECK_ARG(spread >= 0.0 && spread < 0.5, "spread must be in [0,0.5)");
+    uint64_t rng = seed;
+    struct Box {
+        int x0, x1, y0, y1, z0, z1, k, base;
+    };
+    std::vector<Box> stack{{0, nx, 0, ny, 0, nz, nparts, 0}};
+    while (!stack.empty()) {
+        Box b = stack.back();
+        stack.pop_back();
+        if (b.k == 1) {
+            for (int z = b.z0; z < b.z1; ++z)
+                for (int y = b.y0; y < b.y1; ++y)
+                    for (int x = b.x0; x < b.x1; ++x) part[((size_t)z * ny + y) * nx + x] = b.base;
+            continue;
+        }
+        const int k1 = b.k / 2, k2 = b.k - k1;
+        const int ex = b.x1 - b.x0, ey = b.y1 - b.y0, ez = b.z1 - b.z0;
+        int axis = 0, len = ex;
+        if (ey > len) { axis = 1; len = ey; }
+        if (ez > len) { axis = 2; len = ez; }
+        SG_CHECK_ARG(len >= 2, "grid too small for %d parts", nparts);
+        const double f = (double)k1 / b.k * (1.0 + spread * (2.0 * u01(rng) - 1.0));
+        int cut = (int)std::lround(f * len);
+        cut = std::max(1, std::min(len - 1, cut));
+        Box a = b, c = b;
+        a.k = k1;
+        c.k = k2;
+        c.base = b.base + k1;
+        if (axis == 0) { a.x1 = b.x0 + cut; c.x0 = b.x0 + cut; }
+        else if (axis == 1) { a.y1 = b.y0 + cut; c.y0 = b.y0 + cut; }
+        else { a.z1 = b.z0 + cut; c.z0 = b.z0 + cut; }
+        stack.push_back(c);
+        stack.push_back(a);
+    }
+}
+
+// ---------------------------------------------------------------- generators
+// make_poisson_2d / make_poisson_3d (src/mesh/poisson.h:10-74)
+int gen_poisson2d(int nx, int ny, int* rp, int* ci, double* v) {
+    int nz = 0;
+    auto put = [&](int c, double val) {
+        if (ci) { ci[nz] = c; v[nz] = val; }
+        ++nz;
+    };
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) {
+            const int idx = iy * nx + ix;
+            if (rp) rp[idx] = nz;
+            if (iy > 0) put(idx - nx, -1.0);
+            if (ix > 0) put(idx - 1, -1.0);
+            put(idx, 4.0);
+            if (ix < nx - 1) put(idx + 1, -1.0);
+            if (iy < ny - 1) put(idx + nx, -1.0);
+        }
+    if (rp) rp[nx * ny] = nz;
+    return nz;
+}
+
+// 7-point operator with per-face coefficients; k == 1 gives make_poisson_3d
+static int gen_faces3d(int nx, int ny, int nz_, const double* kc, int* rp, int* ci, double* v) {
+    const int nxy = nx * ny;
+    int nz = 0;
+    auto put = [&](int c, double val) {
+        if (ci) { ci[nz] = c; v[nz] = val; }
+        ++nz;
+    };
+    auto face = [&](int a, int b) {
+        if (!kc) return 1.0;
+        return 2.0 * kc[a] * kc[b] / (kc[a] + kc[b]);
+    };
+    for (int iz = 0; iz < nz_; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix) {
+                const int idx = iz * nxy + iy * nx + ix;
+                if (rp) rp[idx] = nz;
+                const double kself = kc ? kc[idx] : 1.0;
+                double diag = 0.0;
+                // the six faces; a face on the boundary couples to the
+                // Dirichlet value 0 with the cell's own coefficient
+                const double fzm = iz > 0 ? face(idx, idx - nxy) : kself;
+                const double fym = iy > 0 ? face(idx, idx - nx) : kself;
+                const double fxm = ix > 0 ? face(idx, idx - 1) : kself;
+                const double fxp = ix < nx - 1 ? face(idx, idx + 1) : kself;
+                const double fyp = iy < ny - 1 ? face(idx, idx + nx) : kself;
+                const double fzp = iz < nz_ - 1 ? face(idx, idx + nxy) : kself;
+                diag = fzm + fym + fxm + fxp + fyp + fzp;
+                if (!kc) diag = 6.0;
+                if (iz > 0) put(idx - nxy, -fzm);
+                if (iy > 0) put(idx - nx, -fym);
+                if (ix > 0) put(idx - 1, -fxm);
+                put(idx, diag);
+                if (ix < nx - 1) put(idx + 1, -fxp);
+                if (iy < ny - 1) put(idx + nx, -fyp);
+                if (iz < nz_ - 1) put(idx + nxy, -fzp);
+            }
+    if (rp) rp[nxy * nz_] = nz;
+    return nz;
+}
+
+int gen_poisson3d(int nx, int ny, int nz, int* rp, int* ci, double* v) {
+    return gen_faces3d(nx, ny, nz, nullptr, rp, ci, v);
+}
+
+// k = exp(sigma * g); g: white noise (Box-Muller over SplitMix64) on the grid
+// extended by the kernel radius, convolved with the separable kernel
+// exp(-d^2/l^2) (whose autocorrelation is the squared-exponential covariance
+// exp(-d^2/(2 l^2)) of correlation length l), then shifted and scaled to
+// zero mean and unit sample variance.
+std::vector<double> gen_log_field(int nx, int ny, int nz, double sigma, double corr, uint64_t seed) {
+    const double sk = corr / std::sqrt(2.0);
+    const int R = std::max(1, (int)std::ceil(3.0 * sk));
+    std::vector<double> ker(2 * R + 1);
+    for (int d = -R; d <= R; ++d) ker[d + R] = std::exp(-(double)d * d / (corr * corr));
+    const int ex = nx + 2 * R, ey = ny + 2 * R, ez = nz + 2 * R;
+    std::vector<double> w((size_t)ex * ey * ez);
+    uint64_t rng = seed;
+    for (size_t i = 0; i < w.size(); i += 2) {
+        const double u1 = 1.0 - u01(rng), u2 = u01(rng);
+        const double r = std::sqrt(-2.0 * std::log(u1));
+        w[i] = r * std::cos(2.0 * M_PI * u2);
+        if (i + 1 < w.size()) w[i + 1] = r * std::sin(2.0 * M_PI * u2);
+    }
+    // x pass: ex*ey*ez -> nx*ey*ez
+    std::vector<double> t1((size_t)nx * ey * ez);
+    for (int z = 0; z < ez; ++z)
+        for (int y = 0; y < ey; ++y)
+            for (int x = 0; x < nx; ++x) {
+                double a = 0.0;
+                const double* src = &w[((size_t)z * ey + y) * ex + x];
+                for (int d = 0; d <= 2 * R; ++d) a += ker[d] * src[d];
+                t1[((size_t)z * ey + y) * nx + x] = a;
+            }
+    std::vector<double>().swap(w);
+    std::vector<double> t2((size_t)nx * ny * ez);
+    for (int z = 0; z < ez; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                double a = 0.0;
+                for (int d = 0; d <= 2 * R; ++d) a += ker[d] * t1[((size_t)z * ey + y + d) * nx + x];
+                t2[((size_t)z * ny + y) * nx + x] = a;
+            }
+    std::vector<double>().swap(t1);
+    std::vector<double> g((size_t)nx * ny * nz);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                double a = 0.0;
+                for (int d = 0; d <= 2 * R; ++d) a += ker[d] * t2[((size_t)(z + d) * ny + y) * nx + x];
+                g[((size_t)z * ny + y) * nx + x] = a;
+            }
+    double mean = 0.0;
+    for (double q : g) mean += q;
+    mean /= (double)g.size();
+    double var = 0.0;
+    for (double q : g) var += (q - mean) * (q - mean);
+    var /= (double)g.size();
+    const double inv = var > 0 ? 1.0 / std::sqrt(var) : 1.0;
+    for (double& q : g) q = std::exp(sigma * (q - mean) * inv);
+    return g;
+}
+
+int gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t seed, int* rp,
+                  int* ci, double* v) {
+    if (!rp) return gen_faces3d(nx, ny, nz, nullptr, nullptr, nullptr, nullptr);
+    std::vector<double> k = gen_log_field(nx, ny, nz, sigma, corr, seed);
+    return gen_faces3d(nx, ny, nz, k.data(), rp, ci, v);
+}
+
+void gen_uniform(uint64_t seed, int n, double lo, double hi, double* out) {
+    uint64_t rng = seed;
+    for (int i = 0; i < n; ++i) out[i] = lo + (hi - lo) * u01(rng);
+}
+
+}  // namespace sg

@@ -1,0 +1,220 @@
+// sg_internal.h -- shared declarations of libsgmres (host + device).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "sgmres.h"
+
+namespace sg {
+
+// --------------------------------------------------------------- errors
+struct Error {
+    sg_status status;
+    std::string msg;
+};
+
+[[noreturn]] void fail(sg_status st, const char* fmt, ...);
+void set_last_error(const char* msg);
+
+#define SG_CUDA(call)                                                                  \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess)                                                         \
+            ::sg::fail(e_ == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA,     \
+                       "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                       __LINE__);                                                      \
+    } while (0)
+
+#define SG_CHECK_ARG(cond, ...)                                                        \
+    do {                                                                               \
+        if (!(cond)) ::sg::fail(SG_ERR_INVALID_ARG, __VA_ARGS__);                      \
+    } while (0)
+
+// --------------------------------------------------------------- device buffers
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        SG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)));
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void upload(const T* h, size_t count, cudaStream_t s) {
+        if (n < count || !p) alloc(count);
+        if (count) SG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T>& v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+    void zero(cudaStream_t s) {
+        if (p) SG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+// --------------------------------------------------------------- solver state
+// Restart lengths up to SG_MMAX are supported.
+constexpr int SG_MMAX = 128;
+
+// Device-resident Arnoldi / Givens state of one solve (FP64 throughout).
+struct SolveState {
+    // control
+    int j;            // current Arnoldi step within the cycle
+    int kcount;       // basis vectors produced in this cycle (for the update)
+    int cycle_active; // 1 while steps of this cycle still run
+    int done;         // 1 once the solve has finished (converged or out of iterations)
+    int converged;
+    int total_iter;
+    int max_iter;
+    int tol_kind;
+    int breakdown;
+    int nonfinite;
+    int hist_len;
+    int cycles;
+    double tol;
+    double bnorm;      // ||b||
+    double rnorm;      // ||b - A x|| at the current cycle start (FP64)
+    double beta;       // ||z|| of the cycle start (the Krylov start norm)
+    double est_scale;  // rnorm / beta: turns |g_{j+1}| into a true-residual estimate
+    double last_res;   // last |g_{j+1}|
+    double ss;         // reduction scratch: sum of squares
+    double g[SG_MMAX + 1];
+    double cs[SG_MMAX];
+    double sn[SG_MMAX];
+    double H[(SG_MMAX + 1) * SG_MMAX];  // column-major, ld = m+1
+    double h[SG_MMAX + 1];              // projection coefficients of the current pass
+    double hsum[SG_MMAX + 1];           // h1 + h2 of the current column
+    double vscale[SG_MMAX + 1];         // basis vector k is stored as raw_k; v_k = vscale[k]*raw_k
+    double y[SG_MMAX];
+};
+
+// Per-context solve workspace (grown on demand, reused across solves).
+struct SolveWork {
+    DBuf<SolveState> st;
+    DBuf<double> r64, b64, x64;  // residual; staging of host b / x
+    DBuf<double> V64, Z64, t64;  // Krylov basis, FGMRES directions, SpMV output
+    DBuf<float> V32, Z32, t32;
+    SolveState* h_st = nullptr;  // pinned mirror of the state
+    cudaGraphExec_t graph = nullptr;
+    ~SolveWork();
+};
+
+}  // namespace sg
+
+struct sg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int num_sms = 0;
+    // reduction scratch shared by the kernels of this context (one stream)
+    sg::DBuf<double> partials;
+    sg::DBuf<unsigned int> counter;
+    // residual history of the running solve (device)
+    sg::DBuf<double> hist;
+    double* hist_d = nullptr;
+    int hist_cap = 0;
+    sg::SolveWork* work = nullptr;
+    // kernels launched by this context (graph launches add their kernel nodes)
+    long long launches = 0;
+    long long captured = 0;
+    bool capturing = false;
+};
+
+namespace sg {
+inline void count_launch(sg_ctx* ctx) {
+    if (ctx->capturing) ctx->captured++;
+    else ctx->launches++;
+}
+}  // namespace sg
+
+struct sg_csr {
+    sg_ctx* ctx = nullptr;
+    int nrows = 0, ncols = 0, nnz = 0;
+    bool sorted = true;  // column indices nondecreasing within each row
+    std::vector<int> h_rp, h_ci;
+    std::vector<double> h_val;
+    sg::DBuf<int> rp, ci;
+    sg::DBuf<double> val;
+    sg::DBuf<float> val32;  // FP32 copy for the FP32 inner Krylov (made on demand)
+    sg::DBuf<float> diag32;
+    void ensure_fp32();
+};
+
+namespace sg {
+
+// Per-subdomain metadata of the batched ILU(0) (device array of these).
+struct SubInfo {
+    int n;        // rows of the subdomain (with overlap)
+    int row_off;  // offset into per-row arrays (dofs, perm_f, perm_b, udiag)
+    int nlev_f, lev_off_f;
+    int nlev_b, lev_off_b;
+    int wl, wu;             // ELL widths of L and U (without the diagonal)
+    long long fl_off, fu_off;  // offsets into the factor arrays
+    int own_off, n_own;     // owned-local list
+    int csr_row_off;        // offset into the local CSR row_ptr array (n+1 per sub)
+    long long csr_nz_off;   // offset into the local CSR entries
+    double cscale;          // 1/sqrt(|owned|) (two-level)
+};
+
+}  // namespace sg
+
+struct sg_precond {
+    sg_ctx* ctx = nullptr;
+    int kind = SG_PC_NONE;
+    sg_precond_opts opts{};
+    bool is_setup = false;
+    int n = 0;
+    int nparts = 0;
+    int overlap = 0;
+    // ---- host integer set-up (kept for parity read-back)
+    std::vector<int> part, owned_ptr, owned, sub_ptr, sub, ownloc_ptr, ownloc;
+    std::vector<int> lrp, lci, ldiag, lmap, lev_lo, lev_up;  // local CSR, per-sub blocks
+    std::vector<sg::SubInfo> h_info;
+    std::vector<int> h_order, h_lev_ptr_f, h_lev_ptr_b;
+    std::vector<uint16_t> h_perm_f16, h_perm_b16;
+    std::vector<int> h_perm_f32, h_perm_b32;
+    std::vector<double> h_cscale;
+    bool wide_cols = false;  // subdomains above 65534 rows use 32-bit local indices
+    long long fl_total = 0, fu_total = 0;
+    int max_n = 0;
+    long long total_rows = 0;
+    bool use_smem = true;
+    // ---- device
+    sg::DBuf<double> inv_diag;  // jacobi
+    sg::DBuf<float> inv_diag32;
+    sg::DBuf<sg::SubInfo> info;
+    sg::DBuf<int> order;  // launch order of subdomains (largest first)
+    sg::DBuf<int> dofs;   // global index of every local row
+    sg::DBuf<uint16_t> perm_f, perm_b;  // level order (16-bit, or 32-bit stored in pairs)
+    sg::DBuf<int> lev_ptr_f, lev_ptr_b;
+    sg::DBuf<uint16_t> lcol, ucol;  // ELL local columns (level-major)
+    sg::DBuf<double> lval64, uval64, udiag64;
+    sg::DBuf<float> lval32, uval32, udiag32;
+    sg::DBuf<uint16_t> lval16, uval16, udiag16;  // bf16 bit patterns
+    sg::DBuf<int> ownloc_d;
+    sg::DBuf<int> owned_d, owned_ptr_d, part_d;
+    sg::DBuf<int> lrp_d, lci_d, ldiag_d, lmap_d;
+    sg::DBuf<double> lu_d;  // FP64 factors in local CSR layout
+    sg::DBuf<double> gscratch64;
+    sg::DBuf<float> gscratch32;
+    // ---- coarse space
+    int nc = 0;
+    sg::DBuf<double> a0, a0inv, lu0, r0, cscale_d;
+    sg::DBuf<int> piv0, status_d;
+    // ---- host-API staging
+    sg::DBuf<double> io_x, io_y;
+};

@@ -1,0 +1,217 @@
+// solver.cu -- restarted GMRES(m) and FGMRES drivers on the device
+// (src/core/gmres.cpp:34-160, src/core/fgmres.cpp:28-144).  Replaces the
+// host-driven loop of src/gpu/gmres_gpu.cu:10-138, which returned every dot
+// product to the host: here one restart cycle is a fixed launch sequence
+// (optionally captured once as a CUDA graph), all scalars stay in a device
+// SolveState, and the host reads the state once per cycle.
+//
+// Precision modes
+//   SG_FP64: basis, SpMV and preconditioner I/O in FP64 (the all-FP64 solver).
+//   SG_FP32: the Krylov basis, the inner SpMV and the preconditioner I/O are
+//            FP32; every cycle starts from the FP64 true residual b - A x and
+//            ends with an FP64 update of x, and the Hessenberg / Givens least
+//            squares stays FP64 -- iterative refinement with a GMRES(m)
+//            cycle as the inner solver (GMRES-IR).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+SolveWork::~SolveWork() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (h_st) cudaFreeHost(h_st);
+}
+
+namespace {
+
+template <class TV>
+struct Basis;
+template <>
+struct Basis<double> {
+    static DBuf<double>& V(SolveWork* w) { return w->V64; }
+    static DBuf<double>& Z(SolveWork* w) { return w->Z64; }
+    static DBuf<double>& T(SolveWork* w) { return w->t64; }
+    static const double* vals(const sg_csr* A) { return A->val.p; }
+};
+template <>
+struct Basis<float> {
+    static DBuf<float>& V(SolveWork* w) { return w->V32; }
+    static DBuf<float>& Z(SolveWork* w) { return w->Z32; }
+    static DBuf<float>& T(SolveWork* w) { return w->t32; }
+    static const float* vals(const sg_csr* A) { return A->val32.p; }
+};
+
+template <class TI, class TO>
+void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int* active) {
+    if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active);
+    else launch_copy<TI, TO>(ctx, x, y, n, active);
+}
+
+// One restart cycle as a launch sequence on ctx->stream.
+template <class TV>
+void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b, double* x,
+                   int m, bool flexible, size_t ldv) {
+    SolveWork* w = ctx->work;
+    SolveState* st = w->st.p;
+    const int n = A->nrows;
+    TV* V = Basis<TV>::V(w).p;
+    TV* Z = flexible ? Basis<TV>::Z(w).p : nullptr;
+    TV* t = Basis<TV>::T(w).p;
+    const TV* aval = Basis<TV>::vals(A);
+    const int* active = &st->cycle_active;
+    // r = b - A x (FP64) and the true-residual test
+    launch_residual(ctx, A, b, x, w->r64.p, st);
+    // Krylov start vector raw_0
+    if (!flexible) apply_pc<double, TV>(ctx, pc, w->r64.p, V, n, active);
+    else launch_copy<double, TV>(ctx, w->r64.p, V, n, active);
+    launch_cycle_init<TV>(ctx, V, n, st, m, flexible);
+    for (int j = 0; j < m; ++j) {
+        TV* vj = V + (size_t)j * ldv;
+        TV* wj = V + (size_t)(j + 1) * ldv;
+        if (!flexible) {
+            // w = M^{-1} A v_j  (src/core/gmres.cpp:280-285)
+            launch_spmv<TV, TV, TV>(ctx, n, A->rp.p, A->ci.p, aval, vj, t, &st->vscale[j], active);
+            apply_pc<TV, TV>(ctx, pc, t, wj, n, active);
+        } else {
+            // z_j = M^{-1} v_j ; w = A z_j  (src/core/fgmres.cpp:133-140)
+            TV* zj = Z + (size_t)j * ldv;
+            apply_pc<TV, TV>(ctx, pc, vj, zj, n, active);
+            launch_spmv<TV, TV, TV>(ctx, n, A->rp.p, A->ci.p, aval, zj, wj, &st->vscale[j], active);
+        }
+        launch_cgs2<TV>(ctx, V, ldv, n, j, m, st, flexible);
+    }
+    launch_backsolve(ctx, st, m);
+    launch_update_x<TV>(ctx, flexible ? Z : V, ldv, n, x, st);
+    launch_cycle_end(ctx, st);
+}
+
+template <class T>
+void ensure(DBuf<T>& b, size_t count) {
+    if (b.n < count) b.alloc(count);
+}
+
+}  // namespace
+
+void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, const double* b,
+                  double* x, const sg_solve_params& prm, sg_solve_result* res) {
+    const int n = A->nrows;
+    const int m = prm.restart;
+    SG_CHECK_ARG(m >= 1 && m <= SG_MMAX, "restart must be in [1,%d] (got %d)", SG_MMAX, m);
+    SG_CHECK_ARG(prm.max_iter >= 0, "max_iter must be >= 0");
+    SG_CHECK_ARG(prm.precision == SG_FP64 || prm.precision == SG_FP32,
+                 "solve precision must be SG_FP64 or SG_FP32");
+    SG_CHECK_ARG(prm.tol_kind >= SG_TOL_REF_ABS && prm.tol_kind <= SG_TOL_TRUE_REL,
+                 "unknown tol_kind %d", prm.tol_kind);
+    const bool flexible = solver == SG_FGMRES;
+    const bool fp32 = prm.precision == SG_FP32;
+    if (!ctx->work) ctx->work = new SolveWork();
+    SolveWork* w = ctx->work;
+    const size_t ldv = ((size_t)n + 31) & ~(size_t)31;
+    ensure(w->st, 1);
+    ensure(w->r64, ldv);
+    if (!w->h_st) SG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&w->h_st), sizeof(SolveState)));
+    if (fp32) {
+        const_cast<sg_csr*>(A)->ensure_fp32();
+        ensure(w->V32, ldv * (m + 1));
+        ensure(w->t32, ldv);
+        if (flexible) ensure(w->Z32, ldv * m);
+    } else {
+        ensure(w->V64, ldv * (m + 1));
+        ensure(w->t64, ldv);
+        if (flexible) ensure(w->Z64, ldv * m);
+    }
+    // history
+    const int hcap = prm.history && prm.history_cap > 0 ? prm.history_cap : 0;
+    if (hcap > 0) {
+        if (ctx->hist.n < (size_t)hcap) ctx->hist.alloc(hcap);
+        ctx->hist_d = ctx->hist.p;
+        ctx->hist_cap = hcap;
+    } else {
+        ctx->hist_d = nullptr;
+        ctx->hist_cap = 0;
+    }
+    // state
+    SolveState* hs = w->h_st;
+    std::memset(hs, 0, sizeof(SolveState));
+    hs->max_iter = prm.max_iter;
+    hs->tol = prm.tol;
+    hs->tol_kind = prm.tol_kind;
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    SG_CUDA(cudaMemcpyAsync(w->st.p, hs, sizeof(SolveState), cudaMemcpyHostToDevice, ctx->stream));
+    launch_bnorm(ctx, b, n, w->st.p);
+
+    const bool use_graph = prm.use_graph != 0;
+    cudaGraphExec_t exec = nullptr;
+    if (use_graph) {
+        cudaGraph_t g = nullptr;
+        SG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+        ctx->capturing = true;
+        ctx->captured = 0;
+        try {
+            if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
+            else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
+        } catch (...) {
+            ctx->capturing = false;
+            cudaStreamEndCapture(ctx->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        ctx->capturing = false;
+        SG_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        SG_CUDA(e);
+    }
+    const size_t ctl_bytes = offsetof(SolveState, g);
+    int cycles = 0;
+    try {
+        while (cycles < prm.max_iter || prm.max_iter == 0) {
+            if (prm.max_iter == 0) break;
+            if (use_graph) {
+                SG_CUDA(cudaGraphLaunch(exec, ctx->stream));
+                ctx->launches += ctx->captured;
+            }
+            else if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
+            else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
+            ++cycles;
+            SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            SG_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (hs->done) break;
+        }
+    } catch (...) {
+        if (exec) cudaGraphExecDestroy(exec);
+        throw;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    // final FP64 true residual for the result
+    const int saved_done = hs->done, saved_conv = hs->converged;
+    launch_residual(ctx, A, b, x, w->r64.p, w->st.p);
+    SG_CUDA(cudaMemcpyAsync(hs, w->st.p, sizeof(SolveState), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const auto t1 = std::chrono::high_resolution_clock::now();
+    hs->done = saved_done;
+    hs->converged = saved_conv;
+    if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->iterations = hs->total_iter;
+        res->cycles = hs->cycles;
+        res->converged = hs->converged;
+        res->history_len = hs->hist_len;
+        res->residual_norm = hs->hist_len > 0 ? hs->last_res : 0.0;
+        res->true_rel_residual = hs->bnorm > 0 ? hs->rnorm / hs->bnorm : hs->rnorm;
+        res->time_solve_s = std::chrono::duration<double>(t1 - t0).count();
+    }
+    if (hcap > 0) {
+        const int cnt = hs->hist_len < hcap ? hs->hist_len : hcap;
+        if (cnt > 0)
+            SG_CUDA(cudaMemcpy(prm.history, ctx->hist.p, sizeof(double) * cnt,
+                               cudaMemcpyDeviceToHost));
+    }
+    if (hs->nonfinite) fail(SG_ERR_NONFINITE, "non-finite value in the right-hand side or iteration");
+}
+
+}  // namespace sg

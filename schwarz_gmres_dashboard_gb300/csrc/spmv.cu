@@ -1,0 +1,204 @@
+// spmv.cu -- CSR sparse matrix-vector products (CSRMatrix::spmv,
+// src/core/sparse_matrix.h:30-37; replaces cusparseSpMV in
+// src/gpu/cuda_sparse.h:53-74).
+//
+// Layout: one warp owns a tile of 32 consecutive rows.  The tile's nonzeros
+// are one contiguous range of the CSR arrays; the warp streams it with
+// 16-byte vector loads (2 FP64 or 4 FP32 values, 2 or 4 column indices per
+// lane), forms the products into a per-warp shared-memory window and each
+// lane then sums its own row from the window (a warp-segmented reduction
+// whose per-row order is the entry order).  In FP64 the products and sums are
+// rounded one by one, so y matches the reference's serial loop bit for bit.
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+namespace {
+
+constexpr int SPMV_WARPS = 8;
+constexpr int SPMV_THREADS = SPMV_WARPS * 32;
+
+template <class T>
+struct VecT;
+template <>
+struct VecT<double> {
+    using V = double2;
+    using I = int2;
+    static constexpr int N = 2;
+};
+template <>
+struct VecT<float> {
+    using V = float4;
+    using I = int4;
+    static constexpr int N = 4;
+};
+
+__device__ __forceinline__ double pmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double padd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float pmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float padd(float a, float b) { return __fadd_rn(a, b); }
+
+template <class T, class V>
+__device__ __forceinline__ void unpack(const V& v, T (&o)[VecT<T>::N]);
+template <>
+__device__ __forceinline__ void unpack<double, double2>(const double2& v, double (&o)[2]) {
+    o[0] = v.x; o[1] = v.y;
+}
+template <>
+__device__ __forceinline__ void unpack<float, float4>(const float4& v, float (&o)[4]) {
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void unpacki(const int2& v, int (&o)[2]) { o[0] = v.x; o[1] = v.y; }
+__device__ __forceinline__ void unpacki(const int4& v, int (&o)[4]) {
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+
+// MODE 0: y = scale * (A x);  MODE 1: y = b - A x with ||y||^2 reduced.
+template <class TV, class TX, class TY, int MODE>
+__global__ void __launch_bounds__(SPMV_THREADS)
+k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+           const TV* __restrict__ val, const TX* __restrict__ x, TY* __restrict__ y,
+           const double* __restrict__ scale, const int* __restrict__ active,
+           const double* __restrict__ b, double* partials, unsigned* counter, SolveState* st) {
+    if (active && *active == 0) return;
+    constexpr int VN = VecT<TV>::N;
+    constexpr int CAP = 32 * VN * 4;
+    using VV = typename VecT<TV>::V;
+    using VI = typename VecT<TV>::I;
+    __shared__ TV buf[SPMV_WARPS][CAP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = gridDim.x * SPMV_WARPS;
+    TV* wbuf = buf[warp];
+    double ss = 0.0;
+    const TV sc = (MODE == 0 && scale) ? (TV)(*scale) : (TV)1;
+    for (int tile = blockIdx.x * SPMV_WARPS + warp; tile * 32 < n; tile += nwarps) {
+        const int r0 = tile * 32;
+        const int r = r0 + lane;
+        int rs = 0, re = 0;
+        if (r < n) {
+            rs = __ldg(&rp[r]);
+            re = __ldg(&rp[r + 1]);
+        }
+        const int lastlane = min(31, n - 1 - r0);
+        const int base = __shfl_sync(0xffffffffu, rs, 0);
+        const int end = __shfl_sync(0xffffffffu, re, lastlane);
+        TV sum = (TV)0;
+        for (int ws = base; ws < end; ws += CAP) {
+            const int we = min(ws + CAP, end);
+            const int a0 = ws & ~(VN - 1);
+            for (int e0 = a0 + lane * VN; e0 < we; e0 += 32 * VN) {
+                TV v[VN];
+                int c[VN];
+                unpack<TV, VV>(__ldg(reinterpret_cast<const VV*>(val + e0)), v);
+                unpacki(__ldg(reinterpret_cast<const VI*>(ci + e0)), c);
+#pragma unroll
+                for (int q = 0; q < VN; ++q) {
+                    const int e = e0 + q;
+                    if (e >= ws && e < we) wbuf[e - ws] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+                }
+            }
+            __syncwarp();
+            const int lo = max(rs, ws), hi = min(re, we);
+            for (int e = lo; e < hi; ++e) sum = padd(sum, wbuf[e - ws]);
+            __syncwarp();
+        }
+        if (r < n) {
+            if (MODE == 0) {
+                y[r] = (TY)(MODE == 0 && scale ? pmul(sum, sc) : sum);
+            } else {
+                const double rv = __dsub_rn(b[r], (double)sum);
+                y[r] = (TY)rv;
+                ss += rv * rv;
+            }
+        }
+    }
+    if (MODE == 1) {
+        __shared__ double red[SPMV_WARPS];
+        __shared__ double bs[1], tot[1];
+        double v1[1] = {ss};
+        block_sum_multi<1>(v1, 1, red, bs);
+        if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0) {
+            const double rn = sqrt(tot[0]);
+            st->rnorm = rn;
+            if (!isfinite(rn)) {
+                st->nonfinite = 1;
+                st->done = 1;
+                st->cycle_active = 0;
+            } else if (st->tol_kind != SG_TOL_REF_ABS && rn <= st->tol * st->bnorm) {
+                st->converged = 1;
+                st->done = 1;
+                st->cycle_active = 0;
+            } else {
+                st->cycle_active = st->done ? 0 : 1;
+            }
+        }
+    }
+}
+
+__global__ void k_bnorm(const double* __restrict__ v, int n, double* partials, unsigned* counter,
+                        SolveState* st) {
+    double ss = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double t = v[i];
+        ss += t * t;
+    }
+    __shared__ double red[32];
+    __shared__ double bs[1], tot[1];
+    double v1[1] = {ss};
+    block_sum_multi<1>(v1, 1, red, bs);
+    if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0) {
+        st->bnorm = sqrt(tot[0]);
+        if (!isfinite(st->bnorm)) {
+            st->nonfinite = 1;
+            st->done = 1;
+            st->cycle_active = 0;
+        }
+    }
+}
+
+int spmv_grid(sg_ctx* ctx, int n) {
+    const long long tiles = (n + 31) / 32;
+    long long blocks = (tiles + SPMV_WARPS - 1) / SPMV_WARPS;
+    const long long cap = (long long)ctx->num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+}  // namespace
+
+template <class TV, class TX, class TY>
+void launch_spmv(sg_ctx* ctx, int n, const int* rp, const int* ci, const TV* val, const TX* x,
+                 TY* y, const double* scale, const int* active) {
+    if (n <= 0) return;
+    k_spmv_csr<TV, TX, TY, 0><<<spmv_grid(ctx, n), SPMV_THREADS, 0, ctx->stream>>>(
+        n, rp, ci, val, x, y, scale, active, nullptr, nullptr, nullptr, nullptr);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double* x, double* r,
+                     SolveState* st) {
+    k_spmv_csr<double, double, double, 1><<<spmv_grid(ctx, A->nrows), SPMV_THREADS, 0,
+                                            ctx->stream>>>(
+        A->nrows, A->rp.p, A->ci.p, A->val.p, x, r, nullptr, nullptr, b, ctx->partials.p, ctx->counter.p, st);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+void launch_bnorm(sg_ctx* ctx, const double* v, int n, SolveState* st) {
+    int blocks = ctx->num_sms * 2;
+    k_bnorm<<<blocks, 512, 0, ctx->stream>>>(v, n, ctx->partials.p, ctx->counter.p, st);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template void launch_spmv<double, double, double>(sg_ctx*, int, const int*, const int*,
+                                                  const double*, const double*, double*,
+                                                  const double*, const int*);
+template void launch_spmv<float, float, float>(sg_ctx*, int, const int*, const int*,
+                                               const float*, const float*, float*,
+                                               const double*, const int*);
+
+}  // namespace sg
