@@ -78,6 +78,16 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    # the schwarz_solve CLI, linked against the library next to it
+    cli_src = os.path.join(CSRC, "cli", "schwarz_solve.cpp")
+    if (not os.path.exists(CLI) or os.path.getmtime(CLI) < os.path.getmtime(cli_src)
+            or os.path.getmtime(CLI) < os.path.getmtime(LIB)):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, cli_src, "-o", CLI, "-L", BUILD,
+               "-lsgmres", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

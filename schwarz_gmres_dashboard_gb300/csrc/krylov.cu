@@ -344,8 +344,8 @@ __global__ void k_copy(const TI* __restrict__ x, TO* __restrict__ y, int n,
 __global__ void k_cycle_end(SolveState* st) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     st->cycles++;
-    st->cycle_active = 0;
     if (!st->done && st->total_iter >= st->max_iter) st->done = 1;
+    st->cycle_active = st->done ? 0 : 1;
 }
 
 int kgrid(sg_ctx* ctx, int n, int per_sm) {

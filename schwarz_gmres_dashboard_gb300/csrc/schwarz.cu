@@ -431,6 +431,12 @@ template <class TS, class TF, class TC, class TI, class TO>
 void sweep_launch(sg_precond* pc, const TF* lval, const TF* uval, const TF* udiag, const TI* x,
                   TO* y, int mode, bool coarse, const int* active, TS* gscratch) {
     sg_ctx* ctx = pc->ctx;
+    // every buffer the kernel dereferences must exist (host-side guard)
+    if (!pc->info.p || !pc->order.p || !pc->dofs.p || !pc->perm_f.p || !pc->perm_b.p ||
+        !pc->lev_ptr_f.p || !pc->lev_ptr_b.p || !pc->lcol.p || !pc->ucol.p || !lval || !uval ||
+        !udiag || !pc->ownloc_d.p || !pc->owned_d.p || (!pc->use_smem && !gscratch) ||
+        (coarse && (!pc->a0inv.p || !pc->r0.p)))
+        fail(SG_ERR_INTERNAL, "preconditioner device buffers missing for this apply");
     size_t smem = 0;
     if (pc->use_smem) {
         smem = ((size_t)(pc->max_n + 1) * sizeof(TS) + 15) & ~(size_t)15;
@@ -519,6 +525,8 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
     pc->ldiag_d.upload(pc->ldiag, st);
     pc->lmap_d.upload(pc->lmap, st);
     pc->ownloc_d.upload(pc->ownloc, st);
+    pc->owned_ptr_d.upload(pc->owned_ptr, st);
+    pc->owned_d.upload(pc->owned, st);
     
     if (pc->wide_cols) {
         pc->perm_f.upload(reinterpret_cast<const uint16_t*>(pc->h_perm_f32.data()),
@@ -548,8 +556,6 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
     if (pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS) {
         const int nc = pc->nparts;
         pc->nc = nc;
-        pc->owned_ptr_d.upload(pc->owned_ptr, st);
-        pc->owned_d.upload(pc->owned, st);
         pc->part_d.upload(pc->part, st);
         pc->cscale_d.upload(pc->h_cscale, st);
         pc->a0.alloc((size_t)nc * nc);
@@ -606,6 +612,8 @@ void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active)
     const bool asm_mode = (pc->kind == SG_PC_ASM || pc->kind == SG_PC_TWOLEVEL_ASM);
     const bool coarse = (pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS);
     if (coarse) {
+        if (!pc->owned_ptr_d.p || !pc->owned_d.p || !pc->cscale_d.p || !pc->r0.p)
+            fail(SG_ERR_INTERNAL, "coarse-space device buffers missing");
         k_restrict<TI><<<pc->nc, 256, 0, ctx->stream>>>(pc->owned_ptr_d.p, pc->owned_d.p,
                                                         pc->cscale_d.p, x, pc->r0.p, active);
         SG_CUDA(cudaGetLastError());

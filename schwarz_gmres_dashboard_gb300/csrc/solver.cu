@@ -63,8 +63,8 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
     TV* t = Basis<TV>::T(w).p;
     const TV* aval = Basis<TV>::vals(A);
     const int* active = &st->cycle_active;
-    // r = b - A x (FP64) and the true-residual test
-    launch_residual(ctx, A, b, x, w->r64.p, st);
+    // r = b - A x is already in w->r64 (computed at the end of the previous
+    // cycle, or before the first one) together with the convergence test.
     // Krylov start vector raw_0
     if (!flexible) apply_pc<double, TV>(ctx, pc, w->r64.p, V, n, active);
     else launch_copy<double, TV>(ctx, w->r64.p, V, n, active);
@@ -86,6 +86,9 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
     }
     launch_backsolve(ctx, st, m);
     launch_update_x<TV>(ctx, flexible ? Z : V, ldv, n, x, st);
+    // FP64 true residual of the updated x: convergence test and the next
+    // cycle's right-hand side
+    launch_residual(ctx, A, b, x, w->r64.p, st);
     launch_cycle_end(ctx, st);
 }
 
@@ -143,8 +146,13 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     const auto t0 = std::chrono::high_resolution_clock::now();
     SG_CUDA(cudaMemcpyAsync(w->st.p, hs, sizeof(SolveState), cudaMemcpyHostToDevice, ctx->stream));
     launch_bnorm(ctx, b, n, w->st.p);
+    launch_residual(ctx, A, b, x, w->r64.p, w->st.p);
+    const size_t ctl_bytes = offsetof(SolveState, g);
+    SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const bool done_at_start = hs->done != 0;
 
-    const bool use_graph = prm.use_graph != 0;
+    const bool use_graph = prm.use_graph != 0 && !done_at_start && prm.max_iter > 0;
     cudaGraphExec_t exec = nullptr;
     if (use_graph) {
         cudaGraph_t g = nullptr;
@@ -166,11 +174,9 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
         cudaGraphDestroy(g);
         SG_CUDA(e);
     }
-    const size_t ctl_bytes = offsetof(SolveState, g);
     int cycles = 0;
     try {
-        while (cycles < prm.max_iter || prm.max_iter == 0) {
-            if (prm.max_iter == 0) break;
+        while (!done_at_start && cycles < prm.max_iter) {
             if (use_graph) {
                 SG_CUDA(cudaGraphLaunch(exec, ctx->stream));
                 ctx->launches += ctx->captured;
@@ -187,14 +193,10 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
         throw;
     }
     if (exec) cudaGraphExecDestroy(exec);
-    // final FP64 true residual for the result
-    const int saved_done = hs->done, saved_conv = hs->converged;
-    launch_residual(ctx, A, b, x, w->r64.p, w->st.p);
-    SG_CUDA(cudaMemcpyAsync(hs, w->st.p, sizeof(SolveState), cudaMemcpyDeviceToHost, ctx->stream));
+    // the state now holds the FP64 true residual of the returned x
+    SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(cudaStreamSynchronize(ctx->stream));
     const auto t1 = std::chrono::high_resolution_clock::now();
-    hs->done = saved_done;
-    hs->converged = saved_conv;
     if (res) {
         std::memset(res, 0, sizeof(*res));
         res->iterations = hs->total_iter;

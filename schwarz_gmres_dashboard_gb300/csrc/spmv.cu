@@ -121,6 +121,9 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
         if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0) {
             const double rn = sqrt(tot[0]);
             st->rnorm = rn;
+            // a new cycle starts from here: no basis vectors yet
+            st->kcount = 0;
+            st->j = 0;
             if (!isfinite(rn)) {
                 st->nonfinite = 1;
                 st->done = 1;
