@@ -377,7 +377,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=128,
+                    help="grid edge (128 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()
+    global N_GRID, NPARTS, WORKLOAD
+    if args.grid != N_GRID:
+        N_GRID = args.grid
+        NPARTS = max(8, min(NPARTS, round(256 * (args.grid / 128) ** 3)))
+        WORKLOAD = WORKLOAD.replace("128^3", f"{N_GRID}^3").replace("256uneven", f"{NPARTS}uneven")
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -67,7 +67,8 @@ typedef struct sg_precond_opts {
     const int* partition; /* optional host array [n] of part ids in [0,nparts);
                              NULL = built-in graph partitioner. Takes the place
                              of METIS_PartGraphKway (src/decomp/domain_decomp.h:23-58) */
-    int reserved[8];
+    int reserved[8];  /* reserved[0] bit 0: use the generic level sweep instead of
+                         the TMA-fed one (testing); other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;
@@ -98,6 +99,12 @@ sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count);
 sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* row_ptr,
                         const int* col_idx, const double* vals, sg_mem mem, sg_csr** out);
 sg_status sg_csr_destroy(sg_csr* A);
+/* SpMV storage used by this matrix: 0 = decided by the autotuner on first
+ * use (times both, keeps the faster), 1 = CSR, 2 = SELL-C-sigma (C = 32).
+ * Both give the same bits.  No counterpart in the reference (cuSPARSE's
+ * CUSPARSE_SPMV_ALG_DEFAULT, src/gpu/cuda_sparse.h:64-68, has no choice). */
+sg_status sg_csr_set_format(sg_csr* A, int format);
+sg_status sg_csr_get_format(sg_csr* A, int* format);
 /* y = A x (CSRMatrix::spmv, src/core/sparse_matrix.h:30-37; replaces
  * DeviceCSRMatrix::spmv, src/gpu/cuda_sparse.h:53-74). FP64, same summation
  * order as the reference row loop. */

@@ -178,6 +178,17 @@ class CSRMatrix:
         _check(_clib.sg_csr_spmv(dev, px, py, mx))
         return y
 
+    @property
+    def format(self) -> int:
+        """SpMV storage: 0 autotune (not decided yet), 1 CSR, 2 SELL-32."""
+        f = C.c_int(0)
+        _check(_clib.sg_csr_get_format(self.device(), C.byref(f)))
+        return f.value
+
+    @format.setter
+    def format(self, fmt: int) -> None:
+        _check(_clib.sg_csr_set_format(self.device(), int(fmt)))
+
     def diagonal(self, i: int) -> float:
         for e in range(self.row_ptr[i], self.row_ptr[i + 1]):
             if self.col_idx[e] == i:
@@ -282,7 +293,9 @@ class Preconditioner:
 
     def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
-                 ctx: Context | None = None):
+                 ctx: Context | None = None, generic_sweep: bool = False):
+        # generic_sweep: level sweep without the TMA record ring (testing)
+        self.generic_sweep = bool(generic_sweep)
         self.ctx = ctx or default_context()
         self.nparts = int(nparts)
         self.overlap = int(overlap)
@@ -295,6 +308,7 @@ class Preconditioner:
         opts.factor_dtype = factor_dtype
         opts.sweep_dtype = sweep_dtype
         opts.partition = self.partition.ctypes.data if self.partition is not None else None
+        opts.reserved[0] = 1 if self.generic_sweep else 0
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),
@@ -373,8 +387,8 @@ class JacobiPrecond(Preconditioner):
     """src/precond/jacobi.h:10-27"""
     kind = "jacobi"
 
-    def __init__(self, sweep_dtype: int = FP64, ctx: Context | None = None):
-        super().__init__(1, 0, None, FP64 if sweep_dtype == FP64 else FP32, sweep_dtype, ctx)
+    def __init__(self, sweep_dtype: int = FP64, ctx: Context | None = None, **kw):
+        super().__init__(1, 0, None, FP64 if sweep_dtype == FP64 else FP32, sweep_dtype, ctx, **kw)
 
 
 class ILU0Precond(Preconditioner):
@@ -382,8 +396,8 @@ class ILU0Precond(Preconditioner):
     kind = "ilu0"
 
     def __init__(self, factor_dtype: int = FP64, sweep_dtype: int = FP64,
-                 ctx: Context | None = None):
-        super().__init__(1, 0, None, factor_dtype, sweep_dtype, ctx)
+                 ctx: Context | None = None, **kw):
+        super().__init__(1, 0, None, factor_dtype, sweep_dtype, ctx, **kw)
 
 
 class ASMPrecond(Preconditioner):
@@ -391,8 +405,8 @@ class ASMPrecond(Preconditioner):
     kind = "asm"
 
     def __init__(self, nparts: int, overlap: int, partition=None, factor_dtype: int = FP64,
-                 sweep_dtype: int = FP64, ctx: Context | None = None):
-        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx)
+                 sweep_dtype: int = FP64, ctx: Context | None = None, **kw):
+        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx, **kw)
 
 
 class RASPrecond(Preconditioner):
@@ -400,8 +414,8 @@ class RASPrecond(Preconditioner):
     kind = "ras"
 
     def __init__(self, nparts: int, overlap: int, partition=None, factor_dtype: int = FP64,
-                 sweep_dtype: int = FP64, ctx: Context | None = None):
-        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx)
+                 sweep_dtype: int = FP64, ctx: Context | None = None, **kw):
+        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx, **kw)
 
 
 class TwoLevelSchwarzPrecond(Preconditioner):
@@ -410,10 +424,10 @@ class TwoLevelSchwarzPrecond(Preconditioner):
 
     def __init__(self, nparts: int, overlap: int, fine_type: FineLevelType = FineLevelType.RAS,
                  partition=None, factor_dtype: int = FP64, sweep_dtype: int = FP64,
-                 ctx: Context | None = None):
+                 ctx: Context | None = None, **kw):
         self.kind = "twolevel_asm" if fine_type == FineLevelType.ASM else "twolevel_ras"
         self.fine_type = fine_type
-        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx)
+        super().__init__(nparts, overlap, partition, factor_dtype, sweep_dtype, ctx, **kw)
 
 
 # ---------------------------------------------------------------- solvers

@@ -71,7 +71,57 @@ void sg_csr::ensure_fp32() {
     std::vector<float> v32(h_val.size() + 16, 0.0f);
     for (size_t i = 0; i < h_val.size(); ++i) v32[i] = (float)h_val[i];
     val32.upload(v32, ctx->stream);
+    if (sell_ok) {
+        // FP32 copy of the SELL values (same slice layout)
+        std::vector<double> sv(sell_entries);
+        SG_CUDA(cudaMemcpyAsync(sv.data(), sl_val.p, sizeof(double) * sell_entries,
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        std::vector<float> s32(sell_entries);
+        for (long long i = 0; i < sell_entries; ++i) s32[i] = (float)sv[i];
+        sl_val32.upload(s32, ctx->stream);
+    }
     SG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+// SELL-32 copy (slices of 32 rows, slice-major, padded per slice).  Kept only
+// when the padding stays under 25% of the nonzeros.
+void sg_csr::build_sell() {
+    sell_ok = false;
+    if (nrows <= 0 || nrows != ncols) return;
+    nslices = (nrows + 31) / 32;
+    std::vector<long long> ptr(nslices + 1, 0);
+    std::vector<int> w(nslices, 0);
+    for (int s = 0; s < nslices; ++s) {
+        int mw = 0;
+        for (int r = s * 32; r < std::min(nrows, s * 32 + 32); ++r)
+            mw = std::max(mw, h_rp[r + 1] - h_rp[r]);
+        w[s] = mw;
+        ptr[s + 1] = ptr[s] + 32ll * mw;
+    }
+    sell_entries = ptr[nslices];
+    if (sell_entries > (long long)nnz + nnz / 4 + 64 || sell_entries >= (1ll << 31)) return;
+    std::vector<int> col(sell_entries > 0 ? sell_entries : 1, 0);
+    std::vector<double> val(sell_entries > 0 ? sell_entries : 1, 0.0);
+    for (int s = 0; s < nslices; ++s)
+        for (int lane = 0; lane < 32; ++lane) {
+            const int r = s * 32 + lane;
+            int k = 0;
+            if (r < nrows)
+                for (int e = h_rp[r]; e < h_rp[r + 1]; ++e, ++k) {
+                    col[ptr[s] + 32ll * k + lane] = h_ci[e];
+                    val[ptr[s] + 32ll * k + lane] = h_val[e];
+                }
+            for (; k < w[s]; ++k) {
+                col[ptr[s] + 32ll * k + lane] = r < nrows ? r : 0;
+                val[ptr[s] + 32ll * k + lane] = 0.0;
+            }
+        }
+    sl_ptr.upload(ptr, ctx->stream);
+    sl_w.upload(w, ctx->stream);
+    sl_col.upload(col, ctx->stream);
+    sl_val.upload(val, ctx->stream);
+    sell_ok = true;
 }
 
 extern "C" {
@@ -223,12 +273,30 @@ sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* r
             A->ci.upload(A->h_ci, ctx->stream);
             A->val.upload(vpad, ctx->stream);
             A->h_ci.resize(nnz);
+            if (A->sorted) A->build_sell();
             SG_CUDA(cudaStreamSynchronize(ctx->stream));
         } catch (...) {
             delete A;
             throw;
         }
         *out = A;
+    });
+}
+
+sg_status sg_csr_set_format(sg_csr* A, int format) {
+    return guard([&] {
+        SG_CHECK_ARG(A, "NULL argument");
+        SG_CHECK_ARG(format >= 0 && format <= 2, "format must be 0 (auto), 1 (CSR) or 2 (SELL)");
+        if (format == 2 && !A->sell_ok)
+            fail(SG_ERR_UNSUPPORTED, "no SELL copy of this matrix (unsorted rows or padding > 25%%)");
+        A->format = format;
+    });
+}
+
+sg_status sg_csr_get_format(sg_csr* A, int* format) {
+    return guard([&] {
+        SG_CHECK_ARG(A && format, "NULL argument");
+        *format = A->format;
     });
 }
 
@@ -255,8 +323,8 @@ sg_status sg_csr_spmv(sg_csr* A, const double* x, double* y, sg_mem mem) {
             dx = w->x64.p;
             dy = w->b64.p;
         }
-        launch_spmv<double, double, double>(ctx, A->nrows, A->rp.p, A->ci.p, A->val.p, dx, dy,
-                                            nullptr, nullptr);
+        spmv_autotune(ctx, A);
+        launch_spmv_a<double, double, double>(ctx, A, dx, dy, nullptr, nullptr);
         if (mem == SG_MEM_HOST)
             SG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * A->nrows, cudaMemcpyDeviceToHost,
                                     ctx->stream));
@@ -348,10 +416,12 @@ sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg
             dx = pc->io_x.p;
             dy = pc->io_y.p;
         }
-        precond_apply_device<double, double>(pc, dx, dy, nullptr);
+        precond_apply_device<double, double>(pc, dx, dy, nullptr, true);
         if (mem == SG_MEM_HOST)
             SG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (sweep_error(pc))
+            fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
     });
 }
 

@@ -110,6 +110,7 @@ __device__ __forceinline__ bool last_block_reduce(double* partials, unsigned* co
     const int nb = gridDim.x;
     for (int k = warp; k < nv; k += nw) {
         double s = 0.0;
+#pragma unroll 8
         for (int b = lane; b < nb; b += 32) s += __ldcg(&partials[(size_t)b * nv + k]);
         s = warp_sum(s);
         if (lane == 0) out[k] = s;

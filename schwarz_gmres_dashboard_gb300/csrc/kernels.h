@@ -12,6 +12,13 @@ namespace sg {
 template <class TV, class TX, class TY>
 void launch_spmv(sg_ctx* ctx, int n, const int* rp, const int* ci, const TV* val, const TX* x,
                  TY* y, const double* scale, const int* active);
+// Matrix-level SpMV: SELL or CSR as chosen for A (same bits in FP64).
+// fp32 selects the FP32 copy of the values (inner Krylov).
+template <class TV, class TX, class TY>
+void launch_spmv_a(sg_ctx* ctx, const sg_csr* A, const TX* x, TY* y, const double* scale,
+                   const int* active);
+// Times both formats on A and keeps the faster one (autotuner).
+void spmv_autotune(sg_ctx* ctx, sg_csr* A);
 // r = b - A x in FP64 with ||r||; the last block updates the solve state
 // (rnorm, true-residual convergence test).
 void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double* x, double* r,
@@ -42,8 +49,18 @@ void launch_cycle_end(sg_ctx* ctx, SolveState* st);
 
 // ---------------------------------------------------------------- schwarz.cu
 void precond_setup_device(sg_precond* pc, const sg_csr* A);
+// exact: FP64 sweeps round each product and difference (reference bits);
+// otherwise they use fused multiply-adds (the solver's FP64 mode)
 template <class TI, class TO>
-void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active);
+void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active,
+                          bool exact = true);
+
+// ---------------------------------------------------------------- sweep.cu
+void rec_setup_device(sg_precond* pc);
+template <class TI, class TO>
+bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
+               const int* active);
+int sweep_error(sg_precond* pc);
 // copy the FP64 factors of subdomain s back to the host
 void precond_read_factors(sg_precond* pc, int s, double* lu_out);
 void precond_read_coarse(sg_precond* pc, double* a0_out);

@@ -240,16 +240,16 @@ k_upd_norm(const TV* __restrict__ raw, size_t ldv, int n, int j, int m, TV* __re
     __shared__ TV cf[SG_MMAX + 1];
     for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
     __syncthreads();
-    double ss = 0.0;
+    TV ss = (TV)0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         TV wi = w[i];
         for (int k = 0; k < nk; ++k) wi -= cf[k] * raw[(size_t)k * ldv + i];
         w[i] = wi;
-        ss += (double)wi * (double)wi;
+        ss += wi * wi;
     }
     __shared__ double red[KT / 32];
     __shared__ double bs[1], tot[1];
-    double v1[1] = {ss};
+    double v1[1] = {(double)ss};
     block_sum_multi<1>(v1, 1, red, bs);
     if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0)
         arnoldi_finalize(st, j, m, tot[0], hist, hist_cap);
@@ -323,13 +323,15 @@ k_update_x(const TV* __restrict__ basis, size_t ldv, int n, double* __restrict__
            SolveState* st) {
     const int k = st->kcount;
     if (k <= 0) return;
-    __shared__ double cf[SG_MMAX];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) cf[i] = st->y[i] * st->vscale[i];
+    // the correction d = V y is formed in the basis precision (FP32 for the
+    // mixed solver: the inner solve's precision) and added to x in FP64
+    __shared__ TV cf[SG_MMAX];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) cf[i] = (TV)(st->y[i] * st->vscale[i]);
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double xi = x[i];
-        for (int q = 0; q < k; ++q) xi += cf[q] * (double)basis[(size_t)q * ldv + i];
-        x[i] = xi;
+        TV d = (TV)0;
+        for (int q = 0; q < k; ++q) d += cf[q] * basis[(size_t)q * ldv + i];
+        x[i] += (double)d;
     }
 }
 

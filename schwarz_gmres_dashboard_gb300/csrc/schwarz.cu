@@ -23,7 +23,7 @@ namespace sg {
 
 namespace {
 
-constexpr int SWEEP_T = 256;
+constexpr int SWEEP_T = 512;
 
 // ---------------------------------------------------------------- Jacobi
 __global__ void k_jacobi_setup(int n, const int* __restrict__ rp, const int* __restrict__ ci,
@@ -65,7 +65,7 @@ __global__ void k_gather_vals(long long nz, const int* __restrict__ map,
 // skip rule, same first-match search, product and difference rounded
 // separately).
 template <class TC>
-__global__ void __launch_bounds__(SWEEP_T)
+__global__ void __launch_bounds__(SWEEP_T, 2)
 k_factor(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
          const int* __restrict__ lci, const int* __restrict__ ldiag,
          const TC* __restrict__ perm_f, const int* __restrict__ lev_f, double* lu) {
@@ -117,7 +117,7 @@ __device__ __forceinline__ uint16_t cvt_factor<uint16_t>(double v) {
 
 // Factored local CSR -> level-major ELL slices of type TF.
 template <class TF, class TC>
-__global__ void __launch_bounds__(SWEEP_T)
+__global__ void __launch_bounds__(SWEEP_T, 2)
 k_pack(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
        const int* __restrict__ lci, const int* __restrict__ ldiag,
        const double* __restrict__ lu, const TC* __restrict__ perm_f,
@@ -158,9 +158,100 @@ k_pack(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
 }
 
 // ---------------------------------------------------------------- sweeps
+// One triangular sweep of a subdomain held in shared memory `t`.  Rows of a
+// level are independent; a __syncthreads separates levels.  The factor
+// entries, columns and row index of the next level are loaded into registers
+// before the current level is computed, so the global-memory latency of level
+// l+1 overlaps the arithmetic and the barrier of level l.  The per-row order
+// of the subtractions (and the final division of the backward sweep) is the
+// reference's (src/precond/ilu0.h:62-76).
+constexpr int SWEEP_WP = 4;  // ELL widths up to this are prefetched
+
+template <class TS, class TF, class TC, bool BACK>
+__device__ __forceinline__ void sweep_levels(TS* t, int n, int nlev, const int* __restrict__ lptr,
+                                             const TC* __restrict__ perm,
+                                             const TC* __restrict__ col,
+                                             const TF* __restrict__ val,
+                                             const TF* __restrict__ diag, int w) {
+    if (w > SWEEP_WP) {
+        for (int l = 0; l < nlev; ++l) {
+            const int p0 = lptr[l], p1 = lptr[l + 1];
+            for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+                const int r = perm[p];
+                TS acc = t[r];
+                for (int k = 0; k < w; ++k)
+                    acc = msub(acc, Load<TS>::f(val[(size_t)k * n + p]), t[col[(size_t)k * n + p]]);
+                if (BACK) acc = acc / Load<TS>::f(diag[p]);
+                t[r] = acc;
+            }
+            __syncthreads();
+        }
+        return;
+    }
+    // registers for the first pass of the next level
+    bool have = false;
+    int r = 0;
+    TS v[SWEEP_WP];
+    int c[SWEEP_WP];
+    TS d = (TS)1;
+    auto fetch = [&](int p) {
+        r = perm[p];
+#pragma unroll
+        for (int k = 0; k < SWEEP_WP; ++k) {
+            if (k < w) {
+                v[k] = Load<TS>::f(val[(size_t)k * n + p]);
+                c[k] = col[(size_t)k * n + p];
+            }
+        }
+        if (BACK) d = Load<TS>::f(diag[p]);
+    };
+    if (nlev > 0) {
+        const int p = lptr[0] + threadIdx.x;
+        have = p < lptr[1];
+        if (have) fetch(p);
+    }
+    for (int l = 0; l < nlev; ++l) {
+        const int p0 = lptr[l], p1 = lptr[l + 1];
+        const bool cur = have;
+        const int rc = r;
+        TS vc[SWEEP_WP];
+        int cc[SWEEP_WP];
+#pragma unroll
+        for (int k = 0; k < SWEEP_WP; ++k) {
+            vc[k] = v[k];
+            cc[k] = c[k];
+        }
+        const TS dc = d;
+        have = false;
+        if (l + 1 < nlev) {
+            const int q = p1 + threadIdx.x;
+            have = q < lptr[l + 2];
+            if (have) fetch(q);
+        }
+        if (cur) {
+            TS acc = t[rc];
+#pragma unroll
+            for (int k = 0; k < SWEEP_WP; ++k)
+                if (k < w) acc = msub(acc, vc[k], t[cc[k]]);
+            if (BACK) acc = acc / dc;
+            t[rc] = acc;
+        }
+        // rows of this level beyond the first pass
+        for (int q = p0 + threadIdx.x + blockDim.x; q < p1; q += blockDim.x) {
+            const int rr = perm[q];
+            TS acc = t[rr];
+            for (int k = 0; k < w; ++k)
+                acc = msub(acc, Load<TS>::f(val[(size_t)k * n + q]), t[col[(size_t)k * n + q]]);
+            if (BACK) acc = acc / Load<TS>::f(diag[q]);
+            t[rr] = acc;
+        }
+        __syncthreads();
+    }
+}
+
 // mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
 template <class TI, class TO, class TS, class TF, class TC>
-__global__ void __launch_bounds__(SWEEP_T)
+__global__ void __launch_bounds__(SWEEP_T, 2)
 k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
         const int* __restrict__ dofs, const TC* __restrict__ perm_f,
         const int* __restrict__ lev_f, const TC* __restrict__ lcol, const TF* __restrict__ lval,
@@ -197,45 +288,13 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
         }
     }
     __syncthreads();
-    // forward sweep, unit lower triangle
-    {
-        const TC* pf = perm_f + inf.row_off;
-        const int* lf = lev_f + inf.lev_off_f;
-        const TC* lc = lcol + inf.fl_off;
-        const TF* lv = lval + inf.fl_off;
-        const int wl = inf.wl;
-        for (int l = 0; l < inf.nlev_f; ++l) {
-            const int p0 = lf[l], p1 = lf[l + 1];
-            for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-                const int r = pf[p];
-                TS acc = t[r];
-                for (int k = 0; k < wl; ++k)
-                    acc = msub(acc, Load<TS>::f(lv[(size_t)k * n + p]), t[lc[(size_t)k * n + p]]);
-                t[r] = acc;
-            }
-            __syncthreads();
-        }
-    }
-    // backward sweep, upper triangle and diagonal
-    {
-        const TC* pb = perm_b + inf.row_off;
-        const int* lb = lev_b + inf.lev_off_b;
-        const TC* uc = ucol + inf.fu_off;
-        const TF* uv = uval + inf.fu_off;
-        const TF* ud = udiag + inf.row_off;
-        const int wu = inf.wu;
-        for (int l = 0; l < inf.nlev_b; ++l) {
-            const int p0 = lb[l], p1 = lb[l + 1];
-            for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-                const int r = pb[p];
-                TS acc = t[r];
-                for (int k = 0; k < wu; ++k)
-                    acc = msub(acc, Load<TS>::f(uv[(size_t)k * n + p]), t[uc[(size_t)k * n + p]]);
-                t[r] = acc / Load<TS>::f(ud[p]);
-            }
-            __syncthreads();
-        }
-    }
+    // forward sweep (unit lower triangle), then backward sweep (upper
+    // triangle and diagonal), level by level
+    sweep_levels<TS, TF, TC, false>(t, n, inf.nlev_f, lev_f + inf.lev_off_f, perm_f + inf.row_off,
+                                    lcol + inf.fl_off, lval + inf.fl_off, nullptr, inf.wl);
+    sweep_levels<TS, TF, TC, true>(t, n, inf.nlev_b, lev_b + inf.lev_off_b, perm_b + inf.row_off,
+                                   ucol + inf.fu_off, uval + inf.fu_off, udiag + inf.row_off,
+                                   inf.wu);
     const double zc = coarse ? s_zc : 0.0;
     if (mode == 0) {
         // restricted prolongation: owned rows only (src/precond/ras.h:64-68)
@@ -402,16 +461,23 @@ __global__ void __launch_bounds__(256) k_inv(int n, const double* __restrict__ L
 
 // r0[s] = c_s * sum of x over the owned rows of s
 template <class TI>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024)
 k_restrict(const int* __restrict__ owned_ptr, const int* __restrict__ owned,
            const double* __restrict__ cscale, const TI* __restrict__ x, double* r0,
            const int* __restrict__ active) {
     if (active && *active == 0) return;
-    __shared__ double red[8];
+    __shared__ double red[32];
     const int s = blockIdx.x;
-    double acc = 0.0;
-    for (int q = owned_ptr[s] + threadIdx.x; q < owned_ptr[s + 1]; q += blockDim.x)
-        acc += (double)x[owned[q]];
+    // four independent gathers in flight per thread, summed in a fixed order
+    TI a[4] = {(TI)0, (TI)0, (TI)0, (TI)0};
+    const int q0 = owned_ptr[s], q1 = owned_ptr[s + 1];
+    int q = q0 + threadIdx.x;
+    for (; q + 3 * (int)blockDim.x < q1; q += 4 * blockDim.x) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] += x[owned[q + u * blockDim.x]];
+    }
+    for (; q < q1; q += blockDim.x) a[0] += x[owned[q]];
+    double acc = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
     acc = warp_sum(acc);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
@@ -485,6 +551,17 @@ void factor_and_pack(sg_precond* pc) {
         pc->info.p, pc->lrp_d.p, pc->lci_d.p, pc->ldiag_d.p,
         reinterpret_cast<const TC*>(pc->perm_f.p), pc->lev_ptr_f.p, pc->lu_d.p);
     SG_CUDA(cudaGetLastError());
+    // level records for the TMA-fed sweep; the ELL slices below are built
+    // only for the fallback sweep (subdomains too large for the records)
+    rec_setup_device(pc);
+    if (pc->use_rec) return;
+    if (pc->wide_cols) {
+        pc->lcol.alloc((size_t)pc->fl_total * 2);
+        pc->ucol.alloc((size_t)pc->fu_total * 2);
+    } else {
+        pc->lcol.alloc((size_t)pc->fl_total);
+        pc->ucol.alloc((size_t)pc->fu_total);
+    }
     const size_t fl = (size_t)pc->fl_total, fu = (size_t)pc->fu_total, nr = (size_t)pc->total_rows;
     if (pc->opts.sweep_dtype == SG_FP64) {
         pc->lval64.alloc(fl); pc->uval64.alloc(fu); pc->udiag64.alloc(nr);
@@ -533,13 +610,9 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
                           pc->h_perm_f32.size() * 2, st);
         pc->perm_b.upload(reinterpret_cast<const uint16_t*>(pc->h_perm_b32.data()),
                           pc->h_perm_b32.size() * 2, st);
-        pc->lcol.alloc((size_t)pc->fl_total * 2);
-        pc->ucol.alloc((size_t)pc->fu_total * 2);
     } else {
         pc->perm_f.upload(pc->h_perm_f16, st);
         pc->perm_b.upload(pc->h_perm_b16, st);
-        pc->lcol.alloc((size_t)pc->fl_total);
-        pc->ucol.alloc((size_t)pc->fu_total);
     }
     const long long nz = (long long)pc->lci.size();
     pc->lu_d.alloc((size_t)nz);
@@ -547,7 +620,7 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
     SG_CUDA(cudaGetLastError());
     if (pc->wide_cols) factor_and_pack<int>(pc);
     else factor_and_pack<uint16_t>(pc);
-    if (!pc->use_smem) {
+    if (!pc->use_smem && !pc->use_rec) {
         const size_t cnt = (size_t)pc->total_rows + (size_t)pc->nparts;
         if (pc->opts.sweep_dtype == SG_FP64) pc->gscratch64.alloc(cnt);
         else pc->gscratch32.alloc(cnt);
@@ -590,7 +663,7 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
 
 // ---------------------------------------------------------------- apply
 template <class TI, class TO>
-void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active) {
+void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active, bool exact) {
     sg_ctx* ctx = pc->ctx;
     const int n = pc->n;
     const int grid = ctx->num_sms * 4;
@@ -614,12 +687,13 @@ void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active)
     if (coarse) {
         if (!pc->owned_ptr_d.p || !pc->owned_d.p || !pc->cscale_d.p || !pc->r0.p)
             fail(SG_ERR_INTERNAL, "coarse-space device buffers missing");
-        k_restrict<TI><<<pc->nc, 256, 0, ctx->stream>>>(pc->owned_ptr_d.p, pc->owned_d.p,
+        k_restrict<TI><<<pc->nc, 1024, 0, ctx->stream>>>(pc->owned_ptr_d.p, pc->owned_d.p,
                                                         pc->cscale_d.p, x, pc->r0.p, active);
         SG_CUDA(cudaGetLastError());
         count_launch(ctx);
     }
     if (asm_mode) SG_CUDA(cudaMemsetAsync(y, 0, sizeof(TO) * (size_t)n, ctx->stream));
+    if (sweep_tma<TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, exact, active)) return;
     if (pc->wide_cols) sweep_dispatch<int, TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, active);
     else sweep_dispatch<uint16_t, TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, active);
 }
@@ -638,8 +712,11 @@ void precond_read_coarse(sg_precond* pc, double* a0_out) {
     SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
 }
 
-template void precond_apply_device<double, double>(sg_precond*, const double*, double*, const int*);
-template void precond_apply_device<double, float>(sg_precond*, const double*, float*, const int*);
-template void precond_apply_device<float, float>(sg_precond*, const float*, float*, const int*);
+template void precond_apply_device<double, double>(sg_precond*, const double*, double*,
+                                                  const int*, bool);
+template void precond_apply_device<double, float>(sg_precond*, const double*, float*,
+                                                 const int*, bool);
+template void precond_apply_device<float, float>(sg_precond*, const float*, float*, const int*,
+                                                bool);
 
 }  // namespace sg

@@ -216,6 +216,42 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
     }
     const size_t elt = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
     pc->use_smem = (size_t)(max_n + 1) * elt <= 220u * 1024u;
+    // level records (TMA-fed sweep): rows padded to a multiple of 8 so every
+    // segment of a record (2-byte rows/columns, 2/4/8-byte values) is a
+    // multiple of 16 bytes and every record starts 16-byte aligned
+    {
+        const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
+                             : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
+        pc->h_rec_off_f.assign(pc->h_lev_ptr_f.size(), 0);
+        pc->h_rec_off_b.assign(pc->h_lev_ptr_b.size(), 0);
+        pc->h_rec_rows_f.assign(pc->h_lev_ptr_f.size(), 0);
+        pc->h_rec_rows_b.assign(pc->h_lev_ptr_b.size(), 0);
+        long long cur = 0, mx = 0;
+        for (int s = 0; s < nparts; ++s) {
+            const SubInfo& inf = pc->h_info[s];
+            for (int l = 0; l < inf.nlev_f; ++l) {
+                const int c = pc->h_lev_ptr_f[inf.lev_off_f + l + 1] - pc->h_lev_ptr_f[inf.lev_off_f + l];
+                const int cp = (c + 7) & ~7;
+                const long long bytes = (long long)cp * (2 + inf.wl * (2 + sf));
+                pc->h_rec_off_f[inf.lev_off_f + l] = cur;
+                pc->h_rec_rows_f[inf.lev_off_f + l] = cp;
+                cur += bytes;
+                mx = std::max(mx, bytes);
+            }
+            for (int l = 0; l < inf.nlev_b; ++l) {
+                const int c = pc->h_lev_ptr_b[inf.lev_off_b + l + 1] - pc->h_lev_ptr_b[inf.lev_off_b + l];
+                const int cp = (c + 7) & ~7;
+                const long long bytes = (long long)cp * (2 + inf.wu * (2 + sf) + sf);
+                pc->h_rec_off_b[inf.lev_off_b + l] = cur;
+                pc->h_rec_rows_b[inf.lev_off_b + l] = cp;
+                cur += bytes;
+                mx = std::max(mx, bytes);
+            }
+        }
+        pc->rec_total = cur;
+        pc->rec_stage_bytes = mx;
+        pc->use_rec = !pc->wide_cols && pc->use_smem && mx > 0;
+    }
     pc->h_cscale.resize(nparts);
     for (int s = 0; s < nparts; ++s) pc->h_cscale[s] = pc->h_info[s].cscale;
     // launch order: largest subdomains first

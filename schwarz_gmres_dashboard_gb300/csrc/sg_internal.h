@@ -150,8 +150,19 @@ struct sg_csr {
     sg::DBuf<int> rp, ci;
     sg::DBuf<double> val;
     sg::DBuf<float> val32;  // FP32 copy for the FP32 inner Krylov (made on demand)
-    sg::DBuf<float> diag32;
+    // SELL-C-sigma copy (C = 32, sigma = 1): slice s holds rows 32s..32s+31,
+    // entry k of its lane at sl_ptr[s] + 32k + lane, padded to the slice's
+    // longest row with (0, own row)
+    int nslices = 0;
+    long long sell_entries = 0;
+    bool sell_ok = false;  // padding small enough to keep the copy
+    int format = 0;        // 0 undecided, 1 CSR, 2 SELL (set by the autotuner)
+    sg::DBuf<long long> sl_ptr;
+    sg::DBuf<int> sl_w, sl_col;
+    sg::DBuf<double> sl_val;
+    sg::DBuf<float> sl_val32;
     void ensure_fp32();
+    void build_sell();
 };
 
 namespace sg {
@@ -193,6 +204,14 @@ struct sg_precond {
     int max_n = 0;
     long long total_rows = 0;
     bool use_smem = true;
+    // level records for the TMA-fed sweep: per level one 16-byte-aligned
+    // record [rows | columns | values (| diagonal)], rows padded to 8
+    bool use_rec = false;
+    int rec_depth = 0;               // ring stages in shared memory
+    long long rec_stage_bytes = 0;   // largest record
+    long long rec_total = 0;
+    std::vector<long long> h_rec_off_f, h_rec_off_b;  // byte offset per level
+    std::vector<int> h_rec_rows_f, h_rec_rows_b;      // padded rows per level
     // ---- device
     sg::DBuf<double> inv_diag;  // jacobi
     sg::DBuf<float> inv_diag32;
@@ -209,6 +228,10 @@ struct sg_precond {
     sg::DBuf<int> owned_d, owned_ptr_d, part_d;
     sg::DBuf<int> lrp_d, lci_d, ldiag_d, lmap_d;
     sg::DBuf<double> lu_d;  // FP64 factors in local CSR layout
+    sg::DBuf<long long> rec_off_f_d, rec_off_b_d;
+    sg::DBuf<int> rec_rows_f_d, rec_rows_b_d;
+    sg::DBuf<unsigned char> rec_d;
+    sg::DBuf<int> err_d;  // device error word of the sweeps (bounded waits)
     sg::DBuf<double> gscratch64;
     sg::DBuf<float> gscratch32;
     // ---- coarse space

@@ -47,7 +47,8 @@ struct Basis<float> {
 
 template <class TI, class TO>
 void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int* active) {
-    if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active);
+    // inside the solver FP64 sweeps may fuse multiply-adds (exact = false)
+    if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active, false);
     else launch_copy<TI, TO>(ctx, x, y, n, active);
 }
 
@@ -61,7 +62,6 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
     TV* V = Basis<TV>::V(w).p;
     TV* Z = flexible ? Basis<TV>::Z(w).p : nullptr;
     TV* t = Basis<TV>::T(w).p;
-    const TV* aval = Basis<TV>::vals(A);
     const int* active = &st->cycle_active;
     // r = b - A x is already in w->r64 (computed at the end of the previous
     // cycle, or before the first one) together with the convergence test.
@@ -74,13 +74,13 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
         TV* wj = V + (size_t)(j + 1) * ldv;
         if (!flexible) {
             // w = M^{-1} A v_j  (src/core/gmres.cpp:280-285)
-            launch_spmv<TV, TV, TV>(ctx, n, A->rp.p, A->ci.p, aval, vj, t, &st->vscale[j], active);
+            launch_spmv_a<TV, TV, TV>(ctx, A, vj, t, &st->vscale[j], active);
             apply_pc<TV, TV>(ctx, pc, t, wj, n, active);
         } else {
             // z_j = M^{-1} v_j ; w = A z_j  (src/core/fgmres.cpp:133-140)
             TV* zj = Z + (size_t)j * ldv;
             apply_pc<TV, TV>(ctx, pc, vj, zj, n, active);
-            launch_spmv<TV, TV, TV>(ctx, n, A->rp.p, A->ci.p, aval, zj, wj, &st->vscale[j], active);
+            launch_spmv_a<TV, TV, TV>(ctx, A, zj, wj, &st->vscale[j], active);
         }
         launch_cgs2<TV>(ctx, V, ldv, n, j, m, st, flexible);
     }
@@ -113,10 +113,15 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     const bool fp32 = prm.precision == SG_FP32;
     if (!ctx->work) ctx->work = new SolveWork();
     SolveWork* w = ctx->work;
-    const size_t ldv = ((size_t)n + 31) & ~(size_t)31;
+    // basis stride: a multiple of 32 elements plus 32, so consecutive basis
+    // vectors never sit a power of two apart (equal strides of 2^k bytes map
+    // every vector's element i to the same HBM channel)
+    const size_t ldv = (((size_t)n + 31) & ~(size_t)31) + 32;
     ensure(w->st, 1);
     ensure(w->r64, ldv);
     if (!w->h_st) SG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&w->h_st), sizeof(SolveState)));
+    // SpMV format: the faster of CSR and SELL on this matrix (same results)
+    spmv_autotune(ctx, const_cast<sg_csr*>(A));
     if (fp32) {
         const_cast<sg_csr*>(A)->ensure_fp32();
         ensure(w->V32, ldv * (m + 1));
@@ -213,6 +218,8 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
             SG_CUDA(cudaMemcpy(prm.history, ctx->hist.p, sizeof(double) * cnt,
                                cudaMemcpyDeviceToHost));
     }
+    if (pc && sweep_error(pc))
+        fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
     if (hs->nonfinite) fail(SG_ERR_NONFINITE, "non-finite value in the right-hand side or iteration");
 }
 

@@ -56,7 +56,7 @@ __device__ __forceinline__ void unpacki(const int4& v, int (&o)[4]) {
 
 // MODE 0: y = scale * (A x);  MODE 1: y = b - A x with ||y||^2 reduced.
 template <class TV, class TX, class TY, int MODE>
-__global__ void __launch_bounds__(SPMV_THREADS)
+__global__ void __launch_bounds__(SPMV_THREADS, 4)
 k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
            const TV* __restrict__ val, const TX* __restrict__ x, TY* __restrict__ y,
            const double* __restrict__ scale, const int* __restrict__ active,
@@ -139,6 +139,100 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
     }
 }
 
+// SELL-32 SpMV: a warp per slice of 32 rows, a lane per row; every load of
+// a step k is one contiguous 32-element segment.  Same per-row order and
+// rounding as the CSR kernel (padding adds exact zeros at the end of a row).
+template <class TV, class TX, class TY, int MODE>
+__global__ void __launch_bounds__(SPMV_THREADS, 4)
+k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* __restrict__ sw,
+            const int* __restrict__ col, const TV* __restrict__ val, const TX* __restrict__ x,
+            TY* __restrict__ y, const double* __restrict__ scale, const int* __restrict__ active,
+            const double* __restrict__ b, double* partials, unsigned* counter, SolveState* st) {
+    if (active && *active == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * SPMV_WARPS;
+    double ss = 0.0;
+    const TV sc = (MODE == 0 && scale) ? (TV)(*scale) : (TV)1;
+    for (int sl = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5); sl < nslices; sl += nwarps) {
+        const long long base = sptr[sl] + lane;
+        const int w = sw[sl];
+        TV sum = (TV)0;
+        int k = 0;
+        for (; k + 4 <= w; k += 4) {
+            TV v[4];
+            int c[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                v[q] = __ldg(&val[base + (long long)(k + q) * 32]);
+                c[q] = __ldg(&col[base + (long long)(k + q) * 32]);
+            }
+            TV p[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) p[q] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+#pragma unroll
+            for (int q = 0; q < 4; ++q) sum = padd(sum, p[q]);
+        }
+        for (; k < w; ++k) {
+            const TV v = __ldg(&val[base + (long long)k * 32]);
+            const int c = __ldg(&col[base + (long long)k * 32]);
+            sum = padd(sum, pmul(v, (TV)__ldg(&x[c])));
+        }
+        const int r = sl * 32 + lane;
+        if (r < n) {
+            if (MODE == 0) {
+                y[r] = (TY)(scale ? pmul(sum, sc) : sum);
+            } else {
+                const double rv = __dsub_rn(b[r], (double)sum);
+                y[r] = (TY)rv;
+                ss += rv * rv;
+            }
+        }
+    }
+    if (MODE == 1) {
+        __shared__ double red[SPMV_WARPS];
+        __shared__ double bs[1], tot[1];
+        double v1[1] = {ss};
+        block_sum_multi<1>(v1, 1, red, bs);
+        if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0) {
+            const double rn = sqrt(tot[0]);
+            st->rnorm = rn;
+            st->kcount = 0;
+            st->j = 0;
+            if (!isfinite(rn)) {
+                st->nonfinite = 1;
+                st->done = 1;
+                st->cycle_active = 0;
+            } else if (st->tol_kind != SG_TOL_REF_ABS && rn <= st->tol * st->bnorm) {
+                st->converged = 1;
+                st->done = 1;
+                st->cycle_active = 0;
+            } else {
+                st->cycle_active = st->done ? 0 : 1;
+            }
+        }
+    }
+}
+
+int sell_grid(sg_ctx* ctx, int nslices) {
+    long long blocks = ((long long)nslices + SPMV_WARPS - 1) / SPMV_WARPS;
+    const long long cap = (long long)ctx->num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    return blocks < 1 ? 1 : (int)blocks;
+}
+
+template <class TV>
+const TV* sell_vals(const sg_csr* A);
+template <>
+const double* sell_vals<double>(const sg_csr* A) { return A->sl_val.p; }
+template <>
+const float* sell_vals<float>(const sg_csr* A) { return A->sl_val32.p; }
+template <class TV>
+const TV* csr_vals(const sg_csr* A);
+template <>
+const double* csr_vals<double>(const sg_csr* A) { return A->val.p; }
+template <>
+const float* csr_vals<float>(const sg_csr* A) { return A->val32.p; }
+
 __global__ void k_bnorm(const double* __restrict__ v, int n, double* partials, unsigned* counter,
                         SolveState* st) {
     double ss = 0.0;
@@ -183,11 +277,65 @@ void launch_spmv(sg_ctx* ctx, int n, const int* rp, const int* ci, const TV* val
 
 void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double* x, double* r,
                      SolveState* st) {
-    k_spmv_csr<double, double, double, 1><<<spmv_grid(ctx, A->nrows), SPMV_THREADS, 0,
-                                            ctx->stream>>>(
-        A->nrows, A->rp.p, A->ci.p, A->val.p, x, r, nullptr, nullptr, b, ctx->partials.p, ctx->counter.p, st);
+    if (A->format == 2 && A->sell_ok) {
+        k_spmv_sell<double, double, double, 1><<<sell_grid(ctx, A->nslices), SPMV_THREADS, 0,
+                                                 ctx->stream>>>(
+            A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, A->sl_val.p, x, r, nullptr,
+            nullptr, b, ctx->partials.p, ctx->counter.p, st);
+    } else {
+        k_spmv_csr<double, double, double, 1><<<spmv_grid(ctx, A->nrows), SPMV_THREADS, 0,
+                                                ctx->stream>>>(
+            A->nrows, A->rp.p, A->ci.p, A->val.p, x, r, nullptr, nullptr, b, ctx->partials.p,
+            ctx->counter.p, st);
+    }
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
+}
+
+template <class TV, class TX, class TY>
+void launch_spmv_a(sg_ctx* ctx, const sg_csr* A, const TX* x, TY* y, const double* scale,
+                   const int* active) {
+    if (A->nrows <= 0) return;
+    if (A->format == 2 && A->sell_ok) {
+        k_spmv_sell<TV, TX, TY, 0><<<sell_grid(ctx, A->nslices), SPMV_THREADS, 0, ctx->stream>>>(
+            A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, sell_vals<TV>(A), x, y,
+            scale, active, nullptr, nullptr, nullptr, nullptr);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+    } else {
+        launch_spmv<TV, TX, TY>(ctx, A->nrows, A->rp.p, A->ci.p, csr_vals<TV>(A), x, y, scale,
+                                active);
+    }
+}
+
+void spmv_autotune(sg_ctx* ctx, sg_csr* A) {
+    if (A->format != 0) return;
+    if (!A->sell_ok || A->nrows < 4096) {
+        A->format = 1;
+        return;
+    }
+    DBuf<double> xb, yb;
+    xb.alloc(A->ncols);
+    yb.alloc(A->nrows);
+    xb.zero(ctx->stream);
+    double* x = xb.p;
+    double* y = yb.p;
+    cudaEvent_t e0, e1;
+    SG_CUDA(cudaEventCreate(&e0));
+    SG_CUDA(cudaEventCreate(&e1));
+    float best[3] = {0, 0, 0};
+    for (int f = 1; f <= 2; ++f) {
+        A->format = f;
+        launch_spmv_a<double, double, double>(ctx, A, x, y, nullptr, nullptr);  // warm
+        SG_CUDA(cudaEventRecord(e0, ctx->stream));
+        for (int i = 0; i < 5; ++i) launch_spmv_a<double, double, double>(ctx, A, x, y, nullptr, nullptr);
+        SG_CUDA(cudaEventRecord(e1, ctx->stream));
+        SG_CUDA(cudaEventSynchronize(e1));
+        SG_CUDA(cudaEventElapsedTime(&best[f], e0, e1));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    A->format = best[2] < best[1] ? 2 : 1;
 }
 
 void launch_bnorm(sg_ctx* ctx, const double* v, int n, SolveState* st) {
@@ -203,5 +351,9 @@ template void launch_spmv<double, double, double>(sg_ctx*, int, const int*, cons
 template void launch_spmv<float, float, float>(sg_ctx*, int, const int*, const int*,
                                                const float*, const float*, float*,
                                                const double*, const int*);
+template void launch_spmv_a<double, double, double>(sg_ctx*, const sg_csr*, const double*,
+                                                    double*, const double*, const int*);
+template void launch_spmv_a<float, float, float>(sg_ctx*, const sg_csr*, const float*, float*,
+                                                 const double*, const int*);
 
 }  // namespace sg

@@ -1,0 +1,449 @@
+// sweep.cu -- the batched ILU(0) subdomain solve fed by TMA bulk copies.
+//
+// One CTA owns one subdomain (RAS/ASM, src/precond/ras.h:45-70,
+// src/precond/asm.h:34-60).  The overlapped right-hand side is gathered into
+// shared memory (the restriction that replaces the reference's MPI halo
+// exchange), then the forward and backward sweeps of src/precond/ilu0.h:57-79
+// run level by level: rows of one level are independent and a __syncthreads
+// separates levels.
+//
+// A level's factor data is one contiguous, 16-byte-aligned record
+//   [row index u16 x C][column u16 x C x w][value x C x w](diagonal x C)
+// (C = rows rounded up to 8).  Thread 0 streams the records into a ring of D
+// shared-memory stages with cp.async.bulk, D levels ahead of the level being
+// computed, each stage tracked by an mbarrier (expect_tx / complete_tx).  So
+// a level costs shared-memory latency plus one barrier instead of a
+// global-memory round trip.  Every mbarrier wait is bounded (about one second
+// of clock cycles); on expiry the CTA records an error word, waits (bounded
+// again) for the copies it issued, and returns without touching the output.
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+namespace {
+
+constexpr int SW_T = 512;
+constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, "
+        "1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false when the phase did not complete within the budget
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long budget) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity))
+        if (clock64() - t0 > budget) return false;
+    return true;
+}
+
+template <class TS, bool EXACT>
+__device__ __forceinline__ TS sub_mul(TS acc, TS a, TS b);
+template <>
+__device__ __forceinline__ double sub_mul<double, true>(double acc, double a, double b) {
+    return __dsub_rn(acc, __dmul_rn(a, b));
+}
+template <>
+__device__ __forceinline__ double sub_mul<double, false>(double acc, double a, double b) {
+    return fma(-a, b, acc);
+}
+template <>
+__device__ __forceinline__ float sub_mul<float, true>(float acc, float a, float b) {
+    return fmaf(-a, b, acc);
+}
+template <>
+__device__ __forceinline__ float sub_mul<float, false>(float acc, float a, float b) {
+    return fmaf(-a, b, acc);
+}
+
+template <class TF>
+__device__ __forceinline__ TF to_factor(double v);
+template <>
+__device__ __forceinline__ double to_factor<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float to_factor<float>(double v) { return (float)v; }
+template <>
+__device__ __forceinline__ uint16_t to_factor<uint16_t>(double v) {
+    return __bfloat16_as_ushort(__float2bfloat16_rn((float)v));
+}
+
+// Factored local CSR (FP64, reference layout) -> level records of type TF.
+template <class TF>
+__global__ void __launch_bounds__(256)
+k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
+           const int* __restrict__ lci, const int* __restrict__ ldiag,
+           const double* __restrict__ lu, const uint16_t* __restrict__ perm_f,
+           const uint16_t* __restrict__ perm_b, const int* __restrict__ lev_f,
+           const int* __restrict__ lev_b, const long long* __restrict__ off_f,
+           const long long* __restrict__ off_b, const int* __restrict__ rows_f,
+           const int* __restrict__ rows_b, unsigned char* rec) {
+    const SubInfo inf = info[blockIdx.x];
+    const int* rp = lrp + inf.csr_row_off;
+    const int* ci = lci + inf.csr_nz_off;
+    const double* v = lu + inf.csr_nz_off;
+    const int* dg = ldiag + inf.row_off;
+    for (int l = 0; l < inf.nlev_f; ++l) {
+        const int p0 = lev_f[inf.lev_off_f + l], c = lev_f[inf.lev_off_f + l + 1] - p0;
+        const int C = rows_f[inf.lev_off_f + l];
+        unsigned char* R = rec + off_f[inf.lev_off_f + l];
+        uint16_t* rr = reinterpret_cast<uint16_t*>(R);
+        uint16_t* cc = rr + C;
+        TF* vv = reinterpret_cast<TF*>(cc + (size_t)C * inf.wl);
+        for (int q = threadIdx.x; q < C; q += blockDim.x) {
+            int k = 0;
+            if (q < c) {
+                const int r = perm_f[inf.row_off + p0 + q];
+                rr[q] = (uint16_t)r;
+                for (int e = rp[r]; e < rp[r + 1] && k < inf.wl; ++e) {
+                    const int col = ci[e];
+                    if (col >= r) break;
+                    cc[(size_t)k * C + q] = (uint16_t)col;
+                    vv[(size_t)k * C + q] = to_factor<TF>(v[e]);
+                    ++k;
+                }
+            } else {
+                rr[q] = 0;
+            }
+            for (; k < inf.wl; ++k) {
+                cc[(size_t)k * C + q] = (uint16_t)inf.n;
+                vv[(size_t)k * C + q] = to_factor<TF>(0.0);
+            }
+        }
+    }
+    for (int l = 0; l < inf.nlev_b; ++l) {
+        const int p0 = lev_b[inf.lev_off_b + l], c = lev_b[inf.lev_off_b + l + 1] - p0;
+        const int C = rows_b[inf.lev_off_b + l];
+        unsigned char* R = rec + off_b[inf.lev_off_b + l];
+        uint16_t* rr = reinterpret_cast<uint16_t*>(R);
+        uint16_t* cc = rr + C;
+        TF* vv = reinterpret_cast<TF*>(cc + (size_t)C * inf.wu);
+        TF* dd = vv + (size_t)C * inf.wu;
+        for (int q = threadIdx.x; q < C; q += blockDim.x) {
+            int k = 0;
+            if (q < c) {
+                const int r = perm_b[inf.row_off + p0 + q];
+                rr[q] = (uint16_t)r;
+                for (int e = dg[r] + 1; e < rp[r + 1] && k < inf.wu; ++e) {
+                    cc[(size_t)k * C + q] = (uint16_t)ci[e];
+                    vv[(size_t)k * C + q] = to_factor<TF>(v[e]);
+                    ++k;
+                }
+                dd[q] = to_factor<TF>(v[dg[r]]);
+            } else {
+                rr[q] = 0;
+                dd[q] = to_factor<TF>(1.0);
+            }
+            for (; k < inf.wu; ++k) {
+                cc[(size_t)k * C + q] = (uint16_t)inf.n;
+                vv[(size_t)k * C + q] = to_factor<TF>(0.0);
+            }
+        }
+    }
+}
+
+struct RecArgs {
+    const SubInfo* info;
+    const int* order;
+    const int* dofs;
+    const int* lev_f;
+    const int* lev_b;
+    const long long* off_f;
+    const long long* off_b;
+    const int* rows_f;
+    const int* rows_b;
+    const unsigned char* rec;
+    const int* ownloc;
+    const int* owned;
+    const double* a0inv;
+    const double* r0;
+    int nc;
+    int depth;
+    int stage_bytes;
+    int* err;
+};
+
+// mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
+template <class TI, class TO, class TS, class TF, bool EXACT>
+__global__ void __launch_bounds__(SW_T, 1)
+k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, int coarse,
+            const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __shared__ double s_red[SW_T / 32];
+    __shared__ double s_zc;
+    const int D = a.depth;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // D x 8 B
+    unsigned char* stages = smraw + 128;                               // D x stage_bytes
+    TS* t = reinterpret_cast<TS*>(stages + (size_t)D * a.stage_bytes);  // n + 1
+    const int s = a.order[blockIdx.x];
+    const SubInfo inf = a.info[s];
+    const int n = inf.n;
+    const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
+    const int sf = (int)sizeof(TF);
+
+    auto rec_of = [&](int g, const unsigned char*& src, uint32_t& bytes) {
+        if (g < nf) {
+            const int C = a.rows_f[inf.lev_off_f + g];
+            src = a.rec + a.off_f[inf.lev_off_f + g];
+            bytes = (uint32_t)C * (uint32_t)(2 + inf.wl * (2 + sf));
+        } else {
+            const int l = g - nf;
+            const int C = a.rows_b[inf.lev_off_b + l];
+            src = a.rec + a.off_b[inf.lev_off_b + l];
+            bytes = (uint32_t)C * (uint32_t)(2 + inf.wu * (2 + sf) + sf);
+        }
+    };
+    auto issue = [&](int g) {
+        const unsigned char* src;
+        uint32_t bytes;
+        rec_of(g, src, bytes);
+        const int st = g % D;
+        const uint32_t bar = smem_u32(&bars[st]);
+        mbar_expect_tx(bar, bytes);
+        bulk_g2s(smem_u32(stages + (size_t)st * a.stage_bytes), src, bytes, bar);
+    };
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < D; ++i) mbar_init(smem_u32(&bars[i]), 1);
+        fence_mbar_init();
+        fence_proxy_async();
+        const int pre = T < D ? T : D;
+        for (int g = 0; g < pre; ++g) issue(g);
+    }
+    // gather while the first records are in flight
+    const int* dof = a.dofs + inf.row_off;
+    for (int li = threadIdx.x; li < n; li += blockDim.x) t[li] = Load<TS>::f(x[dof[li]]);
+    if (threadIdx.x == 0) t[n] = (TS)0;
+    if (coarse) {
+        double acc = 0.0;
+        const double* row = a.a0inv + (size_t)s * a.nc;
+        for (int q = threadIdx.x; q < a.nc; q += blockDim.x) acc += row[q] * a.r0[q];
+        acc = warp_sum(acc);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double z = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) z += s_red[w];
+            s_zc = inf.cscale * z;
+        }
+    }
+    __syncthreads();
+
+    for (int g = 0; g < T; ++g) {
+        const int st = g % D;
+        // every thread observes the phase itself (acquires the bulk copy)
+        const bool ok = mbar_wait(smem_u32(&bars[st]), (uint32_t)((g / D) & 1), WAIT_CYCLES);
+        if (__syncthreads_or(!ok)) {
+            // a record never arrived: report, drain what was issued, leave y alone
+            if (threadIdx.x == 0) {
+                atomicExch(a.err, 1);
+                const int last = (g + D < T ? g + D : T);
+                for (int h = g + 1; h < last; ++h)
+                    mbar_wait(smem_u32(&bars[h % D]), (uint32_t)((h / D) & 1), WAIT_CYCLES / 8);
+            }
+            return;
+        }
+        const unsigned char* R = stages + (size_t)st * a.stage_bytes;
+        const bool back = g >= nf;
+        const int l = back ? g - nf : g;
+        const int* lp = back ? a.lev_b + inf.lev_off_b : a.lev_f + inf.lev_off_f;
+        const int c = lp[l + 1] - lp[l];
+        const int C = back ? a.rows_b[inf.lev_off_b + l] : a.rows_f[inf.lev_off_f + l];
+        const int w = back ? inf.wu : inf.wl;
+        const uint16_t* rr = reinterpret_cast<const uint16_t*>(R);
+        const uint16_t* cc = rr + C;
+        const TF* vv = reinterpret_cast<const TF*>(cc + (size_t)C * w);
+        for (int q = threadIdx.x; q < c; q += blockDim.x) {
+            const int r = rr[q];
+            TS acc = t[r];
+            for (int k = 0; k < w; ++k)
+                acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vv[(size_t)k * C + q]),
+                                         t[cc[(size_t)k * C + q]]);
+            if (back) acc = acc / Load<TS>::f(vv[(size_t)w * C + q]);
+            t[r] = acc;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && g + D < T) {
+            fence_proxy_async();
+            issue(g + D);
+        }
+    }
+
+    const double zc = coarse ? s_zc : 0.0;
+    if (mode == 0) {
+        const int* ol = a.ownloc + inf.own_off;
+        const int* og = a.owned + inf.own_off;
+        for (int q = threadIdx.x; q < inf.n_own; q += blockDim.x) {
+            const int li = ol[q];
+            if (coarse) y[og[q]] = Store<TO>::f(__dadd_rn((double)t[li], zc));
+            else y[og[q]] = Store<TO>::f(t[li]);
+        }
+    } else {
+        for (int li = threadIdx.x; li < n; li += blockDim.x)
+            atomicAdd(&y[dof[li]], Store<TO>::f(t[li]));
+        if (coarse) {
+            const int* og = a.owned + inf.own_off;
+            for (int q = threadIdx.x; q < inf.n_own; q += blockDim.x)
+                atomicAdd(&y[og[q]], Store<TO>::f(zc));
+        }
+    }
+}
+
+RecArgs rec_args(sg_precond* pc) {
+    RecArgs a;
+    a.info = pc->info.p;
+    a.order = pc->order.p;
+    a.dofs = pc->dofs.p;
+    a.lev_f = pc->lev_ptr_f.p;
+    a.lev_b = pc->lev_ptr_b.p;
+    a.off_f = pc->rec_off_f_d.p;
+    a.off_b = pc->rec_off_b_d.p;
+    a.rows_f = pc->rec_rows_f_d.p;
+    a.rows_b = pc->rec_rows_b_d.p;
+    a.rec = pc->rec_d.p;
+    a.ownloc = pc->ownloc_d.p;
+    a.owned = pc->owned_d.p;
+    a.a0inv = pc->a0inv.p;
+    a.r0 = pc->r0.p;
+    a.nc = pc->nc;
+    a.depth = pc->rec_depth;
+    a.stage_bytes = (int)pc->rec_stage_bytes;
+    a.err = pc->err_d.p;
+    return a;
+}
+
+size_t sweep_smem(const sg_precond* pc, int depth) {
+    const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
+    return 128 + (size_t)depth * (size_t)pc->rec_stage_bytes + (size_t)(pc->max_n + 1) * ts;
+}
+
+template <class TI, class TO, class TS, class TF, bool EXACT>
+void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active) {
+    const size_t smem = sweep_smem(pc, pc->rec_depth);
+    SG_CUDA(cudaFuncSetAttribute(k_sweep_tma<TI, TO, TS, TF, EXACT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sweep_tma<TI, TO, TS, TF, EXACT><<<pc->nparts, SW_T, smem, pc->ctx->stream>>>(
+        rec_args(pc), x, y, mode, coarse ? 1 : 0, active);
+    SG_CUDA(cudaGetLastError());
+    count_launch(pc->ctx);
+}
+
+}  // namespace
+
+// Packs the level records of the configured factor type and picks the ring
+// depth: as deep as fits while as many subdomains as possible run at once.
+void rec_setup_device(sg_precond* pc) {
+    if (!pc->use_rec) return;
+    sg_ctx* ctx = pc->ctx;
+    cudaStream_t st = ctx->stream;
+    if (pc->rec_stage_bytes % 16 != 0 || pc->rec_total % 16 != 0)
+        fail(SG_ERR_INTERNAL, "level records are not 16-byte multiples");
+    int max_smem = 0;
+    SG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                   ctx->device));
+    int sm_smem = 0;
+    SG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                   ctx->device));
+    const int static_smem = 1024;  // reduction scratch and the like
+    // CTAs per SM needed to keep every subdomain resident at once
+    const int want = (pc->nparts + ctx->num_sms - 1) / ctx->num_sms;
+    int depth = 0;
+    for (int per_sm = want < 1 ? 1 : want; per_sm >= 1 && depth == 0; --per_sm) {
+        const long long budget = (long long)sm_smem / per_sm - static_smem - 1024;
+        for (int d : {8, 6, 4, 3, 2}) {
+            const long long need = (long long)sweep_smem(pc, d);
+            if (need <= budget && need <= max_smem - static_smem) {
+                depth = d;
+                break;
+            }
+        }
+    }
+    // an mbarrier transaction count stays below 2^20 bytes
+    if (depth == 0 || pc->rec_stage_bytes >= (1 << 20) || (pc->opts.reserved[0] & 1)) {
+        pc->use_rec = false;
+        return;
+    }
+    pc->rec_depth = depth;
+    pc->rec_off_f_d.upload(pc->h_rec_off_f, st);
+    pc->rec_off_b_d.upload(pc->h_rec_off_b, st);
+    pc->rec_rows_f_d.upload(pc->h_rec_rows_f, st);
+    pc->rec_rows_b_d.upload(pc->h_rec_rows_b, st);
+    pc->rec_d.alloc((size_t)pc->rec_total);
+    pc->err_d.alloc(1);
+    pc->err_d.zero(st);
+    const uint16_t* pf = pc->perm_f.p;
+    const uint16_t* pb = pc->perm_b.p;
+#define SG_PACK(TF)                                                                        \
+    k_pack_rec<TF><<<pc->nparts, 256, 0, st>>>(                                            \
+        pc->info.p, pc->lrp_d.p, pc->lci_d.p, pc->ldiag_d.p, pc->lu_d.p, pf, pb,            \
+        pc->lev_ptr_f.p, pc->lev_ptr_b.p, pc->rec_off_f_d.p, pc->rec_off_b_d.p,             \
+        pc->rec_rows_f_d.p, pc->rec_rows_b_d.p, pc->rec_d.p)
+    if (pc->opts.sweep_dtype == SG_FP64) SG_PACK(double);
+    else if (pc->opts.factor_dtype == SG_BF16) SG_PACK(uint16_t);
+    else SG_PACK(float);
+#undef SG_PACK
+    SG_CUDA(cudaGetLastError());
+}
+
+template <class TI, class TO>
+bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
+               const int* active) {
+    if (!pc->use_rec || pc->rec_depth == 0) return false;
+    if (pc->opts.sweep_dtype == SG_FP64) {
+        if (exact) launch_tma<TI, TO, double, double, true>(pc, x, y, mode, coarse, active);
+        else launch_tma<TI, TO, double, double, false>(pc, x, y, mode, coarse, active);
+    } else if (pc->opts.factor_dtype == SG_BF16) {
+        launch_tma<TI, TO, float, uint16_t, false>(pc, x, y, mode, coarse, active);
+    } else {
+        launch_tma<TI, TO, float, float, false>(pc, x, y, mode, coarse, active);
+    }
+    return true;
+}
+
+int sweep_error(sg_precond* pc) {
+    if (!pc->err_d.p) return 0;
+    int e = 0;
+    SG_CUDA(cudaMemcpyAsync(&e, pc->err_d.p, sizeof(int), cudaMemcpyDeviceToHost, pc->ctx->stream));
+    SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
+    return e;
+}
+
+template bool sweep_tma<double, double>(sg_precond*, const double*, double*, int, bool, bool,
+                                        const int*);
+template bool sweep_tma<double, float>(sg_precond*, const double*, float*, int, bool, bool,
+                                       const int*);
+template bool sweep_tma<float, float>(sg_precond*, const float*, float*, int, bool, bool,
+                                      const int*);
+
+}  // namespace sg

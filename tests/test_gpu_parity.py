@@ -28,19 +28,20 @@ def to_sg(sg, A):
     return sg.CSRMatrix(A.nrows, A.ncols, A.row_ptr, A.col_idx, A.vals)
 
 
-def make_pc(sg, kind, nparts, overlap, part, fdt=None, sdt=None):
+def make_pc(sg, kind, nparts, overlap, part, fdt=None, sdt=None, generic=False):
     fdt = sg.FP64 if fdt is None else fdt
     sdt = sg.FP64 if sdt is None else sdt
+    kw = {"generic_sweep": generic}
     if kind == "jacobi":
-        return sg.JacobiPrecond(sweep_dtype=sdt)
+        return sg.JacobiPrecond(sweep_dtype=sdt, **kw)
     if kind == "ilu0":
-        return sg.ILU0Precond(factor_dtype=fdt, sweep_dtype=sdt)
+        return sg.ILU0Precond(factor_dtype=fdt, sweep_dtype=sdt, **kw)
     if kind == "asm":
-        return sg.ASMPrecond(nparts, overlap, part, fdt, sdt)
+        return sg.ASMPrecond(nparts, overlap, part, fdt, sdt, **kw)
     if kind == "ras":
-        return sg.RASPrecond(nparts, overlap, part, fdt, sdt)
+        return sg.RASPrecond(nparts, overlap, part, fdt, sdt, **kw)
     ft = sg.FineLevelType.ASM if kind == "twolevel_asm" else sg.FineLevelType.RAS
-    return sg.TwoLevelSchwarzPrecond(nparts, overlap, ft, part, fdt, sdt)
+    return sg.TwoLevelSchwarzPrecond(nparts, overlap, ft, part, fdt, sdt, **kw)
 
 
 def rel(a, b):
@@ -68,8 +69,9 @@ def _irregular(n, seed):
     return HostCSR(rp, ci, v)
 
 
+@pytest.mark.parametrize("fmt", [1, 2])
 @pytest.mark.parametrize("maker", ["p3d", "varcoef", "irregular", "tiny"])
-def test_spmv_matches_oracle(sg, oracle, maker):
+def test_spmv_matches_oracle(sg, oracle, maker, fmt):
     if maker == "p3d":
         A = sg.make_poisson_3d(40, 37, 23)
     elif maker == "varcoef":
@@ -81,7 +83,29 @@ def test_spmv_matches_oracle(sg, oracle, maker):
         A = sg.make_poisson_2d(1, 3)
     x = sg.uniform(A.ncols, seed=11)
     H = HostCSR(A.row_ptr, A.col_idx, A.vals)
+    try:
+        A.format = fmt
+    except sg.SgError as e:  # no SELL copy (padding too large): CSR only
+        assert fmt == 2 and e.status == 8
+        return
     assert np.array_equal(A.spmv(x), oracle.spmv(H, x))
+
+
+@pytest.mark.parametrize("fmt", [1, 2])
+def test_solve_same_bits_in_both_formats(sg, fmt):
+    """The SpMV storage is a pure performance choice: FP64 solves give the
+    same bits whichever format runs."""
+    A = sg.make_poisson_3d(30, 30, 30)
+    b = A.spmv(sg.uniform(A.nrows, seed=3))
+    pc = sg.RASPrecond(8, 1)
+    pc.setup(A)
+    out = []
+    for f in (1, fmt):
+        A.format = f
+        x = np.zeros(A.nrows)
+        sg.gmres(A, b, x, pc, sg.GMRESParams(restart=30, max_iter=500, tol=1e-10))
+        out.append(x)
+    assert np.array_equal(out[0], out[1])
 
 
 def test_spmv_device_pointers(sg):
@@ -163,6 +187,27 @@ def test_apply_low_precision(sg, oracle, kind, dt):
     y = pc.apply(x)
     ref = oracle.precond(kind, H, 8, 1, part).apply(x)
     assert rel(y, ref) <= (1e-5 if dt == "fp32" else 2e-2)
+
+
+@pytest.mark.parametrize("kind", ["ilu0", "asm", "ras", "twolevel_ras"])
+@pytest.mark.parametrize("dt", ["fp64", "fp32", "bf16"])
+def test_generic_and_tma_sweeps_agree(sg, kind, dt):
+    """The TMA-fed sweep and the generic level sweep compute the same thing
+    (bit-exact in FP64; FP32/BF16 up to the atomic order of ASM)."""
+    A = sg.make_varcoef_3d(20, 22, 18, 1.0, 5.0, 4)
+    part = sg.partition_boxes(20, 22, 18, 12, 0.1, 2)
+    x = sg.uniform(A.nrows, seed=9)
+    fdt = {"fp64": sg.FP64, "fp32": sg.FP32, "bf16": sg.BF16}[dt]
+    sdt = sg.FP64 if dt == "fp64" else sg.FP32
+    ys = []
+    for generic in (False, True):
+        pc = make_pc(sg, kind, 12, 1, part, fdt, sdt, generic=generic)
+        pc.setup(A)
+        ys.append(pc.apply(x))
+    if kind == "asm":
+        assert rel(ys[0], ys[1]) <= 1e-6
+    else:
+        assert np.array_equal(ys[0], ys[1])
 
 
 def test_apply_large_subdomains_and_many_parts(sg, oracle):
