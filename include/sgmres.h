@@ -67,8 +67,10 @@ typedef struct sg_precond_opts {
     const int* partition; /* optional host array [n] of part ids in [0,nparts);
                              NULL = built-in graph partitioner. Takes the place
                              of METIS_PartGraphKway (src/decomp/domain_decomp.h:23-58) */
-    int reserved[8];  /* reserved[0] bit 0: use the generic level sweep instead of
-                         the TMA-fed one (testing); other entries must be 0 */
+    int reserved[8];  /* reserved[0]: sweep variant (testing/comparison): 0 the
+                         TMA-fed level sweep, 1 a level sweep reading factors
+                         from global memory, 4 the sync-free sweep (per-row
+                         ready flags); other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;
@@ -91,6 +93,14 @@ sg_status sg_ctx_synchronize(sg_ctx* ctx);
 /* Kernels launched through this context so far (a CUDA-graph launch adds
  * the kernel nodes it replays).  No counterpart in the reference. */
 sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count);
+/* Kernel-class timers: with timing on, solves that run without a CUDA graph
+ * record a CUDA event pair on the context stream around every kernel class:
+ * kind 0 Krylov SpMV, 1 FP64 residual, 2 preconditioner, 3 orthogonalisation
+ * (CGS2 passes, Givens), 4 back-solve and update.  get_timing returns the
+ * accumulated milliseconds and the number of timed launches of a kind.
+ * Turning timing on resets the sums.  No counterpart in the reference. */
+sg_status sg_ctx_set_timing(sg_ctx* ctx, int on);
+sg_status sg_ctx_get_timing(sg_ctx* ctx, int kind, double* ms, long long* count);
 
 /* ---- matrix ----------------------------------------------------------- */
 /* Copies a CSR matrix to the device (CSRMatrix, src/core/sparse_matrix.h:13-28;
@@ -187,6 +197,18 @@ typedef struct sg_solve_result {
 sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* pc,
                    const double* b, double* x, int n, sg_mem mem,
                    const sg_solve_params* params, sg_solve_result* result);
+
+/* ---- BLAS-1 (src/core/vector.h:11-44) --------------------------------- */
+/* dot (vector.h:11-16), FP64, deterministic order (block partial sums added
+ * in block order); the value is returned to the host in *result. */
+sg_status sg_dot(sg_ctx* ctx, const double* x, const double* y, int n, sg_mem mem,
+                 double* result);
+/* norm2 (vector.h:23-25) = sqrt(dot(x, x)) */
+sg_status sg_norm2(sg_ctx* ctx, const double* x, int n, sg_mem mem, double* result);
+/* axpy y += alpha x (vector.h:31-34), same bits as the reference loop */
+sg_status sg_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n, sg_mem mem);
+/* scale x *= alpha (vector.h:40-44), same bits as the reference loop */
+sg_status sg_scale(sg_ctx* ctx, double alpha, double* x, int n, sg_mem mem);
 
 /* ---- problem generators and partitions (host side, deterministic) ----- */
 /* make_poisson_2d / make_poisson_3d (src/mesh/poisson.h:10-74).  Call with

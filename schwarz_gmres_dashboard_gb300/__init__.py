@@ -31,7 +31,7 @@ _clib = L.load()
 __all__ = [
     "SgError", "Context", "default_context", "CSRMatrix", "make_identity", "make_poisson_2d",
     "make_poisson_3d", "make_varcoef_3d", "uniform", "partition_graph", "partition_boxes",
-    "schwarz_structure",
+    "schwarz_structure", "dot", "norm2", "axpy", "scale",
     "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
     "TwoLevelSchwarzPrecond", "FineLevelType", "GMRESParams", "GMRESResult", "gmres", "fgmres",
     "FP64", "FP32", "BF16", "TOL_REF_ABS", "TOL_TRUE_REL_CYCLE", "TOL_TRUE_REL",
@@ -66,6 +66,20 @@ class Context:
 
     def synchronize(self) -> None:
         _check(_clib.sg_ctx_synchronize(self.handle))
+
+    TIMER_KINDS = ("spmv", "residual", "precond", "ortho", "update")
+
+    def set_timing(self, on: bool) -> None:
+        """Kernel-class CUDA-event timers for solves run without a graph."""
+        _check(_clib.sg_ctx_set_timing(self.handle, 1 if on else 0))
+
+    def timing(self) -> dict:
+        out = {}
+        for k, nm in enumerate(self.TIMER_KINDS):
+            ms, cnt = C.c_double(0.0), C.c_longlong(0)
+            _check(_clib.sg_ctx_get_timing(self.handle, k, C.byref(ms), C.byref(cnt)))
+            out[nm] = (ms.value, int(cnt.value))
+        return out
 
     @property
     def launch_count(self) -> int:
@@ -278,6 +292,51 @@ def schwarz_structure(A: CSRMatrix, part, nparts: int, overlap: int) -> dict:
     return out
 
 
+# ---------------------------------------------------------------- BLAS-1
+def dot(a, b, ctx: Context | None = None) -> float:
+    """dot (src/core/vector.h:11-16) on the GPU, FP64, deterministic order."""
+    ctx = ctx or default_context()
+    n = len(a) if not hasattr(a, "__cuda_array_interface__") else a.__cuda_array_interface__["shape"][0]
+    pa, ma, _ka = _vec(a, n)
+    pb, mb, _kb = _vec(b, n)
+    if ma != mb:
+        raise TypeError("a and b must both be host or both be device arrays")
+    out = C.c_double(0.0)
+    _check(_clib.sg_dot(ctx.handle, pa, pb, n, ma, C.byref(out)))
+    return out.value
+
+
+def norm2(a, ctx: Context | None = None) -> float:
+    """norm2 (src/core/vector.h:23-25)."""
+    ctx = ctx or default_context()
+    n = len(a) if not hasattr(a, "__cuda_array_interface__") else a.__cuda_array_interface__["shape"][0]
+    pa, ma, _ka = _vec(a, n)
+    out = C.c_double(0.0)
+    _check(_clib.sg_norm2(ctx.handle, pa, n, ma, C.byref(out)))
+    return out.value
+
+
+def axpy(alpha: float, x, y, ctx: Context | None = None):
+    """y += alpha x in place (src/core/vector.h:31-34)."""
+    ctx = ctx or default_context()
+    n = len(y) if not hasattr(y, "__cuda_array_interface__") else y.__cuda_array_interface__["shape"][0]
+    px, mx, _kx = _vec(x, n)
+    py, my, _ky = _vec(y, n, writable=True)
+    if mx != my:
+        raise TypeError("x and y must both be host or both be device arrays")
+    _check(_clib.sg_axpy(ctx.handle, C.c_double(alpha), px, py, n, my))
+    return y
+
+
+def scale(alpha: float, x, ctx: Context | None = None):
+    """x *= alpha in place (src/core/vector.h:40-44)."""
+    ctx = ctx or default_context()
+    n = len(x) if not hasattr(x, "__cuda_array_interface__") else x.__cuda_array_interface__["shape"][0]
+    px, mx, _kx = _vec(x, n, writable=True)
+    _check(_clib.sg_scale(ctx.handle, C.c_double(alpha), px, n, mx))
+    return x
+
+
 # ---------------------------------------------------------------- preconditioners
 class FineLevelType(enum.Enum):
     """src/precond/two_level_schwarz.h:21"""
@@ -293,9 +352,13 @@ class Preconditioner:
 
     def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
-                 ctx: Context | None = None, generic_sweep: bool = False):
-        # generic_sweep: level sweep without the TMA record ring (testing)
-        self.generic_sweep = bool(generic_sweep)
+                 ctx: Context | None = None, generic_sweep: bool = False,
+                 sweep: str = "tma"):
+        # sweep variant (testing/comparison): "tma" (default: TMA-fed level
+        # records), "level" (factors read from global memory), "syncfree"
+        if generic_sweep:
+            sweep = "level"
+        self.sweep = sweep
         self.ctx = ctx or default_context()
         self.nparts = int(nparts)
         self.overlap = int(overlap)
@@ -308,7 +371,7 @@ class Preconditioner:
         opts.factor_dtype = factor_dtype
         opts.sweep_dtype = sweep_dtype
         opts.partition = self.partition.ctypes.data if self.partition is not None else None
-        opts.reserved[0] = 1 if self.generic_sweep else 0
+        opts.reserved[0] = {"tma": 0, "level": 1, "syncfree": 4}[self.sweep]
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),

@@ -67,6 +67,8 @@ PROTOTYPES = {
     "sg_ctx_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "sg_ctx_synchronize": (C.c_int, [_vp]),
     "sg_ctx_get_launch_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "sg_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
+    "sg_ctx_get_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "sg_csr_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int,
                                 C.POINTER(_vp)]),
     "sg_csr_destroy": (C.c_int, [_vp]),
@@ -82,6 +84,10 @@ PROTOTYPES = {
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "sg_solve": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int,
                            C.POINTER(SolveParams), C.POINTER(SolveResult)]),
+    "sg_dot": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, _dp]),
+    "sg_norm2": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _dp]),
+    "sg_axpy": (C.c_int, [_vp, C.c_double, _vp, _vp, C.c_int, C.c_int]),
+    "sg_scale": (C.c_int, [_vp, C.c_double, _vp, C.c_int, C.c_int]),
     "sg_gen_poisson2d": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _ip]),
     "sg_gen_poisson3d": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _ip]),
     "sg_gen_varcoef3d": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,

@@ -3,6 +3,7 @@
 // stream, and turns internal failures into an sg_status plus a thread-local
 // message.
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstring>
 #include <exception>
@@ -182,6 +183,9 @@ sg_status sg_ctx_destroy(sg_ctx* ctx) {
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
         delete ctx->work;
         ctx->work = nullptr;
+        collect_timers(ctx);
+        for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+        ctx->ev_pool.clear();
         ctx->partials.release();
         ctx->counter.release();
         ctx->hist.release();
@@ -210,6 +214,29 @@ sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count) {
     return guard([&] {
         SG_CHECK_ARG(ctx && count, "NULL argument");
         *count = ctx->launches;
+    });
+}
+
+sg_status sg_ctx_set_timing(sg_ctx* ctx, int on) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx, "ctx is NULL");
+        ctx->timing = on != 0;
+        for (int k = 0; k < 8; ++k) {
+            ctx->class_ms[k] = 0.0;
+            ctx->class_count[k] = 0;
+        }
+    });
+}
+
+sg_status sg_ctx_get_timing(sg_ctx* ctx, int kind, double* ms, long long* count) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && ms && count, "NULL argument");
+        SG_CHECK_ARG(kind >= 0 && kind < 8, "kind must be in [0,8)");
+        use_device(ctx);
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        collect_timers(ctx);
+        *ms = ctx->class_ms[kind];
+        *count = ctx->class_count[kind];
     });
 }
 
@@ -290,6 +317,8 @@ sg_status sg_csr_set_format(sg_csr* A, int format) {
         if (format == 2 && !A->sell_ok)
             fail(SG_ERR_UNSUPPORTED, "no SELL copy of this matrix (unsorted rows or padding > 25%%)");
         A->format = format;
+        A->format32 = format;
+        A->format_user = format != 0;
     });
 }
 
@@ -550,6 +579,82 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
             }
         } cb{ctx, x, dx, n, mem == SG_MEM_HOST};
         solve_device(ctx, solver, A, pc, db, dx, prm, result);
+    });
+}
+
+// ------------------------------------------------------------------ BLAS-1
+namespace {
+// host or device vector -> device pointer (host data staged in ctx buffers)
+struct Staged {
+    sg::DBuf<double> buf;
+    const double* ptr(sg_ctx* ctx, const double* v, int n, sg_mem mem) {
+        if (mem == SG_MEM_DEVICE) return v;
+        buf.upload(v, (size_t)n, ctx->stream);
+        return buf.p;
+    }
+};
+void check_vec_args(sg_ctx* ctx, int n, sg_mem mem) {
+    SG_CHECK_ARG(ctx, "ctx is NULL");
+    SG_CHECK_ARG(n >= 0, "n must be >= 0");
+    SG_CHECK_ARG(mem == SG_MEM_HOST || mem == SG_MEM_DEVICE, "bad memory kind");
+}
+}  // namespace
+
+sg_status sg_dot(sg_ctx* ctx, const double* x, const double* y, int n, sg_mem mem,
+                 double* result) {
+    return guard([&] {
+        check_vec_args(ctx, n, mem);
+        SG_CHECK_ARG(result && (n == 0 || (x && y)), "NULL argument");
+        use_device(ctx);
+        Staged sx, sy;
+        const double* dx = sx.ptr(ctx, x, n, mem);
+        const double* dy = x == y ? dx : sy.ptr(ctx, y, n, mem);
+        DBuf<double> out;
+        out.alloc(1);
+        out.zero(ctx->stream);
+        if (n > 0) launch_dot(ctx, dx, dy, n, out.p);
+        SG_CUDA(cudaMemcpyAsync(result, out.p, sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+sg_status sg_norm2(sg_ctx* ctx, const double* x, int n, sg_mem mem, double* result) {
+    sg_status st = sg_dot(ctx, x, x, n, mem, result);
+    if (st == SG_OK) *result = std::sqrt(*result);
+    return st;
+}
+
+sg_status sg_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n, sg_mem mem) {
+    return guard([&] {
+        check_vec_args(ctx, n, mem);
+        SG_CHECK_ARG(n == 0 || (x && y), "NULL argument");
+        use_device(ctx);
+        if (n == 0) return;
+        Staged sx, sy;
+        const double* dx = sx.ptr(ctx, x, n, mem);
+        double* dy = const_cast<double*>(sy.ptr(ctx, y, n, mem));
+        launch_axpy(ctx, alpha, dx, dy, n);
+        if (mem == SG_MEM_HOST)
+            SG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+sg_status sg_scale(sg_ctx* ctx, double alpha, double* x, int n, sg_mem mem) {
+    return guard([&] {
+        check_vec_args(ctx, n, mem);
+        SG_CHECK_ARG(n == 0 || x, "NULL argument");
+        use_device(ctx);
+        if (n == 0) return;
+        Staged sx;
+        double* dx = const_cast<double*>(sx.ptr(ctx, x, n, mem));
+        launch_scale(ctx, alpha, dx, n);
+        if (mem == SG_MEM_HOST)
+            SG_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
     });
 }
 

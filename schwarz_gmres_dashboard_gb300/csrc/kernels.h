@@ -44,6 +44,11 @@ void launch_update_x(sg_ctx* ctx, const TV* basis, size_t ldv, int n, double* x,
 // y = x with type conversion (no preconditioner)
 template <class TI, class TO>
 void launch_copy(sg_ctx* ctx, const TI* x, TO* y, int n, const int* active);
+// BLAS-1 (src/core/vector.h): dot into device memory, axpy, scale
+void launch_dot(sg_ctx* ctx, const double* x, const double* y, int n, double* out_dev);
+void launch_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n);
+void launch_scale(sg_ctx* ctx, double alpha, double* x, int n);
+int dot_grid(int num_sms, int n);
 // cycle bookkeeping after the update: cycles++, out-of-iterations test
 void launch_cycle_end(sg_ctx* ctx, SolveState* st);
 

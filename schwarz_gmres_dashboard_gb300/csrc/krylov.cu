@@ -133,40 +133,71 @@ __device__ __forceinline__ void vstore<float>(float* p, const float (&o)[4]) {
     *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// ---- pass A (and generic second dots): s_k = raw_{k0+k} . w for k < kc
-template <class TV, int KMAX>
+// ---- pass A (and generic second dots): s_k = raw_{k0+k} . w for k < kc.
+// The kc <= 32 vectors are split over the 8 warps of a block (vector k is
+// handled by warp k % 8), so a thread keeps at most 4 accumulators; a row
+// tile is 32 lanes x one 16-byte vector of elements.
+constexpr int KW = KT / 32;  // warps per block
+constexpr int KPW = 4;       // basis vectors per warp
+
+template <class TV>
+__device__ __forceinline__ TV dotv(const TV (&a)[Vec<TV>::N], const TV (&b)[Vec<TV>::N]) {
+    TV s = (TV)0;
+#pragma unroll
+    for (int e = 0; e < Vec<TV>::N; ++e) s += a[e] * b[e];
+    return s;
+}
+
+// per-warp accumulators -> block sums bs[k] (k < kc), fixed order
+template <class TV>
+__device__ __forceinline__ void warp_split_sums(const TV (&acc)[KPW], int kc, double* bs) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < KPW; ++q) {
+        const int k = warp + KW * q;
+        const double v = warp_sum((double)acc[q]);
+        if (lane == 0 && k < kc) bs[k] = v;
+    }
+    __syncthreads();
+}
+
+template <class TV>
 __global__ void __launch_bounds__(KT)
 k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* __restrict__ w,
        SolveState* st, int second, double* partials, unsigned* counter) {
     if (!st->cycle_active) return;
     constexpr int VN = Vec<TV>::N;
-    TV acc[KMAX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    TV acc[KPW];
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k) acc[k] = (TV)0;
+    for (int q = 0; q < KPW; ++q) acc[q] = (TV)0;
     const int nvec = n / VN;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nvec; q += gridDim.x * blockDim.x) {
+    for (int u = blockIdx.x * 32 + lane; u < nvec + 31; u += gridDim.x * 32) {
+        if (u >= nvec) break;
         TV wv[VN];
-        vload<TV>(w + (size_t)q * VN, wv);
+        vload<TV>(w + (size_t)u * VN, wv);
 #pragma unroll
-        for (int k = 0; k < KMAX; ++k) {
+        for (int q = 0; q < KPW; ++q) {
+            const int k = warp + KW * q;
             if (k < kc) {
                 TV vv[VN];
-                vload<TV>(raw + (size_t)(k0 + k) * ldv + (size_t)q * VN, vv);
-#pragma unroll
-                for (int e = 0; e < VN; ++e) acc[k] += vv[e] * wv[e];
+                vload<TV>(raw + (size_t)(k0 + k) * ldv + (size_t)u * VN, vv);
+                acc[q] += dotv<TV>(vv, wv);
             }
         }
     }
-    for (int i = nvec * VN + blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x) {
-        const TV wi = w[i];
+    if (blockIdx.x == 0) {  // elements past the last full vector
+        const int i = nvec * VN + lane;
+        if (lane < n - nvec * VN) {
 #pragma unroll
-        for (int k = 0; k < KMAX; ++k)
-            if (k < kc) acc[k] += raw[(size_t)(k0 + k) * ldv + i] * wi;
+            for (int q = 0; q < KPW; ++q) {
+                const int k = warp + KW * q;
+                if (k < kc) acc[q] += raw[(size_t)(k0 + k) * ldv + i] * w[i];
+            }
+        }
     }
-    __shared__ double red[(KT / 32) * KMAX];
-    __shared__ double bs[KMAX], tot[KMAX];
-    block_sum_multi<KMAX>(acc, kc, red, bs);
+    __shared__ double bs[KW * KPW], tot[KW * KPW];
+    warp_split_sums<TV>(acc, kc, bs);
     if (last_block_reduce(partials, counter, bs, kc, tot)) {
         for (int k = threadIdx.x; k < kc; k += blockDim.x) {
             const double h = st->vscale[k0 + k] * tot[k];
@@ -176,35 +207,114 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
     }
 }
 
-// ---- pass B fused: w' = w - sum c_k raw_k ; s2_k = raw_k . w'   (nk <= KMAX)
-template <class TV, int KMAX>
+// ---- pass B fused (nk <= 32): w' = w - sum_k c_k raw_k ; s2_k = raw_k . w'.
+// Each warp forms the update of its own vectors for the tile; the 8 partial
+// updates meet in shared memory (summed in warp order), every warp rebuilds
+// w' from them and dots it with the vector values it still holds.
+template <class TV>
 __global__ void __launch_bounds__(KT)
 k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict__ w,
            SolveState* st, double* partials, unsigned* counter) {
     if (!st->cycle_active) return;
-    __shared__ TV cf[KMAX];
+    constexpr int VN = Vec<TV>::N;
+    constexpr int TE = 32 * VN;  // elements of a tile
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ TV cf[KW * KPW];
+    __shared__ TV upd[KW][TE];
+    __shared__ TV wsh[TE];
     for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
     __syncthreads();
-    TV acc[KMAX];
+    TV acc[KPW];
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k) acc[k] = (TV)0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        TV v[KMAX];
-        TV wi = w[i];
+    for (int q = 0; q < KPW; ++q) acc[q] = (TV)0;
+    const int nvec = n / VN;
+    const int ntiles = (nvec + 31) / 32;
+    const int nfull = nvec * VN;  // elements covered by whole vectors
+    // registers of the current tile and of the next one (loaded ahead); the
+    // first TE threads also hold one element of w each
+    TV vv[KPW][VN], nv[KPW][VN];
+    TV wt = (TV)0, nwt = (TV)0;
+    auto load_tile = [&](int tile, TV (&v)[KPW][VN], TV& we) {
+        const int u = tile * 32 + lane;
+        const bool ok = u < nvec;
 #pragma unroll
-        for (int k = 0; k < KMAX; ++k)
-            if (k < nk) v[k] = raw[(size_t)k * ldv + i];
+        for (int q = 0; q < KPW; ++q) {
+            const int k = warp + KW * q;
+            if (k < nk && ok) {
+                vload<TV>(raw + (size_t)k * ldv + (size_t)u * VN, v[q]);
+            } else {
 #pragma unroll
-        for (int k = 0; k < KMAX; ++k)
-            if (k < nk) wi -= cf[k] * v[k];
-        w[i] = wi;
+                for (int e = 0; e < VN; ++e) v[q][e] = (TV)0;
+            }
+        }
+        const int i = tile * TE + threadIdx.x;
+        we = (threadIdx.x < TE && i < nfull) ? w[i] : (TV)0;
+    };
+    int tile = blockIdx.x;
+    if (tile < ntiles) load_tile(tile, vv, wt);
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int next = tile + gridDim.x;
+        if (next < ntiles) load_tile(next, nv, nwt);
+        // this warp's share of the update for the tile
+        TV part[VN];
 #pragma unroll
-        for (int k = 0; k < KMAX; ++k)
-            if (k < nk) acc[k] += v[k] * wi;
+        for (int e = 0; e < VN; ++e) part[e] = (TV)0;
+#pragma unroll
+        for (int q = 0; q < KPW; ++q) {
+            const int k = warp + KW * q;
+            if (k < nk) {
+#pragma unroll
+                for (int e = 0; e < VN; ++e) part[e] += cf[k] * vv[q][e];
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < VN; ++e) upd[warp][lane * VN + e] = part[e];
+        __syncthreads();
+        // w' = w - (sum of the 8 shares, in warp order), once per element
+        if (threadIdx.x < TE) {
+            const int i = tile * TE + threadIdx.x;
+            TV sum = (TV)0;
+#pragma unroll
+            for (int g = 0; g < KW; ++g) sum += upd[g][threadIdx.x];
+            const TV wn = wt - sum;
+            wsh[threadIdx.x] = wn;
+            if (i < nfull) w[i] = wn;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < KPW; ++q) {
+            TV d = (TV)0;
+#pragma unroll
+            for (int e = 0; e < VN; ++e) d += vv[q][e] * wsh[lane * VN + e];
+            acc[q] += d;
+        }
+#pragma unroll
+        for (int q = 0; q < KPW; ++q)
+#pragma unroll
+            for (int e = 0; e < VN; ++e) vv[q][e] = nv[q][e];
+        wt = nwt;
     }
-    __shared__ double red[(KT / 32) * KMAX];
-    __shared__ double bs[KMAX], tot[KMAX];
-    block_sum_multi<KMAX>(acc, nk, red, bs);
+    if (blockIdx.x == 0 && warp == 0) {  // tail elements: one warp, serial over k
+        const int i = nfull + lane;
+        if (lane < n - nfull) {
+            TV wi = w[i];
+            for (int k = 0; k < nk; ++k) wi -= cf[k] * raw[(size_t)k * ldv + i];
+            w[i] = wi;
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        const int i = nfull + lane;
+        if (lane < n - nfull) {
+#pragma unroll
+            for (int q = 0; q < KPW; ++q) {
+                const int k = warp + KW * q;
+                if (k < nk) acc[q] += raw[(size_t)k * ldv + i] * w[i];
+            }
+        }
+    }
+    __shared__ double bs[KW * KPW], tot[KW * KPW];
+    warp_split_sums<TV>(acc, nk, bs);
     if (last_block_reduce(partials, counter, bs, nk, tot)) {
         for (int k = threadIdx.x; k < nk; k += blockDim.x) {
             const double h = st->vscale[k] * tot[k];
@@ -230,18 +340,46 @@ k_upd(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict__ w,
     }
 }
 
-// ---- pass C: w'' = w' - sum c_k raw_k ; ||w''||^2 -> Arnoldi finalize
+// ---- pass C: w'' = w' - sum c_k raw_k ; ||w''||^2 -> Arnoldi finalize.
+// 16-byte vectors of elements per thread, the k loop unrolled by 4 so four
+// basis loads are in flight per thread.
 template <class TV>
 __global__ void __launch_bounds__(KT)
 k_upd_norm(const TV* __restrict__ raw, size_t ldv, int n, int j, int m, TV* __restrict__ w,
            SolveState* st, double* partials, unsigned* counter, double* hist, int hist_cap) {
     if (!st->cycle_active) return;
+    constexpr int VN = Vec<TV>::N;
     const int nk = j + 1;
     __shared__ TV cf[SG_MMAX + 1];
     for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
     __syncthreads();
     TV ss = (TV)0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int nvec = n / VN;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nvec; u += gridDim.x * blockDim.x) {
+        TV wv[VN];
+        vload<TV>(w + (size_t)u * VN, wv);
+        int k = 0;
+        for (; k + 4 <= nk; k += 4) {
+            TV a[4][VN];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) vload<TV>(raw + (size_t)(k + q) * ldv + (size_t)u * VN, a[q]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int e = 0; e < VN; ++e) wv[e] -= cf[k + q] * a[q][e];
+        }
+        for (; k < nk; ++k) {
+            TV a[VN];
+            vload<TV>(raw + (size_t)k * ldv + (size_t)u * VN, a);
+#pragma unroll
+            for (int e = 0; e < VN; ++e) wv[e] -= cf[k] * a[e];
+        }
+        vstore<TV>(w + (size_t)u * VN, wv);
+#pragma unroll
+        for (int e = 0; e < VN; ++e) ss += wv[e] * wv[e];
+    }
+    for (int i = nvec * VN + blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
         TV wi = w[i];
         for (int k = 0; k < nk; ++k) wi -= cf[k] * raw[(size_t)k * ldv + i];
         w[i] = wi;
@@ -350,6 +488,33 @@ __global__ void k_cycle_end(SolveState* st) {
     st->cycle_active = st->done ? 0 : 1;
 }
 
+// ---- BLAS-1 of src/core/vector.h:11-44
+// dot: per-thread sums in a fixed grid-stride order, block sums, then the
+// last block adds the block partials in block order (deterministic).
+__global__ void __launch_bounds__(KT)
+k_dot(const double* __restrict__ x, const double* __restrict__ y, int n, double* partials,
+      unsigned* counter, double* out) {
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        acc = fma(x[i], y[i], acc);
+    __shared__ double red[KT / 32];
+    __shared__ double bs[1], tot[1];
+    double v1[1] = {acc};
+    block_sum_multi<1>(v1, 1, red, bs);
+    if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0) *out = tot[0];
+}
+
+// y += alpha x, product and sum rounded separately (the reference's bits)
+__global__ void k_axpy(double alpha, const double* __restrict__ x, double* __restrict__ y, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = __dadd_rn(y[i], __dmul_rn(alpha, x[i]));
+}
+
+__global__ void k_scale(double alpha, double* __restrict__ x, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] = __dmul_rn(x[i], alpha);
+}
+
 int kgrid(sg_ctx* ctx, int n, int per_sm) {
     long long need = ((long long)n + KT - 1) / KT;
     long long cap = (long long)ctx->num_sms * per_sm;
@@ -367,23 +532,15 @@ void launch_cycle_init(sg_ctx* ctx, const TV* raw0, int n, SolveState* st, int m
     count_launch(ctx);
 }
 
-template <class TV, int KMAX>
-static void dots_launch(sg_ctx* ctx, const TV* raw, size_t ldv, int n, int k0, int kc,
-                        const TV* w, SolveState* st, int second) {
-    k_dots<TV, KMAX><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(raw, ldv, n, k0, kc, w, st, second,
-                                                                ctx->partials.p, ctx->counter.p);
-    SG_CUDA(cudaGetLastError());
-    count_launch(ctx);
-}
-
 template <class TV>
 static void dots_any(sg_ctx* ctx, const TV* raw, size_t ldv, int n, int nk, const TV* w,
                      SolveState* st, int second) {
-    for (int k0 = 0; k0 < nk; k0 += 32) {
-        const int kc = nk - k0 < 32 ? nk - k0 : 32;
-        if (kc <= 8) dots_launch<TV, 8>(ctx, raw, ldv, n, k0, kc, w, st, second);
-        else if (kc <= 16) dots_launch<TV, 16>(ctx, raw, ldv, n, k0, kc, w, st, second);
-        else dots_launch<TV, 32>(ctx, raw, ldv, n, k0, kc, w, st, second);
+    for (int k0 = 0; k0 < nk; k0 += KW * KPW) {
+        const int kc = nk - k0 < KW * KPW ? nk - k0 : KW * KPW;
+        k_dots<TV><<<kgrid(ctx, (n + 3) / 4 * 8, 4), KT, 0, ctx->stream>>>(
+            raw, ldv, n, k0, kc, w, st, second, ctx->partials.p, ctx->counter.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
     }
 }
 
@@ -396,26 +553,19 @@ void launch_cgs2(sg_ctx* ctx, TV* raw, size_t ldv, int n, int j, int m, SolveSta
     // pass A
     dots_any<TV>(ctx, raw, ldv, n, nk, w, st, 0);
     // pass B
-    const int gB = kgrid(ctx, n, 2);
-    if (nk <= 8) {
-        k_upd_dots<TV, 8><<<gB, KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st, ctx->partials.p,
-                                                      ctx->counter.p);
-    } else if (nk <= 16) {
-        k_upd_dots<TV, 16><<<gB, KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st, ctx->partials.p,
-                                                       ctx->counter.p);
-    } else if (nk <= 32) {
-        k_upd_dots<TV, 32><<<gB, KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st, ctx->partials.p,
-                                                       ctx->counter.p);
+    if (nk <= KW * KPW) {
+        k_upd_dots<TV><<<kgrid(ctx, (n + 3) / 4 * 8, 3), KT, 0, ctx->stream>>>(
+            raw, ldv, n, nk, w, st, ctx->partials.p, ctx->counter.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
     } else {
         k_upd<TV><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(raw, ldv, n, nk, w, st);
         SG_CUDA(cudaGetLastError());
         count_launch(ctx);
         dots_any<TV>(ctx, raw, ldv, n, nk, w, st, 1);
     }
-    SG_CUDA(cudaGetLastError());
-    if (nk <= 32) count_launch(ctx);
     // pass C
-    k_upd_norm<TV><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(
+    k_upd_norm<TV><<<kgrid(ctx, n / Vec<TV>::N + 1, 4), KT, 0, ctx->stream>>>(
         raw, ldv, n, j, m, w, st, ctx->partials.p, ctx->counter.p, ctx->hist_d, ctx->hist_cap);
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
@@ -437,6 +587,34 @@ void launch_update_x(sg_ctx* ctx, const TV* basis, size_t ldv, int n, double* x,
 template <class TI, class TO>
 void launch_copy(sg_ctx* ctx, const TI* x, TO* y, int n, const int* active) {
     k_copy<TI, TO><<<kgrid(ctx, n, 4), KT, 0, ctx->stream>>>(x, y, n, active);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+// grid of the dot-product reduction: at most 1024 blocks
+int dot_grid(int num_sms, int n) {
+    long long need = ((long long)n + KT - 1) / KT;
+    long long cap = (long long)num_sms * 2;
+    if (cap > 1024) cap = 1024;
+    if (need > cap) need = cap;
+    return need < 1 ? 1 : (int)need;
+}
+
+void launch_dot(sg_ctx* ctx, const double* x, const double* y, int n, double* out_dev) {
+    k_dot<<<dot_grid(ctx->num_sms, n), KT, 0, ctx->stream>>>(x, y, n, ctx->partials.p,
+                                                              ctx->counter.p, out_dev);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+void launch_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n) {
+    k_axpy<<<kgrid(ctx, n, 8), KT, 0, ctx->stream>>>(alpha, x, y, n);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+void launch_scale(sg_ctx* ctx, double alpha, double* x, int n) {
+    k_scale<<<kgrid(ctx, n, 8), KT, 0, ctx->stream>>>(alpha, x, n);
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
 }

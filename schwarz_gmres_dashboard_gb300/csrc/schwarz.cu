@@ -157,6 +157,54 @@ k_pack(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
     }
 }
 
+// ---------------------------------------------------------------- gather / scatter
+// Restriction x -> t over the subdomain rows and restricted prolongation of
+// the owned rows, four independent index/value loads in flight per thread.
+template <class TS, class TI>
+__device__ __forceinline__ void gather_rows(TS* t, const TI* __restrict__ x,
+                                            const int* __restrict__ dof, int n) {
+    const int bs = blockDim.x;
+    int li = threadIdx.x;
+    for (; li + 3 * bs < n; li += 4 * bs) {
+        int d[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) d[u] = dof[li + u * bs];
+        TI v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = x[d[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[li + u * bs] = Load<TS>::f(v[u]);
+    }
+    for (; li < n; li += bs) t[li] = Load<TS>::f(x[dof[li]]);
+}
+
+template <class TS, class TO>
+__device__ __forceinline__ void scatter_owned(const TS* t, TO* __restrict__ y,
+                                              const int* __restrict__ ol,
+                                              const int* __restrict__ og, int n_own, int coarse,
+                                              double zc) {
+    const int bs = blockDim.x;
+    int q = threadIdx.x;
+    for (; q + 3 * bs < n_own; q += 4 * bs) {
+        int l[4], g[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            l[u] = ol[q + u * bs];
+            g[u] = og[q + u * bs];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (coarse) y[g[u]] = Store<TO>::f(__dadd_rn((double)t[l[u]], zc));
+            else y[g[u]] = Store<TO>::f(t[l[u]]);
+        }
+    }
+    for (; q < n_own; q += bs) {
+        const int li = ol[q];
+        if (coarse) y[og[q]] = Store<TO>::f(__dadd_rn((double)t[li], zc));
+        else y[og[q]] = Store<TO>::f(t[li]);
+    }
+}
+
 // ---------------------------------------------------------------- sweeps
 // One triangular sweep of a subdomain held in shared memory `t`.  Rows of a
 // level are independent; a __syncthreads separates levels.  The factor
@@ -271,7 +319,7 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
     TS* t = use_smem ? reinterpret_cast<TS*>(smraw) : gscratch + inf.row_off + s;
     const int* dof = dofs + inf.row_off;
     // restriction R_s x (gather with overlap)
-    for (int li = threadIdx.x; li < n; li += blockDim.x) t[li] = Load<TS>::f(x[dof[li]]);
+    gather_rows<TS>(t, x, dof, n);
     if (threadIdx.x == 0) t[n] = (TS)0;
     if (coarse) {
         // z0_s = (A0^{-1} r0)_s, scaled by the part's coarse basis value
@@ -300,13 +348,163 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
         // restricted prolongation: owned rows only (src/precond/ras.h:64-68)
         const int* ol = ownloc + inf.own_off;
         const int* og = owned_glob + inf.own_off;
-        for (int q = threadIdx.x; q < inf.n_own; q += blockDim.x) {
-            const int li = ol[q];
-            if (coarse) y[og[q]] = Store<TO>::f(__dadd_rn((double)t[li], zc));
-            else y[og[q]] = Store<TO>::f(t[li]);
-        }
+        scatter_owned<TS, TO>(t, y, ol, og, inf.n_own, coarse, zc);
     } else {
         // additive prolongation of every row (src/precond/asm.h:138-142)
+        for (int li = threadIdx.x; li < n; li += blockDim.x)
+            atomicAdd(&y[dof[li]], Store<TO>::f(t[li]));
+        if (coarse) {
+            const int* og = owned_glob + inf.own_off;
+            for (int q = threadIdx.x; q < inf.n_own; q += blockDim.x)
+                atomicAdd(&y[og[q]], Store<TO>::f(zc));
+        }
+    }
+}
+
+// ---------------------------------------------------------------- sync-free sweeps
+// The same forward/backward sweeps without a barrier per level.  Thread t
+// takes the rows at level-order positions t, t + blockDim, ... and, before
+// using row c, waits until c's ready flag (one byte in shared memory) shows
+// the current sweep; it then publishes its own row (value, block fence,
+// flag).  Every dependency sits at an earlier position and each thread walks
+// its positions in increasing order, so the waits always end; they are
+// bounded anyway (on expiry the thread records an error word and carries on).
+// The next row's factor entries are loaded before the current row's waits,
+// so their global-memory latency overlaps the dependency chain.
+constexpr long long SF_SPIN_LIMIT = 1ll << 24;
+
+template <class TS, bool EXACT>
+__device__ __forceinline__ TS sf_sub(TS acc, TS a, TS b) {
+    if (EXACT) return msub(acc, a, b);
+    return acc - a * b;  // contracts to a fused multiply-add
+}
+
+template <class TS, class TF, class TC, bool BACK, bool EXACT>
+__device__ __forceinline__ void sweep_sf(TS* t, volatile unsigned char* fl, int n,
+                                         const TC* __restrict__ perm, const TC* __restrict__ col,
+                                         const TF* __restrict__ val, const TF* __restrict__ diag,
+                                         int w, unsigned char epoch, int* err) {
+    auto wait_row = [&](int c) {
+        long long it = 0;
+        while (fl[c] < epoch) {
+            if (++it > SF_SPIN_LIMIT) {
+                atomicExch(err, 2);
+                break;
+            }
+        }
+        __threadfence_block();
+    };
+    if (w > SWEEP_WP) {
+        for (int p = threadIdx.x; p < n; p += blockDim.x) {
+            const int r = perm[p];
+            TS acc = t[r];
+            for (int k = 0; k < w; ++k) {
+                const int c = col[(size_t)k * n + p];
+                const TS v = Load<TS>::f(val[(size_t)k * n + p]);
+                wait_row(c);
+                acc = sf_sub<TS, EXACT>(acc, v, t[c]);
+            }
+            if (BACK) acc = acc / Load<TS>::f(diag[p]);
+            t[r] = acc;
+            __threadfence_block();
+            fl[r] = epoch;
+        }
+        return;
+    }
+    int r = 0, c[SWEEP_WP];
+    TS v[SWEEP_WP], d = (TS)1;
+    auto fetch = [&](int p) {
+        r = perm[p];
+#pragma unroll
+        for (int k = 0; k < SWEEP_WP; ++k)
+            if (k < w) {
+                c[k] = col[(size_t)k * n + p];
+                v[k] = Load<TS>::f(val[(size_t)k * n + p]);
+            }
+        if (BACK) d = Load<TS>::f(diag[p]);
+    };
+    int p = threadIdx.x;
+    if (p < n) fetch(p);
+    for (; p < n; p += blockDim.x) {
+        const int rc = r;
+        int cc[SWEEP_WP];
+        TS vc[SWEEP_WP];
+#pragma unroll
+        for (int k = 0; k < SWEEP_WP; ++k) {
+            cc[k] = c[k];
+            vc[k] = v[k];
+        }
+        const TS dc = d;
+        if (p + (int)blockDim.x < n) fetch(p + blockDim.x);
+        TS acc = t[rc];
+#pragma unroll
+        for (int k = 0; k < SWEEP_WP; ++k) {
+            if (k < w) {
+                wait_row(cc[k]);
+                acc = sf_sub<TS, EXACT>(acc, vc[k], t[cc[k]]);
+            }
+        }
+        if (BACK) acc = acc / dc;
+        t[rc] = acc;
+        __threadfence_block();
+        fl[rc] = epoch;
+    }
+}
+
+template <class TI, class TO, class TS, class TF, class TC, bool EXACT>
+__global__ void __launch_bounds__(SWEEP_T, 2)
+k_sweep_sf(const SubInfo* __restrict__ info, const int* __restrict__ order,
+           const int* __restrict__ dofs, const TC* __restrict__ perm_f,
+           const TC* __restrict__ lcol, const TF* __restrict__ lval,
+           const TC* __restrict__ perm_b, const TC* __restrict__ ucol,
+           const TF* __restrict__ uval, const TF* __restrict__ udiag,
+           const int* __restrict__ ownloc, const int* __restrict__ owned_glob,
+           const TI* __restrict__ x, TO* __restrict__ y, int mode, int coarse,
+           const double* __restrict__ a0inv, const double* __restrict__ r0, int nc, int* err,
+           const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double s_red[SWEEP_T / 32];
+    __shared__ double s_zc;
+    const int s = order[blockIdx.x];
+    const SubInfo inf = info[s];
+    const int n = inf.n;
+    TS* t = reinterpret_cast<TS*>(smraw);
+    volatile unsigned char* fl =
+        smraw + (((size_t)(n + 1) * sizeof(TS) + 15) & ~(size_t)15);
+    const int* dof = dofs + inf.row_off;
+    gather_rows<TS>(t, x, dof, n);
+    for (int li = threadIdx.x; li < n; li += blockDim.x) fl[li] = 0;
+    if (threadIdx.x == 0) {
+        t[n] = (TS)0;  // padded entries read this zero
+        fl[n] = 2;
+    }
+    if (coarse) {
+        double acc = 0.0;
+        const double* row = a0inv + (size_t)s * nc;
+        for (int q = threadIdx.x; q < nc; q += blockDim.x) acc += row[q] * r0[q];
+        acc = warp_sum(acc);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double z = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) z += s_red[w];
+            s_zc = inf.cscale * z;
+        }
+    }
+    __syncthreads();
+    sweep_sf<TS, TF, TC, false, EXACT>(t, fl, n, perm_f + inf.row_off, lcol + inf.fl_off,
+                                       lval + inf.fl_off, nullptr, inf.wl, 1, err);
+    __syncthreads();  // every forward read is done before rows change again
+    sweep_sf<TS, TF, TC, true, EXACT>(t, fl, n, perm_b + inf.row_off, ucol + inf.fu_off,
+                                      uval + inf.fu_off, udiag + inf.row_off, inf.wu, 2, err);
+    __syncthreads();
+    const double zc = coarse ? s_zc : 0.0;
+    if (mode == 0) {
+        const int* ol = ownloc + inf.own_off;
+        const int* og = owned_glob + inf.own_off;
+        scatter_owned<TS, TO>(t, y, ol, og, inf.n_own, coarse, zc);
+    } else {
         for (int li = threadIdx.x; li < n; li += blockDim.x)
             atomicAdd(&y[dof[li]], Store<TO>::f(t[li]));
         if (coarse) {
@@ -520,6 +718,52 @@ void sweep_launch(sg_precond* pc, const TF* lval, const TF* uval, const TF* udia
     count_launch(ctx);
 }
 
+size_t sf_smem(const sg_precond* pc) {
+    const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
+    return (((size_t)(pc->max_n + 1) * ts + 15) & ~(size_t)15) + (size_t)pc->max_n + 16;
+}
+
+template <class TS, class TF, class TC, bool EXACT, class TI, class TO>
+void sf_launch(sg_precond* pc, const TF* lval, const TF* uval, const TF* udiag, const TI* x,
+               TO* y, int mode, bool coarse, const int* active) {
+    sg_ctx* ctx = pc->ctx;
+    if (!pc->info.p || !pc->order.p || !pc->dofs.p || !pc->perm_f.p || !pc->perm_b.p ||
+        !pc->lcol.p || !pc->ucol.p || !lval || !uval || !udiag || !pc->ownloc_d.p ||
+        !pc->owned_d.p || !pc->err_d.p || (coarse && (!pc->a0inv.p || !pc->r0.p)))
+        fail(SG_ERR_INTERNAL, "preconditioner device buffers missing for this apply");
+    const size_t smem = sf_smem(pc);
+    SG_CUDA(cudaFuncSetAttribute(k_sweep_sf<TI, TO, TS, TF, TC, EXACT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sweep_sf<TI, TO, TS, TF, TC, EXACT><<<pc->nparts, SWEEP_T, smem, ctx->stream>>>(
+        pc->info.p, pc->order.p, pc->dofs.p, reinterpret_cast<const TC*>(pc->perm_f.p),
+        reinterpret_cast<const TC*>(pc->lcol.p), lval, reinterpret_cast<const TC*>(pc->perm_b.p),
+        reinterpret_cast<const TC*>(pc->ucol.p), uval, udiag, pc->ownloc_d.p, pc->owned_d.p, x, y,
+        mode, coarse ? 1 : 0, pc->a0inv.p, pc->r0.p, pc->nc, pc->err_d.p, active);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+template <class TC, class TI, class TO>
+bool sf_dispatch(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
+                 const int* active) {
+    if (!pc->use_sf) return false;
+    if (pc->opts.sweep_dtype == SG_FP64) {
+        if (exact)
+            sf_launch<double, double, TC, true>(pc, pc->lval64.p, pc->uval64.p, pc->udiag64.p, x, y,
+                                                mode, coarse, active);
+        else
+            sf_launch<double, double, TC, false>(pc, pc->lval64.p, pc->uval64.p, pc->udiag64.p, x,
+                                                 y, mode, coarse, active);
+    } else if (pc->opts.factor_dtype == SG_BF16) {
+        sf_launch<float, uint16_t, TC, false>(pc, pc->lval16.p, pc->uval16.p, pc->udiag16.p, x, y,
+                                              mode, coarse, active);
+    } else {
+        sf_launch<float, float, TC, false>(pc, pc->lval32.p, pc->uval32.p, pc->udiag32.p, x, y,
+                                           mode, coarse, active);
+    }
+    return true;
+}
+
 template <class TC, class TI, class TO>
 void sweep_dispatch(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse,
                     const int* active) {
@@ -551,10 +795,23 @@ void factor_and_pack(sg_precond* pc) {
         pc->info.p, pc->lrp_d.p, pc->lci_d.p, pc->ldiag_d.p,
         reinterpret_cast<const TC*>(pc->perm_f.p), pc->lev_ptr_f.p, pc->lu_d.p);
     SG_CUDA(cudaGetLastError());
-    // level records for the TMA-fed sweep; the ELL slices below are built
-    // only for the fallback sweep (subdomains too large for the records)
+    // sweep variants: TMA-fed level records (default), a barrier per level
+    // with the factors read from global memory (reserved[0] = 1), sync-free
+    // with per-row ready flags (reserved[0] = 4)
+    const int variant = pc->opts.reserved[0];  // 0 TMA records, 1 level, 4 sync-free
+    if (variant != 0) pc->use_rec = false;
     rec_setup_device(pc);
     if (pc->use_rec) return;
+    {
+        int max_smem = 0;
+        SG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                       ctx->device));
+        pc->use_sf = (variant & 4) && pc->use_smem && sf_smem(pc) + 1024 <= (size_t)max_smem;
+    }
+    if (!pc->err_d.p) {
+        pc->err_d.alloc(1);
+        pc->err_d.zero(ctx->stream);
+    }
     if (pc->wide_cols) {
         pc->lcol.alloc((size_t)pc->fl_total * 2);
         pc->ucol.alloc((size_t)pc->fu_total * 2);
@@ -694,6 +951,12 @@ void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active,
     }
     if (asm_mode) SG_CUDA(cudaMemsetAsync(y, 0, sizeof(TO) * (size_t)n, ctx->stream));
     if (sweep_tma<TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, exact, active)) return;
+    if (pc->wide_cols) {
+        if (sf_dispatch<int, TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, exact, active)) return;
+    } else {
+        if (sf_dispatch<uint16_t, TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, exact, active))
+            return;
+    }
     if (pc->wide_cols) sweep_dispatch<int, TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, active);
     else sweep_dispatch<uint16_t, TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, active);
 }

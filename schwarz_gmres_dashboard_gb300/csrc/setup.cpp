@@ -249,6 +249,9 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
             }
         }
         pc->rec_total = cur;
+        pc->max_levels = 0;
+        for (int s2 = 0; s2 < nparts; ++s2)
+            pc->max_levels = std::max(pc->max_levels, pc->h_info[s2].nlev_f + pc->h_info[s2].nlev_b);
         pc->rec_stage_bytes = mx;
         pc->use_rec = !pc->wide_cols && pc->use_smem && mx > 0;
     }

@@ -128,6 +128,16 @@ struct sg_ctx {
     double* hist_d = nullptr;
     int hist_cap = 0;
     sg::SolveWork* work = nullptr;
+    // kernel-class timers (CUDA events on the context stream, eager solves)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    struct EvPair {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<EvPair> ev_pending;
+    double class_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long class_count[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     // kernels launched by this context (graph launches add their kernel nodes)
     long long launches = 0;
     long long captured = 0;
@@ -135,6 +145,19 @@ struct sg_ctx {
 };
 
 namespace sg {
+// kernel classes of the timers
+enum { TK_SPMV = 0, TK_RESIDUAL = 1, TK_PRECOND = 2, TK_ORTHO = 3, TK_UPDATE = 4 };
+// Records a CUDA event pair around the launches made during its lifetime
+// when the context's timers are on (not while a graph is being captured).
+struct ClassTimer {
+    sg_ctx* ctx;
+    int kind;
+    cudaEvent_t a = nullptr;
+    ClassTimer(sg_ctx* c, int k);
+    ~ClassTimer();
+};
+// adds the elapsed times of completed pairs (call after a stream sync)
+void collect_timers(sg_ctx* ctx);
 inline void count_launch(sg_ctx* ctx) {
     if (ctx->capturing) ctx->captured++;
     else ctx->launches++;
@@ -157,6 +180,8 @@ struct sg_csr {
     long long sell_entries = 0;
     bool sell_ok = false;  // padding small enough to keep the copy
     int format = 0;        // 0 undecided, 1 CSR, 2 SELL (set by the autotuner)
+    int format32 = 0;      // same for the FP32 copy (0: follow `format`)
+    bool format_user = false;  // set by the caller: the autotuner keeps it
     sg::DBuf<long long> sl_ptr;
     sg::DBuf<int> sl_w, sl_col;
     sg::DBuf<double> sl_val;
@@ -202,11 +227,13 @@ struct sg_precond {
     bool wide_cols = false;  // subdomains above 65534 rows use 32-bit local indices
     long long fl_total = 0, fu_total = 0;
     int max_n = 0;
+    int max_levels = 0;  // largest nlev_f + nlev_b of a subdomain
     long long total_rows = 0;
     bool use_smem = true;
     // level records for the TMA-fed sweep: per level one 16-byte-aligned
     // record [rows | columns | values (| diagonal)], rows padded to 8
     bool use_rec = false;
+    bool use_sf = false;   // sync-free sweep (per-row ready flags)
     int rec_depth = 0;               // ring stages in shared memory
     long long rec_stage_bytes = 0;   // largest record
     long long rec_total = 0;

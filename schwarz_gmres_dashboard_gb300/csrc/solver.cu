@@ -26,6 +26,43 @@ SolveWork::~SolveWork() {
     if (h_st) cudaFreeHost(h_st);
 }
 
+static cudaEvent_t take_event(sg_ctx* ctx) {
+    if (!ctx->ev_pool.empty()) {
+        cudaEvent_t e = ctx->ev_pool.back();
+        ctx->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    SG_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+ClassTimer::ClassTimer(sg_ctx* c, int k) : ctx(c), kind(k) {
+    if (!ctx->timing || ctx->capturing) return;
+    a = take_event(ctx);
+    SG_CUDA(cudaEventRecord(a, ctx->stream));
+}
+
+ClassTimer::~ClassTimer() {
+    if (!a) return;
+    cudaEvent_t b = take_event(ctx);
+    cudaEventRecord(b, ctx->stream);
+    ctx->ev_pending.push_back({kind, a, b});
+}
+
+void collect_timers(sg_ctx* ctx) {
+    for (auto& p : ctx->ev_pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess && p.kind >= 0 && p.kind < 8) {
+            ctx->class_ms[p.kind] += ms;
+            ctx->class_count[p.kind] += 1;
+        }
+        ctx->ev_pool.push_back(p.a);
+        ctx->ev_pool.push_back(p.b);
+    }
+    ctx->ev_pending.clear();
+}
+
 namespace {
 
 template <class TV>
@@ -66,29 +103,50 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
     // r = b - A x is already in w->r64 (computed at the end of the previous
     // cycle, or before the first one) together with the convergence test.
     // Krylov start vector raw_0
-    if (!flexible) apply_pc<double, TV>(ctx, pc, w->r64.p, V, n, active);
-    else launch_copy<double, TV>(ctx, w->r64.p, V, n, active);
-    launch_cycle_init<TV>(ctx, V, n, st, m, flexible);
+    {
+        ClassTimer tm(ctx, TK_PRECOND);
+        if (!flexible) apply_pc<double, TV>(ctx, pc, w->r64.p, V, n, active);
+        else launch_copy<double, TV>(ctx, w->r64.p, V, n, active);
+    }
+    {
+        ClassTimer tm(ctx, TK_ORTHO);
+        launch_cycle_init<TV>(ctx, V, n, st, m, flexible);
+    }
     for (int j = 0; j < m; ++j) {
         TV* vj = V + (size_t)j * ldv;
         TV* wj = V + (size_t)(j + 1) * ldv;
         if (!flexible) {
             // w = M^{-1} A v_j  (src/core/gmres.cpp:280-285)
-            launch_spmv_a<TV, TV, TV>(ctx, A, vj, t, &st->vscale[j], active);
+            {
+                ClassTimer tm(ctx, TK_SPMV);
+                launch_spmv_a<TV, TV, TV>(ctx, A, vj, t, &st->vscale[j], active);
+            }
+            ClassTimer tm(ctx, TK_PRECOND);
             apply_pc<TV, TV>(ctx, pc, t, wj, n, active);
         } else {
             // z_j = M^{-1} v_j ; w = A z_j  (src/core/fgmres.cpp:133-140)
             TV* zj = Z + (size_t)j * ldv;
-            apply_pc<TV, TV>(ctx, pc, vj, zj, n, active);
+            {
+                ClassTimer tm(ctx, TK_PRECOND);
+                apply_pc<TV, TV>(ctx, pc, vj, zj, n, active);
+            }
+            ClassTimer tm(ctx, TK_SPMV);
             launch_spmv_a<TV, TV, TV>(ctx, A, zj, wj, &st->vscale[j], active);
         }
+        ClassTimer tm(ctx, TK_ORTHO);
         launch_cgs2<TV>(ctx, V, ldv, n, j, m, st, flexible);
     }
-    launch_backsolve(ctx, st, m);
-    launch_update_x<TV>(ctx, flexible ? Z : V, ldv, n, x, st);
+    {
+        ClassTimer tm(ctx, TK_UPDATE);
+        launch_backsolve(ctx, st, m);
+        launch_update_x<TV>(ctx, flexible ? Z : V, ldv, n, x, st);
+    }
     // FP64 true residual of the updated x: convergence test and the next
     // cycle's right-hand side
-    launch_residual(ctx, A, b, x, w->r64.p, st);
+    {
+        ClassTimer tm(ctx, TK_RESIDUAL);
+        launch_residual(ctx, A, b, x, w->r64.p, st);
+    }
     launch_cycle_end(ctx, st);
 }
 
@@ -120,10 +178,11 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     ensure(w->st, 1);
     ensure(w->r64, ldv);
     if (!w->h_st) SG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&w->h_st), sizeof(SolveState)));
-    // SpMV format: the faster of CSR and SELL on this matrix (same results)
+    if (fp32) const_cast<sg_csr*>(A)->ensure_fp32();
+    // SpMV format: the faster of CSR and SELL on this matrix (same results);
+    // the FP32 copy gets its own choice once it exists
     spmv_autotune(ctx, const_cast<sg_csr*>(A));
     if (fp32) {
-        const_cast<sg_csr*>(A)->ensure_fp32();
         ensure(w->V32, ldv * (m + 1));
         ensure(w->t32, ldv);
         if (flexible) ensure(w->Z32, ldv * m);
@@ -191,6 +250,7 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
             ++cycles;
             SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
             SG_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (ctx->timing) collect_timers(ctx);
             if (hs->done) break;
         }
     } catch (...) {

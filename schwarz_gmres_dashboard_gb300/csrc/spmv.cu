@@ -157,25 +157,25 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
         const long long base = sptr[sl] + lane;
         const int w = sw[sl];
         TV sum = (TV)0;
-        int k = 0;
-        for (; k + 4 <= w; k += 4) {
-            TV v[4];
-            int c[4];
+        // up to 8 entries of a row per round: all value/column loads first,
+        // then all gathers of x, then the sum in entry order
+        for (int k = 0; k < w; k += 8) {
+            TV v[8];
+            int c[8];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                v[q] = __ldg(&val[base + (long long)(k + q) * 32]);
-                c[q] = __ldg(&col[base + (long long)(k + q) * 32]);
+            for (int q = 0; q < 8; ++q) {
+                if (k + q < w) {
+                    v[q] = __ldg(&val[base + (long long)(k + q) * 32]);
+                    c[q] = __ldg(&col[base + (long long)(k + q) * 32]);
+                }
             }
-            TV p[4];
+            TV p[8];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) p[q] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+            for (int q = 0; q < 8; ++q)
+                if (k + q < w) p[q] = pmul(v[q], (TV)__ldg(&x[c[q]]));
 #pragma unroll
-            for (int q = 0; q < 4; ++q) sum = padd(sum, p[q]);
-        }
-        for (; k < w; ++k) {
-            const TV v = __ldg(&val[base + (long long)k * 32]);
-            const int c = __ldg(&col[base + (long long)k * 32]);
-            sum = padd(sum, pmul(v, (TV)__ldg(&x[c])));
+            for (int q = 0; q < 8; ++q)
+                if (k + q < w) sum = padd(sum, p[q]);
         }
         const int r = sl * 32 + lane;
         if (r < n) {
@@ -292,11 +292,18 @@ void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double
     count_launch(ctx);
 }
 
+template <class TV>
+int format_of(const sg_csr* A);
+template <>
+int format_of<double>(const sg_csr* A) { return A->format; }
+template <>
+int format_of<float>(const sg_csr* A) { return A->format32 ? A->format32 : A->format; }
+
 template <class TV, class TX, class TY>
 void launch_spmv_a(sg_ctx* ctx, const sg_csr* A, const TX* x, TY* y, const double* scale,
                    const int* active) {
     if (A->nrows <= 0) return;
-    if (A->format == 2 && A->sell_ok) {
+    if (format_of<TV>(A) == 2 && A->sell_ok) {
         k_spmv_sell<TV, TX, TY, 0><<<sell_grid(ctx, A->nslices), SPMV_THREADS, 0, ctx->stream>>>(
             A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, sell_vals<TV>(A), x, y,
             scale, active, nullptr, nullptr, nullptr, nullptr);
@@ -308,34 +315,65 @@ void launch_spmv_a(sg_ctx* ctx, const sg_csr* A, const TX* x, TY* y, const doubl
     }
 }
 
+// Autotuner: times CSR and SELL on A (5 launches each after a warm-up) and
+// keeps the faster, separately for the FP64 values and for the FP32 copy.
+// Both formats give the same bits, so the choice never changes a result.  A
+// format set by the caller (sg_csr_set_format) is left alone.
 void spmv_autotune(sg_ctx* ctx, sg_csr* A) {
-    if (A->format != 0) return;
+    if (A->format_user) return;
+    const bool need64 = A->format == 0;
+    const bool need32 = A->val32.p && A->format32 == 0;
+    if (!need64 && !need32) return;
     if (!A->sell_ok || A->nrows < 4096) {
-        A->format = 1;
+        if (need64) A->format = 1;
+        if (need32) A->format32 = 1;
         return;
     }
-    DBuf<double> xb, yb;
-    xb.alloc(A->ncols);
-    yb.alloc(A->nrows);
-    xb.zero(ctx->stream);
-    double* x = xb.p;
-    double* y = yb.p;
     cudaEvent_t e0, e1;
     SG_CUDA(cudaEventCreate(&e0));
     SG_CUDA(cudaEventCreate(&e1));
-    float best[3] = {0, 0, 0};
-    for (int f = 1; f <= 2; ++f) {
-        A->format = f;
-        launch_spmv_a<double, double, double>(ctx, A, x, y, nullptr, nullptr);  // warm
+    auto time_it = [&](auto&& run) {
+        run();
         SG_CUDA(cudaEventRecord(e0, ctx->stream));
-        for (int i = 0; i < 5; ++i) launch_spmv_a<double, double, double>(ctx, A, x, y, nullptr, nullptr);
+        for (int i = 0; i < 5; ++i) run();
         SG_CUDA(cudaEventRecord(e1, ctx->stream));
         SG_CUDA(cudaEventSynchronize(e1));
-        SG_CUDA(cudaEventElapsedTime(&best[f], e0, e1));
+        float ms = 0.f;
+        SG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        return ms;
+    };
+    if (need64) {
+        DBuf<double> xb, yb;
+        xb.alloc(A->ncols);
+        yb.alloc(A->nrows);
+        xb.zero(ctx->stream);
+        float t[3] = {0, 0, 0};
+        for (int f = 1; f <= 2; ++f) {
+            A->format = f;
+            t[f] = time_it([&] {
+                launch_spmv_a<double, double, double>(ctx, A, xb.p, yb.p, nullptr, nullptr);
+            });
+        }
+        A->format = t[2] < t[1] ? 2 : 1;
+    }
+    if (need32 && A->sl_val32.p) {
+        DBuf<float> xb, yb;
+        xb.alloc(A->ncols);
+        yb.alloc(A->nrows);
+        xb.zero(ctx->stream);
+        float t[3] = {0, 0, 0};
+        for (int f = 1; f <= 2; ++f) {
+            A->format32 = f;
+            t[f] = time_it([&] {
+                launch_spmv_a<float, float, float>(ctx, A, xb.p, yb.p, nullptr, nullptr);
+            });
+        }
+        A->format32 = t[2] < t[1] ? 2 : 1;
+    } else if (need32) {
+        A->format32 = 1;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    A->format = best[2] < best[1] ? 2 : 1;
 }
 
 void launch_bnorm(sg_ctx* ctx, const double* v, int n, SolveState* st) {

@@ -190,6 +190,8 @@ struct RecArgs {
     int nc;
     int depth;
     int stage_bytes;
+    int max_n;
+    int max_levels;  // largest nlev_f + nlev_b over the subdomains
     int* err;
 };
 
@@ -202,6 +204,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ double s_red[SW_T / 32];
     __shared__ double s_zc;
+    __shared__ int s_fail;
     const int D = a.depth;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // D x 8 B
     unsigned char* stages = smraw + 128;                               // D x stage_bytes
@@ -211,39 +214,65 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     const int n = inf.n;
     const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
     const int sf = (int)sizeof(TF);
-
-    auto rec_of = [&](int g, const unsigned char*& src, uint32_t& bytes) {
+    // per-level metadata of both sweeps, staged once: rows, padded rows,
+    // record offset (so the level loop touches global memory only through TMA)
+    long long* m_off = reinterpret_cast<long long*>(
+        reinterpret_cast<unsigned char*>(t) + (((size_t)(a.max_n + 1) * sizeof(TS) + 15) & ~(size_t)15));
+    int* m_c = reinterpret_cast<int*>(m_off + a.max_levels);
+    int* m_C = m_c + a.max_levels;
+    for (int g = threadIdx.x; g < T; g += blockDim.x) {
         if (g < nf) {
-            const int C = a.rows_f[inf.lev_off_f + g];
-            src = a.rec + a.off_f[inf.lev_off_f + g];
-            bytes = (uint32_t)C * (uint32_t)(2 + inf.wl * (2 + sf));
+            const int i = inf.lev_off_f + g;
+            m_c[g] = a.lev_f[i + 1] - a.lev_f[i];
+            m_C[g] = a.rows_f[i];
+            m_off[g] = a.off_f[i];
         } else {
-            const int l = g - nf;
-            const int C = a.rows_b[inf.lev_off_b + l];
-            src = a.rec + a.off_b[inf.lev_off_b + l];
-            bytes = (uint32_t)C * (uint32_t)(2 + inf.wu * (2 + sf) + sf);
+            const int i = inf.lev_off_b + (g - nf);
+            m_c[g] = a.lev_b[i + 1] - a.lev_b[i];
+            m_C[g] = a.rows_b[i];
+            m_off[g] = a.off_b[i];
         }
-    };
+    }
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+
+    const uint32_t bytes_f = (uint32_t)(2 + inf.wl * (2 + sf));
+    const uint32_t bytes_b = (uint32_t)(2 + inf.wu * (2 + sf) + sf);
     auto issue = [&](int g) {
-        const unsigned char* src;
-        uint32_t bytes;
-        rec_of(g, src, bytes);
+        const uint32_t bytes = (uint32_t)m_C[g] * (g < nf ? bytes_f : bytes_b);
         const int st = g % D;
         const uint32_t bar = smem_u32(&bars[st]);
         mbar_expect_tx(bar, bytes);
-        bulk_g2s(smem_u32(stages + (size_t)st * a.stage_bytes), src, bytes, bar);
+        bulk_g2s(smem_u32(stages + (size_t)st * a.stage_bytes), a.rec + m_off[g], bytes, bar);
     };
 
-    if (threadIdx.x == 0) {
+    // the producer is the block's last thread: levels rarely have rows for
+    // it, so issuing the next copy overlaps the other threads' work
+    const bool producer = threadIdx.x == blockDim.x - 1;
+    if (producer) {
         for (int i = 0; i < D; ++i) mbar_init(smem_u32(&bars[i]), 1);
         fence_mbar_init();
         fence_proxy_async();
         const int pre = T < D ? T : D;
         for (int g = 0; g < pre; ++g) issue(g);
     }
-    // gather while the first records are in flight
+    // gather while the first records are in flight (four loads in flight)
     const int* dof = a.dofs + inf.row_off;
-    for (int li = threadIdx.x; li < n; li += blockDim.x) t[li] = Load<TS>::f(x[dof[li]]);
+    {
+        const int bs = blockDim.x;
+        int li = threadIdx.x;
+        for (; li + 3 * bs < n; li += 4 * bs) {
+            int d[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) d[u] = dof[li + u * bs];
+            TI v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = x[d[u]];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) t[li + u * bs] = Load<TS>::f(v[u]);
+        }
+        for (; li < n; li += bs) t[li] = Load<TS>::f(x[dof[li]]);
+    }
     if (threadIdx.x == 0) t[n] = (TS)0;
     if (coarse) {
         double acc = 0.0;
@@ -262,11 +291,34 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
 
     for (int g = 0; g < T; ++g) {
         const int st = g % D;
-        // every thread observes the phase itself (acquires the bulk copy)
+        // every thread observes the phase itself (acquires the bulk copy); a
+        // thread whose wait expires computes nothing and raises the flag
         const bool ok = mbar_wait(smem_u32(&bars[st]), (uint32_t)((g / D) & 1), WAIT_CYCLES);
-        if (__syncthreads_or(!ok)) {
+        if (ok) {
+            const unsigned char* R = stages + (size_t)st * a.stage_bytes;
+            const bool back = g >= nf;
+            const int c = m_c[g];
+            const int C = m_C[g];
+            const int w = back ? inf.wu : inf.wl;
+            const uint16_t* rr = reinterpret_cast<const uint16_t*>(R);
+            const uint16_t* cc = rr + C;
+            const TF* vv = reinterpret_cast<const TF*>(cc + (size_t)C * w);
+            for (int q = threadIdx.x; q < c; q += blockDim.x) {
+                const int r = rr[q];
+                TS acc = t[r];
+                for (int k = 0; k < w; ++k)
+                    acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vv[(size_t)k * C + q]),
+                                             t[cc[(size_t)k * C + q]]);
+                if (back) acc = acc / Load<TS>::f(vv[(size_t)w * C + q]);
+                t[r] = acc;
+            }
+        } else {
+            s_fail = 1;
+        }
+        __syncthreads();
+        if (s_fail) {
             // a record never arrived: report, drain what was issued, leave y alone
-            if (threadIdx.x == 0) {
+            if (producer) {
                 atomicExch(a.err, 1);
                 const int last = (g + D < T ? g + D : T);
                 for (int h = g + 1; h < last; ++h)
@@ -274,27 +326,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             }
             return;
         }
-        const unsigned char* R = stages + (size_t)st * a.stage_bytes;
-        const bool back = g >= nf;
-        const int l = back ? g - nf : g;
-        const int* lp = back ? a.lev_b + inf.lev_off_b : a.lev_f + inf.lev_off_f;
-        const int c = lp[l + 1] - lp[l];
-        const int C = back ? a.rows_b[inf.lev_off_b + l] : a.rows_f[inf.lev_off_f + l];
-        const int w = back ? inf.wu : inf.wl;
-        const uint16_t* rr = reinterpret_cast<const uint16_t*>(R);
-        const uint16_t* cc = rr + C;
-        const TF* vv = reinterpret_cast<const TF*>(cc + (size_t)C * w);
-        for (int q = threadIdx.x; q < c; q += blockDim.x) {
-            const int r = rr[q];
-            TS acc = t[r];
-            for (int k = 0; k < w; ++k)
-                acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vv[(size_t)k * C + q]),
-                                         t[cc[(size_t)k * C + q]]);
-            if (back) acc = acc / Load<TS>::f(vv[(size_t)w * C + q]);
-            t[r] = acc;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && g + D < T) {
+        if (producer && g + D < T) {
             fence_proxy_async();
             issue(g + D);
         }
@@ -304,7 +336,22 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     if (mode == 0) {
         const int* ol = a.ownloc + inf.own_off;
         const int* og = a.owned + inf.own_off;
-        for (int q = threadIdx.x; q < inf.n_own; q += blockDim.x) {
+        const int bs = blockDim.x;
+        int q = threadIdx.x;
+        for (; q + 3 * bs < inf.n_own; q += 4 * bs) {
+            int l[4], g[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                l[u] = ol[q + u * bs];
+                g[u] = og[q + u * bs];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (coarse) y[g[u]] = Store<TO>::f(__dadd_rn((double)t[l[u]], zc));
+                else y[g[u]] = Store<TO>::f(t[l[u]]);
+            }
+        }
+        for (; q < inf.n_own; q += bs) {
             const int li = ol[q];
             if (coarse) y[og[q]] = Store<TO>::f(__dadd_rn((double)t[li], zc));
             else y[og[q]] = Store<TO>::f(t[li]);
@@ -339,13 +386,17 @@ RecArgs rec_args(sg_precond* pc) {
     a.nc = pc->nc;
     a.depth = pc->rec_depth;
     a.stage_bytes = (int)pc->rec_stage_bytes;
+    a.max_n = pc->max_n;
+    a.max_levels = pc->max_levels;
     a.err = pc->err_d.p;
     return a;
 }
 
 size_t sweep_smem(const sg_precond* pc, int depth) {
     const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
-    return 128 + (size_t)depth * (size_t)pc->rec_stage_bytes + (size_t)(pc->max_n + 1) * ts;
+    const size_t tbytes = ((size_t)(pc->max_n + 1) * ts + 15) & ~(size_t)15;
+    return 128 + (size_t)depth * (size_t)pc->rec_stage_bytes + tbytes +
+           (size_t)pc->max_levels * 16;
 }
 
 template <class TI, class TO, class TS, class TF, bool EXACT>

@@ -28,10 +28,10 @@ def to_sg(sg, A):
     return sg.CSRMatrix(A.nrows, A.ncols, A.row_ptr, A.col_idx, A.vals)
 
 
-def make_pc(sg, kind, nparts, overlap, part, fdt=None, sdt=None, generic=False):
+def make_pc(sg, kind, nparts, overlap, part, fdt=None, sdt=None, sweep="tma"):
     fdt = sg.FP64 if fdt is None else fdt
     sdt = sg.FP64 if sdt is None else sdt
-    kw = {"generic_sweep": generic}
+    kw = {"sweep": sweep}
     if kind == "jacobi":
         return sg.JacobiPrecond(sweep_dtype=sdt, **kw)
     if kind == "ilu0":
@@ -119,6 +119,38 @@ def test_spmv_device_pointers(sg):
     assert np.array_equal(yd.cpu().numpy(), A.spmv(x))
 
 
+# ------------------------------------------------------------------ BLAS-1
+@pytest.mark.parametrize("n", [0, 1, 31, 1000, 262144 + 17])
+def test_blas1_vs_reference_loops(sg, n):
+    """dot/norm2 within 1e-14 relative (summation order); axpy/scale bit-exact
+    (src/core/vector.h:11-44)."""
+    x = sg.uniform(n, seed=5)
+    y = sg.uniform(n, seed=6)
+    ref_dot = 0.0
+    for a, b in zip(x.tolist(), y.tolist()):
+        ref_dot += a * b
+    d = sg.dot(x, y)
+    assert abs(d - ref_dot) <= 1e-14 * max(1.0, np.abs(x * y).sum())
+    assert abs(sg.norm2(x) - np.sqrt(np.dot(x, x))) <= 1e-14 * max(1.0, np.sqrt(np.dot(x, x)))
+    z = y.copy()
+    sg.axpy(-0.37, x, z)
+    assert np.array_equal(z, y + (-0.37) * x)
+    w = x.copy()
+    sg.scale(1.7, w)
+    assert np.array_equal(w, x * 1.7)
+
+
+def test_blas1_device_pointers(sg):
+    torch = pytest.importorskip("torch")
+    x = sg.uniform(100000, seed=1)
+    y = sg.uniform(100000, seed=2)
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    assert sg.dot(xd, yd) == sg.dot(x, y)
+    sg.axpy(2.0, xd, yd)
+    torch.cuda.synchronize()
+    assert np.array_equal(yd.cpu().numpy(), y + 2.0 * x)
+
+
 # ------------------------------------------------------------------ set-up
 @pytest.mark.parametrize("case", CASES)
 def test_device_ilu_factors_bit_exact(sg, oracle, golden, case):
@@ -191,23 +223,25 @@ def test_apply_low_precision(sg, oracle, kind, dt):
 
 @pytest.mark.parametrize("kind", ["ilu0", "asm", "ras", "twolevel_ras"])
 @pytest.mark.parametrize("dt", ["fp64", "fp32", "bf16"])
-def test_generic_and_tma_sweeps_agree(sg, kind, dt):
-    """The TMA-fed sweep and the generic level sweep compute the same thing
-    (bit-exact in FP64; FP32/BF16 up to the atomic order of ASM)."""
+def test_sweep_variants_agree(sg, kind, dt):
+    """The sync-free sweep, the level sweep (a barrier per level) and the
+    TMA-fed level sweep compute the same thing: bit-exact (same operations in
+    the same order per row), up to the atomic order of the ASM sums."""
     A = sg.make_varcoef_3d(20, 22, 18, 1.0, 5.0, 4)
     part = sg.partition_boxes(20, 22, 18, 12, 0.1, 2)
     x = sg.uniform(A.nrows, seed=9)
     fdt = {"fp64": sg.FP64, "fp32": sg.FP32, "bf16": sg.BF16}[dt]
     sdt = sg.FP64 if dt == "fp64" else sg.FP32
     ys = []
-    for generic in (False, True):
-        pc = make_pc(sg, kind, 12, 1, part, fdt, sdt, generic=generic)
+    for sweep in ("tma", "level", "syncfree"):
+        pc = make_pc(sg, kind, 12, 1, part, fdt, sdt, sweep=sweep)
         pc.setup(A)
         ys.append(pc.apply(x))
-    if kind == "asm":
-        assert rel(ys[0], ys[1]) <= 1e-6
-    else:
-        assert np.array_equal(ys[0], ys[1])
+    for y in ys[1:]:
+        if kind == "asm":
+            assert rel(y, ys[0]) <= 1e-6
+        else:
+            assert np.array_equal(y, ys[0])
 
 
 def test_apply_large_subdomains_and_many_parts(sg, oracle):
@@ -383,6 +417,28 @@ def test_two_level_varcoef_true_residual(sg, oracle, solver):
         xo, _ = _oracle_true_rel(oracle, H, b, oracle.precond("twolevel_ras", H, 32, 1, part),
                                  30, 1e-8, fgmres=solver == "fgmres")
         assert rel(x, xo) <= 1e-5
+
+
+@pytest.mark.parametrize("solver", ["gmres", "fgmres"])
+def test_mixed_keeps_fp64_iteration_count(sg, solver):
+    """The FP32 inner Krylov cycle (CGS2 in FP32) keeps the basis orthogonal:
+    on a 48^3 two-level problem it needs about the FP64 solver's iterations;
+    a loss of orthogonality shows up as many extra iterations."""
+    A = sg.make_varcoef_3d(48, 48, 48, 1.0, 8.0, 1)
+    b = A.spmv(sg.uniform(A.nrows, seed=3))
+    part = sg.partition_boxes(48, 48, 48, 27, 0.08, 2)
+    its = {}
+    for prec in (sg.FP64, sg.FP32):
+        sd = sg.FP64 if prec == sg.FP64 else sg.FP32
+        pc = sg.TwoLevelSchwarzPrecond(27, 1, sg.FineLevelType.RAS, part, sd, sd)
+        pc.setup(A)
+        x = np.zeros(A.nrows)
+        fn = sg.gmres if solver == "gmres" else sg.fgmres
+        r = fn(A, b, x, pc, sg.GMRESParams(restart=30, max_iter=3000, tol=1e-8,
+                                            tol_kind=sg.TOL_TRUE_REL, precision=prec))
+        assert r.converged and r.true_rel_residual <= 1e-8
+        its[prec] = r.iterations
+    assert its[sg.FP32] <= 1.15 * its[sg.FP64] + 5, its
 
 
 def test_solve_device_pointers(sg):
