@@ -210,6 +210,25 @@ sg_status sg_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n, 
 /* scale x *= alpha (vector.h:40-44), same bits as the reference loop */
 sg_status sg_scale(sg_ctx* ctx, double alpha, double* x, int n, sg_mem mem);
 
+/* ---- allocation-free dot product -------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need a reduction -- code running while its stream is
+ * captured into a CUDA graph (no cudaMalloc/cudaFree during capture), plug-ins
+ * inside an application that owns all device memory through its own pool,
+ * real-time loops that cannot pay cudaFree's device-wide synchronisation.
+ * Computes *result = dot(x, y) like sg_dot, but takes its per-block partial
+ * sums from a fixed 64 KiB array inside the library instead of a context,
+ * needs no sg_ctx, and calls no allocator.  x, y and result are device
+ * pointers on the current device; the kernel runs on `stream` (NULL: the
+ * default stream) and the call does not wait for it.
+ * Limits: n <= SG_DOT_NOALLOC_MAX_N, else SG_ERR_INVALID_ARG and nothing runs.
+ * All calls on a device share the array: calls whose kernels overlap on the
+ * GPU race and return wrong sums.  The first call on a device (with that
+ * device current) looks up the array's address; make it before any stream
+ * capture. */
+#define SG_DOT_NOALLOC_MAX_N 33554432
+sg_status sg_dot_noalloc(const double* x, const double* y, int n, double* result, void* stream);
+
 /* ---- problem generators and partitions (host side, deterministic) ----- */
 /* make_poisson_2d / make_poisson_3d (src/mesh/poisson.h:10-74).  Call with
  * NULL arrays to get nnz, then with arrays of n+1 / nnz / nnz entries. */

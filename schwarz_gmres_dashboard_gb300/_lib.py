@@ -88,6 +88,7 @@ PROTOTYPES = {
     "sg_norm2": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _dp]),
     "sg_axpy": (C.c_int, [_vp, C.c_double, _vp, _vp, C.c_int, C.c_int]),
     "sg_scale": (C.c_int, [_vp, C.c_double, _vp, C.c_int, C.c_int]),
+    "sg_dot_noalloc": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
     "sg_gen_poisson2d": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _ip]),
     "sg_gen_poisson3d": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _ip]),
     "sg_gen_varcoef3d": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,

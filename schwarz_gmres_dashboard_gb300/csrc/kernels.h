@@ -49,6 +49,9 @@ void launch_dot(sg_ctx* ctx, const double* x, const double* y, int n, double* ou
 void launch_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n);
 void launch_scale(sg_ctx* ctx, double alpha, double* x, int n);
 int dot_grid(int num_sms, int n);
+// the dot kernel with caller-provided scratch (blocks partial sums) and stream
+void launch_dot_scratch(cudaStream_t stream, const double* x, const double* y, int n,
+                        int blocks, double* partials, unsigned* counter, double* out_dev);
 // cycle bookkeeping after the update: cycles++, out-of-iterations test
 void launch_cycle_end(sg_ctx* ctx, SolveState* st);
 

@@ -607,6 +607,12 @@ void launch_dot(sg_ctx* ctx, const double* x, const double* y, int n, double* ou
     count_launch(ctx);
 }
 
+void launch_dot_scratch(cudaStream_t stream, const double* x, const double* y, int n,
+                        int blocks, double* partials, unsigned* counter, double* out_dev) {
+    k_dot<<<blocks, KT, 0, stream>>>(x, y, n, partials, counter, out_dev);
+    SG_CUDA(cudaGetLastError());
+}
+
 void launch_axpy(sg_ctx* ctx, double alpha, const double* x, double* y, int n) {
     k_axpy<<<kgrid(ctx, n, 8), KT, 0, ctx->stream>>>(alpha, x, y, n);
     SG_CUDA(cudaGetLastError());

@@ -1,0 +1,61 @@
+"""sg_dot_noalloc: the dot product for callers that cannot allocate device memory.
+
+Who needs it: code that runs while its stream is being captured into a CUDA
+graph (cudaMalloc/cudaFree are not allowed during capture), plug-ins inside an
+application that owns all device memory through its own pool, and real-time
+loops that cannot pay cudaFree's device-wide synchronisation.  sg_dot takes
+its reduction scratch from a context, which allocates; sg_dot_noalloc keeps
+that scratch in a fixed array inside the library.
+
+The test calls the entry point through the C ABI (ctypes) twice in a row,
+on different sizes (the second call finds the first call's partial sums still
+in the shared array), and checks each result against sg_dot -- the existing
+entry point -- within the dot-product tolerance the other tests use
+(1e-14 relative to sum |x_i y_i|: the two kernels add the same terms in
+different block orders).  The device buffers come from torch; the entry point
+itself allocates nothing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MAX_N = 33554432  # SG_DOT_NOALLOC_MAX_N
+
+
+def test_dot_noalloc_matches_sg_dot_on_two_calls(sg):
+    torch = pytest.importorskip("torch")
+    from schwarz_gmres_dashboard_gb300 import _lib
+
+    lib = _lib.load()
+    for n, seed in ((1_000_003, 1), (262_147, 2)):
+        x = sg.uniform(n, seed=seed)
+        y = sg.uniform(n, seed=seed + 10)
+        xd = torch.from_numpy(x).cuda()
+        yd = torch.from_numpy(y).cuda()
+        out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        st = lib.sg_dot_noalloc(C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr()), n,
+                                C.c_void_p(out.data_ptr()), None)
+        assert st == 0, lib.sg_last_error().decode()
+        torch.cuda.synchronize()
+        got = float(out.item())
+        ref = sg.dot(xd, yd)  # the existing entry point (context scratch)
+        assert abs(got - ref) <= 1e-14 * float(np.abs(x * y).sum()), (got, ref)
+
+
+def test_dot_noalloc_rejects_sizes_beyond_its_scratch(sg):
+    torch = pytest.importorskip("torch")
+    from schwarz_gmres_dashboard_gb300 import _lib
+
+    lib = _lib.load()
+    xd = torch.zeros(8, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    st = lib.sg_dot_noalloc(C.c_void_p(xd.data_ptr()), C.c_void_p(xd.data_ptr()), MAX_N + 1,
+                            C.c_void_p(out.data_ptr()), None)
+    assert st == 1  # SG_ERR_INVALID_ARG, nothing launched
+    assert b"exceeds" in lib.sg_last_error()
