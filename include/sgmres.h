@@ -229,6 +229,74 @@ sg_status sg_scale(sg_ctx* ctx, double alpha, double* x, int n, sg_mem mem);
 #define SG_DOT_NOALLOC_MAX_N 33554432
 sg_status sg_dot_noalloc(const double* x, const double* y, int n, double* result, void* stream);
 
+/* ---- learned coarse-correction stage ---------------------------------- */
+/* No counterpart in the reference (its FGMRES accepts any preconditioner,
+ * src/core/fgmres.cpp:164-172, which is where this stage plugs in).
+ * Attached to a Schwarz preconditioner M, an apply becomes
+ *   z1 = M v;  r1 = v - A z1;  s = rms(R r1);
+ *   z  = z1 + s * c * P(CNN([R r1 / s, f]))
+ * with R the mean over 2x2x2 cells (an nx^3 grid, nx a multiple of 16, to
+ * (nx/2)^3), f the standardised restricted log A_ii, CNN four 3x3x3
+ * convolutions with 16 channels and ReLU (BF16 weights and activations,
+ * FP32 accumulation, tensor cores), c an output scale and P cell-centred
+ * trilinear prolongation.  The stage is nonlinear: sg_solve accepts it with
+ * SG_FGMRES only.  After every restart cycle a device monitor switches it
+ * off for the rest of the solve when the cycle reduced the FP64 true
+ * residual by less than the stagnation ratio (the plain M is the fallback).
+ *
+ * Parameters: sg_learned_num_params() floats = 4 layers x (27*16*16 weights
+ * in [tap][c_in][c_out] order, tap = (dz+1)*9 + (dy+1)*3 + (dx+1), then 16
+ * biases), then c.  Padded channels (inputs 2-15 of layer 1, outputs 1-15 of
+ * layer 4) are kept at 0. */
+typedef struct sg_learned sg_learned;
+int sg_learned_num_params(void);
+sg_status sg_learned_create(sg_ctx* ctx, int nx, int ny, int nz, sg_learned** out);
+/* Detaches it from its preconditioner first. */
+sg_status sg_learned_destroy(sg_learned* L);
+/* The operator of the residual r1 and the source of the feature f; kept by
+ * pointer (it must outlive its use by the stage). */
+sg_status sg_learned_set_matrix(sg_learned* L, const sg_csr* A);
+/* Seeded He-uniform initialisation (last layer x0.1); resets Adam. */
+sg_status sg_learned_init_weights(sg_learned* L, uint64_t seed);
+sg_status sg_learned_set_weights(sg_learned* L, const float* w, int count);
+sg_status sg_learned_get_weights(sg_learned* L, float* w, int count);
+/* Training pair from a plain solve: residual r = b - A x_k and error
+ * e = x* - x_k.  Stores the input R r1 / s, the feature f and the target
+ * R(e - M r) / s on the device (M: pc without any learned stage). */
+sg_status sg_learned_add_pair(sg_learned* L, sg_precond* pc, const double* r, const double* e,
+                              int n, sg_mem mem);
+sg_status sg_learned_num_samples(sg_learned* L, int* count);
+sg_status sg_learned_clear_samples(sg_learned* L);
+/* Copies stored sample i (each array nc = (nx/2)^3 floats; NULL skips). */
+sg_status sg_learned_get_sample(sg_learned* L, int i, float* input, float* feature,
+                                float* target);
+/* Adam (lr, betas 0.9/0.999, eps 1e-8) on the mean squared error between
+ * the network output and target / c over samples [first, first+count), in
+ * shuffled mini-batches (SplitMix64(seed) Fisher-Yates per epoch); sets c to
+ * the rms of those targets first.  epoch_loss (optional) receives the mean
+ * batch loss of every epoch. */
+sg_status sg_learned_train(sg_learned* L, int first, int count, int epochs, int batch, double lr,
+                           uint64_t seed, double* epoch_loss);
+/* Mean loss of the current network over samples [first, first+count). */
+sg_status sg_learned_eval(sg_learned* L, int first, int count, double* loss);
+/* The network alone on host inputs x [batch][nc][2] (channel-last FP32,
+ * rounded to BF16 on the device): y [batch][nc]. */
+sg_status sg_learned_forward(sg_learned* L, const float* x, int batch, float* y);
+/* loss = mean over batch*nc of (y - t)^2 and its gradient with respect to the
+ * network parameters (grad: sg_learned_num_params() - 1 floats). */
+sg_status sg_learned_gradient(sg_learned* L, const float* x, const float* t, int batch,
+                              float* grad, double* loss);
+/* Switch the stage on/off for later applies and solves. */
+sg_status sg_learned_set_enabled(sg_learned* L, int on);
+/* enabled: 1 while on; fallback_cycle: restart cycle after which the monitor
+ * switched it off in the last solve (-1: never); applies: stage applies so far. */
+sg_status sg_learned_get_state(sg_learned* L, int* enabled, int* fallback_cycle,
+                               long long* applies);
+/* Attach L after pc's apply (ASM/RAS and two-level kinds), with the monitor's
+ * stagnation ratio (0: no monitor); L == NULL detaches.  A learned stage
+ * serves one preconditioner at a time. */
+sg_status sg_precond_set_learned(sg_precond* pc, sg_learned* L, double stagnation);
+
 /* ---- problem generators and partitions (host side, deterministic) ----- */
 /* make_poisson_2d / make_poisson_3d (src/mesh/poisson.h:10-74).  Call with
  * NULL arrays to get nnz, then with arrays of n+1 / nnz / nnz entries. */

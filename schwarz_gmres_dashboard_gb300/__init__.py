@@ -35,6 +35,7 @@ __all__ = [
     "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
     "TwoLevelSchwarzPrecond", "FineLevelType", "GMRESParams", "GMRESResult", "gmres", "fgmres",
     "FP64", "FP32", "BF16", "TOL_REF_ABS", "TOL_TRUE_REL_CYCLE", "TOL_TRUE_REL",
+    "LearnedCorrection", "collect_pairs",
 ]
 
 FP64, FP32, BF16 = L.FP64, L.FP32, L.BF16
@@ -562,3 +563,6 @@ def fgmres(A: CSRMatrix, b, x, M: Optional[Preconditioner] = None,
            params: Optional[GMRESParams] = None) -> GMRESResult:
     """FGMRES(m), right preconditioning (src/core/fgmres.h:42-47)."""
     return _solve(L.FGMRES, A, b, x, M, params)
+
+
+from .learned import LearnedCorrection, collect_pairs  # noqa: E402  (uses the names above)

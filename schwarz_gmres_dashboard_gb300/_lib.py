@@ -99,6 +99,25 @@ PROTOTYPES = {
                                      C.c_uint64, _vp]),
     "sg_schwarz_structure": (C.c_int, [C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp,
                                        C.c_int, _ip]),
+    "sg_learned_num_params": (C.c_int, []),
+    "sg_learned_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "sg_learned_destroy": (C.c_int, [_vp]),
+    "sg_learned_set_matrix": (C.c_int, [_vp, _vp]),
+    "sg_learned_init_weights": (C.c_int, [_vp, C.c_uint64]),
+    "sg_learned_set_weights": (C.c_int, [_vp, _vp, C.c_int]),
+    "sg_learned_get_weights": (C.c_int, [_vp, _vp, C.c_int]),
+    "sg_learned_add_pair": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int]),
+    "sg_learned_num_samples": (C.c_int, [_vp, _ip]),
+    "sg_learned_clear_samples": (C.c_int, [_vp]),
+    "sg_learned_get_sample": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "sg_learned_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                   C.c_uint64, _vp]),
+    "sg_learned_eval": (C.c_int, [_vp, C.c_int, C.c_int, _dp]),
+    "sg_learned_forward": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "sg_learned_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _dp]),
+    "sg_learned_set_enabled": (C.c_int, [_vp, C.c_int]),
+    "sg_learned_get_state": (C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_longlong)]),
+    "sg_precond_set_learned": (C.c_int, [_vp, _vp, C.c_double]),
 }
 
 _lib = None

@@ -446,6 +446,7 @@ sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg
             dy = pc->io_y.p;
         }
         precond_apply_device<double, double>(pc, dx, dy, nullptr, true);
+        if (pc->learned) learned_apply<double, double>(pc->learned, dx, dy, n, nullptr);
         if (mem == SG_MEM_HOST)
             SG_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -458,6 +459,7 @@ sg_status sg_precond_destroy(sg_precond* pc) {
     return guard([&] {
         if (!pc) return;
         cudaSetDevice(pc->ctx->device);
+        learned_detach(pc->learned);
         delete pc;
     });
 }
@@ -543,6 +545,8 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
             SG_CHECK_ARG(pc->ctx == ctx, "preconditioner belongs to a different context");
             if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
             SG_CHECK_ARG(pc->n == n, "preconditioner was set up for n=%d", pc->n);
+            SG_CHECK_ARG(!pc->learned || solver == SG_FGMRES,
+                         "a learned stage makes the preconditioner nonlinear: use SG_FGMRES");
         }
         sg_solve_params prm{};
         if (params) prm = *params;

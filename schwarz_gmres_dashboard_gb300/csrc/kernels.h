@@ -69,6 +69,16 @@ template <class TI, class TO>
 bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
                const int* active);
 int sweep_error(sg_precond* pc);
+// ---------------------------------------------------------------- learned.cu
+// y += learned correction of the preconditioned vector y = M x (x: the
+// vector M was applied to; n: its length, checked against the stage's grid)
+template <class TI, class TO>
+void learned_apply(sg_learned* L, const TI* x, TO* y, int n, const int* active);
+// solve start (stage on, monitor reset) and the per-cycle stagnation monitor
+void learned_begin(sg_learned* L, SolveState* st);
+void learned_monitor(sg_learned* L, SolveState* st);
+void learned_detach(sg_learned* L);
+
 // copy the FP64 factors of subdomain s back to the host
 void precond_read_factors(sg_precond* pc, int s, double* lu_out);
 void precond_read_coarse(sg_precond* pc, double* a0_out);

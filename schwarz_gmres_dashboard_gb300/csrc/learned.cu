@@ -1,0 +1,1215 @@
+// learned.cu -- the learned coarse-correction stage (no counterpart in the
+// reference).  Attached to a Schwarz preconditioner M it turns the apply into
+//
+//   z1 = M v                                  (two-level RAS etc.)
+//   r1 = v - A z1                             (what M left unresolved)
+//   s  = rms(R r1)
+//   z  = z1 + s * c * P( CNN( [R r1 / s, f] ) )
+//
+//   R   restriction to the half-resolution grid (mean of the 2x2x2 children)
+//   f   the coefficient feature: restricted log A_ii, standardised
+//   CNN 4 layers of 3x3x3 convolutions, 16 channels, ReLU after layers 1-3,
+//       BF16 weights and activations, FP32 accumulation, output channel 0
+//   c   output scale (rms of the training targets)
+//   P   cell-centred trilinear prolongation back to the fine grid
+//
+// The network learns R(e - M r) / s from (residual r, error e = A^{-1} r)
+// pairs of plain solves: the coarse error left after M.  Scaling by s makes
+// the stage positively homogeneous (FGMRES applies it to unnormalised
+// vectors); the stage is nonlinear, so it runs inside FGMRES only.  A device
+// monitor after every restart cycle switches the stage off for the rest of
+// the solve when the cycle reduced the FP64 true residual by less than the
+// stagnation ratio -- the plain preconditioner is the fallback.
+//
+// Every layer is an implicit GEMM on the tensor cores (mma.sync m16n8k16,
+// BF16 x BF16 -> FP32): a CTA owns an 8x8x8 block of output voxels, stages
+// the 10x10x10 input halo (16 channels, channel-last) and the layer's weights
+// in shared memory, and each warp accumulates one z-plane of 64 voxels over
+// the 27 taps (K = 16 channels per tap).  The input gradient is the same
+// kernel with flipped, transposed weights and the ReLU mask of the layer
+// input in the epilogue; the weight gradient is a second mma kernel (M =
+// input channel, N = output channel, K = the tile's voxels) whose per-CTA
+// partials a reduction kernel adds in a fixed order.  Channels are padded to
+// 16 everywhere (layer 1 reads 2, layer 4 writes 1); padded weights stay 0.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+constexpr int LC = 16;                    // channels (padded)
+constexpr int LTAPS = 27;
+constexpr int LAYER_W = LTAPS * LC * LC;  // weights of one layer, master layout [tap][ci][co]
+constexpr int LAYER_P = LAYER_W + LC;     // + bias
+constexpr int NLAYERS = 4;
+constexpr int NET_PARAMS = NLAYERS * LAYER_P;
+constexpr int LEARN_PARAMS = NET_PARAMS + 1;  // + output scale c
+
+// device control block of one learned stage
+struct LearnedCtl {
+    float snorm;         // s of the current apply
+    float out_scale;     // c
+    int enabled;         // 0: the stage is skipped (fallback or switched off)
+    int fallback_cycle;  // restart cycle after which the monitor switched it off (-1)
+    double prev_rnorm;   // true residual at the previous cycle end
+    double stag;         // stagnation ratio of the monitor (0: no monitor)
+    unsigned long long applies;
+    float pair_s;        // s of the last training pair
+    float scratch_s;
+};
+
+namespace {
+
+constexpr int CT = 256;  // threads of the conv kernels (8 warps)
+constexpr int TB = 8;    // output tile edge
+constexpr int HB = TB + 2;
+constexpr int HALO_U32 = HB * HB * HB * 8;
+constexpr int TILE_U32 = TB * TB * TB * 8;
+constexpr int W_U32 = LTAPS * LC * 8;
+constexpr int WGRAD_SMEM = (HALO_U32 + TILE_U32) * 4 + CT * 4;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+enum { EPI_RELU = 0, EPI_LINEAR_F32 = 1, EPI_MASK = 2 };
+
+__device__ __forceinline__ bool skip(const int* enabled, const int* active) {
+    return (active && *active == 0) || (enabled && *enabled == 0);
+}
+
+// Loads the 10x10x10 halo of the tile at (z0,y0,x0) of a [D][D][D][16] BF16
+// volume (zero outside) into smem as uint32 channel pairs: halo[v*8 + pair].
+__device__ __forceinline__ void load_halo(uint32_t* halo, const uint32_t* __restrict__ in, int D,
+                                          int z0, int y0, int x0) {
+    for (int q = threadIdx.x; q < HB * HB * HB * 2; q += blockDim.x) {
+        const int v = q >> 1, half = q & 1;
+        const int hz = v / (HB * HB), hy = (v / HB) % HB, hx = v % HB;
+        const int z = z0 + hz - 1, y = y0 + hy - 1, x = x0 + hx - 1;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (z >= 0 && z < D && y >= 0 && y < D && x >= 0 && x < D)
+            val = reinterpret_cast<const uint4*>(in)[(((size_t)z * D + y) * D + x) * 2 + half];
+        reinterpret_cast<uint4*>(halo)[q] = val;
+    }
+}
+
+// conv3d 3x3x3, 16 -> 16 channels, one 8^3 output tile per CTA, grid =
+// tiles x batch.  w: BF16 [27][co][ci] (ci contiguous).  Epilogues:
+//  RELU        out = relu(acc + bias) as BF16 [V][16]
+//  LINEAR_F32  outf[v] = acc[ch 0] + bias[0] (FP32, one channel)
+//  MASK        out = acc * (mask[v][ch] > 0) as BF16 (input gradient; no bias)
+__global__ void __launch_bounds__(CT)
+k_conv3d(const uint32_t* __restrict__ in, const uint32_t* __restrict__ w,
+         const float* __restrict__ bias, int D, int epi, uint32_t* __restrict__ out,
+         float* __restrict__ outf, const uint32_t* __restrict__ mask, const int* enabled,
+         const int* active) {
+    if (skip(enabled, active)) return;
+    __shared__ __align__(16) uint32_t halo[HALO_U32];
+    __shared__ __align__(16) uint32_t ws[W_U32];
+    const int tiles = D / TB;
+    const int nt3 = tiles * tiles * tiles;
+    const int b = blockIdx.x / nt3;
+    const int t = blockIdx.x % nt3;
+    const int z0 = (t / (tiles * tiles)) * TB, y0 = ((t / tiles) % tiles) * TB, x0 = (t % tiles) * TB;
+    const size_t V = (size_t)D * D * D;
+    load_halo(halo, in + (size_t)b * V * 8, D, z0, y0, x0);
+    for (int q = threadIdx.x; q < W_U32 / 4; q += blockDim.x)
+        reinterpret_cast<uint4*>(ws)[q] = reinterpret_cast<const uint4*>(w)[q];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, tg = lane & 3;
+    const int z = warp;  // this warp's z-plane of the tile
+    float acc[4][2][4];
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[mt][nt][e] = 0.f;
+    for (int tap = 0; tap < LTAPS; ++tap) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        uint32_t bf[2][2];
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+            const uint32_t* wr = ws + (tap * LC + nt * 8 + g) * 8;
+            bf[nt][0] = wr[tg];
+            bf[nt][1] = wr[tg + 4];
+        }
+        // M-tile mt covers rows y = 2mt, 2mt+1 of the plane: row r -> (y = 2mt + r/8, x = r%8)
+        const int hbase = (z + 1 + dz) * HB * HB + (1 + dy) * HB + (1 + dx);
+#pragma unroll
+        for (int mt = 0; mt < 4; ++mt) {
+            const int h0 = hbase + (2 * mt) * HB + g;
+            const int h1 = h0 + HB;
+            uint32_t af[4];
+            af[0] = halo[h0 * 8 + tg];
+            af[1] = halo[h1 * 8 + tg];
+            af[2] = halo[h0 * 8 + tg + 4];
+            af[3] = halo[h1 * 8 + tg + 4];
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) mma_bf16(acc[mt][nt], af, bf[nt]);
+        }
+    }
+    // C fragment: rows g / g+8 of the M-tile (y = 2mt / 2mt+1, x = g),
+    // columns nt*8 + 2tg, +1
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt) {
+#pragma unroll
+        for (int hr = 0; hr < 2; ++hr) {
+            const int yy = y0 + 2 * mt + hr, xx = x0 + g, zz = z0 + z;
+            const size_t v = (size_t)b * V + ((size_t)zz * D + yy) * D + xx;
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) {
+                const int ch = nt * 8 + 2 * tg;
+                float a0 = acc[mt][nt][2 * hr], a1 = acc[mt][nt][2 * hr + 1];
+                if (epi == EPI_RELU) {
+                    a0 = fmaxf(a0 + bias[ch], 0.f);
+                    a1 = fmaxf(a1 + bias[ch + 1], 0.f);
+                    out[v * 8 + ch / 2] = pack_bf16(a0, a1);
+                } else if (epi == EPI_MASK) {
+                    const uint32_t mk = mask[v * 8 + ch / 2];
+                    a0 = bf_lo(mk) > 0.f ? a0 : 0.f;
+                    a1 = bf_hi(mk) > 0.f ? a1 : 0.f;
+                    out[v * 8 + ch / 2] = pack_bf16(a0, a1);
+                } else if (ch == 0) {
+                    outf[v] = a0 + bias[0];
+                }
+            }
+        }
+    }
+}
+
+// Weight-gradient partials of one tile: dW[tap][ci][co] = sum over the tile's
+// voxels v of X[v + off(tap)][ci] * G[v][co]; dB[co] = sum_v G[v][co].
+// mma with M = ci (16), N = co (2 x 8), K = voxels (16 per step).  Dynamic
+// smem: halo | G tile | bias scratch.
+__global__ void __launch_bounds__(CT)
+k_conv3d_wgrad(const uint32_t* __restrict__ X, const uint32_t* __restrict__ G, int D,
+               float* __restrict__ part) {
+    extern __shared__ __align__(16) uint32_t wsm[];
+    uint32_t* halo = wsm;
+    uint32_t* gt = wsm + HALO_U32;
+    float* bred = reinterpret_cast<float*>(wsm + HALO_U32 + TILE_U32);
+    const int tiles = D / TB;
+    const int nt3 = tiles * tiles * tiles;
+    const int b = blockIdx.x / nt3;
+    const int t = blockIdx.x % nt3;
+    const int z0 = (t / (tiles * tiles)) * TB, y0 = ((t / tiles) % tiles) * TB, x0 = (t % tiles) * TB;
+    const size_t V = (size_t)D * D * D;
+    load_halo(halo, X + (size_t)b * V * 8, D, z0, y0, x0);
+    for (int q = threadIdx.x; q < TB * TB * TB * 2; q += blockDim.x) {
+        const int v = q >> 1, half = q & 1;
+        const int vz = v / (TB * TB), vy = (v / TB) % TB, vx = v % TB;
+        const size_t gv = ((size_t)(z0 + vz) * D + (y0 + vy)) * D + (x0 + vx);
+        reinterpret_cast<uint4*>(gt)[q] =
+            reinterpret_cast<const uint4*>(G)[((size_t)b * V + gv) * 2 + half];
+    }
+    __syncthreads();
+    const unsigned short* hs = reinterpret_cast<const unsigned short*>(halo);
+    const unsigned short* gs = reinterpret_cast<const unsigned short*>(gt);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, tg = lane & 3;
+    float* pb = part + (size_t)blockIdx.x * LAYER_P;
+    for (int tap = warp; tap < LTAPS; tap += CT / 32) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+        for (int ks = 0; ks < TB * TB * TB / 16; ++ks) {
+            // K index kk in [0,16): voxel 16 ks + kk of the tile; 16 voxels =
+            // two x-runs of 8 (rows y = 2(ks%4), +1 of plane z = ks/4)
+            const int vz = ks >> 2, vy = 2 * (ks & 3);
+            const int base = (vz + 1 + dz) * HB * HB + (vy + 1 + dy) * HB + (1 + dx);
+            const int k0 = 2 * tg;  // columns k0, k0+1 (first run), k0+8, k0+9 (second)
+            const int ha = base + k0, hc = base + HB + k0;
+            uint32_t af[4];
+            af[0] = (uint32_t)hs[ha * 16 + g] | ((uint32_t)hs[(ha + 1) * 16 + g] << 16);
+            af[1] = (uint32_t)hs[ha * 16 + g + 8] | ((uint32_t)hs[(ha + 1) * 16 + g + 8] << 16);
+            af[2] = (uint32_t)hs[hc * 16 + g] | ((uint32_t)hs[(hc + 1) * 16 + g] << 16);
+            af[3] = (uint32_t)hs[hc * 16 + g + 8] | ((uint32_t)hs[(hc + 1) * 16 + g + 8] << 16);
+            const int va = 16 * ks + k0, vc = va + 8;
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) {
+                const int co = nt * 8 + g;
+                uint32_t bf[2];
+                bf[0] = (uint32_t)gs[va * 16 + co] | ((uint32_t)gs[(va + 1) * 16 + co] << 16);
+                bf[1] = (uint32_t)gs[vc * 16 + co] | ((uint32_t)gs[(vc + 1) * 16 + co] << 16);
+                mma_bf16(acc[nt], af, bf);
+            }
+        }
+        // C: row = ci (g / g+8), column = co (nt*8 + 2tg, +1)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int ci = g + (e >= 2 ? 8 : 0);
+                const int co = nt * 8 + 2 * tg + (e & 1);
+                pb[(tap * LC + ci) * LC + co] = acc[nt][e];
+            }
+    }
+    // bias gradient: 16 sums over the tile's 512 voxels (16 slices of 32)
+    {
+        const int co = threadIdx.x & 15, slice = threadIdx.x >> 4;
+        float s = 0.f;
+        for (int v = slice * 32; v < slice * 32 + 32; ++v)
+            s += __uint_as_float((uint32_t)gs[v * 16 + co] << 16);
+        bred[threadIdx.x] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < LC) {
+        float s = 0.f;
+        for (int sl = 0; sl < CT / 16; ++sl) s += bred[sl * 16 + threadIdx.x];
+        pb[LAYER_W + threadIdx.x] = s;
+    }
+}
+
+// grad[i] = mask[i] * sum over CTAs of part[cta][i] (CTA order)
+__global__ void k_wgrad_reduce(const float* __restrict__ part, int nblk,
+                               const float* __restrict__ pmask, float* __restrict__ grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= LAYER_P) return;
+    float s = 0.f;
+    for (int c = 0; c < nblk; ++c) s += part[(size_t)c * LAYER_P + i];
+    grad[i] = s * pmask[i];
+}
+
+// master FP32 [layer][tap][ci][co] -> forward BF16 [layer][tap][co][ci] and
+// the flipped, transposed BF16 weights of the input gradient
+// [layer][26 - tap][ci][co]
+__global__ void k_prep_weights(const float* __restrict__ master, __nv_bfloat16* __restrict__ wf,
+                               __nv_bfloat16* __restrict__ wt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NLAYERS * LAYER_W) return;
+    const int l = i / LAYER_W, r = i % LAYER_W;
+    const int tap = r / (LC * LC), ci = (r / LC) % LC, co = r % LC;
+    const __nv_bfloat16 v = __float2bfloat16_rn(master[(size_t)l * LAYER_P + r]);
+    wf[(size_t)l * LAYER_W + (tap * LC + co) * LC + ci] = v;
+    wt[(size_t)l * LAYER_W + ((LTAPS - 1 - tap) * LC + ci) * LC + co] = v;
+}
+
+// Adam (Kingma & Ba 2015) on the network parameters; padded entries stay 0
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ grad,
+                       float* __restrict__ m1, float* __restrict__ m2,
+                       const float* __restrict__ pmask, int count, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float gr = grad[i];
+    const float a = b1 * m1[i] + (1.f - b1) * gr;
+    const float v = b2 * m2[i] + (1.f - b2) * gr * gr;
+    m1[i] = a;
+    m2[i] = v;
+    p[i] = (p[i] - lr * (a / c1) / (sqrtf(v / c2) + eps)) * pmask[i];
+}
+
+// MSE over `count` outputs: loss += sum (Y - T)^2 / count (block sums added
+// atomically -- reporting only); G[v] = (2 (Y - T) / count, 0, ..., 0) as BF16
+__global__ void k_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, size_t count,
+                            uint32_t* __restrict__ G, float* __restrict__ loss) {
+    float s = 0.f;
+    const float inv = 1.f / (float)count;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float d = Y[i] - T[i];
+        s += d * d;
+        if (G) {
+            uint4* g4 = reinterpret_cast<uint4*>(G + i * 8);
+            g4[0] = make_uint4(pack_bf16(2.f * d * inv, 0.f), 0u, 0u, 0u);
+            g4[1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    s = warp_sum(s);
+    __shared__ float red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        atomicAdd(loss, t * inv);
+    }
+}
+
+// rc[c] = mean over the 8 children f of c of (v[f] - (A z)[f]) (z == nullptr:
+// of v[f]); s_out = sqrt(mean rc^2).  TA: arithmetic of the residual rows.
+template <class TA, class TI, class TO, class TV>
+__global__ void __launch_bounds__(256)
+k_resid_restrict(const int* __restrict__ rp, const int* __restrict__ ci, const TV* __restrict__ val,
+                 const TI* __restrict__ v, const TO* __restrict__ z, int nx, int ny, int nz,
+                 float* __restrict__ rc, double* partials, unsigned* counter, float* s_out,
+                 const int* enabled, const int* active) {
+    if (skip(enabled, active)) return;
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    const int nc = cx * cy * cz;
+    double ss = 0.0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int i = c % cx, j = (c / cx) % cy, k = c / (cx * cy);
+        TA s = 0;
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            const int fx = 2 * i + (o & 1), fy = 2 * j + ((o >> 1) & 1), fz = 2 * k + (o >> 2);
+            const int f = (fz * ny + fy) * nx + fx;
+            TA r = (TA)v[f];
+            if (z) {
+                TA az = 0;
+                for (int q = rp[f]; q < rp[f + 1]; ++q) az += (TA)val[q] * (TA)z[ci[q]];
+                r -= az;
+            }
+            s += r;
+        }
+        const float m = (float)(s * (TA)0.125);
+        rc[c] = m;
+        ss += (double)m * m;
+    }
+    __shared__ double red[8];
+    __shared__ double bs[1], tot[1];
+    double v1[1] = {ss};
+    block_sum_multi<1>(v1, 1, red, bs);
+    if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0)
+        *s_out = (float)sqrt(tot[0] / (double)nc);
+}
+
+// network input of one sample: channel 0 = rc / s, channel 1 = f, 2..15 = 0
+__global__ void k_pack_input(const float* __restrict__ rc, const float* __restrict__ feat, int nc,
+                             const float* __restrict__ snorm, const int* enabled,
+                             const int* active, uint32_t* __restrict__ X) {
+    if (skip(enabled, active)) return;
+    const float s = *snorm;
+    const float inv = s > 0.f ? 1.f / s : 0.f;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        uint4* x4 = reinterpret_cast<uint4*>(X + (size_t)c * 8);
+        x4[0] = make_uint4(pack_bf16(rc[c] * inv, feat[c]), 0u, 0u, 0u);
+        x4[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// packed inputs of a batch of stored samples (idx[b] = sample of batch entry
+// b; idx == nullptr: entry b is sample b); targets scaled by inv_c
+__global__ void k_pack_batch(const float* __restrict__ in, const float* __restrict__ feat,
+                             const float* __restrict__ tgt, const int* __restrict__ idx, int batch,
+                             int nc, float inv_c, uint32_t* __restrict__ X, float* __restrict__ T) {
+    const size_t total = (size_t)batch * nc;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(q / nc), c = (int)(q % nc);
+        const size_t src = (size_t)(idx ? idx[b] : b) * nc + c;
+        uint4* x4 = reinterpret_cast<uint4*>(X + q * 8);
+        x4[0] = make_uint4(pack_bf16(in[src], feat[src]), 0u, 0u, 0u);
+        x4[1] = make_uint4(0u, 0u, 0u, 0u);
+        if (T && tgt) T[q] = tgt[src] * inv_c;
+    }
+}
+
+// cell-centred trilinear stencil along one axis: fine index fc -> coarse
+// cells c = fc/2 (weight 3/4) and its neighbour towards fc (weight 1/4,
+// clamped to the grid)
+__device__ __forceinline__ void tri_axis(int fc, int nc, int (&id)[2]) {
+    const int c = fc >> 1;
+    const int o = (fc & 1) ? c + 1 : c - 1;
+    id[0] = c;
+    id[1] = o < 0 ? 0 : (o >= nc ? nc - 1 : o);
+}
+
+// z[f] += s * c * trilinear(Y)[f]
+template <class TO>
+__global__ void k_prolong_add(const float* __restrict__ Y, int nx, int ny, int nz,
+                              LearnedCtl* ctl, const int* active, TO* __restrict__ z) {
+    if (skip(&ctl->enabled, active)) return;
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    const float sc = ctl->snorm * ctl->out_scale;
+    const size_t n = (size_t)nx * ny * nz;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->applies += 1;
+    const float w[2] = {0.75f, 0.25f};
+    for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < n;
+         f += (size_t)gridDim.x * blockDim.x) {
+        const int fx = (int)(f % nx), fy = (int)((f / nx) % ny), fz = (int)(f / ((size_t)nx * ny));
+        int ia[2], ja[2], ka[2];
+        tri_axis(fx, cx, ia);
+        tri_axis(fy, cy, ja);
+        tri_axis(fz, cz, ka);
+        float acc = 0.f;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 2; ++bb) {
+                const float* row = Y + ((size_t)ka[a] * cy + ja[bb]) * cx;
+                acc += w[a] * w[bb] * (0.75f * row[ia[0]] + 0.25f * row[ia[1]]);
+            }
+        z[f] = z[f] + (TO)(sc * acc);
+    }
+}
+
+// training pair: in[slot] = rc / s, tgt[slot] = ec / s, feat[slot] = f
+__global__ void k_store_pair(const float* __restrict__ rc, const float* __restrict__ ec,
+                             const float* __restrict__ f, int nc, const LearnedCtl* ctl,
+                             float* __restrict__ in, float* __restrict__ tgt,
+                             float* __restrict__ feat) {
+    const float s = ctl->pair_s;
+    const float inv = s > 0.f ? 1.f / s : 0.f;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        in[c] = rc[c] * inv;
+        tgt[c] = ec[c] * inv;
+        feat[c] = f[c];
+    }
+}
+
+// out = a - b (FP64)
+__global__ void k_sub64(const double* __restrict__ a, const double* __restrict__ b, int n,
+                        double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = a[i] - b[i];
+}
+
+// solve start: stage on (unless switched off), monitor reference = initial residual
+__global__ void k_learned_begin(LearnedCtl* ctl, const SolveState* st, int on) {
+    ctl->enabled = on;
+    ctl->fallback_cycle = -1;
+    ctl->prev_rnorm = st->rnorm;
+}
+
+// after every restart cycle: switch the stage off when the cycle reduced the
+// FP64 true residual by less than the stagnation ratio (or it is not finite)
+__global__ void k_learned_monitor(LearnedCtl* ctl, const SolveState* st) {
+    if (!ctl->enabled || (st->done && st->converged)) return;
+    const double cur = st->rnorm;
+    if (ctl->stag > 0.0 && !(cur <= ctl->stag * ctl->prev_rnorm)) {
+        ctl->enabled = 0;
+        ctl->fallback_cycle = st->cycles;
+    }
+    ctl->prev_rnorm = cur;
+}
+
+}  // namespace
+
+// ============================================================ host side
+struct LearnedImpl {
+    sg_ctx* ctx = nullptr;
+    int nx = 0, ny = 0, nz = 0, cx = 0, cy = 0, cz = 0;
+    int nc = 0;  // coarse cells
+    const sg_csr* A = nullptr;
+    sg_precond* attached = nullptr;
+    bool on = true;
+    DBuf<float> master, grad, m1, m2, pmask;  // NET_PARAMS each
+    DBuf<__nv_bfloat16> wf, wt;              // NLAYERS * LAYER_W
+    DBuf<LearnedCtl> ctl;
+    DBuf<float> feat;                        // coefficient feature of A
+    DBuf<double> partials;
+    DBuf<unsigned> counter;
+    // inference scratch (one sample)
+    DBuf<float> rc, ec, yout;
+    DBuf<uint32_t> act[4];
+    // training pairs
+    DBuf<double> r64, e64, z64, t64;
+    DBuf<float> s_in, s_tgt, s_feat;
+    int nsamples = 0, cap = 0;
+    // training scratch
+    int tb = 0;
+    DBuf<uint32_t> tact[4], tg[2];
+    DBuf<float> ty, tt, tpart, tloss;
+    long long adam_t = 0;
+    float out_scale = 1.f;
+};
+
+}  // namespace sg
+
+struct sg_learned : sg::LearnedImpl {};
+
+namespace sg {
+
+namespace {
+
+int kblocks(sg_ctx* ctx, size_t n) {
+    const size_t b = (n + 255) / 256;
+    return (int)std::min<size_t>(std::max<size_t>(b, 1), (size_t)ctx->num_sms * 8);
+}
+
+void prep_weights(sg_learned* L) {
+    k_prep_weights<<<(NLAYERS * LAYER_W + 255) / 256, 256, 0, L->ctx->stream>>>(L->master.p, L->wf.p,
+                                                                             L->wt.p);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+}
+
+void conv(sg_learned* L, const uint32_t* in, int l, bool transposed, int epi, int batch,
+          uint32_t* out, float* outf, const uint32_t* mask, const int* enabled, const int* active) {
+    const int tiles = L->cx / TB;
+    const __nv_bfloat16* w = (transposed ? L->wt.p : L->wf.p) + (size_t)l * LAYER_W;
+    k_conv3d<<<tiles * tiles * tiles * batch, CT, 0, L->ctx->stream>>>(
+        in, reinterpret_cast<const uint32_t*>(w), L->master.p + (size_t)l * LAYER_P + LAYER_W,
+        L->cx, epi, out, outf, mask, enabled, active);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+}
+
+void forward(sg_learned* L, const uint32_t* X0, uint32_t* A1, uint32_t* A2, uint32_t* A3,
+             float* Y, int batch, const int* enabled, const int* active) {
+    conv(L, X0, 0, false, EPI_RELU, batch, A1, nullptr, nullptr, enabled, active);
+    conv(L, A1, 1, false, EPI_RELU, batch, A2, nullptr, nullptr, enabled, active);
+    conv(L, A2, 2, false, EPI_RELU, batch, A3, nullptr, nullptr, enabled, active);
+    conv(L, A3, 3, false, EPI_LINEAR_F32, batch, nullptr, Y, nullptr, enabled, active);
+}
+
+void wgrad(sg_learned* L, const uint32_t* X, const uint32_t* G, int l, int batch) {
+    const int tiles = L->cx / TB;
+    const int nblk = tiles * tiles * tiles * batch;
+    k_conv3d_wgrad<<<nblk, CT, WGRAD_SMEM, L->ctx->stream>>>(X, G, L->cx, L->tpart.p);
+    SG_CUDA(cudaGetLastError());
+    k_wgrad_reduce<<<(LAYER_P + 255) / 256, 256, 0, L->ctx->stream>>>(
+        L->tpart.p, nblk, L->pmask.p + (size_t)l * LAYER_P, L->grad.p + (size_t)l * LAYER_P);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+    count_launch(L->ctx);
+}
+
+void ensure_train(sg_learned* L, int batch) {
+    if (L->tb >= batch) return;
+    const size_t V = (size_t)L->nc;
+    for (int i = 0; i < 4; ++i) L->tact[i].alloc(V * 8 * batch);
+    for (int i = 0; i < 2; ++i) L->tg[i].alloc(V * 8 * batch);
+    L->ty.alloc(V * batch);
+    L->tt.alloc(V * batch);
+    const int tiles = L->cx / TB;
+    L->tpart.alloc((size_t)tiles * tiles * tiles * batch * LAYER_P);
+    L->tloss.alloc(1);
+    L->tb = batch;
+}
+
+// forward, loss and (with_grad) the parameter gradient of the packed batch in
+// tact[0] with targets tt; the loss is added to tloss
+void loss_grad(sg_learned* L, int batch, bool with_grad) {
+    const size_t V = (size_t)L->nc;
+    uint32_t *X0 = L->tact[0].p, *A1 = L->tact[1].p, *A2 = L->tact[2].p, *A3 = L->tact[3].p;
+    forward(L, X0, A1, A2, A3, L->ty.p, batch, nullptr, nullptr);
+    uint32_t* G = L->tg[0].p;
+    uint32_t* H = L->tg[1].p;
+    k_loss_grad<<<kblocks(L->ctx, V * batch), 256, 0, L->ctx->stream>>>(
+        L->ty.p, L->tt.p, V * batch, with_grad ? G : nullptr, L->tloss.p);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+    if (!with_grad) return;
+    // layer 4 (input A3), 3 (A2), 2 (A1), 1 (X0); the input gradient of a
+    // layer is masked by the ReLU of its input (the previous layer's output)
+    wgrad(L, A3, G, 3, batch);
+    conv(L, G, 3, true, EPI_MASK, batch, H, nullptr, A3, nullptr, nullptr);
+    wgrad(L, A2, H, 2, batch);
+    conv(L, H, 2, true, EPI_MASK, batch, G, nullptr, A2, nullptr, nullptr);
+    wgrad(L, A1, G, 1, batch);
+    conv(L, G, 1, true, EPI_MASK, batch, H, nullptr, A1, nullptr, nullptr);
+    wgrad(L, X0, H, 0, batch);
+}
+
+void adam_step(sg_learned* L, float lr) {
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    L->adam_t += 1;
+    const float c1 = 1.f - (float)std::pow((double)b1, (double)L->adam_t);
+    const float c2 = 1.f - (float)std::pow((double)b2, (double)L->adam_t);
+    k_adam<<<(NET_PARAMS + 255) / 256, 256, 0, L->ctx->stream>>>(
+        L->master.p, L->grad.p, L->m1.p, L->m2.p, L->pmask.p, NET_PARAMS, lr, b1, b2, eps, c1, c2);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+    prep_weights(L);
+}
+
+void grow_samples(sg_learned* L, int need) {
+    if (need <= L->cap) return;
+    const int ncap = std::max(need, std::max(16, 2 * L->cap));
+    const size_t nc = (size_t)L->nc;
+    auto grow = [&](DBuf<float>& b) {
+        DBuf<float> nb;
+        nb.alloc((size_t)ncap * nc);
+        if (L->nsamples > 0)
+            SG_CUDA(cudaMemcpyAsync(nb.p, b.p, sizeof(float) * nc * L->nsamples,
+                                    cudaMemcpyDeviceToDevice, L->ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+        std::swap(nb.p, b.p);
+        std::swap(nb.n, b.n);
+    };
+    grow(L->s_in);
+    grow(L->s_tgt);
+    grow(L->s_feat);
+    L->cap = ncap;
+}
+
+// restricted residual of v - A z (z may be null) into rc, s into *s_out
+template <class TA, class TI, class TO, class TV>
+void resid_restrict(sg_learned* L, const TV* val, const TI* v, const TO* z, float* rc, float* s_out,
+                    const int* enabled, const int* active) {
+    const sg_csr* A = L->A;
+    const int grid = std::min(kblocks(L->ctx, (size_t)L->nc), 4096);
+    k_resid_restrict<TA, TI, TO, TV><<<grid, 256, 0, L->ctx->stream>>>(
+        A->rp.p, A->ci.p, val, v, z, L->nx, L->ny, L->nz, rc, L->partials.p, L->counter.p, s_out,
+        enabled, active);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+}
+
+void check_ready(const sg_learned* L) {
+    if (!L->A) fail(SG_ERR_NOT_SETUP, "learned stage has no matrix (sg_learned_set_matrix)");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- hooks
+template <class TI, class TO>
+void learned_apply(sg_learned* L, const TI* x, TO* y, int n, const int* active) {
+    check_ready(L);
+    if ((long long)L->nx * L->ny * L->nz != (long long)n)
+        fail(SG_ERR_INVALID_ARG, "learned stage grid %dx%dx%d does not match n = %d", L->nx, L->ny,
+             L->nz, n);
+    LearnedCtl* c = L->ctl.p;
+    const int* en = &c->enabled;
+    resid_restrict<float, TI, TO, float>(L, L->A->val32.p, x, y, L->rc.p, &c->snorm, en, active);
+    k_pack_input<<<kblocks(L->ctx, (size_t)L->nc), 256, 0, L->ctx->stream>>>(
+        L->rc.p, L->feat.p, L->nc, &c->snorm, en, active, L->act[0].p);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+    forward(L, L->act[0].p, L->act[1].p, L->act[2].p, L->act[3].p, L->yout.p, 1, en, active);
+    k_prolong_add<TO><<<kblocks(L->ctx, (size_t)n), 256, 0, L->ctx->stream>>>(L->yout.p, L->nx, L->ny,
+                                                                      L->nz, c, active, y);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+}
+
+template void learned_apply<double, double>(sg_learned*, const double*, double*, int, const int*);
+template void learned_apply<double, float>(sg_learned*, const double*, float*, int, const int*);
+template void learned_apply<float, float>(sg_learned*, const float*, float*, int, const int*);
+
+void learned_detach(sg_learned* L) {
+    if (L) L->attached = nullptr;
+}
+
+void learned_begin(sg_learned* L, SolveState* st) {
+    check_ready(L);
+    k_learned_begin<<<1, 1, 0, L->ctx->stream>>>(L->ctl.p, st, L->on ? 1 : 0);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+}
+
+void learned_monitor(sg_learned* L, SolveState* st) {
+    k_learned_monitor<<<1, 1, 0, L->ctx->stream>>>(L->ctl.p, st);
+    SG_CUDA(cudaGetLastError());
+    count_launch(L->ctx);
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+namespace {
+template <class F>
+sg_status lguard(F&& f) {
+    try {
+        f();
+        sg::set_last_error("");
+        return SG_OK;
+    } catch (const sg::Error& e) {
+        sg::set_last_error(e.msg.c_str());
+        return e.status;
+    } catch (const std::exception& e) {
+        sg::set_last_error(e.what());
+        return SG_ERR_INTERNAL;
+    }
+}
+
+void write_ctl(sg_learned* L, const LearnedCtl& h) {
+    SG_CUDA(cudaMemcpyAsync(L->ctl.p, &h, sizeof(h), cudaMemcpyHostToDevice, L->ctx->stream));
+    SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+}
+
+LearnedCtl read_ctl(sg_learned* L) {
+    LearnedCtl h{};
+    SG_CUDA(cudaMemcpyAsync(&h, L->ctl.p, sizeof(h), cudaMemcpyDeviceToHost, L->ctx->stream));
+    SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    return h;
+}
+
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double unit(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+void split_pairs(const float* x, size_t V, std::vector<float>& in, std::vector<float>& ft) {
+    in.resize(V);
+    ft.resize(V);
+    for (size_t q = 0; q < V; ++q) {
+        in[q] = x[2 * q];
+        ft[q] = x[2 * q + 1];
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int sg_learned_num_params(void) { return LEARN_PARAMS; }
+
+sg_status sg_learned_create(sg_ctx* ctx, int nx, int ny, int nz, sg_learned** out) {
+    return lguard([&] {
+        SG_CHECK_ARG(ctx && out, "NULL argument");
+        *out = nullptr;
+        SG_CHECK_ARG(nx == ny && ny == nz, "the learned stage needs a cubic grid (got %dx%dx%d)",
+                     nx, ny, nz);
+        SG_CHECK_ARG(nx > 0 && nx % (2 * TB) == 0,
+                     "grid edge must be a positive multiple of %d (got %d)", 2 * TB, nx);
+        SG_CHECK_ARG((long long)nx * ny * nz < (1ll << 31), "grid too large");
+        SG_CUDA(cudaSetDevice(ctx->device));
+        auto* L = new sg_learned();
+        try {
+            L->ctx = ctx;
+            L->nx = nx; L->ny = ny; L->nz = nz;
+            L->cx = nx / 2; L->cy = ny / 2; L->cz = nz / 2;
+            L->nc = L->cx * L->cy * L->cz;
+            L->master.alloc(NET_PARAMS);
+            L->grad.alloc(NET_PARAMS);
+            L->m1.alloc(NET_PARAMS);
+            L->m2.alloc(NET_PARAMS);
+            L->pmask.alloc(NET_PARAMS);
+            L->wf.alloc((size_t)NLAYERS * LAYER_W);
+            L->wt.alloc((size_t)NLAYERS * LAYER_W);
+            // real parameters: layer 1 reads channels 0-1, layer 4 writes channel 0
+            std::vector<float> mask(NET_PARAMS, 1.f);
+            for (int l = 0; l < NLAYERS; ++l)
+                for (int i = 0; i < LAYER_P; ++i) {
+                    float& m = mask[(size_t)l * LAYER_P + i];
+                    if (i < LAYER_W) {
+                        const int ci = (i / LC) % LC, co = i % LC;
+                        if (l == 0 && ci >= 2) m = 0.f;
+                        if (l == NLAYERS - 1 && co >= 1) m = 0.f;
+                    } else if (l == NLAYERS - 1 && i - LAYER_W >= 1) {
+                        m = 0.f;
+                    }
+                }
+            L->pmask.upload(mask, ctx->stream);
+            L->master.zero(ctx->stream);
+            L->grad.zero(ctx->stream);
+            L->m1.zero(ctx->stream);
+            L->m2.zero(ctx->stream);
+            L->ctl.alloc(1);
+            LearnedCtl h{};
+            h.out_scale = 1.f;
+            h.enabled = 1;
+            h.fallback_cycle = -1;
+            L->ctl.upload(&h, 1, ctx->stream);
+            L->partials.alloc(4096);
+            L->counter.alloc(1);
+            L->counter.zero(ctx->stream);
+            L->rc.alloc(L->nc);
+            L->ec.alloc(L->nc);
+            L->yout.alloc(L->nc);
+            for (int i = 0; i < 4; ++i) L->act[i].alloc((size_t)L->nc * 8);
+            L->feat.alloc(L->nc);
+            L->feat.zero(ctx->stream);
+            SG_CUDA(cudaFuncSetAttribute(k_conv3d_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         WGRAD_SMEM));
+            prep_weights(L);
+            SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        } catch (...) {
+            delete L;
+            throw;
+        }
+        *out = L;
+    });
+}
+
+sg_status sg_learned_destroy(sg_learned* L) {
+    return lguard([&] {
+        if (!L) return;
+        cudaSetDevice(L->ctx->device);
+        if (L->attached) L->attached->learned = nullptr;
+        delete L;
+    });
+}
+
+sg_status sg_learned_set_matrix(sg_learned* L, const sg_csr* A) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && A, "NULL argument");
+        SG_CHECK_ARG(A->ctx == L->ctx, "matrix belongs to a different context");
+        SG_CHECK_ARG(A->nrows == A->ncols &&
+                         (long long)L->nx * L->ny * L->nz == (long long)A->nrows,
+                     "matrix of %d rows does not match the %dx%dx%d grid", A->nrows, L->nx, L->ny,
+                     L->nz);
+        // coefficient feature: log A_ii restricted to the coarse cells, standardised
+        std::vector<double> ld(A->nrows, 0.0);
+        for (int i = 0; i < A->nrows; ++i) {
+            double d = 0.0;
+            for (int q = A->h_rp[i]; q < A->h_rp[i + 1]; ++q)
+                if (A->h_ci[q] == i) d += A->h_val[q];
+            if (!(d > 0.0)) fail(SG_ERR_INVALID_ARG, "row %d has a non-positive diagonal", i);
+            ld[i] = std::log(d);
+        }
+        std::vector<float> c((size_t)L->nc);
+        std::vector<double> cd((size_t)L->nc);
+        double mean = 0.0;
+        for (int k = 0; k < L->cz; ++k)
+            for (int j = 0; j < L->cy; ++j)
+                for (int i = 0; i < L->cx; ++i) {
+                    double s = 0.0;
+                    for (int o = 0; o < 8; ++o) {
+                        const int fx = 2 * i + (o & 1), fy = 2 * j + ((o >> 1) & 1),
+                                  fz = 2 * k + (o >> 2);
+                        s += ld[((size_t)fz * L->ny + fy) * L->nx + fx];
+                    }
+                    cd[((size_t)k * L->cy + j) * L->cx + i] = s / 8.0;
+                    mean += s / 8.0;
+                }
+        mean /= (double)cd.size();
+        double var = 0.0;
+        for (double v : cd) var += (v - mean) * (v - mean);
+        var /= (double)cd.size();
+        const double inv = var > 1e-24 ? 1.0 / std::sqrt(var) : 0.0;
+        for (size_t q = 0; q < cd.size(); ++q) c[q] = (float)((cd[q] - mean) * inv);
+        const_cast<sg_csr*>(A)->ensure_fp32();
+        L->feat.upload(c, L->ctx->stream);
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+        L->A = A;
+    });
+}
+
+sg_status sg_learned_init_weights(sg_learned* L, uint64_t seed) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        // He-uniform over the real fan-in; the last layer starts 10x smaller so
+        // the untrained stage adds little
+        std::vector<float> w(NET_PARAMS, 0.f);
+        uint64_t s = seed;
+        for (int l = 0; l < NLAYERS; ++l) {
+            const int fan_in = LTAPS * (l == 0 ? 2 : LC);
+            double bound = std::sqrt(6.0 / fan_in);
+            if (l == NLAYERS - 1) bound *= 0.1;
+            for (int i = 0; i < LAYER_W; ++i) {
+                const int ci = (i / LC) % LC, co = i % LC;
+                const double u = unit(s);
+                if ((l == 0 && ci >= 2) || (l == NLAYERS - 1 && co >= 1)) continue;
+                w[(size_t)l * LAYER_P + i] = (float)((2.0 * u - 1.0) * bound);
+            }
+        }
+        L->master.upload(w, L->ctx->stream);
+        L->m1.zero(L->ctx->stream);
+        L->m2.zero(L->ctx->stream);
+        L->adam_t = 0;
+        prep_weights(L);
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    });
+}
+
+sg_status sg_learned_set_weights(sg_learned* L, const float* w, int count) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && w, "NULL argument");
+        SG_CHECK_ARG(count == LEARN_PARAMS, "expected %d parameters (got %d)", LEARN_PARAMS, count);
+        SG_CHECK_ARG(std::isfinite(w[NET_PARAMS]) && w[NET_PARAMS] > 0.f,
+                     "output scale must be positive");
+        std::vector<float> mask(NET_PARAMS);
+        SG_CUDA(cudaMemcpy(mask.data(), L->pmask.p, sizeof(float) * NET_PARAMS,
+                           cudaMemcpyDeviceToHost));
+        std::vector<float> h(w, w + NET_PARAMS);
+        for (int i = 0; i < NET_PARAMS; ++i) {
+            SG_CHECK_ARG(std::isfinite(h[i]), "parameter %d is not finite", i);
+            h[i] *= mask[i];
+        }
+        L->master.upload(h, L->ctx->stream);
+        L->out_scale = w[NET_PARAMS];
+        LearnedCtl c = read_ctl(L);
+        c.out_scale = L->out_scale;
+        write_ctl(L, c);
+        L->m1.zero(L->ctx->stream);
+        L->m2.zero(L->ctx->stream);
+        L->adam_t = 0;
+        prep_weights(L);
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    });
+}
+
+sg_status sg_learned_get_weights(sg_learned* L, float* w, int count) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && w, "NULL argument");
+        SG_CHECK_ARG(count == LEARN_PARAMS, "expected %d parameters (got %d)", LEARN_PARAMS, count);
+        SG_CUDA(cudaMemcpyAsync(w, L->master.p, sizeof(float) * NET_PARAMS, cudaMemcpyDeviceToHost,
+                                L->ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+        w[NET_PARAMS] = L->out_scale;
+    });
+}
+
+sg_status sg_learned_add_pair(sg_learned* L, sg_precond* pc, const double* r, const double* e,
+                              int n, sg_mem mem) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && pc && r && e, "NULL argument");
+        check_ready(L);
+        SG_CHECK_ARG(pc->ctx == L->ctx, "preconditioner belongs to a different context");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        SG_CHECK_ARG(n == L->A->nrows && pc->n == n, "n (%d) does not match the grid", n);
+        sg_ctx* ctx = L->ctx;
+        SG_CUDA(cudaSetDevice(ctx->device));
+        const double* dr = r;
+        const double* de = e;
+        if (mem == SG_MEM_HOST) {
+            L->r64.upload(r, n, ctx->stream);
+            L->e64.upload(e, n, ctx->stream);
+            dr = L->r64.p;
+            de = L->e64.p;
+        }
+        if (L->z64.n < (size_t)n) L->z64.alloc(n);
+        if (L->t64.n < (size_t)n) L->t64.alloc(n);
+        // z1 = M r (the plain preconditioner); r1 = r - A z1; e1 = e - z1
+        precond_apply_device<double, double>(pc, dr, L->z64.p, nullptr, false);
+        LearnedCtl* c = L->ctl.p;
+        resid_restrict<double, double, double, double>(L, L->A->val.p, dr, L->z64.p, L->rc.p,
+                                                       &c->pair_s, nullptr, nullptr);
+        k_sub64<<<kblocks(ctx, n), 256, 0, ctx->stream>>>(de, L->z64.p, n, L->t64.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        resid_restrict<double, double, double, double>(L, L->A->val.p, L->t64.p,
+                                                       static_cast<const double*>(nullptr), L->ec.p,
+                                                       &c->scratch_s, nullptr, nullptr);
+        grow_samples(L, L->nsamples + 1);
+        const size_t off = (size_t)L->nsamples * L->nc;
+        k_store_pair<<<kblocks(ctx, (size_t)L->nc), 256, 0, ctx->stream>>>(
+            L->rc.p, L->ec.p, L->feat.p, L->nc, c, L->s_in.p + off, L->s_tgt.p + off,
+            L->s_feat.p + off);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (sweep_error(pc))
+            fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+        L->nsamples += 1;
+    });
+}
+
+sg_status sg_learned_num_samples(sg_learned* L, int* count) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && count, "NULL argument");
+        *count = L->nsamples;
+    });
+}
+
+sg_status sg_learned_clear_samples(sg_learned* L) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        L->nsamples = 0;
+    });
+}
+
+sg_status sg_learned_get_sample(sg_learned* L, int i, float* input, float* feature,
+                                float* target) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        SG_CHECK_ARG(i >= 0 && i < L->nsamples, "sample %d out of range [0,%d)", i, L->nsamples);
+        const size_t off = (size_t)i * L->nc, bytes = sizeof(float) * L->nc;
+        if (input) SG_CUDA(cudaMemcpy(input, L->s_in.p + off, bytes, cudaMemcpyDeviceToHost));
+        if (feature) SG_CUDA(cudaMemcpy(feature, L->s_feat.p + off, bytes, cudaMemcpyDeviceToHost));
+        if (target) SG_CUDA(cudaMemcpy(target, L->s_tgt.p + off, bytes, cudaMemcpyDeviceToHost));
+    });
+}
+
+sg_status sg_learned_train(sg_learned* L, int first, int count, int epochs, int batch, double lr,
+                           uint64_t seed, double* epoch_loss) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        SG_CHECK_ARG(first >= 0 && count >= 1 && first + count <= L->nsamples,
+                     "samples [%d,%d) out of range [0,%d)", first, first + count, L->nsamples);
+        SG_CHECK_ARG(epochs >= 0 && batch >= 1 && batch <= 64, "bad epochs/batch");
+        SG_CHECK_ARG(lr > 0 && std::isfinite(lr), "learning rate must be positive");
+        sg_ctx* ctx = L->ctx;
+        SG_CUDA(cudaSetDevice(ctx->device));
+        ensure_train(L, batch);
+        // output scale: rms of the training targets
+        {
+            std::vector<float> t((size_t)count * L->nc);
+            SG_CUDA(cudaMemcpy(t.data(), L->s_tgt.p + (size_t)first * L->nc,
+                               sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
+            double ss = 0.0;
+            for (float v : t) ss += (double)v * v;
+            const double rms = std::sqrt(ss / (double)t.size());
+            L->out_scale = rms > 0 && std::isfinite(rms) ? (float)rms : 1.f;
+            LearnedCtl c = read_ctl(L);
+            c.out_scale = L->out_scale;
+            write_ctl(L, c);
+        }
+        const float inv_c = 1.f / L->out_scale;
+        uint64_t s = seed;
+        std::vector<int> perm(count);
+        DBuf<int> dperm;
+        dperm.alloc(count);
+        for (int ep = 0; ep < epochs; ++ep) {
+            for (int i = 0; i < count; ++i) perm[i] = first + i;
+            for (int i = count - 1; i > 0; --i) {
+                const int j = (int)(splitmix(s) % (uint64_t)(i + 1));
+                std::swap(perm[i], perm[j]);
+            }
+            dperm.upload(perm, ctx->stream);
+            L->tloss.zero(ctx->stream);
+            int nb = 0;
+            for (int b0 = 0; b0 < count; b0 += batch, ++nb) {
+                const int bs = std::min(batch, count - b0);
+                k_pack_batch<<<kblocks(ctx, (size_t)bs * L->nc), 256, 0, ctx->stream>>>(
+                    L->s_in.p, L->s_feat.p, L->s_tgt.p, dperm.p + b0, bs, L->nc, inv_c,
+                    L->tact[0].p, L->tt.p);
+                SG_CUDA(cudaGetLastError());
+                count_launch(ctx);
+                loss_grad(L, bs, true);
+                adam_step(L, (float)lr);
+            }
+            float lsum = 0.f;
+            SG_CUDA(cudaMemcpyAsync(&lsum, L->tloss.p, sizeof(float), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            SG_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (epoch_loss) epoch_loss[ep] = (double)lsum / nb;
+            if (!std::isfinite(lsum)) fail(SG_ERR_NONFINITE, "training loss is not finite");
+        }
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+sg_status sg_learned_eval(sg_learned* L, int first, int count, double* loss) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && loss, "NULL argument");
+        SG_CHECK_ARG(first >= 0 && count >= 1 && first + count <= L->nsamples,
+                     "samples [%d,%d) out of range [0,%d)", first, first + count, L->nsamples);
+        sg_ctx* ctx = L->ctx;
+        SG_CUDA(cudaSetDevice(ctx->device));
+        const int batch = L->tb > 0 ? std::min(L->tb, 8) : 8;
+        ensure_train(L, batch);
+        const float inv_c = 1.f / L->out_scale;
+        std::vector<int> idx(count);
+        for (int i = 0; i < count; ++i) idx[i] = first + i;
+        DBuf<int> didx;
+        didx.upload(idx, ctx->stream);
+        double total = 0.0;
+        for (int b0 = 0; b0 < count; b0 += batch) {
+            const int bs = std::min(batch, count - b0);
+            L->tloss.zero(ctx->stream);
+            k_pack_batch<<<kblocks(ctx, (size_t)bs * L->nc), 256, 0, ctx->stream>>>(
+                L->s_in.p, L->s_feat.p, L->s_tgt.p, didx.p + b0, bs, L->nc, inv_c, L->tact[0].p,
+                L->tt.p);
+            SG_CUDA(cudaGetLastError());
+            count_launch(ctx);
+            loss_grad(L, bs, false);
+            float l = 0.f;
+            SG_CUDA(cudaMemcpyAsync(&l, L->tloss.p, sizeof(float), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            SG_CUDA(cudaStreamSynchronize(ctx->stream));
+            total += (double)l * bs;
+        }
+        *loss = total / count;
+    });
+}
+
+sg_status sg_learned_forward(sg_learned* L, const float* x, int batch, float* y) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && x && y, "NULL argument");
+        SG_CHECK_ARG(batch >= 1 && batch <= 64, "batch must be in [1,64]");
+        sg_ctx* ctx = L->ctx;
+        SG_CUDA(cudaSetDevice(ctx->device));
+        ensure_train(L, batch);
+        const size_t V = (size_t)L->nc * batch;
+        std::vector<float> in, ft;
+        split_pairs(x, V, in, ft);
+        DBuf<float> din, dft;
+        din.upload(in, ctx->stream);
+        dft.upload(ft, ctx->stream);
+        k_pack_batch<<<kblocks(ctx, V), 256, 0, ctx->stream>>>(din.p, dft.p, nullptr, nullptr, batch,
+                                                              L->nc, 1.f, L->tact[0].p, nullptr);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        forward(L, L->tact[0].p, L->tact[1].p, L->tact[2].p, L->tact[3].p, L->ty.p, batch, nullptr,
+                nullptr);
+        SG_CUDA(cudaMemcpyAsync(y, L->ty.p, sizeof(float) * V, cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+sg_status sg_learned_gradient(sg_learned* L, const float* x, const float* t, int batch,
+                              float* grad, double* loss) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && x && t && grad && loss, "NULL argument");
+        SG_CHECK_ARG(batch >= 1 && batch <= 64, "batch must be in [1,64]");
+        sg_ctx* ctx = L->ctx;
+        SG_CUDA(cudaSetDevice(ctx->device));
+        ensure_train(L, batch);
+        const size_t V = (size_t)L->nc * batch;
+        std::vector<float> in, ft;
+        split_pairs(x, V, in, ft);
+        DBuf<float> din, dft, dt;
+        din.upload(in, ctx->stream);
+        dft.upload(ft, ctx->stream);
+        dt.upload(t, V, ctx->stream);
+        k_pack_batch<<<kblocks(ctx, V), 256, 0, ctx->stream>>>(din.p, dft.p, dt.p, nullptr, batch,
+                                                              L->nc, 1.f, L->tact[0].p, L->tt.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        L->tloss.zero(ctx->stream);
+        loss_grad(L, batch, true);
+        float l = 0.f;
+        SG_CUDA(cudaMemcpyAsync(&l, L->tloss.p, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(cudaMemcpyAsync(grad, L->grad.p, sizeof(float) * NET_PARAMS, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        *loss = l;
+    });
+}
+
+sg_status sg_learned_set_enabled(sg_learned* L, int on) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        L->on = on != 0;
+        LearnedCtl c = read_ctl(L);
+        c.enabled = L->on ? 1 : 0;
+        write_ctl(L, c);
+    });
+}
+
+sg_status sg_learned_get_state(sg_learned* L, int* enabled, int* fallback_cycle,
+                               long long* applies) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        const LearnedCtl c = read_ctl(L);
+        if (enabled) *enabled = c.enabled;
+        if (fallback_cycle) *fallback_cycle = c.fallback_cycle;
+        if (applies) *applies = (long long)c.applies;
+    });
+}
+
+sg_status sg_precond_set_learned(sg_precond* pc, sg_learned* L, double stagnation) {
+    return lguard([&] {
+        SG_CHECK_ARG(pc, "NULL argument");
+        if (!L) {
+            if (pc->learned) pc->learned->attached = nullptr;
+            pc->learned = nullptr;
+            return;
+        }
+        SG_CHECK_ARG(L->ctx == pc->ctx, "learned stage belongs to a different context");
+        SG_CHECK_ARG(pc->kind >= SG_PC_ASM, "the learned stage attaches to Schwarz preconditioners");
+        SG_CHECK_ARG(stagnation >= 0.0 && std::isfinite(stagnation),
+                     "stagnation ratio must be >= 0");
+        check_ready(L);
+        if (pc->is_setup)
+            SG_CHECK_ARG(pc->n == L->A->nrows, "preconditioner size %d != grid size %d", pc->n,
+                         L->A->nrows);
+        if (L->attached && L->attached != pc) L->attached->learned = nullptr;
+        if (pc->learned && pc->learned != L) pc->learned->attached = nullptr;
+        L->attached = pc;
+        pc->learned = L;
+        LearnedCtl c = read_ctl(L);
+        c.stag = stagnation;
+        write_ctl(L, c);
+    });
+}
+
+}  // extern "C"

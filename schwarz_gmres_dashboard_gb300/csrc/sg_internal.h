@@ -267,4 +267,6 @@ struct sg_precond {
     sg::DBuf<int> piv0, status_d;
     // ---- host-API staging
     sg::DBuf<double> io_x, io_y;
+    // ---- learned coarse-correction stage applied after M (not owned)
+    sg_learned* learned = nullptr;
 };

@@ -87,6 +87,7 @@ void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int*
     // inside the solver FP64 sweeps may fuse multiply-adds (exact = false)
     if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active, false);
     else launch_copy<TI, TO>(ctx, x, y, n, active);
+    if (pc && pc->learned) learned_apply<TI, TO>(pc->learned, x, y, n, active);
 }
 
 // One restart cycle as a launch sequence on ctx->stream.
@@ -148,6 +149,7 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
         launch_residual(ctx, A, b, x, w->r64.p, st);
     }
     launch_cycle_end(ctx, st);
+    if (pc && pc->learned) learned_monitor(pc->learned, st);
 }
 
 template <class T>
@@ -211,6 +213,7 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     SG_CUDA(cudaMemcpyAsync(w->st.p, hs, sizeof(SolveState), cudaMemcpyHostToDevice, ctx->stream));
     launch_bnorm(ctx, b, n, w->st.p);
     launch_residual(ctx, A, b, x, w->r64.p, w->st.p);
+    if (pc && pc->learned) learned_begin(pc->learned, w->st.p);
     const size_t ctl_bytes = offsetof(SolveState, g);
     SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -1,0 +1,162 @@
+"""Learned coarse-correction stage on the GPU against the oracle
+(oracle/learned_oracle.py), plus what the trained stage gains inside FGMRES.
+
+Tolerances.  The GPU network stores weights, activations and activation
+gradients in BF16 and accumulates in FP32; the oracle rounds the same
+tensors to BF16 and accumulates in FP64.  The two differ by FP32 rounding of
+the accumulations, which now and then moves a stored activation by one BF16
+ulp (2^-8 relative): outputs agree to a relative L2 error of 5e-3, gradients
+to 2e-2 per layer.  Training pairs are FP64 arithmetic stored in FP32
+(relative 1e-6).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import learned_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _he_params(seed, c=1.7, bias=0.05):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(lo.NUM_PARAMS)
+    for l in range(lo.LAYERS):
+        fan = 27 * (2 if l == 0 else 16)
+        base = l * lo.LAYER_P
+        p[base: base + lo.LAYER_W] = rng.uniform(-1, 1, lo.LAYER_W) * np.sqrt(6.0 / fan)
+        p[base + lo.LAYER_W: base + lo.LAYER_P] = rng.uniform(-bias, bias, 16)
+    p[: lo.NET_PARAMS] *= lo.param_mask()
+    p[lo.NET_PARAMS] = c
+    return p.astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def stage32(sg):
+    st = sg.LearnedCorrection(32)
+    yield st
+    st.close()
+
+
+def test_parameter_count(sg):
+    assert sg.learned.NUM_PARAMS == lo.NUM_PARAMS
+
+
+@pytest.mark.parametrize("batch", [1, 3])
+def test_forward_matches_oracle(stage32, batch):
+    p = _he_params(11)
+    stage32.weights = p
+    rng = np.random.default_rng(12 + batch)
+    x2 = rng.standard_normal((batch, stage32.nc, 2)).astype(np.float32)
+    y = stage32.forward(x2)
+    yo, _ = lo.forward(p.astype(np.float64), x2, 16, emulate_bf16=True)
+    assert _rel(y, yo) <= 5e-3, _rel(y, yo)
+    assert np.max(np.abs(y - yo)) <= 3e-2 * np.max(np.abs(yo))
+
+
+def test_weights_round_trip_and_padding(stage32):
+    p = _he_params(13)
+    q = p.copy()
+    q[: lo.NET_PARAMS][lo.param_mask() == 0] = 1.0  # padded entries are forced to 0
+    stage32.weights = q
+    assert np.array_equal(stage32.weights, p)
+
+
+@pytest.mark.parametrize("batch", [1, 2])
+def test_gradient_matches_oracle(stage32, batch):
+    p = _he_params(21)
+    stage32.weights = p
+    rng = np.random.default_rng(22 + batch)
+    x2 = rng.standard_normal((batch, stage32.nc, 2)).astype(np.float32)
+    t = rng.standard_normal((batch, stage32.nc)).astype(np.float32)
+    loss, g = stage32.gradient(x2, t)
+    lo_loss, go = lo.loss_and_grad(p.astype(np.float64), x2, t, 16, emulate_bf16=True)
+    assert abs(loss - lo_loss) <= 1e-3 * lo_loss
+    for l in range(lo.LAYERS):
+        sl = slice(l * lo.LAYER_P, (l + 1) * lo.LAYER_P)
+        assert _rel(g[sl], go[sl]) <= 2e-2, (l, _rel(g[sl], go[sl]))
+    assert np.all(g[lo.param_mask() == 0] == 0)
+
+
+def _problem(sg, oracle, N, NP, seed, fp64=True):
+    A = sg.make_varcoef_3d(N, N, N, 1.0, 8.0 * N / 96, seed)
+    part = sg.partition_boxes(N, N, N, NP, 0.08, 7)
+    dt = sg.FP64 if fp64 else sg.FP32
+    M = sg.TwoLevelSchwarzPrecond(NP, 1, sg.FineLevelType.RAS, partition=part,
+                                  factor_dtype=dt, sweep_dtype=dt)
+    M.setup(A)
+    S = sp.csr_matrix((A.vals, A.col_idx, A.row_ptr), shape=(A.nrows, A.nrows))
+    opc = oracle.precond("twolevel_ras", A, NP, 1, part) if oracle is not None else None
+    return A, M, S, opc
+
+
+def test_training_pair_matches_oracle(sg, oracle):
+    N = 32
+    A, M, S, opc = _problem(sg, oracle, N, 8, 5)
+    st = sg.LearnedCorrection(N)
+    st.set_matrix(A)
+    rng = np.random.default_rng(31)
+    r = rng.standard_normal(A.nrows)
+    e = rng.standard_normal(A.nrows)
+    st.add_pair(M, r, e)
+    assert st.num_samples == 1
+    a, f, t = st.sample(0)
+    ao, fo, to = lo.training_pair(lambda x: S @ x, opc.apply, S.diagonal(), r, e, N)
+    assert _rel(a, ao) <= 1e-6 and _rel(t, to) <= 1e-6
+    assert np.max(np.abs(f - fo)) <= 1e-5
+    st.clear_samples()
+    assert st.num_samples == 0
+    st.close()
+
+
+def test_stage_apply_matches_oracle(sg, oracle):
+    N = 32
+    A, M, S, opc = _problem(sg, oracle, N, 8, 6)
+    st = sg.LearnedCorrection(N)
+    st.set_matrix(A)
+    p = _he_params(41)
+    st.weights = p
+    st.attach(M, stagnation=0.0)
+    v = np.random.default_rng(42).standard_normal(A.nrows)
+    z = M.apply(v)
+    zo, z1o = lo.stage_apply(p.astype(np.float64), lambda x: S @ x, opc.apply, S.diagonal(), v, N)
+    corr, corr_o = z - z1o, zo - z1o
+    assert np.linalg.norm(corr_o) > 1e-3 * np.linalg.norm(z1o)  # the stage does something
+    assert _rel(corr, corr_o) <= 2e-2, _rel(corr, corr_o)
+    assert st.state()["applies"] >= 1
+    # switched off: the plain preconditioner exactly
+    st.enabled = False
+    assert np.array_equal(M.apply(v), opc.apply(v)) or _rel(M.apply(v), opc.apply(v)) <= 1e-14
+    st.enabled = True
+    st.detach()
+    assert _rel(M.apply(v), z1o) <= 1e-14
+    st.close()
+
+
+def test_gmres_rejects_a_learned_stage(sg):
+    N = 32
+    A, M, _S, _ = _problem(sg, None, N, 8, 7)
+    st = sg.LearnedCorrection(N)
+    st.set_matrix(A)
+    st.init_weights(1)
+    st.attach(M)
+    b = np.ones(A.nrows)
+    x = np.zeros(A.nrows)
+    with pytest.raises(sg.SgError) as ei:
+        sg.gmres(A, b, x, M, sg.GMRESParams(restart=30, max_iter=30, tol=1e-8))
+    assert ei.value.status == 1
+    st.close()
+
+
+def test_create_rejects_bad_grids(sg):
+    for bad in (30, 0, 24):
+        with pytest.raises(sg.SgError):
+            sg.LearnedCorrection(bad)
