@@ -18,7 +18,17 @@ needed between steps.
           copies inside the timed region), host wall clock.
   fp64_gpu : the all-FP64 GPU solver on the same workload (the comparison
           the target ratio is quoted against).
-  roofline : FP64 CSR SpMV of the operator, algorithmic bytes / kernel time.
+  roofline : the dominant kernel class of the mixed solve -- the two-level
+          RAS apply (coarse restriction + TMA-fed ILU(0) sweeps) -- algorithmic
+          bytes per apply / its CUDA-event time per apply in an eager solve
+          (kernel-class timers on the launching stream); `kernels` lists every
+          class the same way, the FP32 SpMV among them.
+
+`--workload learned` runs the learned-correction workload instead: FGMRES(40)
+with two-level RAS (108 uneven boxes) on the 96^3 operator, plus the learned
+stage on the 48^3 grid, trained on the GPU from ~2,000 (residual, error)
+pairs of plain solves over 200 seeded coefficient fields and timed on 20
+held-out fields against plain two-level RAS FGMRES(40).
 
 `--impl reference` times the oracle (the CPU restatement of the reference's
 OpenMP path, with the sparse restatement of its coarse space) on the same
@@ -83,6 +93,56 @@ def profile_traffic(name):
     except OSError:
         pass
     return None
+
+
+def local_sizes(sg, A, part, nparts, overlap):
+    """(sum of subdomain rows, sum of subdomain nonzeros) of the Schwarz set-up."""
+    import ctypes as C
+    from schwarz_gmres_dashboard_gb300 import _clib
+    part = np.ascontiguousarray(part, dtype=np.int32)
+    out = []
+    for which in (4, 8):  # sub, local_col_idx
+        ln = C.c_int(0)
+        st = _clib.sg_schwarz_structure(A.nrows, A.row_ptr.ctypes.data, A.col_idx.ctypes.data,
+                                        part.ctypes.data, nparts, overlap, which, None, 0,
+                                        C.byref(ln))
+        if st != 0:
+            raise RuntimeError("sg_schwarz_structure failed")
+        out.append(int(ln.value))
+    return out[0], out[1]
+
+
+def apply_bytes(n, n_loc, nnz_loc, nparts, w_f, w_v):
+    """Algorithmic bytes of one two-level RAS apply: ILU(0) forward+backward
+    sweeps (factors w_f + 4-byte index per entry, row_ptr + diag_ptr, rhs and
+    solution), overlap gather/scatter, coarse restriction and prolongation."""
+    ilu = nnz_loc * (w_f + 4) + 8 * n_loc + n_loc * 2 * w_v
+    gather = n_loc * (4 + w_v) + n * (4 + w_v)
+    coarse = 2 * (n * (4 + w_v) + nparts * nparts * 8)
+    return ilu + gather + coarse
+
+
+def spmv_bytes(n, nnz, w_v, w_x):
+    return nnz * (w_v + 4) + 4 * (n + 1) + 2 * n * w_x
+
+
+def cgs2_bytes(n, w_v, iterations, restart):
+    """sum over the Arnoldi steps j of 2 [2 (j+1) n w + 3 n w]."""
+    total, left = 0, iterations
+    while left > 0:
+        k = min(left, restart)
+        total += sum(2 * (2 * (j + 1) * n * w_v + 3 * n * w_v) for j in range(k))
+        left -= k
+    return total
+
+
+def class_breakdown(ctx, solve):
+    """Kernel-class CUDA-event times of one eager solve (no graph)."""
+    ctx.set_timing(True)
+    res = solve()
+    t = ctx.timing()
+    ctx.set_timing(False)
+    return t, res
 
 
 class Clocks:
@@ -220,9 +280,39 @@ def run_ours(args):
             e2e.append(t1 - t0)
     e2e_s = statistics.mean(e2e)
 
-    # roofline: FP64 CSR SpMV of the operator
+    # kernel classes of one eager mixed solve (CUDA events on the launching
+    # stream), and the FP64 SpMV of the operator alone
     nnz = A.nnz()
-    spmv_bytes = nnz * (8 + 4) + 4 * (n + 1) + 2 * n * 8
+    peak, peak_kind = peaks()
+    p_eager = sg.GMRESParams(restart=RESTART, max_iter=20000, tol=RTOL,
+                             tol_kind=sg.TOL_TRUE_REL, precision=sg.FP32, use_graph=False)
+    classes, res_eager = class_breakdown(ctx, lambda: device_solve(pc_mixed, p_eager))
+    n_loc, nnz_loc = local_sizes(sg, A, part, NPARTS, OVERLAP)
+    it = res_eager.iterations
+    per = {}
+    model = {
+        "spmv": ("spmv_fp32 (SELL/CSR, autotuned)", spmv_bytes(n, nnz, 4, 4)),
+        "precond": ("two_level_ras_apply (k_restrict + k_sweep_tma, BF16 factors, FP32 sweep)",
+                    apply_bytes(n, n_loc, nnz_loc, NPARTS, 2, 4)),
+        "residual": ("residual_fp64", spmv_bytes(n, nnz, 8, 8) + 2 * n * 8),
+    }
+    for name, (ms, cnt) in classes.items():
+        if cnt == 0:
+            continue
+        entry = {"ms": ms, "launches": cnt, "us_per_launch": ms * 1e3 / cnt}
+        if name in model:
+            kname, byt = model[name]
+            entry.update({"kernel": kname, "algorithmic_bytes": byt,
+                          "achieved_gbs": byt / (ms / cnt / 1e3) / 1e9})
+            entry["frac"] = entry["achieved_gbs"] / peak
+        if name == "ortho":
+            byt = cgs2_bytes(n, 4, it, RESTART)
+            entry.update({"kernel": "cgs2 passes (k_dots, k_upd_dots, k_upd_norm) per step",
+                          "algorithmic_bytes_total": byt,
+                          "achieved_gbs": byt / (ms / 1e3) / 1e9})
+            entry["frac"] = entry["achieved_gbs"] / peak
+        per[name] = entry
+    dom = per["precond"]
     yd = torch.empty_like(bd)
     for _ in range(3):
         A.spmv(bd, yd)
@@ -234,9 +324,12 @@ def run_ours(args):
         A.spmv(bd, yd)
     s1.record(stream)
     torch.cuda.synchronize()
-    spmv_s = s0.elapsed_time(s1) / 1e3 / reps
-    peak, peak_kind = peaks()
-    achieved = spmv_bytes / spmv_s / 1e9
+    spmv64_s = s0.elapsed_time(s1) / 1e3 / reps
+    per["spmv_fp64_alone"] = {"kernel": "spmv_fp64 (sg_csr_spmv, reference summation order)",
+                              "us_per_launch": spmv64_s * 1e6,
+                              "algorithmic_bytes": spmv_bytes(n, nnz, 8, 8),
+                              "achieved_gbs": spmv_bytes(n, nnz, 8, 8) / spmv64_s / 1e9}
+    per["spmv_fp64_alone"]["frac"] = per["spmv_fp64_alone"]["achieved_gbs"] / peak
 
     if rank != 0:
         return
@@ -281,11 +374,14 @@ def run_ours(args):
         "setup_s": {"mixed": setup_mixed, "fp64": setup_fp64},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * n * 8,
                 "d2h_bytes_per_step": n * 8},
-        "roofline": {"kernel": "spmv_csr_fp64", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind,
-                     "traffic": profile_traffic("spmv_csr_fp64_varcoef128.md"),
-                     "algorithmic_bytes": spmv_bytes, "kernel_us": spmv_s * 1e6},
+        "roofline": {"kernel": dom["kernel"], "bound": "hbm",
+                     "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": dom["achieved_gbs"] / peak, "peak_source": peak_kind,
+                     "traffic": profile_traffic("two_level_ras_apply_varcoef128_mixed.md"),
+                     "algorithmic_bytes": dom["algorithmic_bytes"],
+                     "us_per_launch": dom["us_per_launch"],
+                     "timing": "CUDA events around every apply of one eager solve"},
+        "kernels": per,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -311,6 +407,228 @@ def cpu_baseline_sample(A, part, b, iterations):
                           f"RAS solve, {dt:.2f} s, scaled to the {iterations} iterations the "
                           f"FP64 solver needs"}
     except Exception as e:  # the baseline is reported, never required
+        return {"value": None, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                "sample": f"failed: {e}"}
+
+
+# ---------------------------------------------------------------- learned workload
+L_GRID = 96
+L_NPARTS = 108
+L_RESTART = 40
+L_SNAPSHOTS = (2, 4, 6, 9, 12, 16, 20, 25, 30, 36)
+L_WORKLOAD = ("varcoef3d_96^3_two_level_ras_108uneven_ov1_fgmres40_plus_learned_cnn48^3: "
+              "-div(exp(g) grad u), sigma 1, corr 8 cells, n=884736")
+
+
+def learned_flops(nc):
+    """Real multiply-adds x 2 of one network inference (padded channels excluded)."""
+    return 2 * nc * 27 * (2 * 16 + 16 * 16 * 2 + 16 * 1)
+
+
+def run_learned(args):
+    import torch
+
+    import schwarz_gmres_dashboard_gb300 as sg
+
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    ctx = sg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    N = L_GRID
+    part = sg.partition_boxes(N, N, N, L_NPARTS, SPREAD, seed=1)
+    M = sg.TwoLevelSchwarzPrecond(L_NPARTS, OVERLAP, sg.FineLevelType.RAS, part,
+                                  factor_dtype=sg.BF16, sweep_dtype=sg.FP32, ctx=ctx)
+    stage = sg.LearnedCorrection(N, ctx=ctx)
+    stage.init_weights(0)
+
+    def field(seed):
+        A = sg.make_varcoef_3d(N, N, N, 1.0, 8.0, seed=seed + 100000 * rank)
+        A.upload(ctx)
+        M.setup(A)  # same pattern every time: only the device factorisation reruns
+        return A
+
+    # training pairs from plain solves over seeded fields (+ 2 validation fields)
+    t0 = time.time()
+    keep = []
+    for f in range(args.fields):
+        A = field(1000 + f)
+        sg.collect_pairs(stage, A, M, sg.uniform(A.nrows, seed=3000 + f), L_SNAPSHOTS)
+        keep.append(A)
+        if len(keep) > 2:
+            keep.pop(0)
+    ntrain = stage.num_samples
+    for f in range(2):
+        A = field(9000 + f)
+        sg.collect_pairs(stage, A, M, sg.uniform(A.nrows, seed=9500 + f), L_SNAPSHOTS)
+        keep.append(A)
+    nval = stage.num_samples - ntrain
+    gen_s = time.time() - t0
+    torch.cuda.synchronize()
+    t0 = time.time()
+    losses = stage.train(0, ntrain, epochs=args.epochs, batch=8, lr=1e-3, seed=1)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    val_loss = stage.eval(ntrain, nval)
+
+    prm = sg.GMRESParams(restart=L_RESTART, max_iter=4000, tol=RTOL, tol_kind=sg.TOL_TRUE_REL,
+                         precision=sg.FP32)
+    rows = []
+    e2e = []
+    launches = 0
+    breakdown = None
+    with Clocks(local) as clk:
+        for i in range(args.held_out):
+            seed = 5000 + i
+            A = field(seed)
+            n = A.nrows
+            xs = sg.uniform(n, seed=seed + 7)
+            b = A.spmv(xs)
+            bd = torch.from_numpy(b).to(f"cuda:{local}")
+            xd = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+            row = {"seed": seed}
+            for variant in ("plain", "learned"):
+                if variant == "learned":
+                    stage.set_matrix(A)
+                    stage.attach(M, stagnation=0.5)
+
+                def solve(p=prm):
+                    with torch.cuda.stream(stream):
+                        xd.zero_()
+                    return sg.fgmres(A, bd, xd, M, p)
+
+                for _ in range(args.warmup if i == 0 else 0):
+                    solve()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                l0 = ctx.launch_count
+                e0.record(stream)
+                r = solve()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if variant == "learned":
+                    launches += ctx.launch_count - l0
+                relres = float(torch.linalg.norm(bd - torch.from_numpy(A.spmv(xd.cpu().numpy()))
+                                                 .to(bd.device)) / torch.linalg.norm(bd))
+                row[variant] = {"s": e0.elapsed_time(e1) / 1e3, "iterations": r.iterations,
+                                "true_rel_residual": relres, "converged": r.converged}
+                if variant == "learned":
+                    row["learned"]["fallback_cycle"] = stage.state()["fallback_cycle"]
+                    if i < 5:  # e2e: host b and x through the C ABI
+                        xh = np.zeros(n)
+                        torch.cuda.synchronize()
+                        t1 = time.perf_counter()
+                        sg.fgmres(A, b, xh, M, prm)
+                        e2e.append(time.perf_counter() - t1)
+                    if i == 0:
+                        p_eager = sg.GMRESParams(**{**prm.__dict__, "use_graph": False})
+                        breakdown, _ = class_breakdown(ctx, lambda: solve(p_eager))
+                    stage.detach()
+            rows.append(row)
+    if rank != 0:
+        return
+    mean = statistics.mean
+    t_plain = mean(r["plain"]["s"] for r in rows)
+    t_learned = mean(r["learned"]["s"] for r in rows)
+    it_plain = mean(r["plain"]["iterations"] for r in rows)
+    it_learned = mean(r["learned"]["iterations"] for r in rows)
+    nc = (N // 2) ** 3
+    peak_hbm, peak_kind = peaks()
+    bf16_peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16_peak = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        bf16_peak = 1900.0
+    kern = {}
+    if breakdown:
+        for name, (ms, cnt) in breakdown.items():
+            if cnt:
+                kern[name] = {"ms": ms, "launches": cnt, "us_per_launch": ms * 1e3 / cnt}
+    lrn = kern.get("learned")
+    roofline = None
+    if lrn:
+        fl = learned_flops(nc)
+        ach = fl / (lrn["us_per_launch"] / 1e6) / 1e12
+        roofline = {"kernel": "learned stage (FP32 residual+restrict, 4 x k_conv3d mma.sync "
+                              "BF16, prolong)", "bound": "tensor", "achieved": ach,
+                    "peak": bf16_peak, "unit": "TFLOP/s", "frac": ach / bf16_peak,
+                    "traffic": None, "flops_per_apply": fl,
+                    "us_per_apply": lrn["us_per_launch"]}
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline_learned(rows[0]["plain"]["iterations"])
+    line = {
+        "metric": METRIC,
+        "value": t_learned,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": len(rows),
+        "warmup": args.warmup,
+        "ms_per_step": t_learned * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16 cnn + fp32/bf16 preconditioner / f64 outer",
+        "data": "synthetic: seeded Gaussian random field coefficients, x* ~ U[-1,1]",
+        "config": {"workload": L_WORKLOAD, "n": N ** 3, "nparts": L_NPARTS,
+                   "overlap": OVERLAP, "restart": L_RESTART, "rtol": RTOL,
+                   "solver": "FGMRES(40), FP32 Krylov cycle from FP64 residual",
+                   "held_out_fields": len(rows), "l2": "working set > L2 (no flush)",
+                   "parallelism": f"replicas x{world}"},
+        "iterations": it_learned,
+        "plain_two_level_ras": {"value": t_plain, "unit": "s", "iterations": it_plain},
+        "speedup_vs_plain": t_plain / t_learned,
+        "iteration_ratio": it_learned / it_plain,
+        "fallbacks": sum(1 for r in rows if r["learned"]["fallback_cycle"] >= 0),
+        "max_true_rel_residual": max(max(r["plain"]["true_rel_residual"],
+                                         r["learned"]["true_rel_residual"]) for r in rows),
+        "all_converged": all(r["plain"]["converged"] and r["learned"]["converged"] for r in rows),
+        "training": {"fields": args.fields, "pairs": ntrain, "validation_pairs": nval,
+                     "epochs": args.epochs, "batch": 8, "lr": 1e-3, "pair_gen_s": gen_s,
+                     "train_s": train_s, "loss_first_epoch": float(losses[0]) if len(losses) else None,
+                     "loss_last_epoch": float(losses[-1]) if len(losses) else None,
+                     "validation_loss": val_loss},
+        "per_field": rows,
+        "e2e": {"value": statistics.mean(e2e) if e2e else None, "unit": "s",
+                "h2d_bytes_per_step": 2 * N ** 3 * 8, "d2h_bytes_per_step": N ** 3 * 8},
+        "roofline": roofline,
+        "kernels": kern,
+        "hbm_peak": {"value": peak_hbm, "source": peak_kind},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+def cpu_baseline_learned(iterations):
+    """The oracle's plain two-level RAS FGMRES(40) (the reference has no
+    learned stage): one 40-step restart cycle on held-out field 5000 with all
+    host threads, scaled to the iterations the GPU plain solve needed."""
+    try:
+        import schwarz_gmres_dashboard_gb300 as sg
+        from oracle.oracle import Oracle
+        A = sg.make_varcoef_3d(L_GRID, L_GRID, L_GRID, 1.0, 8.0, seed=5000)
+        part = sg.partition_boxes(L_GRID, L_GRID, L_GRID, L_NPARTS, SPREAD, seed=1)
+        orc = Oracle()
+        threads = os.cpu_count() or 1
+        orc.set_threads(threads)
+        b = orc.spmv(A, sg.uniform(A.nrows, seed=5007))
+        pc = orc.precond("twolevel_ras", A, L_NPARTS, OVERLAP, part)
+        t0 = time.perf_counter()
+        orc.fgmres(A, b, np.zeros(A.nrows), pc, restart=L_RESTART, max_iter=L_RESTART, tol=0.0)
+        dt = time.perf_counter() - t0
+        return {"value": dt / L_RESTART * iterations, "unit": "s", "cores": threads,
+                "kind": "port",
+                "sample": f"one FGMRES(40) restart cycle of the oracle's plain two-level RAS "
+                          f"solve on held-out field 5000, {dt:.2f} s, scaled to {iterations} "
+                          f"iterations"}
+    except Exception as e:
         return {"value": None, "unit": "s", "cores": os.cpu_count(), "kind": "port",
                 "sample": f"failed: {e}"}
 
@@ -379,6 +697,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=128,
                     help="grid edge (128 = the benchmark workload; smaller for profiling)")
+    ap.add_argument("--workload", default="cfg3", choices=["cfg3", "learned"],
+                    help="cfg3: the 128^3 two-level RAS GMRES(30) solve (default); learned: "
+                         "FGMRES(40) + learned stage on 96^3 vs plain two-level RAS")
+    ap.add_argument("--fields", type=int, default=200, help="learned: training fields")
+    ap.add_argument("--held-out", type=int, default=20, help="learned: held-out test fields")
+    ap.add_argument("--epochs", type=int, default=20, help="learned: training epochs")
     args = ap.parse_args()
     global N_GRID, NPARTS, WORKLOAD
     if args.grid != N_GRID:
@@ -389,6 +713,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_ours(args)
 

@@ -96,7 +96,8 @@ sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count);
 /* Kernel-class timers: with timing on, solves that run without a CUDA graph
  * record a CUDA event pair on the context stream around every kernel class:
  * kind 0 Krylov SpMV, 1 FP64 residual, 2 preconditioner, 3 orthogonalisation
- * (CGS2 passes, Givens), 4 back-solve and update.  get_timing returns the
+ * (CGS2 passes, Givens), 4 back-solve and update, 5 the learned stage (also
+ * counted inside kind 2).  get_timing returns the
  * accumulated milliseconds and the number of timed launches of a kind.
  * Turning timing on resets the sums.  No counterpart in the reference. */
 sg_status sg_ctx_set_timing(sg_ctx* ctx, int on);
@@ -123,7 +124,10 @@ sg_status sg_csr_spmv(sg_csr* A, const double* x, double* y, sg_mem mem);
 /* ---- preconditioner plugin (src/precond/preconditioner.h:7-20) ------- */
 sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_opts* opts,
                             sg_precond** out);
-/* Preconditioner::setup(const CSRMatrix&) */
+/* Preconditioner::setup(const CSRMatrix&).  A second set-up with a matrix of
+ * the same sparsity pattern (and the same partition and options) keeps the
+ * host integer set-up (decomposition, local structures, level schedules) and
+ * redoes only the device factorisation -- e.g. a new coefficient field. */
 sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A);
 /* Preconditioner::apply(const double* x, double* y, int n) const:
  * overwrites all of y with M^{-1} x. */

@@ -68,7 +68,7 @@ class Context:
     def synchronize(self) -> None:
         _check(_clib.sg_ctx_synchronize(self.handle))
 
-    TIMER_KINDS = ("spmv", "residual", "precond", "ortho", "update")
+    TIMER_KINDS = ("spmv", "residual", "precond", "ortho", "update", "learned")
 
     def set_timing(self, on: bool) -> None:
         """Kernel-class CUDA-event timers for solves run without a graph."""

@@ -391,6 +391,25 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
     });
 }
 
+namespace {
+// FNV-1a over everything the host set-up of a Schwarz preconditioner reads
+uint64_t structure_key(const sg_precond* pc, const sg_csr* A, const int* part, int nparts,
+                       int overlap) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t bytes) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    };
+    const int head[6] = {pc->kind, A->nrows, A->ncols, A->nnz, nparts, overlap};
+    mix(head, sizeof(head));
+    mix(pc->opts.reserved, sizeof(pc->opts.reserved));
+    mix(A->h_rp.data(), sizeof(int) * A->h_rp.size());
+    mix(A->h_ci.data(), sizeof(int) * A->h_ci.size());
+    mix(part, sizeof(int) * (size_t)A->nrows);
+    return h;
+}
+}  // namespace
+
 sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
     return guard([&] {
         SG_CHECK_ARG(pc && A, "NULL argument");
@@ -424,7 +443,17 @@ sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
                 partition_graph(A->nrows, A->h_rp.data(), A->h_ci.data(), nparts, part.data());
         }
         pc->overlap = overlap;
-        build_schwarz_host(pc, A, part.data(), nparts, overlap);
+        // The integer set-up depends only on the sparsity pattern, the
+        // partition and the options: a matrix with the same structure as the
+        // previous set-up (new values, e.g. another coefficient field) keeps
+        // it and only redoes the device factorisation.
+        const uint64_t key = structure_key(pc, A, part.data(), nparts, overlap);
+        if (!(pc->has_structure && pc->structure_key == key)) {
+            pc->has_structure = false;
+            build_schwarz_host(pc, A, part.data(), nparts, overlap);
+            pc->structure_key = key;
+            pc->has_structure = true;
+        }
         precond_setup_device(pc, A);
         pc->is_setup = true;
     });

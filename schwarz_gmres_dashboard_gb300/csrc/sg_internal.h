@@ -146,7 +146,8 @@ struct sg_ctx {
 
 namespace sg {
 // kernel classes of the timers
-enum { TK_SPMV = 0, TK_RESIDUAL = 1, TK_PRECOND = 2, TK_ORTHO = 3, TK_UPDATE = 4 };
+// (TK_LEARNED runs inside TK_PRECOND: the preconditioner class includes it)
+enum { TK_SPMV = 0, TK_RESIDUAL = 1, TK_PRECOND = 2, TK_ORTHO = 3, TK_UPDATE = 4, TK_LEARNED = 5 };
 // Records a CUDA event pair around the launches made during its lifetime
 // when the context's timers are on (not while a graph is being captured).
 struct ClassTimer {
@@ -213,6 +214,8 @@ struct sg_precond {
     int kind = SG_PC_NONE;
     sg_precond_opts opts{};
     bool is_setup = false;
+    bool has_structure = false;   // host integer set-up done for structure_key
+    uint64_t structure_key = 0;
     int n = 0;
     int nparts = 0;
     int overlap = 0;

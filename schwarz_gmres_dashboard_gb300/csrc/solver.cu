@@ -87,7 +87,10 @@ void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int*
     // inside the solver FP64 sweeps may fuse multiply-adds (exact = false)
     if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active, false);
     else launch_copy<TI, TO>(ctx, x, y, n, active);
-    if (pc && pc->learned) learned_apply<TI, TO>(pc->learned, x, y, n, active);
+    if (pc && pc->learned) {
+        ClassTimer tm(ctx, TK_LEARNED);
+        learned_apply<TI, TO>(pc->learned, x, y, n, active);
+    }
 }
 
 // One restart cycle as a launch sequence on ctx->stream.

@@ -201,7 +201,8 @@ def collect_pairs(stage: LearnedCorrection, A: CSRMatrix, M: Preconditioner, x_s
     for k in snapshots:
         x = np.zeros(A.nrows)
         fgmres(A, b, x, M, GMRESParams(restart=int(k), max_iter=int(k), tol=0.0,
-                                       tol_kind=TOL_TRUE_REL_CYCLE, precision=precision))
+                                       tol_kind=TOL_TRUE_REL_CYCLE, precision=precision,
+                                       use_graph=False))
         r = b - A.spmv(x)
         stage.add_pair(M, r, x_star - x)
     return len(snapshots)
