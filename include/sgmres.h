@@ -265,8 +265,10 @@ sg_status sg_learned_init_weights(sg_learned* L, uint64_t seed);
 sg_status sg_learned_set_weights(sg_learned* L, const float* w, int count);
 sg_status sg_learned_get_weights(sg_learned* L, float* w, int count);
 /* Training pair from a plain solve: residual r = b - A x_k and error
- * e = x* - x_k.  Stores the input R r1 / s, the feature f and the target
- * R(e - M r) / s on the device (M: pc without any learned stage). */
+ * e = x* - x_k.  Stores on the device the input R r1 / s, the feature f, the
+ * coarse target R(e1) / s and the fine target e1 / s with e1 = e - M r (M: pc
+ * without any learned stage), and the current matrix's FP32 values once per
+ * sg_learned_set_matrix (every pair's matrix must share one pattern). */
 sg_status sg_learned_add_pair(sg_learned* L, sg_precond* pc, const double* r, const double* e,
                               int n, sg_mem mem);
 sg_status sg_learned_num_samples(sg_learned* L, int* count);
@@ -274,11 +276,22 @@ sg_status sg_learned_clear_samples(sg_learned* L);
 /* Copies stored sample i (each array nc = (nx/2)^3 floats; NULL skips). */
 sg_status sg_learned_get_sample(sg_learned* L, int i, float* input, float* feature,
                                 float* target);
-/* Adam (lr, betas 0.9/0.999, eps 1e-8) on the mean squared error between
- * the network output and target / c over samples [first, first+count), in
- * shuffled mini-batches (SplitMix64(seed) Fisher-Yates per epoch); sets c to
- * the rms of those targets first.  epoch_loss (optional) receives the mean
- * batch loss of every epoch. */
+/* Fine-grid data of stored sample i: the energy target e1 / s (n floats),
+ * its energy (e1/s)^T A (e1/s) and the index of its field (NULL skips). */
+sg_status sg_learned_get_sample_fine(sg_learned* L, int i, float* err, float* energy, int* field);
+/* Training loss: 0 (default) the energy norm of the field's A,
+ *   mean over samples of ||e1/s - c P y||_A^2 / ||e1/s||_A^2;
+ * 1 the mean squared error between y and the coarse target / c. */
+sg_status sg_learned_set_loss(sg_learned* L, int kind);
+/* Loss and parameter gradient of the current network over stored samples
+ * [first, first+count) as one batch (count <= 64). */
+sg_status sg_learned_sample_gradient(sg_learned* L, int first, int count, float* grad,
+                                     double* loss);
+/* Adam (lr, betas 0.9/0.999, eps 1e-8) on the training loss over samples
+ * [first, first+count), in shuffled mini-batches (SplitMix64(seed)
+ * Fisher-Yates per epoch); sets c to the rms of those samples' coarse
+ * targets first.  epoch_loss (optional) receives the mean batch loss of
+ * every epoch. */
 sg_status sg_learned_train(sg_learned* L, int first, int count, int epochs, int batch, double lr,
                            uint64_t seed, double* epoch_loss);
 /* Mean loss of the current network over samples [first, first+count). */

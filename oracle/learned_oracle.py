@@ -7,6 +7,10 @@ oracle restates the stage's own definition in numpy:
     z1 = M v;  r1 = v - A z1;  rc = R r1;  s = rms(rc)
     z  = z1 + s * c * P(net([rc / s, f]))
 
+and its two training losses: the energy norm ||e1/s - c P y||_A^2 /
+||e1/s||_A^2 with e1 = e - M r the error left after M, and the coarse mean
+squared error against R e1 / (s c).
+
 R: mean of the 2x2x2 children; P: cell-centred trilinear prolongation with
 the neighbour index clamped at the boundary; f: standardised restricted
 log A_ii; net: four 3x3x3 convolutions (16 channels, zero padding, ReLU after
@@ -136,7 +140,6 @@ def forward(params, x2, D, emulate_bf16=True):
 def loss_and_grad(params, x2, t, D, emulate_bf16=True):
     """mean (y - t)^2 and its gradient (NET_PARAMS, library layout, padded 0)."""
     rnd = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
-    layers, _c = unpack(params)
     y, acts = forward(params, x2, D, emulate_bf16)
     t = np.asarray(t, dtype=np.float64).reshape(y.shape)
     count = y.size
@@ -144,6 +147,31 @@ def loss_and_grad(params, x2, t, D, emulate_bf16=True):
     B = y.shape[0]
     G = np.zeros((B, D, D, D, C))
     G[..., 0] = rnd((2.0 * (y - t) / count)).reshape(B, D, D, D)
+    return loss, backward(params, acts, G, emulate_bf16)
+
+
+def energy_loss_and_grad(params, x2, err, energy, spmvs, nx, emulate_bf16=True):
+    """Energy-norm loss mean_b ||err_b - c P y_b||_A^2 / energy_b and its
+    gradient; spmvs[b](u) = A_b u, energy_b = err_b^T A_b err_b."""
+    rnd = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
+    D = nx // 2
+    y, acts = forward(params, x2, D, emulate_bf16)
+    _layers, c = unpack(params)
+    B = y.shape[0]
+    loss = 0.0
+    G = np.zeros((B, D, D, D, C))
+    for b in range(B):
+        u = np.asarray(err[b], dtype=np.float64) - c * prolong(y[b], nx)
+        w = spmvs[b](u)
+        loss += float(u @ w) / (energy[b] * B)
+        G[b, ..., 0] = rnd(-2.0 * c * prolong_t(w, nx) / (energy[b] * B)).reshape(D, D, D)
+    return loss, backward(params, acts, G, emulate_bf16)
+
+
+def backward(params, acts, G, emulate_bf16=True):
+    """Parameter gradient from the output gradient G [B, D, D, D, 16] (channel 0)."""
+    rnd = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
+    layers, _c = unpack(params)
     grads = [None] * LAYERS
     for l in range(LAYERS - 1, -1, -1):
         dW, db = conv3d_weight_grad(acts[l], G)
@@ -155,7 +183,7 @@ def loss_and_grad(params, x2, t, D, emulate_bf16=True):
     for l, (dW, db) in enumerate(grads):
         flat[l * LAYER_P: l * LAYER_P + LAYER_W] = dW.reshape(-1)
         flat[l * LAYER_P + LAYER_W: (l + 1) * LAYER_P] = db
-    return loss, flat * param_mask()
+    return flat * param_mask()
 
 
 # ------------------------------------------------------------------ grid transfer
@@ -186,6 +214,14 @@ def prolong(c, nx, ny=None, nz=None):
     return out.reshape(-1)
 
 
+def prolong_t(w, nx, ny=None, nz=None):
+    """Adjoint (transpose) of `prolong`."""
+    ny, nz = ny or nx, nz or nx
+    W = np.asarray(w, dtype=np.float64).reshape(nz, ny, nx)
+    out = np.einsum("ai,bj,ck,abc->ijk", _interp_1d(nz), _interp_1d(ny), _interp_1d(nx), W)
+    return out.reshape(-1)
+
+
 def feature(diag, nx):
     """Standardised restricted log A_ii."""
     c = restrict(np.log(np.asarray(diag, dtype=np.float64)), nx)
@@ -208,10 +244,13 @@ def stage_apply(params, spmv, apply_m, diag, v, nx):
 
 
 def training_pair(spmv, apply_m, diag, r, e, nx):
-    """(input R r1 / s, feature f, target R(e - M r) / s) of a pair (r, e)."""
+    """(input R r1 / s, feature f, coarse target R(e1) / s, fine target e1 / s,
+    energy (e1/s)^T A (e1/s)) of a pair (r, e), e1 = e - M r."""
     z1 = apply_m(r)
     rc = restrict(r - spmv(z1), nx)
-    ec = restrict(e - z1, nx)
+    e1 = e - z1
+    ec = restrict(e1, nx)
     s = float(np.sqrt(np.mean(rc ** 2)))
     inv = 1.0 / s if s > 0 else 0.0
-    return rc * inv, feature(diag, nx), ec * inv
+    fine = e1 * inv
+    return rc * inv, feature(diag, nx), ec * inv, fine, float(fine @ spmv(fine))

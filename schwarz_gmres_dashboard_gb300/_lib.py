@@ -110,6 +110,9 @@ PROTOTYPES = {
     "sg_learned_num_samples": (C.c_int, [_vp, _ip]),
     "sg_learned_clear_samples": (C.c_int, [_vp]),
     "sg_learned_get_sample": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "sg_learned_get_sample_fine": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "sg_learned_set_loss": (C.c_int, [_vp, C.c_int]),
+    "sg_learned_sample_gradient": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _dp]),
     "sg_learned_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                    C.c_uint64, _vp]),
     "sg_learned_eval": (C.c_int, [_vp, C.c_int, C.c_int, _dp]),

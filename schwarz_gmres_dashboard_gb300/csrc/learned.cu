@@ -13,8 +13,11 @@
 //   c   output scale (rms of the training targets)
 //   P   cell-centred trilinear prolongation back to the fine grid
 //
-// The network learns R(e - M r) / s from (residual r, error e = A^{-1} r)
-// pairs of plain solves: the coarse error left after M.  Scaling by s makes
+// The network is trained on (residual r, error e = A^{-1} r) pairs of plain
+// solves to predict the error left after M, e1 = e - M r, in the energy norm
+// of A: loss = ||e1/s - c P y||_A^2 / ||e1/s||_A^2 (the criterion a Galerkin
+// coarse correction minimises; a coarse-MSE loss, also available, lets rough
+// prediction errors blow up the fine-grid residual).  Scaling by s makes
 // the stage positively homogeneous (FGMRES applies it to unnormalised
 // vectors); the stage is nonlinear, so it runs inside FGMRES only.  A device
 // monitor after every restart cycle switches the stage off for the rest of
@@ -475,6 +478,139 @@ __global__ void k_sub64(const double* __restrict__ a, const double* __restrict__
         out[i] = a[i] - b[i];
 }
 
+// energy loss, step 1: u[b][f] = err[idx[b]][f] - c * P(Y[b])[f]
+__global__ void k_energy_u(const float* __restrict__ err, const int* __restrict__ idx, int batch,
+                           const float* __restrict__ Y, int nx, int ny, int nz, float c,
+                           float* __restrict__ u) {
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    const size_t n = (size_t)nx * ny * nz, ncc = (size_t)cx * cy * cz;
+    const float w[2] = {0.75f, 0.25f};
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n * batch;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(q / n);
+        const size_t f = q % n;
+        const int fx = (int)(f % nx), fy = (int)((f / nx) % ny), fz = (int)(f / ((size_t)nx * ny));
+        int ia[2], ja[2], ka[2];
+        tri_axis(fx, cx, ia);
+        tri_axis(fy, cy, ja);
+        tri_axis(fz, cz, ka);
+        const float* Yb = Y + (size_t)b * ncc;
+        float acc = 0.f;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 2; ++bb) {
+                const float* row = Yb + ((size_t)ka[a] * cy + ja[bb]) * cx;
+                acc += w[a] * w[bb] * (0.75f * row[ia[0]] + 0.25f * row[ia[1]]);
+            }
+        u[q] = err[(size_t)idx[b] * n + f] - c * acc;
+    }
+}
+
+// energy loss, step 2: w[b] = A_{field(b)} u[b] (shared pattern, per-field
+// FP32 values); loss += u.w / (energy_b * batch) (block sums added
+// atomically -- reporting only).  blockIdx.y = batch entry.
+__global__ void __launch_bounds__(256)
+k_energy_spmv(const int* __restrict__ rp, const int* __restrict__ ci,
+              const float* __restrict__ fvals, long long nnz, const int* __restrict__ sfield,
+              const int* __restrict__ idx, const float* __restrict__ energy, int n, int batch,
+              const float* __restrict__ u, float* __restrict__ w, float* __restrict__ loss) {
+    const int b = blockIdx.y;
+    const int smp = idx[b];
+    const float* val = fvals + (size_t)sfield[smp] * nnz;
+    const float* ub = u + (size_t)b * n;
+    float* wb = w + (size_t)b * n;
+    float s = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (int q = rp[i]; q < rp[i + 1]; ++q) acc += val[q] * ub[ci[q]];
+        wb[i] = acc;
+        s += acc * ub[i];
+    }
+    s = warp_sum(s);
+    __shared__ float red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+        const float e = energy[smp];
+        if (e > 0.f) atomicAdd(loss, t / (e * (float)batch));
+    }
+}
+
+// adjoint of the trilinear prolongation along one axis: the fine points that
+// coarse cell c contributes to, with their weights (returns the count)
+__device__ __forceinline__ int tri_axis_t(int c, int nc, int (&f)[4], float (&wt)[4]) {
+    int k = 0;
+    f[k] = 2 * c;     wt[k++] = c == 0 ? 1.f : 0.75f;
+    f[k] = 2 * c + 1; wt[k++] = c == nc - 1 ? 1.f : 0.75f;
+    if (c >= 1) { f[k] = 2 * c - 1; wt[k++] = 0.25f; }
+    if (c <= nc - 2) { f[k] = 2 * c + 2; wt[k++] = 0.25f; }
+    return k;
+}
+
+// energy loss, step 3: G[b][c] = (-2 c / (energy_b * batch)) (P^T w_b)[c] in
+// channel 0 (BF16), channels 1-15 zero
+__global__ void k_energy_grad(const float* __restrict__ w, const int* __restrict__ idx,
+                              const float* __restrict__ energy, int batch, int nx, int ny, int nz,
+                              float c, uint32_t* __restrict__ G) {
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    const size_t n = (size_t)nx * ny * nz, ncc = (size_t)cx * cy * cz;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < ncc * batch;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(q / ncc);
+        const size_t cc = q % ncc;
+        const int i = (int)(cc % cx), j = (int)((cc / cx) % cy), k = (int)(cc / ((size_t)cx * cy));
+        int fi[4], fj[4], fk[4];
+        float wi[4], wj[4], wk[4];
+        const int ni = tri_axis_t(i, cx, fi, wi);
+        const int nj = tri_axis_t(j, cy, fj, wj);
+        const int nk = tri_axis_t(k, cz, fk, wk);
+        const float* wb = w + (size_t)b * n;
+        float acc = 0.f;
+        for (int a = 0; a < nk; ++a)
+            for (int bb = 0; bb < nj; ++bb) {
+                const float* row = wb + ((size_t)fk[a] * ny + fj[bb]) * nx;
+                float r = 0.f;
+                for (int cc2 = 0; cc2 < ni; ++cc2) r += wi[cc2] * row[fi[cc2]];
+                acc += wk[a] * wj[bb] * r;
+            }
+        const float e = energy[idx[b]];
+        const float g = e > 0.f ? -2.f * c * acc / (e * (float)batch) : 0.f;
+        uint4* g4 = reinterpret_cast<uint4*>(G + q * 8);
+        g4[0] = make_uint4(pack_bf16(g, 0.f), 0u, 0u, 0u);
+        g4[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// FP32 copy of v * inv into out (the fine training target)
+__global__ void k_scale_store(const double* __restrict__ v, int n, const LearnedCtl* ctl,
+                              float* __restrict__ out) {
+    const float s = ctl->pair_s;
+    const double inv = s > 0.f ? 1.0 / (double)s : 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (float)(v[i] * inv);
+}
+
+// energy of the stored FP32 target: e^T A e with the field's FP32 values, in FP64
+__global__ void __launch_bounds__(256)
+k_energy_norm(const int* __restrict__ rp, const int* __restrict__ ci, const float* __restrict__ val,
+              const float* __restrict__ e, int n, double* partials, unsigned* counter,
+              float* __restrict__ out) {
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int q = rp[i]; q < rp[i + 1]; ++q) acc += (double)val[q] * (double)e[ci[q]];
+        s += acc * (double)e[i];
+    }
+    __shared__ double red[8];
+    __shared__ double bs[1], tot[1];
+    double v1[1] = {s};
+    block_sum_multi<1>(v1, 1, red, bs);
+    if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0) *out = (float)tot[0];
+}
+
 // solve start: stage on (unless switched off), monitor reference = initial residual
 __global__ void k_learned_begin(LearnedCtl* ctl, const SolveState* st, int on) {
     ctl->enabled = on;
@@ -513,16 +649,27 @@ struct LearnedImpl {
     // inference scratch (one sample)
     DBuf<float> rc, ec, yout;
     DBuf<uint32_t> act[4];
-    // training pairs
+    // training pairs: coarse input, feature and target, fine energy target,
+    // its energy, and the field (matrix) it came from
     DBuf<double> r64, e64, z64, t64;
-    DBuf<float> s_in, s_tgt, s_feat;
+    DBuf<float> s_in, s_tgt, s_feat, s_err, s_energy;
+    DBuf<int> s_field;
     int nsamples = 0, cap = 0;
+    std::vector<int> h_field;
+    // fields of the stored pairs: one sparsity pattern, FP32 values per field
+    DBuf<int> f_rp, f_ci;
+    DBuf<float> f_vals;
+    long long f_nnz = 0;
+    int nfields = 0, fcap = 0;
+    bool cur_registered = false;  // the current matrix is already a field
     // training scratch
     int tb = 0;
     DBuf<uint32_t> tact[4], tg[2];
-    DBuf<float> ty, tt, tpart, tloss;
+    DBuf<float> ty, tt, tpart, tloss, tu, tw;
+    DBuf<int> tidx;
     long long adam_t = 0;
     float out_scale = 1.f;
+    int loss_kind = 0;  // 0 energy norm of A, 1 coarse mean squared error
 };
 
 }  // namespace sg
@@ -586,22 +733,51 @@ void ensure_train(sg_learned* L, int batch) {
     const int tiles = L->cx / TB;
     L->tpart.alloc((size_t)tiles * tiles * tiles * batch * LAYER_P);
     L->tloss.alloc(1);
+    L->tidx.alloc(batch);
+    if (L->loss_kind == 0) {
+        const size_t n = (size_t)L->nx * L->ny * L->nz;
+        L->tu.alloc(n * batch);
+        L->tw.alloc(n * batch);
+    }
     L->tb = batch;
 }
 
 // forward, loss and (with_grad) the parameter gradient of the packed batch in
-// tact[0] with targets tt; the loss is added to tloss
-void loss_grad(sg_learned* L, int batch, bool with_grad) {
+// tact[0]; the loss is added to tloss.  energy: samples idx[0..batch) (device)
+// of the stored pairs; otherwise targets tt (coarse mean squared error).
+void loss_grad(sg_learned* L, int batch, bool with_grad, bool energy, const int* idx) {
     const size_t V = (size_t)L->nc;
     uint32_t *X0 = L->tact[0].p, *A1 = L->tact[1].p, *A2 = L->tact[2].p, *A3 = L->tact[3].p;
     forward(L, X0, A1, A2, A3, L->ty.p, batch, nullptr, nullptr);
     uint32_t* G = L->tg[0].p;
     uint32_t* H = L->tg[1].p;
-    k_loss_grad<<<kblocks(L->ctx, V * batch), 256, 0, L->ctx->stream>>>(
-        L->ty.p, L->tt.p, V * batch, with_grad ? G : nullptr, L->tloss.p);
-    SG_CUDA(cudaGetLastError());
-    count_launch(L->ctx);
-    if (!with_grad) return;
+    if (energy) {
+        const int n = L->nx * L->ny * L->nz;
+        if (L->tu.n < (size_t)n * batch) L->tu.alloc((size_t)n * batch);
+        if (L->tw.n < (size_t)n * batch) L->tw.alloc((size_t)n * batch);
+        cudaStream_t st = L->ctx->stream;
+        k_energy_u<<<kblocks(L->ctx, (size_t)n * batch), 256, 0, st>>>(
+            L->s_err.p, idx, batch, L->ty.p, L->nx, L->ny, L->nz, L->out_scale, L->tu.p);
+        SG_CUDA(cudaGetLastError());
+        const dim3 g((unsigned)std::min<long long>((n + 255) / 256, 1024), (unsigned)batch);
+        k_energy_spmv<<<g, 256, 0, st>>>(L->f_rp.p, L->f_ci.p, L->f_vals.p, L->f_nnz, L->s_field.p,
+                                         idx, L->s_energy.p, n, batch, L->tu.p, L->tw.p,
+                                         L->tloss.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(L->ctx);
+        count_launch(L->ctx);
+        if (!with_grad) return;
+        k_energy_grad<<<kblocks(L->ctx, V * batch), 256, 0, st>>>(
+            L->tw.p, idx, L->s_energy.p, batch, L->nx, L->ny, L->nz, L->out_scale, G);
+        SG_CUDA(cudaGetLastError());
+        count_launch(L->ctx);
+    } else {
+        k_loss_grad<<<kblocks(L->ctx, V * batch), 256, 0, L->ctx->stream>>>(
+            L->ty.p, L->tt.p, V * batch, with_grad ? G : nullptr, L->tloss.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(L->ctx);
+        if (!with_grad) return;
+    }
     // layer 4 (input A3), 3 (A2), 2 (A1), 1 (X0); the input gradient of a
     // layer is masked by the ReLU of its input (the previous layer's output)
     wgrad(L, A3, G, 3, batch);
@@ -642,7 +818,69 @@ void grow_samples(sg_learned* L, int need) {
     grow(L->s_in);
     grow(L->s_tgt);
     grow(L->s_feat);
+    {
+        const size_t n = (size_t)L->nx * L->ny * L->nz;
+        DBuf<float> nb;
+        nb.alloc((size_t)ncap * n);
+        if (L->nsamples > 0)
+            SG_CUDA(cudaMemcpyAsync(nb.p, L->s_err.p, sizeof(float) * n * L->nsamples,
+                                    cudaMemcpyDeviceToDevice, L->ctx->stream));
+        DBuf<float> ne;
+        ne.alloc((size_t)ncap);
+        DBuf<int> nf;
+        nf.alloc((size_t)ncap);
+        if (L->nsamples > 0) {
+            SG_CUDA(cudaMemcpyAsync(ne.p, L->s_energy.p, sizeof(float) * L->nsamples,
+                                    cudaMemcpyDeviceToDevice, L->ctx->stream));
+            SG_CUDA(cudaMemcpyAsync(nf.p, L->s_field.p, sizeof(int) * L->nsamples,
+                                    cudaMemcpyDeviceToDevice, L->ctx->stream));
+        }
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+        std::swap(nb.p, L->s_err.p);
+        std::swap(nb.n, L->s_err.n);
+        std::swap(ne.p, L->s_energy.p);
+        std::swap(ne.n, L->s_energy.n);
+        std::swap(nf.p, L->s_field.p);
+        std::swap(nf.n, L->s_field.n);
+    }
     L->cap = ncap;
+}
+
+// the current matrix becomes a field of the stored pairs (FP32 values; the
+// first field fixes the sparsity pattern every later one must share)
+void register_field(sg_learned* L) {
+    if (L->cur_registered) return;
+    const sg_csr* A = L->A;
+    sg_ctx* ctx = L->ctx;
+    if (L->nfields == 0) {
+        L->f_rp.upload(A->h_rp, ctx->stream);
+        L->f_ci.upload(A->h_ci, ctx->stream);
+        L->f_nnz = A->nnz;
+    } else {
+        std::vector<int> rp(A->nrows + 1), ci((size_t)A->nnz);
+        if (A->nnz != L->f_nnz)
+            fail(SG_ERR_INVALID_ARG, "pairs of one learned stage must share the sparsity pattern");
+        SG_CUDA(cudaMemcpy(rp.data(), L->f_rp.p, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost));
+        SG_CUDA(cudaMemcpy(ci.data(), L->f_ci.p, sizeof(int) * ci.size(), cudaMemcpyDeviceToHost));
+        if (rp != A->h_rp || ci != A->h_ci)
+            fail(SG_ERR_INVALID_ARG, "pairs of one learned stage must share the sparsity pattern");
+    }
+    if (L->nfields + 1 > L->fcap) {
+        const int ncap = std::max(4, 2 * L->fcap);
+        DBuf<float> nb;
+        nb.alloc((size_t)ncap * L->f_nnz);
+        if (L->nfields > 0)
+            SG_CUDA(cudaMemcpyAsync(nb.p, L->f_vals.p, sizeof(float) * L->f_nnz * L->nfields,
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        std::swap(nb.p, L->f_vals.p);
+        std::swap(nb.n, L->f_vals.n);
+        L->fcap = ncap;
+    }
+    SG_CUDA(cudaMemcpyAsync(L->f_vals.p + (size_t)L->nfields * L->f_nnz, A->val32.p,
+                            sizeof(float) * L->f_nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+    L->nfields += 1;
+    L->cur_registered = true;
 }
 
 // restricted residual of v - A z (z may be null) into rc, s into *s_out
@@ -879,6 +1117,7 @@ sg_status sg_learned_set_matrix(sg_learned* L, const sg_csr* A) {
         L->feat.upload(c, L->ctx->stream);
         SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
         L->A = A;
+        L->cur_registered = false;
     });
 }
 
@@ -979,12 +1218,26 @@ sg_status sg_learned_add_pair(sg_learned* L, sg_precond* pc, const double* r, co
                                                        static_cast<const double*>(nullptr), L->ec.p,
                                                        &c->scratch_s, nullptr, nullptr);
         grow_samples(L, L->nsamples + 1);
+        register_field(L);
+        const int field = L->nfields - 1;
         const size_t off = (size_t)L->nsamples * L->nc;
         k_store_pair<<<kblocks(ctx, (size_t)L->nc), 256, 0, ctx->stream>>>(
             L->rc.p, L->ec.p, L->feat.p, L->nc, c, L->s_in.p + off, L->s_tgt.p + off,
             L->s_feat.p + off);
         SG_CUDA(cudaGetLastError());
+        // fine energy target (e - M r) / s and its energy in the field's A
+        float* err = L->s_err.p + (size_t)L->nsamples * n;
+        k_scale_store<<<kblocks(ctx, n), 256, 0, ctx->stream>>>(L->t64.p, n, c, err);
+        SG_CUDA(cudaGetLastError());
+        k_energy_norm<<<std::min(kblocks(ctx, n), 4096), 256, 0, ctx->stream>>>(
+            L->f_rp.p, L->f_ci.p, L->f_vals.p + (size_t)field * L->f_nnz, err, n, L->partials.p,
+            L->counter.p, L->s_energy.p + L->nsamples);
+        SG_CUDA(cudaGetLastError());
         count_launch(ctx);
+        count_launch(ctx);
+        count_launch(ctx);
+        SG_CUDA(cudaMemcpyAsync(L->s_field.p + L->nsamples, &field, sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
         if (sweep_error(pc))
             fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
@@ -1003,6 +1256,59 @@ sg_status sg_learned_clear_samples(sg_learned* L) {
     return lguard([&] {
         SG_CHECK_ARG(L, "NULL argument");
         L->nsamples = 0;
+        L->nfields = 0;
+        L->cur_registered = false;
+    });
+}
+
+sg_status sg_learned_get_sample_fine(sg_learned* L, int i, float* err, float* energy, int* field) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        SG_CHECK_ARG(i >= 0 && i < L->nsamples, "sample %d out of range [0,%d)", i, L->nsamples);
+        const size_t n = (size_t)L->nx * L->ny * L->nz;
+        if (err)
+            SG_CUDA(cudaMemcpy(err, L->s_err.p + (size_t)i * n, sizeof(float) * n,
+                               cudaMemcpyDeviceToHost));
+        if (energy)
+            SG_CUDA(cudaMemcpy(energy, L->s_energy.p + i, sizeof(float), cudaMemcpyDeviceToHost));
+        if (field) SG_CUDA(cudaMemcpy(field, L->s_field.p + i, sizeof(int), cudaMemcpyDeviceToHost));
+    });
+}
+
+sg_status sg_learned_set_loss(sg_learned* L, int kind) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        SG_CHECK_ARG(kind == 0 || kind == 1, "loss kind must be 0 (energy) or 1 (coarse MSE)");
+        L->loss_kind = kind;
+    });
+}
+
+sg_status sg_learned_sample_gradient(sg_learned* L, int first, int count, float* grad,
+                                     double* loss) {
+    return lguard([&] {
+        SG_CHECK_ARG(L && grad && loss, "NULL argument");
+        SG_CHECK_ARG(first >= 0 && count >= 1 && count <= 64 && first + count <= L->nsamples,
+                     "samples [%d,%d) out of range [0,%d) or more than 64", first, first + count,
+                     L->nsamples);
+        sg_ctx* ctx = L->ctx;
+        SG_CUDA(cudaSetDevice(ctx->device));
+        ensure_train(L, count);
+        std::vector<int> idx(count);
+        for (int i = 0; i < count; ++i) idx[i] = first + i;
+        L->tidx.upload(idx, ctx->stream);
+        k_pack_batch<<<kblocks(ctx, (size_t)count * L->nc), 256, 0, ctx->stream>>>(
+            L->s_in.p, L->s_feat.p, L->s_tgt.p, L->tidx.p, count, L->nc, 1.f / L->out_scale,
+            L->tact[0].p, L->tt.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        L->tloss.zero(ctx->stream);
+        loss_grad(L, count, true, L->loss_kind == 0, L->tidx.p);
+        float l = 0.f;
+        SG_CUDA(cudaMemcpyAsync(&l, L->tloss.p, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(cudaMemcpyAsync(grad, L->grad.p, sizeof(float) * NET_PARAMS, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        *loss = l;
     });
 }
 
@@ -1063,7 +1369,7 @@ sg_status sg_learned_train(sg_learned* L, int first, int count, int epochs, int 
                     L->tact[0].p, L->tt.p);
                 SG_CUDA(cudaGetLastError());
                 count_launch(ctx);
-                loss_grad(L, bs, true);
+                loss_grad(L, bs, true, L->loss_kind == 0, dperm.p + b0);
                 adam_step(L, (float)lr);
             }
             float lsum = 0.f;
@@ -1100,7 +1406,7 @@ sg_status sg_learned_eval(sg_learned* L, int first, int count, double* loss) {
                 L->tt.p);
             SG_CUDA(cudaGetLastError());
             count_launch(ctx);
-            loss_grad(L, bs, false);
+            loss_grad(L, bs, false, L->loss_kind == 0, didx.p + b0);
             float l = 0.f;
             SG_CUDA(cudaMemcpyAsync(&l, L->tloss.p, sizeof(float), cudaMemcpyDeviceToHost,
                                     ctx->stream));
@@ -1155,7 +1461,7 @@ sg_status sg_learned_gradient(sg_learned* L, const float* x, const float* t, int
         SG_CUDA(cudaGetLastError());
         count_launch(ctx);
         L->tloss.zero(ctx->stream);
-        loss_grad(L, batch, true);
+        loss_grad(L, batch, true, false, nullptr);
         float l = 0.f;
         SG_CUDA(cudaMemcpyAsync(&l, L->tloss.p, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
         SG_CUDA(cudaMemcpyAsync(grad, L->grad.p, sizeof(float) * NET_PARAMS, cudaMemcpyDeviceToHost,

@@ -109,7 +109,31 @@ class LearnedCorrection:
                                            t.ctypes.data))
         return a, f, t
 
+    def sample_fine(self, i: int):
+        """(fine energy target e1 / s, its energy in A, field index) of sample i."""
+        n = self.nx * self.ny * self.nz
+        err = np.empty(n, np.float32)
+        en = np.zeros(1, np.float32)
+        fld = np.zeros(1, np.int32)
+        _check(_clib.sg_learned_get_sample_fine(self.handle, i, err.ctypes.data, en.ctypes.data,
+                                                fld.ctypes.data))
+        return err, float(en[0]), int(fld[0])
+
     # ---- training
+    LOSSES = {"energy": 0, "mse": 1}
+
+    def set_loss(self, kind: str) -> None:
+        """"energy" (default): ||e1/s - c P y||_A^2 / ||e1/s||_A^2; "mse": coarse MSE."""
+        _check(_clib.sg_learned_set_loss(self.handle, self.LOSSES[kind]))
+
+    def sample_gradient(self, first: int, count: int):
+        """(loss, parameter gradient) of stored samples [first, first+count) as one batch."""
+        g = np.empty(NUM_PARAMS - 1, np.float32)
+        loss = C.c_double(0.0)
+        _check(_clib.sg_learned_sample_gradient(self.handle, first, count, g.ctypes.data,
+                                                C.byref(loss)))
+        return loss.value, g
+
     def train(self, first: int, count: int, epochs: int, batch: int = 8, lr: float = 1e-3,
               seed: int = 0) -> np.ndarray:
         """Adam over samples [first, first+count); returns the mean batch loss

@@ -109,11 +109,48 @@ def test_training_pair_matches_oracle(sg, oracle):
     st.add_pair(M, r, e)
     assert st.num_samples == 1
     a, f, t = st.sample(0)
-    ao, fo, to = lo.training_pair(lambda x: S @ x, opc.apply, S.diagonal(), r, e, N)
+    ao, fo, to, eo, en_o = lo.training_pair(lambda x: S @ x, opc.apply, S.diagonal(), r, e, N)
     assert _rel(a, ao) <= 1e-6 and _rel(t, to) <= 1e-6
     assert np.max(np.abs(f - fo)) <= 1e-5
+    err, en, fld = st.sample_fine(0)
+    assert _rel(err, eo) <= 1e-6 and abs(en - en_o) <= 1e-5 * en_o and fld == 0
     st.clear_samples()
     assert st.num_samples == 0
+    st.close()
+
+
+def test_energy_gradient_matches_oracle(sg, oracle):
+    """Energy-norm loss gradient over stored pairs of two fields (the GPU keeps
+    one FP32 copy of each field's values) against the oracle."""
+    N = 32
+    st = sg.LearnedCorrection(N)
+    mats = []
+    rng = np.random.default_rng(51)
+    for seed in (8, 9):
+        A, M, S, _ = _problem(sg, None, N, 8, seed, fp64=True)
+        st.set_matrix(A)
+        for _ in range(2):
+            st.add_pair(M, rng.standard_normal(A.nrows), rng.standard_normal(A.nrows))
+        mats.append((A, S))
+    assert st.num_samples == 4
+    p = _he_params(52, c=3.0)
+    st.weights = p
+    st.set_loss("energy")
+    loss, g = st.sample_gradient(0, 4)
+    x2 = np.stack([np.stack(st.sample(i)[:2], axis=-1) for i in range(4)])
+    fines = [st.sample_fine(i) for i in range(4)]
+    err = np.stack([fi[0] for fi in fines]).astype(np.float64)
+    energy = [fi[1] for fi in fines]
+    assert [fi[2] for fi in fines] == [0, 0, 1, 1]
+    S32 = [S.astype(np.float32).astype(np.float64) for _A, S in mats]
+    spmvs = [S32[fi[2]].__matmul__ for fi in fines]
+    lo_loss, go = lo.energy_loss_and_grad(p.astype(np.float64), x2, err, energy, spmvs, N)
+    assert abs(loss - lo_loss) <= 2e-3 * lo_loss, (loss, lo_loss)
+    for l in range(lo.LAYERS):
+        sl = slice(l * lo.LAYER_P, (l + 1) * lo.LAYER_P)
+        assert _rel(g[sl], go[sl]) <= 2e-2, (l, _rel(g[sl], go[sl]))
+    # eval of the same samples gives the same loss
+    assert abs(st.eval(0, 4) - loss) <= 1e-3 * loss
     st.close()
 
 

@@ -135,3 +135,74 @@ def test_stage_is_positively_homogeneous():
     z1, _ = lo.stage_apply(params, spmv, apply_m, diag, v, nx)
     z2, _ = lo.stage_apply(params, spmv, apply_m, diag, 3.0 * v, nx)
     assert np.allclose(z2, 3.0 * z1, rtol=1e-6, atol=1e-12)
+
+
+def _spd_laplacian(nx, seed):
+    """7-point -div(k grad u) with random positive face coefficients (scipy CSR)."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    n = nx ** 3
+    idx = np.arange(n).reshape(nx, nx, nx)
+    rows, cols, vals = [], [], []
+    diag = np.zeros(n)
+    for axis in range(3):
+        a = np.moveaxis(idx, axis, 0)
+        i0, i1 = a[:-1].reshape(-1), a[1:].reshape(-1)
+        k = np.exp(rng.standard_normal(i0.size))
+        rows += [i0, i1]
+        cols += [i1, i0]
+        vals += [-k, -k]
+        np.add.at(diag, i0, k)
+        np.add.at(diag, i1, k)
+    diag += 1.0  # Dirichlet boundary contributions
+    rows.append(np.arange(n))
+    cols.append(np.arange(n))
+    vals.append(diag)
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                         shape=(n, n))
+
+
+def test_prolong_adjoint_and_torch_interpolate():
+    nx = 16
+    rng = np.random.default_rng(10)
+    c = rng.standard_normal((nx // 2) ** 3)
+    w = rng.standard_normal(nx ** 3)
+    assert abs(lo.prolong(c, nx) @ w - c @ lo.prolong_t(w, nx)) <= 1e-12 * np.abs(w).sum()
+    t = torch.nn.functional.interpolate(torch.tensor(c).reshape(1, 1, 8, 8, 8), scale_factor=2,
+                                        mode="trilinear", align_corners=False)
+    assert np.allclose(t.numpy().reshape(-1), lo.prolong(c, nx), atol=1e-14)
+
+
+def test_energy_gradient_matches_torch_autograd():
+    nx, D, B = 16, 8, 2
+    params = _random_params(11, 0.2)
+    rng = np.random.default_rng(12)
+    x2 = rng.standard_normal((B, D ** 3, 2))
+    mats = [_spd_laplacian(nx, 20 + b) for b in range(B)]
+    err = rng.standard_normal((B, nx ** 3))
+    energy = np.array([err[b] @ (mats[b] @ err[b]) for b in range(B)])
+    loss, g = lo.energy_loss_and_grad(params, x2, err, energy, [m.__matmul__ for m in mats], nx,
+                                      emulate_bf16=False)
+    convs = _torch_net(params)
+    y = _torch_forward(convs, x2, D)
+    c = params[lo.NET_PARAMS]
+    lt = 0.0
+    for b in range(B):
+        up = torch.nn.functional.interpolate(y[b].reshape(1, 1, D, D, D), scale_factor=2,
+                                             mode="trilinear", align_corners=False).reshape(-1)
+        u = torch.tensor(err[b]) - c * up
+        coo = mats[b].tocoo()
+        At = torch.sparse_coo_tensor(np.vstack([coo.row, coo.col]), coo.data, coo.shape)
+        lt = lt + (u @ torch.sparse.mm(At, u[:, None])[:, 0]) / (energy[b] * B)
+    lt.backward()
+    assert abs(loss - lt.item()) <= 1e-12 * abs(lt.item())
+    ref = []
+    for l, conv in enumerate(convs):
+        cin, cout = conv.weight.shape[1], conv.weight.shape[0]
+        gw = np.zeros((3, 3, 3, 16, 16))
+        gw[..., :cin, :cout] = np.transpose(conv.weight.grad.numpy(), (2, 3, 4, 1, 0))
+        gb = np.zeros(16)
+        gb[:cout] = conv.bias.grad.numpy()
+        ref.append(np.concatenate([gw.reshape(-1), gb]))
+    ref = np.concatenate(ref)
+    assert np.max(np.abs(g - ref)) <= 1e-10 * np.max(np.abs(ref))
