@@ -112,14 +112,14 @@ def local_sizes(sg, A, part, nparts, overlap):
     return out[0], out[1]
 
 
-def apply_bytes(n, n_loc, nnz_loc, nparts, w_f, w_v):
-    """Algorithmic bytes of one two-level RAS apply: ILU(0) forward+backward
+def apply_bytes(n, n_loc, nnz_loc, nparts, w_f, w_v, coarse=True):
+    """Algorithmic bytes of one (two-level) RAS apply: ILU(0) forward+backward
     sweeps (factors w_f + 4-byte index per entry, row_ptr + diag_ptr, rhs and
     solution), overlap gather/scatter, coarse restriction and prolongation."""
     ilu = nnz_loc * (w_f + 4) + 8 * n_loc + n_loc * 2 * w_v
     gather = n_loc * (4 + w_v) + n * (4 + w_v)
-    coarse = 2 * (n * (4 + w_v) + nparts * nparts * 8)
-    return ilu + gather + coarse
+    crs = 2 * (n * (4 + w_v) + nparts * nparts * 8) if coarse else 0
+    return ilu + gather + crs
 
 
 def spmv_bytes(n, nnz, w_v, w_x):
@@ -633,6 +633,217 @@ def cpu_baseline_learned(iterations):
                 "sample": f"failed: {e}"}
 
 
+# ---------------------------------------------------------------- batched workload
+B_NSYS = 512
+B_RHS = 4
+B_RESTART = 30
+B_WORKLOAD = ("aniso2d_9pt_batch512x4rhs_ras4-16_ov1_gmres30: -div(K grad u), "
+              "K = R(theta) diag(1, eps) R(theta)^T, eps ~ LogU[1e-3,1], theta ~ U[0,pi), "
+              "n x n with n ~ U{32..256}, b ~ U[-1,1]")
+
+
+def run_batched(args):
+    import torch
+
+    import schwarz_gmres_dashboard_gb300 as sg
+
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    ctx = sg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    # replicas: every rank solves its own batch (independent seeds)
+    prob = sg.make_aniso_batch(B_NSYS, seed=rank)
+    prob.A.upload(ctx)
+    n = prob.n
+
+    def precond(fp64):
+        dt = sg.FP64 if fp64 else sg.FP32
+        M = sg.RASPrecond(prob.nparts, OVERLAP, partition=prob.partition, factor_dtype=dt,
+                          sweep_dtype=dt, ctx=ctx)
+        t0 = time.time()
+        M.setup(prob.A)
+        return M, time.time() - t0
+
+    M32, setup32 = precond(False)
+    M64, setup64 = precond(True)
+    Bh = sg.uniform(B_RHS * n, seed=1000 + rank).reshape(B_RHS, n)
+    Bd = torch.from_numpy(Bh).to(f"cuda:{local}")
+    Xd = torch.zeros_like(Bd)
+    p32 = sg.GMRESParams(restart=B_RESTART, max_iter=20000, tol=RTOL, tol_kind=sg.TOL_TRUE_REL,
+                         precision=sg.FP32)
+    p64 = sg.GMRESParams(restart=B_RESTART, max_iter=20000, tol=RTOL, tol_kind=sg.TOL_TRUE_REL,
+                         precision=sg.FP64)
+
+    def solve(M, prm):
+        with torch.cuda.stream(stream):
+            Xd.zero_()
+        return sg.solve_batched(prob.A, M, prob.sys_row_ptr, B_RHS, Bd, Xd, prm)
+
+    def timed(M, prm, steps, warmup):
+        for _ in range(warmup):
+            solve(M, prm)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        l0 = ctx.launch_count
+        e0.record(stream)
+        out = [solve(M, prm) for _ in range(steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps, out[-1][0], ctx.launch_count - l0
+
+    with Clocks(local) as clk:
+        ms32, res32, launches = timed(M32, p32, args.steps, args.warmup)
+    X32 = Xd.cpu().numpy()
+    ms64, res64, _ = timed(M64, p64, max(1, min(args.steps, 2)), 1)
+    # e2e: host B and X through the C ABI
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        Xh = np.zeros_like(Bh)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        sg.solve_batched(prob.A, M32, prob.sys_row_ptr, B_RHS, Bh, Xh, p32)
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t1)
+    # kernel classes of one eager solve; algorithmic bytes counted for the
+    # work actually done (instances stop at different iterations and the
+    # kernels skip finished ones): per instance its steps x per-system bytes
+    p_eager = sg.GMRESParams(**{**p32.__dict__, "use_graph": False})
+    classes, (res_e, _t) = class_breakdown(ctx, lambda: solve(M32, p_eager))
+    peak, peak_kind = peaks()
+    n_loc, nnz_loc = local_sizes(sg, prob.A, prob.partition, prob.nparts, OVERLAP)
+    nnz = prob.A.nnz()
+    rows = np.diff(prob.sys_row_ptr).astype(np.float64)
+    nnz_sys = np.diff(prob.A.row_ptr[prob.sys_row_ptr]).astype(np.float64)
+    it_e = res_e["iterations"].reshape(B_RHS, prob.nsys).astype(np.float64)
+    cy_e = res_e["cycles"].reshape(B_RHS, prob.nsys).astype(np.float64)
+    apply_per_row = apply_bytes(n, n_loc, nnz_loc, prob.nparts, 4, 4, coarse=False) / n
+    bytes_model = {
+        "precond": ("ras apply (k_sweep_tma, FP32 factors and sweep), gated per subdomain",
+                    float(((it_e + cy_e) * rows).sum() * apply_per_row)),
+        "spmv": ("batched spmv_fp32 (k_b_spmv)",
+                 float((it_e * (nnz_sys * 8 + 4 * (rows + 1) + 2 * rows * 4)).sum())),
+        "residual": ("batched residual_fp64 (k_b_residual)",
+                     float(((cy_e + 1) * (nnz_sys * 12 + 4 * (rows + 1) + 4 * rows * 8)).sum())),
+        "ortho": ("batched cgs2 passes (k_b_dots, k_b_upd_dots, k_b_upd_norm)",
+                  float(sum(cgs2_bytes(int(rows[s]), 4, int(it_e[r, s]), B_RESTART)
+                            for r in range(B_RHS) for s in range(prob.nsys)))),
+    }
+    per = {}
+    for name, (ms, cnt) in classes.items():
+        if cnt == 0:
+            continue
+        entry = {"ms": ms, "launches": cnt, "us_per_launch": ms * 1e3 / cnt}
+        if name in bytes_model:
+            kname, byt = bytes_model[name]
+            entry.update({"kernel": kname, "algorithmic_bytes_total": byt,
+                          "achieved_gbs": byt / (ms / 1e3) / 1e9})
+            entry["frac"] = entry["achieved_gbs"] / peak
+        per[name] = entry
+    dom = max((k for k in bytes_model if k in per), key=lambda k: per[k]["ms"])
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline_batched(prob, Bh)
+    it = res32["iterations"]
+    line = {
+        "metric": "time_to_1e-8_fp64_true_residual_batch",
+        "value": ms32 / 1e3,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms32,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 preconditioner+krylov / f64 outer",
+        "data": "synthetic: seeded anisotropic diffusion problems, b ~ U[-1,1]",
+        "config": {"workload": B_WORKLOAD, "systems": B_NSYS, "rhs_per_system": B_RHS,
+                   "rows_total": n, "nnz_total": nnz, "subdomains_total": prob.nparts,
+                   "restart": B_RESTART, "rtol": RTOL, "overlap": OVERLAP,
+                   "l2": "working set > L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "solves_per_s": B_NSYS * B_RHS / (ms32 / 1e3),
+        "iterations": {"mean": float(np.mean(it)), "max": int(np.max(it)),
+                       "min": int(np.min(it))},
+        "all_converged": bool(np.all(res32["converged"] == 1)),
+        "max_true_rel_residual": float(np.max(res32["true_rel_residual"])),
+        "fp64_gpu": {"value": ms64 / 1e3, "unit": "s",
+                     "iterations_mean": float(np.mean(res64["iterations"])),
+                     "all_converged": bool(np.all(res64["converged"] == 1))},
+        "speedup_vs_fp64_gpu": ms64 / ms32,
+        "setup_s": {"fp32": setup32, "fp64": setup64},
+        "e2e": {"value": statistics.mean(e2e), "unit": "s",
+                "h2d_bytes_per_step": 2 * B_RHS * n * 8, "d2h_bytes_per_step": B_RHS * n * 8},
+        "roofline": {"kernel": per[dom]["kernel"], "bound": "hbm",
+                     "achieved": per[dom]["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": per[dom]["frac"], "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_total": per[dom]["algorithmic_bytes_total"],
+                     "ms_total": per[dom]["ms"],
+                     "timing": "CUDA events around every kernel class of one eager solve; "
+                               "bytes of the steps each instance ran"},
+        "kernels": per,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+def cpu_baseline_batched(prob, Bh, sample=8):
+    """The oracle's RAS GMRES(30) (the reference algorithm, OpenMP subdomain
+    loop) on `sample` systems of the batch, first right-hand side, FP64 true
+    residual checked every restart; scaled to the whole batch by rows x rhs."""
+    try:
+        import scipy.sparse as sp
+
+        import schwarz_gmres_dashboard_gb300 as sg
+        from oracle.oracle import Oracle
+        orc = Oracle()
+        threads = os.cpu_count() or 1
+        orc.set_threads(threads)
+        S = sp.csr_matrix((prob.A.vals, prob.A.col_idx, prob.A.row_ptr), shape=(prob.n, prob.n))
+        t_tot, rows = 0.0, 0
+        for s in range(0, prob.nsys, max(1, prob.nsys // sample))[:sample]:
+            lo, hi = int(prob.sys_row_ptr[s]), int(prob.sys_row_ptr[s + 1])
+            Ss = S[lo:hi, lo:hi].tocsr()
+            Ss.sort_indices()
+            As = sg.CSRMatrix(hi - lo, hi - lo, Ss.indptr.astype(np.int32),
+                              Ss.indices.astype(np.int32), Ss.data)
+            ps = prob.partition[lo:hi] - prob.partition[lo:hi].min()
+            b = Bh[0, lo:hi].copy()
+            bn = np.linalg.norm(b)
+            t0 = time.perf_counter()
+            pc = orc.precond("ras", As, int(ps.max()) + 1, OVERLAP, ps)
+            x = np.zeros(hi - lo)
+            for _ in range(400):
+                x = orc.gmres(As, b, x, pc, restart=B_RESTART, max_iter=B_RESTART, tol=0.0)["x"]
+                if np.linalg.norm(b - Ss @ x) / bn <= RTOL:
+                    break
+            t_tot += time.perf_counter() - t0
+            rows += hi - lo
+        scale = prob.n * Bh.shape[0] / rows
+        return {"value": t_tot * scale, "unit": "s", "cores": threads, "kind": "port",
+                "sample": f"oracle RAS GMRES(30) solves of {sample} systems (1 rhs, "
+                          f"{rows} rows, {t_tot:.2f} s incl. set-up) scaled by rows x rhs "
+                          f"to the {prob.nsys} x {Bh.shape[0]} batch"}
+    except Exception as e:
+        return {"value": None, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                "sample": f"failed: {e}"}
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(args):
     rank, world, _ = env_rank()
@@ -697,9 +908,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=128,
                     help="grid edge (128 = the benchmark workload; smaller for profiling)")
-    ap.add_argument("--workload", default="cfg3", choices=["cfg3", "learned"],
+    ap.add_argument("--workload", default="cfg3", choices=["cfg3", "learned", "batched"],
                     help="cfg3: the 128^3 two-level RAS GMRES(30) solve (default); learned: "
-                         "FGMRES(40) + learned stage on 96^3 vs plain two-level RAS")
+                         "FGMRES(40) + learned stage on 96^3 vs plain two-level RAS; batched: "
+                         "512 anisotropic 2D systems x 4 rhs in one batched GMRES(30)")
     ap.add_argument("--fields", type=int, default=200, help="learned: training fields")
     ap.add_argument("--held-out", type=int, default=20, help="learned: held-out test fields")
     ap.add_argument("--epochs", type=int, default=20, help="learned: training epochs")
@@ -715,6 +927,8 @@ def main():
         run_reference(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

@@ -202,6 +202,31 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
                    const double* b, double* x, int n, sg_mem mem,
                    const sg_solve_params* params, sg_solve_result* result);
 
+/* ---- batched solve ---------------------------------------------------- */
+/* No single reference counterpart (its benches loop over problems,
+ * bench/*.cpp).  nsys independent systems of uneven sizes stacked as one
+ * block-diagonal A (rows of system s at [sys_row_ptr[s], sys_row_ptr[s+1]),
+ * no entry outside its system's block), each with nrhs right-hand sides: b
+ * and x are [nrhs][n] (n = rows of A), host or device pointers per `mem`, x
+ * holding x0 on entry.  Every (system, rhs) pair i = rhs * nsys + s is an
+ * independent left-preconditioned GMRES(restart <= 32) with its own Krylov
+ * space and stopping test (params as sg_solve; default restart 30, tol 1e-8,
+ * SG_TOL_TRUE_REL, SG_FP32 basis, graph on).  pc (may be NULL) is set up on A
+ * with a partition whose parts each lie inside one system, so one set-up and
+ * one sweep launch serve every subdomain of every system.  results (optional,
+ * nsys*nrhs entries) receive each pair's outcome; time_s the wall time. */
+typedef struct sg_batch_result {
+    int iterations;
+    int cycles;
+    int converged;
+    int status;               /* SG_OK or SG_ERR_NONFINITE */
+    double true_rel_residual; /* FP64 ||b - A x|| / ||b|| at exit */
+} sg_batch_result;
+sg_status sg_solve_batched(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys,
+                           const int* sys_row_ptr, int nrhs, const double* b, double* x,
+                           sg_mem mem, const sg_solve_params* params, sg_batch_result* results,
+                           double* time_s);
+
 /* ---- BLAS-1 (src/core/vector.h:11-44) --------------------------------- */
 /* dot (vector.h:11-16), FP64, deterministic order (block partial sums added
  * in block order); the value is returned to the host in *result. */
@@ -328,6 +353,12 @@ sg_status sg_gen_poisson3d(int nx, int ny, int nz, int* row_ptr, int* col_idx, d
  * make_poisson_3d. */
 sg_status sg_gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr_len,
                            uint64_t seed, int* row_ptr, int* col_idx, double* vals, int* nnz);
+/* -div(K grad u) on an nx*ny grid, K = R(theta) diag(1, eps) R(theta)^T,
+ * 9-point stencil (central difference for the cross term), Dirichlet; row
+ * index iy*nx + ix, columns ascending.  Same calling convention as
+ * sg_gen_poisson2d (row_ptr == NULL: only *nnz). */
+sg_status sg_gen_aniso2d(int nx, int ny, double eps, double theta, int* row_ptr, int* col_idx,
+                         double* vals, int* nnz);
 /* n values uniform in [lo,hi): u = (SplitMix64(seed) >> 11) * 2^-53. */
 sg_status sg_gen_uniform(uint64_t seed, int n, double lo, double hi, double* out);
 /* Built-in graph partitioner used when no partition is given: recursive

@@ -35,7 +35,8 @@ __all__ = [
     "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
     "TwoLevelSchwarzPrecond", "FineLevelType", "GMRESParams", "GMRESResult", "gmres", "fgmres",
     "FP64", "FP32", "BF16", "TOL_REF_ABS", "TOL_TRUE_REL_CYCLE", "TOL_TRUE_REL",
-    "LearnedCorrection", "collect_pairs",
+    "LearnedCorrection", "collect_pairs", "make_aniso_2d", "BatchProblem", "make_aniso_batch",
+    "solve_batched",
 ]
 
 FP64, FP32, BF16 = L.FP64, L.FP32, L.BF16
@@ -244,6 +245,12 @@ def make_varcoef_3d(nx: int, ny: int, nz: int, sigma: float = 1.0, corr_len: flo
     `corr_len` cells; harmonic-mean face coefficients."""
     return _gen(_clib.sg_gen_varcoef3d, (nx, ny, nz), nx * ny * nz,
                 C.c_double(sigma), C.c_double(corr_len), C.c_uint64(seed))
+
+
+def make_aniso_2d(nx: int, ny: int, eps: float, theta: float) -> CSRMatrix:
+    """-div(K grad u), K = R(theta) diag(1, eps) R(theta)^T, 9-point stencil,
+    Dirichlet, on an nx*ny grid."""
+    return _gen(_clib.sg_gen_aniso2d, (nx, ny), nx * ny, C.c_double(eps), C.c_double(theta))
 
 
 def uniform(n: int, seed: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
@@ -566,3 +573,4 @@ def fgmres(A: CSRMatrix, b, x, M: Optional[Preconditioner] = None,
 
 
 from .learned import LearnedCorrection, collect_pairs  # noqa: E402  (uses the names above)
+from .batched import BatchProblem, make_aniso_batch, solve_batched  # noqa: E402

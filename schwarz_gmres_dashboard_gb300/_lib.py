@@ -47,6 +47,11 @@ class SolveParams(C.Structure):
                 ("reserved", C.c_int * 8)]
 
 
+class BatchResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("cycles", C.c_int), ("converged", C.c_int),
+                ("status", C.c_int), ("true_rel_residual", C.c_double)]
+
+
 class SolveResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("cycles", C.c_int), ("converged", C.c_int),
                 ("history_len", C.c_int), ("residual_norm", C.c_double),
@@ -84,6 +89,8 @@ PROTOTYPES = {
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "sg_solve": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int,
                            C.POINTER(SolveParams), C.POINTER(SolveResult)]),
+    "sg_solve_batched": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp, C.c_int,
+                                   C.POINTER(SolveParams), _vp, _dp]),
     "sg_dot": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, _dp]),
     "sg_norm2": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _dp]),
     "sg_axpy": (C.c_int, [_vp, C.c_double, _vp, _vp, C.c_int, C.c_int]),
@@ -94,6 +101,7 @@ PROTOTYPES = {
     "sg_gen_varcoef3d": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                    C.c_uint64, _vp, _vp, _vp, _ip]),
     "sg_gen_uniform": (C.c_int, [C.c_uint64, C.c_int, C.c_double, C.c_double, _vp]),
+    "sg_gen_aniso2d": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _ip]),
     "sg_partition_graph": (C.c_int, [C.c_int, _vp, _vp, C.c_int, _vp]),
     "sg_partition_boxes": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_uint64, _vp]),

@@ -37,6 +37,7 @@ int gen_poisson3d(int nx, int ny, int nz, int* rp, int* ci, double* v);
 int gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t seed, int* rp, int* ci,
                   double* v);
 void gen_uniform(uint64_t seed, int n, double lo, double hi, double* out);
+int gen_aniso2d(int nx, int ny, double eps, double theta, int* rp, int* ci, double* v);
 void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, const double* b,
                   double* x, const sg_solve_params& prm, sg_solve_result* res);
 
@@ -183,6 +184,8 @@ sg_status sg_ctx_destroy(sg_ctx* ctx) {
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
         delete ctx->work;
         ctx->work = nullptr;
+        destroy_batch_work(ctx->batch);
+        ctx->batch = nullptr;
         collect_timers(ctx);
         for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
         ctx->ev_pool.clear();
@@ -615,6 +618,44 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
     });
 }
 
+sg_status sg_solve_batched(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys,
+                           const int* sys_row_ptr, int nrhs, const double* b, double* x,
+                           sg_mem mem, const sg_solve_params* params, sg_batch_result* results,
+                           double* time_s) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && A && b && x && sys_row_ptr, "NULL argument");
+        SG_CHECK_ARG(A->ctx == ctx, "matrix belongs to a different context");
+        SG_CHECK_ARG(A->nrows == A->ncols, "the solvers need a square matrix");
+        SG_CHECK_ARG(nsys >= 1 && nrhs >= 1, "nsys and nrhs must be >= 1");
+        SG_CHECK_ARG(mem == SG_MEM_HOST || mem == SG_MEM_DEVICE, "bad memory kind");
+        SG_CHECK_ARG(sys_row_ptr[0] == 0 && sys_row_ptr[nsys] == A->nrows,
+                     "sys_row_ptr must run from 0 to the matrix rows");
+        for (int s = 0; s < nsys; ++s)
+            SG_CHECK_ARG(sys_row_ptr[s + 1] > sys_row_ptr[s], "system %d has no rows", s);
+        if (pc) {
+            SG_CHECK_ARG(pc->ctx == ctx, "preconditioner belongs to a different context");
+            if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+            SG_CHECK_ARG(pc->n == A->nrows, "preconditioner was set up for n=%d", pc->n);
+            SG_CHECK_ARG(!pc->learned, "the batched solver takes no learned stage");
+        }
+        // block-diagonal matrix and system-local subdomains: checked in
+        // solve_batched_device (once per matrix / preconditioner set-up)
+        sg_solve_params prm{};
+        if (params) prm = *params;
+        else {
+            prm.restart = 30;
+            prm.max_iter = 1000;
+            prm.tol = 1e-8;
+            prm.tol_kind = SG_TOL_TRUE_REL;
+            prm.precision = SG_FP32;
+            prm.use_graph = 1;
+        }
+        use_device(ctx);
+        // b and x are copied inside (host or device pointers alike)
+        solve_batched_device(ctx, A, pc, nsys, sys_row_ptr, nrhs, b, x, prm, results, time_s);
+    });
+}
+
 // ------------------------------------------------------------------ BLAS-1
 namespace {
 // host or device vector -> device pointer (host data staged in ctx buffers)
@@ -716,6 +757,17 @@ sg_status sg_gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr_len
         SG_CHECK_ARG(corr_len > 0.0 && sigma >= 0.0, "bad field parameters");
         SG_CHECK_ARG((long long)nx * ny * nz * 7 < (1ll << 31), "grid too large for int32 CSR");
         *nnz = gen_varcoef3d(nx, ny, nz, sigma, corr_len, seed, row_ptr, col_idx, vals);
+    });
+}
+
+sg_status sg_gen_aniso2d(int nx, int ny, double eps, double theta, int* row_ptr, int* col_idx,
+                         double* vals, int* nnz) {
+    return guard([&] {
+        SG_CHECK_ARG(nx > 0 && ny > 0 && nnz, "bad arguments");
+        SG_CHECK_ARG(eps > 0.0 && std::isfinite(eps) && std::isfinite(theta),
+                     "eps must be positive and theta finite");
+        SG_CHECK_ARG((long long)nx * ny * 9 < (1ll << 31), "grid too large for int32 CSR");
+        *nnz = gen_aniso2d(nx, ny, eps, theta, row_ptr, row_ptr ? col_idx : nullptr, vals);
     });
 }
 

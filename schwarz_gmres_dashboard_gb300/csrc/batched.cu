@@ -1,0 +1,908 @@
+// batched.cu -- many independent systems solved at once: A_s x = b_{s,r} for
+// s < S systems of uneven sizes and r < R right-hand sides each, every
+// (s, r) pair an independent restarted GMRES(m) (src/core/gmres.cpp:34-160)
+// with its own Krylov space, Givens rotations and stopping test.
+//
+// Layout.  The systems form one block-diagonal matrix A (rows of system s at
+// [row_ptr[s], row_ptr[s+1])) and the preconditioner is set up on A with a
+// partition whose parts never cross a system, so one set-up and one launch of
+// the subdomain sweeps serve every system (the sweeps of all subdomains of
+// all systems run as one batched kernel).  Vectors of the batch are laid out
+// [r][N] (N = rows of A); instance i = r * S + s owns the segment
+// [r*N + row_ptr[s], r*N + row_ptr[s+1]).
+//
+// Reductions.  Every instance is cut into chunks of at most 2048 rows, one
+// block per chunk.  A block writes its partial sums to its chunk's slot; the
+// last block of an instance to arrive (per-instance ticket) adds the chunk
+// partials in chunk order (deterministic) and updates that instance's state.
+// All instances step in lockstep through the restart cycle (one CUDA graph);
+// an instance that converges, breaks down or reaches the end of its cycle
+// clears its active flag and every later kernel of the cycle skips it.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+namespace {
+
+constexpr int BT = 256;               // threads per block
+constexpr int BRPT = 8;               // rows per thread
+constexpr int BCH = BT * BRPT;        // rows per chunk
+constexpr int BMMAX = 32;             // restart limit of the batched solver
+constexpr int BLD = BMMAX + 1;        // stride of the chunk partials
+
+struct BatchDev {
+    // instances (I = S * R)
+    const long long* ioff;  // first element of instance i
+    const int* in;          // rows
+    const int* ich0;        // first chunk
+    const int* inch;        // number of chunks
+    // chunks
+    const int* cinst;
+    const long long* coff;
+    const int* clen;
+    // per-instance state
+    int* active;     // 1 while the steps of the current cycle run
+    int* done;       // finished (converged, out of iterations or failed)
+    int* conv;
+    int* iters;
+    int* cycles;
+    int* kcount;     // basis vectors of the current cycle
+    int* ran;        // took part in the current cycle
+    int* flags;      // bit 0 non-finite, bit 1 breakdown
+    double* bnorm;
+    double* rnorm;
+    double* est;     // rnorm / beta of the cycle start
+    double* lastres;
+    double* g;       // [I][m+1]
+    double* cs;      // [I][m]
+    double* sn;
+    double* H;       // [I][(m+1) m], column-major, ld m+1
+    double* vscale;  // [I][m+1]
+    double* y;       // [I][m]
+    float* yf;       // [I][m] y_k * vscale_k in FP32 (update of an FP32 basis)
+    double* yd;      // [I][m] y_k * vscale_k in FP64
+    double* h;       // [I][m+1] coefficients of the current pass
+    double* hs;      // [I][m+1] h1 + h2
+    unsigned* ticket;
+    double* part;    // [chunks][BLD]
+    int* notdone;
+    int m, I, S, R;
+    long long N;
+    double tol;
+    int tol_kind, max_iter;
+};
+
+__device__ void b_rot_compute(double& c, double& s, double a, double b) {
+    // src/core/gmres.cpp:9-30
+    if (fabs(b) < 1e-30) {
+        c = 1.0;
+        s = 0.0;
+    } else if (fabs(b) > fabs(a)) {
+        const double t = -a / b;
+        s = 1.0 / sqrt(1.0 + t * t);
+        c = s * t;
+    } else {
+        const double t = -b / a;
+        c = 1.0 / sqrt(1.0 + t * t);
+        s = c * t;
+    }
+}
+__device__ void b_rot_apply(double c, double s, double& h1, double& h2) {
+    const double t1 = c * h1 - s * h2;
+    const double t2 = s * h1 + c * h2;
+    h1 = t1;
+    h2 = t2;
+}
+
+// Block sums of nv per-thread values (warp shuffles, then one pass over the
+// warps), then the instance-level sum by the last chunk of the instance.
+// Returns true in that last block with the totals in out[0..nv).
+__device__ bool seg_reduce(const BatchDev& B, int c, int inst, double (*red)[BLD], int nv,
+                           double* bsum, double* out) {
+    __shared__ unsigned s_t;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+        double s = 0.0;
+        for (int w = 0; w < BT / 32; ++w) s += red[w][k];
+        bsum[k] = s;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) B.part[(size_t)c * BLD + k] = bsum[k];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_t = atomicAdd(&B.ticket[inst], 1u);
+    __syncthreads();
+    if (s_t != (unsigned)B.inch[inst] - 1) return false;
+    __threadfence();
+    const int c0 = B.ich0[inst], nc = B.inch[inst];
+    for (int k = warp; k < nv; k += BT / 32) {
+        double s = 0.0;
+        for (int q = lane; q < nc; q += 32) s += __ldcg(&B.part[(size_t)(c0 + q) * BLD + k]);
+        s = warp_sum(s);
+        if (lane == 0) out[k] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) B.ticket[inst] = 0u;
+    return true;
+}
+
+// ---- FP64 residual r = b - A x per instance (mode 1), or ||b|| (mode 0);
+// the last block of an instance runs the restart test.
+template <int MODE>
+__global__ void __launch_bounds__(BT)
+k_b_residual(BatchDev B, const int* __restrict__ rp, const int* __restrict__ ci,
+             const double* __restrict__ val, const double* __restrict__ b,
+             const double* __restrict__ x, double* __restrict__ r) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (MODE == 1 && B.done[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[1], tot[1];
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    const int rr = inst / B.S;
+    const long long base = (long long)rr * B.N;
+    double ss = 0.0;
+    for (int q = threadIdx.x; q < len; q += BT) {
+        const long long e = off + q;
+        double v = b[e];
+        if (MODE == 1) {
+            const long long mr = e - base;
+            double ax = 0.0;
+            for (int k = rp[mr]; k < rp[mr + 1]; ++k) ax = fma(val[k], x[base + ci[k]], ax);
+            v = v - ax;
+            r[e] = v;
+        }
+        ss += v * v;
+    }
+    ss = warp_sum(ss);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][0] = ss;
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, 1, bsum, tot) || threadIdx.x != 0) return;
+    const double rn = sqrt(tot[0]);
+    if (MODE == 0) {
+        B.bnorm[inst] = rn;
+        if (!isfinite(rn)) {
+            B.flags[inst] |= 1;
+            B.done[inst] = 1;
+        }
+        return;
+    }
+    B.rnorm[inst] = rn;
+    B.kcount[inst] = 0;
+    if (!isfinite(rn)) {
+        B.flags[inst] |= 1;
+        B.done[inst] = 1;
+    } else if (B.tol_kind != SG_TOL_REF_ABS && rn <= B.tol * B.bnorm[inst]) {
+        B.conv[inst] = 1;
+        B.done[inst] = 1;
+    }
+    B.active[inst] = B.done[inst] ? 0 : 1;
+}
+
+// ---- cycle start: beta = ||raw_0|| per instance, g = beta e1, vscale_0 = 1/beta
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_cycle_init(BatchDev B, const TV* __restrict__ raw0) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (!B.active[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[1], tot[1];
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    TV ssv = (TV)0;
+    for (int q = threadIdx.x; q < len; q += BT) {
+        const TV t = raw0[off + q];
+        ssv += t * t;
+    }
+    const double ss = warp_sum((double)ssv);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][0] = ss;
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, 1, bsum, tot)) return;
+    const int m = B.m, ld = m + 1;
+    for (int i = threadIdx.x; i < ld * m; i += BT) B.H[(size_t)inst * ld * m + i] = 0.0;
+    for (int i = threadIdx.x; i <= m; i += BT) B.g[(size_t)inst * ld + i] = 0.0;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double beta = sqrt(tot[0]);
+    B.kcount[inst] = 0;
+    B.ran[inst] = 1;
+    B.flags[inst] &= ~2;
+    if (!isfinite(beta)) {
+        B.flags[inst] |= 1;
+        B.done[inst] = 1;
+        B.active[inst] = 0;
+        return;
+    }
+    if (B.tol_kind == SG_TOL_REF_ABS && beta < B.tol) {
+        B.conv[inst] = 1;
+        B.done[inst] = 1;
+        B.active[inst] = 0;
+        return;
+    }
+    if (!(beta > 0.0)) {
+        B.done[inst] = 1;
+        B.active[inst] = 0;
+        return;
+    }
+    B.vscale[(size_t)inst * ld] = 1.0 / beta;
+    B.g[(size_t)inst * ld] = beta;
+    B.est[inst] = B.rnorm[inst] / beta;
+}
+
+// ---- y = vscale_j * (A x) for the active instances (FP32 or FP64 basis)
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_spmv(BatchDev B, const int* __restrict__ rp, const int* __restrict__ ci,
+         const TV* __restrict__ val, const int* __restrict__ row_sys, const TV* __restrict__ x,
+         TV* __restrict__ y, int j) {
+    const long long total = B.N * B.R;
+    const int ld = B.m + 1;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int rr = (int)(q / B.N);
+        const long long mr = q - (long long)rr * B.N;
+        const int inst = rr * B.S + row_sys[mr];
+        if (!B.active[inst]) continue;
+        const TV* xb = x + (long long)rr * B.N;
+        TV acc = (TV)0;
+        for (int k = rp[mr]; k < rp[mr + 1]; ++k) acc += val[k] * xb[ci[k]];
+        y[q] = (TV)((double)acc * B.vscale[(size_t)inst * ld + j]);
+    }
+}
+
+// ---- CGS2 pass A: h1_k = vscale_k (raw_k . w), k <= j
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_dots(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (!B.active[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[BLD], tot[BLD];
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    const TV* w = V + (size_t)(j + 1) * ldv + off;
+    // per-thread products and sums in the basis precision (FP64 arithmetic
+    // is scarce on this GPU), warp and block sums in FP64
+    TV wv[BRPT];
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        wv[q] = row < len ? w[row] : (TV)0;
+    }
+    for (int k = 0; k <= j; ++k) {
+        const TV* vk = V + (size_t)k * ldv + off;
+        TV acc = (TV)0;
+#pragma unroll
+        for (int q = 0; q < BRPT; ++q) {
+            const int row = threadIdx.x + q * BT;
+            if (row < len) acc += vk[row] * wv[q];
+        }
+        const double a = warp_sum((double)acc);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = a;
+    }
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, j + 1, bsum, tot)) return;
+    const int ld = B.m + 1;
+    for (int k = threadIdx.x; k <= j; k += BT)
+        B.h[(size_t)inst * ld + k] = B.vscale[(size_t)inst * ld + k] * tot[k];
+}
+
+// ---- CGS2 pass B: w' = w - sum_k h1_k v_k ; h2_k = vscale_k (raw_k . w');
+// hs = h1 + h2, h = h2
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_upd_dots(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (!B.active[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[BLD], tot[BLD];
+    __shared__ TV cf[BLD];
+    const int ld = B.m + 1;
+    for (int k = threadIdx.x; k <= j; k += BT)
+        cf[k] = (TV)(B.h[(size_t)inst * ld + k] * B.vscale[(size_t)inst * ld + k]);
+    __syncthreads();
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    TV* w = V + (size_t)(j + 1) * ldv + off;
+    TV wv[BRPT];
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        wv[q] = row < len ? w[row] : (TV)0;
+    }
+    for (int k = 0; k <= j; ++k) {
+        const TV* vk = V + (size_t)k * ldv + off;
+        const TV ck = cf[k];
+#pragma unroll
+        for (int q = 0; q < BRPT; ++q) {
+            const int row = threadIdx.x + q * BT;
+            if (row < len) wv[q] -= ck * vk[row];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        if (row < len) w[row] = wv[q];
+    }
+    for (int k = 0; k <= j; ++k) {
+        const TV* vk = V + (size_t)k * ldv + off;
+        TV acc = (TV)0;
+#pragma unroll
+        for (int q = 0; q < BRPT; ++q) {
+            const int row = threadIdx.x + q * BT;
+            if (row < len) acc += vk[row] * wv[q];
+        }
+        const double a = warp_sum((double)acc);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = a;
+    }
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, j + 1, bsum, tot)) return;
+    for (int k = threadIdx.x; k <= j; k += BT) {
+        const double h2 = B.vscale[(size_t)inst * ld + k] * tot[k];
+        B.hs[(size_t)inst * ld + k] = B.h[(size_t)inst * ld + k] + h2;
+        B.h[(size_t)inst * ld + k] = h2;
+    }
+}
+
+// ---- CGS2 pass C: w'' = w' - sum_k h2_k v_k, ||w''||, then the instance's
+// Hessenberg column, Givens rotations and stopping test
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (!B.active[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[1], tot[1];
+    __shared__ TV cf[BLD];
+    const int m = B.m, ld = m + 1;
+    for (int k = threadIdx.x; k <= j; k += BT)
+        cf[k] = (TV)(B.h[(size_t)inst * ld + k] * B.vscale[(size_t)inst * ld + k]);
+    __syncthreads();
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    TV* w = V + (size_t)(j + 1) * ldv + off;
+    TV wv[BRPT];
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        wv[q] = row < len ? w[row] : (TV)0;
+    }
+    for (int k = 0; k <= j; ++k) {
+        const TV* vk = V + (size_t)k * ldv + off;
+        const TV ck = cf[k];
+#pragma unroll
+        for (int q = 0; q < BRPT; ++q) {
+            const int row = threadIdx.x + q * BT;
+            if (row < len) wv[q] -= ck * vk[row];
+        }
+    }
+    TV ssv = (TV)0;
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        if (row < len) {
+            w[row] = wv[q];
+            ssv += wv[q] * wv[q];
+        }
+    }
+    double ss = warp_sum((double)ssv);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][0] = ss;
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, 1, bsum, tot) || threadIdx.x != 0) return;
+    // Arnoldi step j of this instance (as the single-system solver)
+    const double nrm = sqrt(tot[0]);
+    double* Hc = B.H + (size_t)inst * ld * m + (size_t)j * ld;
+    double* g = B.g + (size_t)inst * ld;
+    double* cs = B.cs + (size_t)inst * m;
+    double* sn = B.sn + (size_t)inst * m;
+    for (int i = 0; i <= j; ++i) Hc[i] = B.hs[(size_t)inst * ld + i];
+    Hc[j + 1] = nrm;
+    if (!(nrm >= 1e-30)) {
+        if (!isfinite(nrm)) {
+            B.flags[inst] |= 1;
+            B.done[inst] = 1;
+        }
+        B.flags[inst] |= 2;
+        B.kcount[inst] = j + 1;
+        B.active[inst] = 0;
+        return;
+    }
+    B.vscale[(size_t)inst * ld + j + 1] = 1.0 / nrm;
+    for (int i = 0; i < j; ++i) b_rot_apply(cs[i], sn[i], Hc[i], Hc[i + 1]);
+    b_rot_compute(cs[j], sn[j], Hc[j], Hc[j + 1]);
+    b_rot_apply(cs[j], sn[j], Hc[j], Hc[j + 1]);
+    b_rot_apply(cs[j], sn[j], g[j], g[j + 1]);
+    const double res = fabs(g[j + 1]);
+    B.lastres[inst] = res;
+    B.iters[inst] += 1;
+    B.kcount[inst] = j + 1;
+    bool stop = false;
+    if (B.tol_kind == SG_TOL_REF_ABS) {
+        if (res < B.tol) {
+            B.conv[inst] = 1;
+            B.done[inst] = 1;
+            stop = true;
+        }
+    } else if (B.tol_kind == SG_TOL_TRUE_REL) {
+        if (res * B.est[inst] <= 0.5 * B.tol * B.bnorm[inst]) stop = true;
+    }
+    if (!isfinite(res)) {
+        B.flags[inst] |= 1;
+        B.done[inst] = 1;
+        stop = true;
+    }
+    if (j + 1 >= m) stop = true;
+    if (stop) B.active[inst] = 0;
+}
+
+// ---- y = H^{-1} g per instance (src/core/gmres.cpp:131-137)
+__global__ void k_b_backsolve(BatchDev B) {
+    const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= B.I || !B.ran[inst]) return;
+    const int k = B.kcount[inst];
+    const int m = B.m, ld = m + 1;
+    const double* H = B.H + (size_t)inst * ld * m;
+    const double* g = B.g + (size_t)inst * ld;
+    double* y = B.y + (size_t)inst * m;
+    for (int i = k - 1; i >= 0; --i) {
+        double yi = g[i];
+        for (int l = i + 1; l < k; ++l) yi -= H[i + l * ld] * y[l];
+        y[i] = yi / H[i + i * ld];
+    }
+    // coefficients of the update x += sum_k (y_k vscale_k) raw_k
+    const double* vs = B.vscale + (size_t)inst * ld;
+    for (int i = 0; i < k; ++i) {
+        const double c = y[i] * vs[i];
+        B.yd[(size_t)inst * m + i] = c;
+        B.yf[(size_t)inst * m + i] = (float)c;
+    }
+}
+
+template <class TV>
+__device__ __forceinline__ const TV* ycoef(const BatchDev& B);
+template <>
+__device__ __forceinline__ const float* ycoef<float>(const BatchDev& B) { return B.yf; }
+template <>
+__device__ __forceinline__ const double* ycoef<double>(const BatchDev& B) { return B.yd; }
+
+// ---- x += sum_k y_k vscale_k raw_k (correction in the basis precision)
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_update_x(BatchDev B, const TV* __restrict__ V, size_t ldv, const int* __restrict__ row_sys,
+             double* __restrict__ x) {
+    const long long total = B.N * B.R;
+    const int m = B.m;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int rr = (int)(q / B.N);
+        const int inst = rr * B.S + row_sys[q - (long long)rr * B.N];
+        if (!B.ran[inst]) continue;
+        const int k = B.kcount[inst];
+        const TV* cf = ycoef<TV>(B) + (size_t)inst * m;
+        TV d = (TV)0;
+        for (int i = 0; i < k; ++i) d += cf[i] * V[(size_t)i * ldv + q];
+        x[q] += (double)d;
+    }
+}
+
+// ---- per-subdomain switches of the next applies: subdomain p of the
+// preconditioner is swept for rhs r only while instance r*S + psys[p] is active
+__global__ void k_b_subon(BatchDev B, const int* __restrict__ psys, int P, int* __restrict__ on) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P * B.R) return;
+    const int rr = q / P, p = q - rr * P;
+    on[q] = B.active[rr * B.S + psys[p]];
+}
+
+// ---- restart bookkeeping per instance; counts the unfinished instances
+__global__ void k_b_cycle_end(BatchDev B) {
+    const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= B.I) return;
+    if (B.ran[inst]) {
+        B.cycles[inst] += 1;
+        B.ran[inst] = 0;
+    }
+    if (!B.done[inst] && B.iters[inst] >= B.max_iter) B.done[inst] = 1;
+    B.active[inst] = B.done[inst] ? 0 : 1;
+    if (!B.done[inst]) atomicAdd(B.notdone, 1);
+}
+
+int bgrid(sg_ctx* ctx, long long n) {
+    const long long need = (n + BT - 1) / BT;
+    const long long cap = (long long)ctx->num_sms * 8;
+    return (int)std::max<long long>(1, std::min(need, cap));
+}
+
+template <class T>
+void dalloc(DBuf<T>& b, size_t n) {
+    if (b.n < n) b.alloc(n);
+}
+
+}  // namespace
+
+struct BatchWork {
+    DBuf<long long> ioff, coff;
+    DBuf<int> in, ich0, inch, cinst, clen, row_sys;
+    DBuf<int> active, done, conv, iters, cycles, kcount, ran, flags, notdone;
+    DBuf<double> bnorm, rnorm, est, lastres, g, cs, sn, H, vscale, y, yd, h, hs, part;
+    DBuf<float> yf;
+    DBuf<unsigned> ticket;
+    DBuf<double> b64, x64, r64;
+    DBuf<float> V32, t32;
+    DBuf<double> V64, t64;
+    int* h_notdone = nullptr;
+    // what the instance/chunk tables and the checks were made for
+    const sg_csr* key_A = nullptr;
+    long long key_nnz = -1;
+    int key_nrhs = -1;
+    std::vector<int> key_rows;
+    const sg_precond* key_pc = nullptr;
+    uint64_t key_pc_structure = 0;
+    int nchunks = 0;
+    // subdomain -> system of key_pc, and the per-rhs subdomain switches
+    DBuf<int> psys, sub_on;
+    int psys_parts = 0;
+    ~BatchWork() {
+        if (h_notdone) cudaFreeHost(h_notdone);
+    }
+};
+
+void destroy_batch_work(BatchWork* w) { delete w; }
+
+namespace {
+
+template <class TV>
+struct BBasis;
+template <>
+struct BBasis<float> {
+    static DBuf<float>& V(BatchWork* w) { return w->V32; }
+    static DBuf<float>& T(BatchWork* w) { return w->t32; }
+    static const float* vals(const sg_csr* A) { return A->val32.p; }
+};
+template <>
+struct BBasis<double> {
+    static DBuf<double>& V(BatchWork* w) { return w->V64; }
+    static DBuf<double>& T(BatchWork* w) { return w->t64; }
+    static const double* vals(const sg_csr* A) { return A->val.p; }
+};
+
+template <class TV>
+void apply_pc_batched(sg_ctx* ctx, sg_precond* pc, const BatchDev& B, BatchWork* w,
+                      const double* r64, TV* out, bool first, const TV* tin) {
+    const long long N = B.N;
+    // sweep only the subdomains of instances still running
+    const bool gate = pc && w->key_pc == pc && w->psys_parts == pc->nparts && pc->nparts > 1;
+    if (gate) {
+        const int q = pc->nparts * B.R;
+        k_b_subon<<<(q + 255) / 256, 256, 0, ctx->stream>>>(B, w->psys.p, pc->nparts,
+                                                            w->sub_on.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+    }
+    struct Reset {
+        sg_precond* pc;
+        ~Reset() {
+            if (pc) pc->sub_on = nullptr;
+        }
+    } reset{pc};
+    for (int rr = 0; rr < B.R; ++rr) {
+        if (gate) pc->sub_on = w->sub_on.p + (size_t)rr * pc->nparts;
+        if (first) {
+            if (pc && pc->kind != SG_PC_NONE)
+                precond_apply_device<double, TV>(pc, r64 + rr * N, out + rr * N, nullptr, false);
+            else
+                launch_copy<double, TV>(ctx, r64 + rr * N, out + rr * N, (int)N, nullptr);
+        } else {
+            if (pc && pc->kind != SG_PC_NONE)
+                precond_apply_device<TV, TV>(pc, tin + rr * N, out + rr * N, nullptr, false);
+            else
+                launch_copy<TV, TV>(ctx, tin + rr * N, out + rr * N, (int)N, nullptr);
+        }
+    }
+}
+
+template <class TV>
+void enqueue_batch_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const BatchDev& B,
+                         BatchWork* w, int nchunks, size_t ldv) {
+    cudaStream_t st = ctx->stream;
+    TV* V = BBasis<TV>::V(w).p;
+    TV* t = BBasis<TV>::T(w).p;
+    const TV* val = BBasis<TV>::vals(A);
+    const long long total = B.N * B.R;
+    SG_CUDA(cudaMemsetAsync(B.notdone, 0, sizeof(int), st));
+    {
+        ClassTimer tm(ctx, TK_PRECOND);
+        apply_pc_batched<TV>(ctx, pc, B, w, w->r64.p, V, true, nullptr);
+    }
+    {
+        ClassTimer tm(ctx, TK_ORTHO);
+        k_b_cycle_init<TV><<<nchunks, BT, 0, st>>>(B, V);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+    }
+    for (int j = 0; j < B.m; ++j) {
+        {
+            ClassTimer tm(ctx, TK_SPMV);
+            k_b_spmv<TV><<<bgrid(ctx, total), BT, 0, st>>>(B, A->rp.p, A->ci.p, val, w->row_sys.p,
+                                                           V + (size_t)j * ldv, t, j);
+            SG_CUDA(cudaGetLastError());
+            count_launch(ctx);
+        }
+        {
+            ClassTimer tm(ctx, TK_PRECOND);
+            apply_pc_batched<TV>(ctx, pc, B, w, nullptr, V + (size_t)(j + 1) * ldv, false, t);
+        }
+        ClassTimer tm(ctx, TK_ORTHO);
+        k_b_dots<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
+        SG_CUDA(cudaGetLastError());
+        k_b_upd_dots<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
+        SG_CUDA(cudaGetLastError());
+        k_b_upd_norm<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        count_launch(ctx);
+        count_launch(ctx);
+    }
+    {
+        ClassTimer tm(ctx, TK_UPDATE);
+        k_b_backsolve<<<(B.I + 127) / 128, 128, 0, st>>>(B);
+        SG_CUDA(cudaGetLastError());
+        k_b_update_x<TV><<<bgrid(ctx, total), BT, 0, st>>>(B, V, ldv, w->row_sys.p, w->x64.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        count_launch(ctx);
+    }
+    {
+        ClassTimer tm(ctx, TK_RESIDUAL);
+        k_b_residual<1><<<nchunks, BT, 0, st>>>(B, A->rp.p, A->ci.p, A->val.p, w->b64.p, w->x64.p,
+                                                w->r64.p);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+    }
+    k_b_cycle_end<<<(B.I + 127) / 128, 128, 0, st>>>(B);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
+
+}  // namespace
+
+void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys,
+                          const int* sys_row_ptr, int nrhs, const double* b, double* x,
+                          const sg_solve_params& prm, sg_batch_result* results, double* time_s) {
+    const long long N = A->nrows;
+    const int m = prm.restart;
+    SG_CHECK_ARG(m >= 1 && m <= BMMAX, "batched restart must be in [1,%d] (got %d)", BMMAX, m);
+    SG_CHECK_ARG(prm.max_iter >= 0, "max_iter must be >= 0");
+    SG_CHECK_ARG(prm.precision == SG_FP64 || prm.precision == SG_FP32,
+                 "solve precision must be SG_FP64 or SG_FP32");
+    SG_CHECK_ARG(prm.tol_kind >= SG_TOL_REF_ABS && prm.tol_kind <= SG_TOL_TRUE_REL,
+                 "unknown tol_kind %d", prm.tol_kind);
+    SG_CHECK_ARG((long long)nrhs * N < (1ll << 31), "batch too large (nrhs * rows >= 2^31)");
+    const bool fp32 = prm.precision == SG_FP32;
+    const int S = nsys, R = nrhs, I = S * R;
+    if (!ctx->batch) ctx->batch = new BatchWork();
+    BatchWork* w = ctx->batch;
+    cudaStream_t st = ctx->stream;
+    const std::vector<int> rows(sys_row_ptr, sys_row_ptr + S + 1);
+    const bool same_tables =
+        w->key_A == A && w->key_nnz == A->nnz && w->key_nrhs == R && w->key_rows == rows;
+    if (!same_tables) {
+        w->key_A = nullptr;
+        w->key_pc = nullptr;
+        // the matrix must be block diagonal over the systems
+        for (int s = 0; s < S; ++s)
+            for (int i = sys_row_ptr[s]; i < sys_row_ptr[s + 1]; ++i)
+                for (int q = A->h_rp[i]; q < A->h_rp[i + 1]; ++q)
+                    SG_CHECK_ARG(A->h_ci[q] >= sys_row_ptr[s] && A->h_ci[q] < sys_row_ptr[s + 1],
+                                 "row %d couples system %d to column %d outside it", i, s,
+                                 A->h_ci[q]);
+        // ---- host tables: instances and chunks
+        std::vector<int> row_sys((size_t)N);
+        for (int s = 0; s < S; ++s)
+            for (int i = sys_row_ptr[s]; i < sys_row_ptr[s + 1]; ++i) row_sys[i] = s;
+        std::vector<long long> ioff(I), coff;
+        std::vector<int> in(I), ich0(I), inch(I), cinst, clen;
+        for (int rr = 0; rr < R; ++rr)
+            for (int s = 0; s < S; ++s) {
+                const int i = rr * S + s;
+                const int n = sys_row_ptr[s + 1] - sys_row_ptr[s];
+                ioff[i] = (long long)rr * N + sys_row_ptr[s];
+                in[i] = n;
+                ich0[i] = (int)cinst.size();
+                for (int q = 0; q < n; q += BCH) {
+                    cinst.push_back(i);
+                    coff.push_back(ioff[i] + q);
+                    clen.push_back(std::min(BCH, n - q));
+                }
+                inch[i] = (int)cinst.size() - ich0[i];
+            }
+        w->ioff.upload(ioff, st);
+        w->in.upload(in, st);
+        w->ich0.upload(ich0, st);
+        w->inch.upload(inch, st);
+        w->cinst.upload(cinst, st);
+        w->coff.upload(coff, st);
+        w->clen.upload(clen, st);
+        w->row_sys.upload(row_sys, st);
+        SG_CUDA(cudaStreamSynchronize(st));
+        w->nchunks = (int)cinst.size();
+        w->key_A = A;
+        w->key_nnz = A->nnz;
+        w->key_nrhs = R;
+        w->key_rows = rows;
+    }
+    // every subdomain inside one system (checked once per set-up)
+    if (pc && !(w->key_pc == pc && w->key_pc_structure == pc->structure_key) &&
+        !pc->part.empty() && pc->nparts > 1) {
+        w->key_pc = nullptr;
+        std::vector<int> psys(pc->nparts, -1);
+        for (int s = 0; s < S; ++s)
+            for (int i = sys_row_ptr[s]; i < sys_row_ptr[s + 1]; ++i) {
+                int& ps = psys[pc->part[i]];
+                SG_CHECK_ARG(ps < 0 || ps == s, "subdomain %d spans systems %d and %d",
+                             pc->part[i], ps, s);
+                ps = s;
+            }
+        w->psys.upload(psys, st);
+        w->psys_parts = pc->nparts;
+        w->key_pc = pc;
+        w->key_pc_structure = pc->structure_key;
+    }
+    if (pc && w->key_pc == pc) dalloc(w->sub_on, (size_t)pc->nparts * R);
+    const int nchunks = w->nchunks;
+    const size_t ld = (size_t)m + 1;
+    for (DBuf<int>* p : {&w->active, &w->done, &w->conv, &w->iters, &w->cycles, &w->kcount,
+                         &w->ran, &w->flags}) {
+        dalloc(*p, (size_t)I);
+        p->zero(st);
+    }
+    dalloc(w->notdone, 1);
+    for (DBuf<double>* p : {&w->bnorm, &w->rnorm, &w->est, &w->lastres}) dalloc(*p, (size_t)I);
+    dalloc(w->g, I * ld);
+    dalloc(w->cs, (size_t)I * m);
+    dalloc(w->sn, (size_t)I * m);
+    dalloc(w->H, I * ld * m);
+    dalloc(w->vscale, I * ld);
+    dalloc(w->y, (size_t)I * m);
+    dalloc(w->yd, (size_t)I * m);
+    dalloc(w->yf, (size_t)I * m);
+    dalloc(w->h, I * ld);
+    dalloc(w->hs, I * ld);
+    dalloc(w->part, (size_t)nchunks * BLD);
+    dalloc(w->ticket, (size_t)I);
+    w->ticket.zero(st);
+    const size_t tot = (size_t)N * R;
+    const size_t ldv = ((tot + 31) & ~(size_t)31) + 32;
+    dalloc(w->r64, tot);
+    if (fp32) {
+        const_cast<sg_csr*>(A)->ensure_fp32();
+        if (w->V32.n < ldv * (m + 1)) {
+            w->V32.alloc(ldv * (m + 1));
+            w->V32.zero(st);
+        }
+        if (w->t32.n < ldv) {
+            w->t32.alloc(ldv);
+            w->t32.zero(st);
+        }
+    } else {
+        if (w->V64.n < ldv * (m + 1)) {
+            w->V64.alloc(ldv * (m + 1));
+            w->V64.zero(st);
+        }
+        if (w->t64.n < ldv) {
+            w->t64.alloc(ldv);
+            w->t64.zero(st);
+        }
+    }
+    if (!w->h_notdone) SG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&w->h_notdone), sizeof(int)));
+    BatchDev B{};
+    B.ioff = w->ioff.p; B.in = w->in.p; B.ich0 = w->ich0.p; B.inch = w->inch.p;
+    B.cinst = w->cinst.p; B.coff = w->coff.p; B.clen = w->clen.p;
+    B.active = w->active.p; B.done = w->done.p; B.conv = w->conv.p; B.iters = w->iters.p;
+    B.cycles = w->cycles.p; B.kcount = w->kcount.p; B.ran = w->ran.p; B.flags = w->flags.p;
+    B.bnorm = w->bnorm.p; B.rnorm = w->rnorm.p; B.est = w->est.p; B.lastres = w->lastres.p;
+    B.g = w->g.p; B.cs = w->cs.p; B.sn = w->sn.p; B.H = w->H.p; B.vscale = w->vscale.p;
+    B.y = w->y.p; B.yd = w->yd.p; B.yf = w->yf.p; B.h = w->h.p; B.hs = w->hs.p; B.ticket = w->ticket.p; B.part = w->part.p;
+    B.notdone = w->notdone.p;
+    B.m = m; B.I = I; B.S = S; B.R = R; B.N = N;
+    B.tol = prm.tol; B.tol_kind = prm.tol_kind; B.max_iter = prm.max_iter;
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    // b and x (device copies in the batch layout)
+    if (w->b64.n < tot) w->b64.alloc(tot);
+    if (w->x64.n < tot) w->x64.alloc(tot);
+    SG_CUDA(cudaMemcpyAsync(w->b64.p, b, sizeof(double) * tot, cudaMemcpyDefault, st));
+    SG_CUDA(cudaMemcpyAsync(w->x64.p, x, sizeof(double) * tot, cudaMemcpyDefault, st));
+    k_b_residual<0><<<nchunks, BT, 0, st>>>(B, A->rp.p, A->ci.p, A->val.p, w->b64.p, w->x64.p,
+                                            w->r64.p);
+    SG_CUDA(cudaGetLastError());
+    k_b_residual<1><<<nchunks, BT, 0, st>>>(B, A->rp.p, A->ci.p, A->val.p, w->b64.p, w->x64.p,
+                                            w->r64.p);
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    count_launch(ctx);
+    const bool use_graph = prm.use_graph != 0 && prm.max_iter > 0;
+    cudaGraphExec_t exec = nullptr;
+    if (use_graph) {
+        cudaGraph_t gph = nullptr;
+        SG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+        ctx->capturing = true;
+        ctx->captured = 0;
+        try {
+            if (fp32) enqueue_batch_cycle<float>(ctx, A, pc, B, w, nchunks, ldv);
+            else enqueue_batch_cycle<double>(ctx, A, pc, B, w, nchunks, ldv);
+        } catch (...) {
+            ctx->capturing = false;
+            cudaStreamEndCapture(st, &gph);
+            if (gph) cudaGraphDestroy(gph);
+            throw;
+        }
+        ctx->capturing = false;
+        SG_CUDA(cudaStreamEndCapture(st, &gph));
+        const cudaError_t e = cudaGraphInstantiate(&exec, gph, 0);
+        cudaGraphDestroy(gph);
+        SG_CUDA(e);
+    }
+    const int max_cycles = prm.max_iter > 0 ? (prm.max_iter + m - 1) / m + 1 : 0;
+    try {
+        for (int cyc = 0; cyc < max_cycles; ++cyc) {
+            if (use_graph) {
+                SG_CUDA(cudaGraphLaunch(exec, st));
+                ctx->launches += ctx->captured;
+            } else if (fp32) {
+                enqueue_batch_cycle<float>(ctx, A, pc, B, w, nchunks, ldv);
+            } else {
+                enqueue_batch_cycle<double>(ctx, A, pc, B, w, nchunks, ldv);
+            }
+            SG_CUDA(cudaMemcpyAsync(w->h_notdone, w->notdone.p, sizeof(int),
+                                    cudaMemcpyDeviceToHost, st));
+            SG_CUDA(cudaStreamSynchronize(st));
+            if (ctx->timing) collect_timers(ctx);
+            if (*w->h_notdone == 0) break;
+        }
+    } catch (...) {
+        if (exec) cudaGraphExecDestroy(exec);
+        throw;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    SG_CUDA(cudaMemcpyAsync(x, w->x64.p, sizeof(double) * tot, cudaMemcpyDefault, st));
+    std::vector<int> h_iters(I), h_cycles(I), h_conv(I), h_flags(I);
+    std::vector<double> h_rn(I), h_bn(I);
+    SG_CUDA(cudaMemcpyAsync(h_iters.data(), w->iters.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaMemcpyAsync(h_cycles.data(), w->cycles.p, sizeof(int) * I, cudaMemcpyDeviceToHost,
+                            st));
+    SG_CUDA(cudaMemcpyAsync(h_conv.data(), w->conv.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaMemcpyAsync(h_flags.data(), w->flags.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaMemcpyAsync(h_rn.data(), w->rnorm.p, sizeof(double) * I, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaMemcpyAsync(h_bn.data(), w->bnorm.p, sizeof(double) * I, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    const auto t1 = std::chrono::high_resolution_clock::now();
+    if (time_s) *time_s = std::chrono::duration<double>(t1 - t0).count();
+    bool nonfinite = false;
+    for (int i = 0; i < I; ++i) {
+        if (h_flags[i] & 1) nonfinite = true;
+        if (!results) continue;
+        results[i].iterations = h_iters[i];
+        results[i].cycles = h_cycles[i];
+        results[i].converged = h_conv[i];
+        results[i].status = (h_flags[i] & 1) ? SG_ERR_NONFINITE : SG_OK;
+        results[i].true_rel_residual = h_bn[i] > 0 ? h_rn[i] / h_bn[i] : h_rn[i];
+    }
+    if (pc && sweep_error(pc))
+        fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+    if (nonfinite)
+        fail(SG_ERR_NONFINITE, "non-finite value in a right-hand side or iteration of the batch");
+}
+
+}  // namespace sg

@@ -79,6 +79,14 @@ void learned_begin(sg_learned* L, SolveState* st);
 void learned_monitor(sg_learned* L, SolveState* st);
 void learned_detach(sg_learned* L);
 
+// ---------------------------------------------------------------- batched.cu
+// nsys independent systems (block-diagonal A, rows of system s at
+// [sys_row_ptr[s], sys_row_ptr[s+1])) x nrhs right-hand sides in the layout
+// [rhs][rows]; b and x may be host or device pointers
+void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys,
+                          const int* sys_row_ptr, int nrhs, const double* b, double* x,
+                          const sg_solve_params& prm, sg_batch_result* results, double* time_s);
+
 // copy the FP64 factors of subdomain s back to the host
 void precond_read_factors(sg_precond* pc, int s, double* lu_out);
 void precond_read_coarse(sg_precond* pc, double* a0_out);

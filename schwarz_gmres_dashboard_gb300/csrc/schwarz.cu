@@ -308,12 +308,14 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
         const TF* __restrict__ udiag, const int* __restrict__ ownloc,
         const int* __restrict__ owned_glob, const TI* __restrict__ x, TO* __restrict__ y,
         int mode, int coarse, const double* __restrict__ a0inv, const double* __restrict__ r0,
-        int nc, TS* gscratch, int use_smem, const int* __restrict__ active) {
+        int nc, TS* gscratch, int use_smem, const int* __restrict__ active,
+        const int* __restrict__ sub_on) {
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double s_red[SWEEP_T / 32];
     __shared__ double s_zc;
     const int s = order[blockIdx.x];
+    if (sub_on && !sub_on[s]) return;  // subdomain not needed by this apply
     const SubInfo inf = info[s];
     const int n = inf.n;
     TS* t = use_smem ? reinterpret_cast<TS*>(smraw) : gscratch + inf.row_off + s;
@@ -461,12 +463,13 @@ k_sweep_sf(const SubInfo* __restrict__ info, const int* __restrict__ order,
            const int* __restrict__ ownloc, const int* __restrict__ owned_glob,
            const TI* __restrict__ x, TO* __restrict__ y, int mode, int coarse,
            const double* __restrict__ a0inv, const double* __restrict__ r0, int nc, int* err,
-           const int* __restrict__ active) {
+           const int* __restrict__ active, const int* __restrict__ sub_on) {
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double s_red[SWEEP_T / 32];
     __shared__ double s_zc;
     const int s = order[blockIdx.x];
+    if (sub_on && !sub_on[s]) return;  // subdomain not needed by this apply
     const SubInfo inf = info[s];
     const int n = inf.n;
     TS* t = reinterpret_cast<TS*>(smraw);
@@ -713,7 +716,7 @@ void sweep_launch(sg_precond* pc, const TF* lval, const TF* uval, const TF* udia
         reinterpret_cast<const TC*>(pc->perm_b.p), pc->lev_ptr_b.p,
         reinterpret_cast<const TC*>(pc->ucol.p), uval, udiag, pc->ownloc_d.p, pc->owned_d.p,
         x, y, mode, coarse ? 1 : 0, pc->a0inv.p, pc->r0.p, pc->nc, gscratch,
-        pc->use_smem ? 1 : 0, active);
+        pc->use_smem ? 1 : 0, active, pc->sub_on);
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
 }
@@ -738,7 +741,7 @@ void sf_launch(sg_precond* pc, const TF* lval, const TF* uval, const TF* udiag, 
         pc->info.p, pc->order.p, pc->dofs.p, reinterpret_cast<const TC*>(pc->perm_f.p),
         reinterpret_cast<const TC*>(pc->lcol.p), lval, reinterpret_cast<const TC*>(pc->perm_b.p),
         reinterpret_cast<const TC*>(pc->ucol.p), uval, udiag, pc->ownloc_d.p, pc->owned_d.p, x, y,
-        mode, coarse ? 1 : 0, pc->a0inv.p, pc->r0.p, pc->nc, pc->err_d.p, active);
+        mode, coarse ? 1 : 0, pc->a0inv.p, pc->r0.p, pc->nc, pc->err_d.p, active, pc->sub_on);
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
 }

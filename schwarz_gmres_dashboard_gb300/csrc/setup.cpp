@@ -412,6 +412,45 @@ int gen_poisson2d(int nx, int ny, int* rp, int* ci, double* v) {
     return nz;
 }
 
+// -div(K grad u) on an nx*ny grid with the constant anisotropic tensor
+// K = R(theta) diag(1, eps) R(theta)^T, unit mesh width, Dirichlet boundary
+// (neighbours outside the grid dropped).  9-point stencil: second
+// differences along x and y, the central difference
+// u_xy ~ (u_NE - u_NW - u_SE + u_SW) / 4 for the cross term, so
+//   centre 2 Kxx + 2 Kyy, W/E -Kxx, S/N -Kyy, SW/NE -Kxy/2, SE/NW +Kxy/2.
+// Row index iy*nx + ix; entries in ascending column order.
+int gen_aniso2d(int nx, int ny, double eps, double theta, int* rp, int* ci, double* v) {
+    const double c = std::cos(theta), s = std::sin(theta);
+    const double kxx = c * c + eps * s * s;
+    const double kyy = s * s + eps * c * c;
+    const double kxy = (1.0 - eps) * s * c;
+    int nz = 0;
+    auto put = [&](int col, double val) {
+        if (ci) { ci[nz] = col; v[nz] = val; }
+        ++nz;
+    };
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) {
+            const int idx = iy * nx + ix;
+            if (rp) rp[idx] = nz;
+            if (iy > 0) {
+                if (ix > 0) put(idx - nx - 1, -0.5 * kxy);
+                put(idx - nx, -kyy);
+                if (ix < nx - 1) put(idx - nx + 1, 0.5 * kxy);
+            }
+            if (ix > 0) put(idx - 1, -kxx);
+            put(idx, 2.0 * kxx + 2.0 * kyy);
+            if (ix < nx - 1) put(idx + 1, -kxx);
+            if (iy < ny - 1) {
+                if (ix > 0) put(idx + nx - 1, 0.5 * kxy);
+                put(idx + nx, -kyy);
+                if (ix < nx - 1) put(idx + nx + 1, -0.5 * kxy);
+            }
+        }
+    if (rp) rp[nx * ny] = nz;
+    return nz;
+}
+
 // 7-point operator with per-face coefficients; k == 1 gives make_poisson_3d
 static int gen_faces3d(int nx, int ny, int nz_, const double* kc, int* rp, int* ci, double* v) {
     const int nxy = nx * ny;

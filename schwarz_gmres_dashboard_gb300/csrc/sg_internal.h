@@ -102,6 +102,9 @@ struct SolveState {
     double y[SG_MMAX];
 };
 
+struct BatchWork;  // workspace of the batched solver (batched.cu)
+void destroy_batch_work(BatchWork* w);
+
 // Per-context solve workspace (grown on demand, reused across solves).
 struct SolveWork {
     DBuf<SolveState> st;
@@ -128,6 +131,7 @@ struct sg_ctx {
     double* hist_d = nullptr;
     int hist_cap = 0;
     sg::SolveWork* work = nullptr;
+    sg::BatchWork* batch = nullptr;
     // kernel-class timers (CUDA events on the context stream, eager solves)
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -238,6 +242,7 @@ struct sg_precond {
     bool use_rec = false;
     bool use_sf = false;   // sync-free sweep (per-row ready flags)
     int rec_depth = 0;               // ring stages in shared memory
+    int sweep_threads = 0;           // threads per CTA of the TMA-fed sweep
     long long rec_stage_bytes = 0;   // largest record
     long long rec_total = 0;
     std::vector<long long> h_rec_off_f, h_rec_off_b;  // byte offset per level
@@ -272,4 +277,7 @@ struct sg_precond {
     sg::DBuf<double> io_x, io_y;
     // ---- learned coarse-correction stage applied after M (not owned)
     sg_learned* learned = nullptr;
+    // optional device array [nparts]: 0 skips that subdomain's sweep (set by
+    // the batched solver around its applies; NULL = every subdomain)
+    const int* sub_on = nullptr;
 };

@@ -193,6 +193,7 @@ struct RecArgs {
     int max_n;
     int max_levels;  // largest nlev_f + nlev_b over the subdomains
     int* err;
+    const int* sub_on;  // optional per-subdomain switch (0: the subdomain is skipped)
 };
 
 // mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
@@ -210,6 +211,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     unsigned char* stages = smraw + 128;                               // D x stage_bytes
     TS* t = reinterpret_cast<TS*>(stages + (size_t)D * a.stage_bytes);  // n + 1
     const int s = a.order[blockIdx.x];
+    if (a.sub_on && !a.sub_on[s]) return;  // subdomain not needed by this apply
     const SubInfo inf = a.info[s];
     const int n = inf.n;
     const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
@@ -389,6 +391,7 @@ RecArgs rec_args(sg_precond* pc) {
     a.max_n = pc->max_n;
     a.max_levels = pc->max_levels;
     a.err = pc->err_d.p;
+    a.sub_on = pc->sub_on;
     return a;
 }
 
@@ -404,7 +407,8 @@ void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const
     const size_t smem = sweep_smem(pc, pc->rec_depth);
     SG_CUDA(cudaFuncSetAttribute(k_sweep_tma<TI, TO, TS, TF, EXACT>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_sweep_tma<TI, TO, TS, TF, EXACT><<<pc->nparts, SW_T, smem, pc->ctx->stream>>>(
+    const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
+    k_sweep_tma<TI, TO, TS, TF, EXACT><<<pc->nparts, nt, smem, pc->ctx->stream>>>(
         rec_args(pc), x, y, mode, coarse ? 1 : 0, active);
     SG_CUDA(cudaGetLastError());
     count_launch(pc->ctx);
@@ -446,6 +450,17 @@ void rec_setup_device(sg_precond* pc) {
         return;
     }
     pc->rec_depth = depth;
+    // threads per CTA: subdomains whose levels hold few rows (2D stencils,
+    // small subdomains) waste most of a 512-thread block at every level;
+    // 128-thread blocks let four times as many subdomains run at once
+    {
+        long long rows = 0, levels = 0;
+        for (const SubInfo& inf : pc->h_info) {
+            rows += inf.n;
+            levels += inf.nlev_f;
+        }
+        pc->sweep_threads = (levels > 0 && rows < 96 * levels) ? 128 : SW_T;
+    }
     pc->rec_off_f_d.upload(pc->h_rec_off_f, st);
     pc->rec_off_b_d.upload(pc->h_rec_off_b, st);
     pc->rec_rows_f_d.upload(pc->h_rec_rows_f, st);

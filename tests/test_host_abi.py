@@ -175,3 +175,42 @@ def test_host_structure_rejects_bad_input(sg):
     with pytest.raises(sg.SgError) as e:
         sg.schwarz_structure(B, np.zeros(2, np.int32), 1, 0)
     assert e.value.status == 4
+
+
+def test_aniso2d_generator(sg):
+    """9-point anisotropic stencil: symmetric, K = R diag(1, eps) R^T, and the
+    eps = 1 case equals the 5-point Laplacian (its corner entries are zeros)."""
+    import scipy.sparse as sp
+    n, eps, th = 7, 0.01, 0.6
+    A = sg.make_aniso_2d(n, n, eps, th)
+    S = sp.csr_matrix((A.vals, A.col_idx, A.row_ptr), shape=(n * n, n * n))
+    assert abs(S - S.T).max() == 0
+    c, s = np.cos(th), np.sin(th)
+    kxx, kyy, kxy = c * c + eps * s * s, s * s + eps * c * c, (1 - eps) * s * c
+    i = 3 * n + 3  # interior point
+    row = dict(zip(A.col_idx[A.row_ptr[i]:A.row_ptr[i + 1]], A.vals[A.row_ptr[i]:A.row_ptr[i + 1]]))
+    assert np.isclose(row[i], 2 * kxx + 2 * kyy) and np.isclose(row[i - 1], -kxx)
+    assert np.isclose(row[i - n], -kyy) and np.isclose(row[i + n + 1], -kxy / 2)
+    assert np.isclose(row[i + n - 1], kxy / 2) and len(row) == 9
+    assert np.all(np.diff(A.col_idx[A.row_ptr[i]:A.row_ptr[i + 1]]) > 0)
+    iso = sg.make_aniso_2d(n, n, 1.0, 0.3)
+    P = sg.make_poisson_2d(n, n)
+    Si = sp.csr_matrix((iso.vals, iso.col_idx, iso.row_ptr), shape=(n * n, n * n))
+    Sp = sp.csr_matrix((P.vals, P.col_idx, P.row_ptr), shape=(n * n, n * n))
+    assert abs(Si - Sp).max() < 1e-15
+
+
+def test_aniso_batch_layout(sg):
+    prob = sg.make_aniso_batch(9, seed=4, nmin=20, nmax=40, rows_per_part=200)
+    assert prob.sys_row_ptr[-1] == prob.n == int((prob.sizes ** 2).sum())
+    assert np.all((prob.sizes >= 20) & (prob.sizes <= 40))
+    assert np.all((prob.eps >= 1e-3) & (prob.eps <= 1.0))
+    # block diagonal, every part inside one system
+    for s in range(prob.nsys):
+        lo, hi = prob.sys_row_ptr[s], prob.sys_row_ptr[s + 1]
+        cols = prob.A.col_idx[prob.A.row_ptr[lo]:prob.A.row_ptr[hi]]
+        assert cols.min() >= lo and cols.max() < hi
+        ps = np.unique(prob.partition[lo:hi])
+        assert len(ps) == prob.parts[s]
+        others = np.concatenate([prob.partition[:lo], prob.partition[hi:]])
+        assert not np.isin(ps, others).any()
