@@ -70,7 +70,9 @@ typedef struct sg_precond_opts {
     int reserved[8];  /* reserved[0]: sweep variant (testing/comparison): 0 the
                          TMA-fed level sweep, 1 a level sweep reading factors
                          from global memory, 4 the sync-free sweep (per-row
-                         ready flags); other entries must be 0 */
+                         ready flags); reserved[1]: threads per CTA of the
+                         TMA-fed sweep (128, 256 or 512; 0 = the fastest,
+                         timed at set-up); other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;
@@ -111,10 +113,15 @@ sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* r
                         const int* col_idx, const double* vals, sg_mem mem, sg_csr** out);
 sg_status sg_csr_destroy(sg_csr* A);
 /* SpMV storage used by this matrix: 0 = decided by the autotuner on first
- * use (times both, keeps the faster), 1 = CSR, 2 = SELL-C-sigma (C = 32).
- * Both give the same bits.  No counterpart in the reference (cuSPARSE's
+ * use (times every available format, keeps the fastest), 1 = CSR,
+ * 2 = SELL-C-sigma (C = 32), 3 = SELL-32 with 16-bit column offsets from the
+ * row (when every |column - row| <= 32767).  All give the same bits.  No counterpart in the reference (cuSPARSE's
  * CUSPARSE_SPMV_ALG_DEFAULT, src/gpu/cuda_sparse.h:64-68, has no choice). */
 sg_status sg_csr_set_format(sg_csr* A, int format);
+/* Forces one SELL launch variant of the autotuner's set (testing and
+ * comparison): column width, resident blocks, grid and the software-pipelined
+ * kernel; SG_ERR_UNSUPPORTED when the matrix does not allow it. */
+sg_status sg_csr_set_spmv_variant(sg_csr* A, int variant);
 sg_status sg_csr_get_format(sg_csr* A, int* format);
 /* y = A x (CSRMatrix::spmv, src/core/sparse_matrix.h:30-37; replaces
  * DeviceCSRMatrix::spmv, src/gpu/cuda_sparse.h:53-74). FP64, same summation

@@ -196,7 +196,8 @@ class CSRMatrix:
 
     @property
     def format(self) -> int:
-        """SpMV storage: 0 autotune (not decided yet), 1 CSR, 2 SELL-32."""
+        """SpMV storage: 0 autotune (not decided yet), 1 CSR, 2 SELL-32,
+        3 SELL-32 with 16-bit column offsets."""
         f = C.c_int(0)
         _check(_clib.sg_csr_get_format(self.device(), C.byref(f)))
         return f.value
@@ -204,6 +205,10 @@ class CSRMatrix:
     @format.setter
     def format(self, fmt: int) -> None:
         _check(_clib.sg_csr_set_format(self.device(), int(fmt)))
+
+    def set_spmv_variant(self, variant: int) -> None:
+        """Force one SELL launch variant of the autotuner's set (testing)."""
+        _check(_clib.sg_csr_set_spmv_variant(self.device(), int(variant)))
 
     def diagonal(self, i: int) -> float:
         for e in range(self.row_ptr[i], self.row_ptr[i + 1]):
@@ -361,7 +366,7 @@ class Preconditioner:
     def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
                  ctx: Context | None = None, generic_sweep: bool = False,
-                 sweep: str = "tma"):
+                 sweep: str = "tma", sweep_threads: int = 0):
         # sweep variant (testing/comparison): "tma" (default: TMA-fed level
         # records), "level" (factors read from global memory), "syncfree"
         if generic_sweep:
@@ -380,6 +385,8 @@ class Preconditioner:
         opts.sweep_dtype = sweep_dtype
         opts.partition = self.partition.ctypes.data if self.partition is not None else None
         opts.reserved[0] = {"tma": 0, "level": 1, "syncfree": 4}[self.sweep]
+        # threads per CTA of the TMA-fed sweep (0: timed at set-up)
+        opts.reserved[1] = int(sweep_threads)
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),

@@ -38,6 +38,8 @@ int gen_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t se
                   double* v);
 void gen_uniform(uint64_t seed, int n, double lo, double hi, double* out);
 int gen_aniso2d(int nx, int ny, double eps, double theta, int* rp, int* ci, double* v);
+int sell_variant_count();
+int sell_variant_info(int variant, int what);
 void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, const double* b,
                   double* x, const sg_solve_params& prm, sg_solve_result* res);
 
@@ -102,6 +104,8 @@ void sg_csr::build_sell() {
         ptr[s + 1] = ptr[s] + 32ll * mw;
     }
     sell_entries = ptr[nslices];
+    sell_maxw = 0;
+    for (int s = 0; s < nslices; ++s) sell_maxw = std::max(sell_maxw, w[s]);
     if (sell_entries > (long long)nnz + nnz / 4 + 64 || sell_entries >= (1ll << 31)) return;
     std::vector<int> col(sell_entries > 0 ? sell_entries : 1, 0);
     std::vector<double> val(sell_entries > 0 ? sell_entries : 1, 0.0);
@@ -123,6 +127,29 @@ void sg_csr::build_sell() {
     sl_w.upload(w, ctx->stream);
     sl_col.upload(col, ctx->stream);
     sl_val.upload(val, ctx->stream);
+    // 16-bit column offsets when every |column - row| fits (banded matrices)
+    sl_dcol.release();
+    {
+        bool fits = true;
+        std::vector<int16_t> dcol(col.size());
+        for (int s = 0; s < nslices && fits; ++s)
+            for (long long e = ptr[s]; e < ptr[s + 1]; ++e) {
+                const int r = s * 32 + (int)((e - ptr[s]) % 32);
+                const long long d = (long long)col[e] - (r < nrows ? r : 0);
+                if (r >= nrows) {
+                    // lanes past the last row: result never stored; point the
+                    // load at row n-1 (offset >= -31)
+                    dcol[e] = (int16_t)((nrows - 1) - r);
+                    continue;
+                }
+                if (d < -32768 || d > 32767) {
+                    fits = false;
+                    break;
+                }
+                dcol[e] = (int16_t)d;
+            }
+        if (fits) sl_dcol.upload(dcol, ctx->stream);
+    }
     sell_ok = true;
 }
 
@@ -316,12 +343,32 @@ sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* r
 sg_status sg_csr_set_format(sg_csr* A, int format) {
     return guard([&] {
         SG_CHECK_ARG(A, "NULL argument");
-        SG_CHECK_ARG(format >= 0 && format <= 2, "format must be 0 (auto), 1 (CSR) or 2 (SELL)");
-        if (format == 2 && !A->sell_ok)
+        SG_CHECK_ARG(format >= 0 && format <= 3,
+                     "format must be 0 (auto), 1 (CSR), 2 (SELL) or 3 (SELL, 16-bit columns)");
+        if (format >= 2 && !A->sell_ok)
             fail(SG_ERR_UNSUPPORTED, "no SELL copy of this matrix (unsorted rows or padding > 25%%)");
+        if (format == 3 && !A->sl_dcol.p)
+            fail(SG_ERR_UNSUPPORTED, "a column lies more than 32767 away from its row");
         A->format = format;
         A->format32 = format;
         A->format_user = format != 0;
+    });
+}
+
+sg_status sg_csr_set_spmv_variant(sg_csr* A, int variant) {
+    return guard([&] {
+        SG_CHECK_ARG(A, "NULL argument");
+        const int nv = sell_variant_count();
+        SG_CHECK_ARG(variant >= 0 && variant < nv, "variant must be in [0,%d)", nv);
+        if (!A->sell_ok) fail(SG_ERR_UNSUPPORTED, "no SELL copy of this matrix");
+        const int dcol = sell_variant_info(variant, 0), pipe = sell_variant_info(variant, 1);
+        if (dcol && !A->sl_dcol.p)
+            fail(SG_ERR_UNSUPPORTED, "a column lies more than 32767 away from its row");
+        if (pipe && A->sell_maxw > 8)
+            fail(SG_ERR_UNSUPPORTED, "a row holds more than 8 entries");
+        A->format = A->format32 = dcol ? 3 : 2;
+        A->sell_cfg = A->sell_cfg32 = variant;
+        A->format_user = true;
     });
 }
 
@@ -380,6 +427,11 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             pc->opts.overlap = 1;
             pc->opts.factor_dtype = SG_FP64;
             pc->opts.sweep_dtype = SG_FP64;
+        }
+        const int swt = pc->opts.reserved[1];
+        if (!(swt == 0 || swt == 128 || swt == 256 || swt == 512)) {
+            delete pc;
+            fail(SG_ERR_INVALID_ARG, "sweep threads (reserved[1]) must be 0, 128, 256 or 512");
         }
         const int sd = pc->opts.sweep_dtype, fd = pc->opts.factor_dtype;
         const bool ok = (sd == SG_FP64 && fd == SG_FP64) ||

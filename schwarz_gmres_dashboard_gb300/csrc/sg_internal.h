@@ -184,11 +184,15 @@ struct sg_csr {
     int nslices = 0;
     long long sell_entries = 0;
     bool sell_ok = false;  // padding small enough to keep the copy
-    int format = 0;        // 0 undecided, 1 CSR, 2 SELL (set by the autotuner)
+    int format = 0;        // 0 undecided, 1 CSR, 2 SELL, 3 SELL with 16-bit column offsets
     int format32 = 0;      // same for the FP32 copy (0: follow `format`)
+    int sell_maxw = 0;     // widest SELL slice (entries per row)
+    int sell_cfg = -1;     // tuned SELL launch variant (FP64 values; -1 default)
+    int sell_cfg32 = -1;   // same for the FP32 copy
     bool format_user = false;  // set by the caller: the autotuner keeps it
     sg::DBuf<long long> sl_ptr;
     sg::DBuf<int> sl_w, sl_col;
+    sg::DBuf<int16_t> sl_dcol;  // column - row when every entry fits in 16 bits
     sg::DBuf<double> sl_val;
     sg::DBuf<float> sl_val32;
     void ensure_fp32();

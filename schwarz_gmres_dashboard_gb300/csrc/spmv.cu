@@ -139,13 +139,21 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
     }
 }
 
+// column of SELL entry: absolute int32, or a 16-bit offset from the row
+__device__ __forceinline__ int sell_col(const int* col, long long e, int) { return __ldg(&col[e]); }
+__device__ __forceinline__ int sell_col(const int16_t* col, long long e, int r) {
+    return r + (int)__ldg(&col[e]);
+}
+
 // SELL-32 SpMV: a warp per slice of 32 rows, a lane per row; every load of
 // a step k is one contiguous 32-element segment.  Same per-row order and
 // rounding as the CSR kernel (padding adds exact zeros at the end of a row).
-template <class TV, class TX, class TY, int MODE>
-__global__ void __launch_bounds__(SPMV_THREADS, 4)
+// TC = int: absolute columns; TC = int16_t: column - row (banded matrices
+// such as grid stencils), 6 instead of 8 bytes per FP32 entry.
+template <class TV, class TX, class TY, int MODE, class TC = int, int MINB = 4>
+__global__ void __launch_bounds__(SPMV_THREADS, MINB)
 k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* __restrict__ sw,
-            const int* __restrict__ col, const TV* __restrict__ val, const TX* __restrict__ x,
+            const TC* __restrict__ col, const TV* __restrict__ val, const TX* __restrict__ x,
             TY* __restrict__ y, const double* __restrict__ scale, const int* __restrict__ active,
             const double* __restrict__ b, double* partials, unsigned* counter, SolveState* st) {
     if (active && *active == 0) return;
@@ -156,6 +164,7 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
     for (int sl = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5); sl < nslices; sl += nwarps) {
         const long long base = sptr[sl] + lane;
         const int w = sw[sl];
+        const int row = sl * 32 + lane;
         TV sum = (TV)0;
         // up to 8 entries of a row per round: all value/column loads first,
         // then all gathers of x, then the sum in entry order
@@ -166,7 +175,7 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
             for (int q = 0; q < 8; ++q) {
                 if (k + q < w) {
                     v[q] = __ldg(&val[base + (long long)(k + q) * 32]);
-                    c[q] = __ldg(&col[base + (long long)(k + q) * 32]);
+                    c[q] = sell_col(col, base + (long long)(k + q) * 32, row);
                 }
             }
             TV p[8];
@@ -213,12 +222,71 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
     }
 }
 
-int sell_grid(sg_ctx* ctx, int nslices) {
+// SELL-32 for matrices whose slices hold at most 8 entries per row (grid
+// stencils), software-pipelined: a warp issues the value/column loads of its
+// next slice before it gathers x for the current one, so its DRAM requests
+// stay in flight while the gathers (mostly L2 hits) complete.  Same per-row
+// order and rounding as k_spmv_sell.
+template <class TV, class TX, class TY, class TC, int MINB>
+__global__ void __launch_bounds__(SPMV_THREADS, MINB)
+k_spmv_sell_pipe(int n, int nslices, const long long* __restrict__ sptr,
+                 const int* __restrict__ sw, const TC* __restrict__ col,
+                 const TV* __restrict__ val, const TX* __restrict__ x, TY* __restrict__ y,
+                 const double* __restrict__ scale, const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * SPMV_WARPS;
+    const TV sc = scale ? (TV)(*scale) : (TV)1;
+    int sl = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
+    TV v[8], vn[8];
+    int c[8], cn[8];
+    int w = 0, wn = 0;
+    auto load = [&](int s, TV (&vv)[8], int (&cc)[8], int& ww) {
+        ww = sw[s];
+        const long long base = sptr[s] + lane;
+        const int row = s * 32 + lane;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            if (q < ww) {
+                vv[q] = __ldg(&val[base + (long long)q * 32]);
+                cc[q] = sell_col(col, base + (long long)q * 32, row);
+            }
+        }
+    };
+    if (sl < nslices) load(sl, v, c, w);
+    while (sl < nslices) {
+        const int nx = sl + nwarps;
+        if (nx < nslices) load(nx, vn, cn, wn);
+        TV p[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < w) p[q] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+        TV sum = (TV)0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < w) sum = padd(sum, p[q]);
+        const int r = sl * 32 + lane;
+        if (r < n) y[r] = (TY)(scale ? pmul(sum, sc) : sum);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            v[q] = vn[q];
+            c[q] = cn[q];
+        }
+        w = wn;
+        sl = nx;
+    }
+}
+
+// grid of the SELL kernel: at most `per_sm` blocks per SM, warps loop over
+// slices (MODE 1 reduces per block into the context's partials: 8 per SM)
+int sell_grid(sg_ctx* ctx, int nslices, int per_sm = 8) {
     long long blocks = ((long long)nslices + SPMV_WARPS - 1) / SPMV_WARPS;
-    const long long cap = (long long)ctx->num_sms * 8;
+    const long long cap = (long long)ctx->num_sms * per_sm;
     if (blocks > cap) blocks = cap;
     return blocks < 1 ? 1 : (int)blocks;
 }
+
+
 
 template <class TV>
 const TV* sell_vals(const sg_csr* A);
@@ -232,6 +300,54 @@ template <>
 const double* csr_vals<double>(const sg_csr* A) { return A->val.p; }
 template <>
 const float* csr_vals<float>(const sg_csr* A) { return A->val32.p; }
+
+// SELL launch variants the autotuner chooses from: columns (int32 or 16-bit
+// offsets), registers (min 4 or 6 blocks per SM) and grid (blocks per SM)
+struct SellCfg {
+    bool dcol;
+    int minb;
+    int per_sm;
+    bool pipe;  // software-pipelined kernel (slices of at most 8 entries per row)
+};
+constexpr SellCfg kSellCfgs[] = {
+    {false, 4, 8, false}, {false, 6, 12, false}, {false, 6, 24, false},
+    {true, 4, 8, false},  {true, 6, 12, false},  {true, 6, 24, false},
+    {false, 4, 8, true},  {false, 4, 16, true},  {true, 4, 8, true},  {true, 4, 16, true}};
+constexpr int kNumSellCfgs = (int)(sizeof(kSellCfgs) / sizeof(kSellCfgs[0]));
+
+template <class TV, class TX, class TY>
+void launch_sell(sg_ctx* ctx, const sg_csr* A, int cfg, const TX* x, TY* y, const double* scale,
+                 const int* active) {
+    const SellCfg c = kSellCfgs[cfg];
+    const int grid = sell_grid(ctx, A->nslices, c.per_sm);
+    if (c.pipe) {
+        if (c.dcol)
+            k_spmv_sell_pipe<TV, TX, TY, int16_t, 4><<<grid, SPMV_THREADS, 0, ctx->stream>>>(
+                A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_dcol.p, sell_vals<TV>(A), x, y,
+                scale, active);
+        else
+            k_spmv_sell_pipe<TV, TX, TY, int, 4><<<grid, SPMV_THREADS, 0, ctx->stream>>>(
+                A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, sell_vals<TV>(A), x, y,
+                scale, active);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        return;
+    }
+#define SG_SELL(TC, MB, COLS)                                                                   \
+    k_spmv_sell<TV, TX, TY, 0, TC, MB><<<grid, SPMV_THREADS, 0, ctx->stream>>>(                  \
+        A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, COLS, sell_vals<TV>(A), x, y, scale, active, \
+        nullptr, nullptr, nullptr, nullptr)
+    if (c.dcol) {
+        if (c.minb == 6) SG_SELL(int16_t, 6, A->sl_dcol.p);
+        else SG_SELL(int16_t, 4, A->sl_dcol.p);
+    } else {
+        if (c.minb == 6) SG_SELL(int, 6, A->sl_col.p);
+        else SG_SELL(int, 4, A->sl_col.p);
+    }
+#undef SG_SELL
+    SG_CUDA(cudaGetLastError());
+    count_launch(ctx);
+}
 
 __global__ void k_bnorm(const double* __restrict__ v, int n, double* partials, unsigned* counter,
                         SolveState* st) {
@@ -277,7 +393,12 @@ void launch_spmv(sg_ctx* ctx, int n, const int* rp, const int* ci, const TV* val
 
 void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double* x, double* r,
                      SolveState* st) {
-    if (A->format == 2 && A->sell_ok) {
+    if (A->format == 3 && A->sell_ok && A->sl_dcol.p) {
+        k_spmv_sell<double, double, double, 1, int16_t><<<sell_grid(ctx, A->nslices),
+                                                          SPMV_THREADS, 0, ctx->stream>>>(
+            A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_dcol.p, A->sl_val.p, x, r,
+            nullptr, nullptr, b, ctx->partials.p, ctx->counter.p, st);
+    } else if (A->format >= 2 && A->sell_ok) {
         k_spmv_sell<double, double, double, 1><<<sell_grid(ctx, A->nslices), SPMV_THREADS, 0,
                                                  ctx->stream>>>(
             A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, A->sl_val.p, x, r, nullptr,
@@ -292,6 +413,20 @@ void launch_residual(sg_ctx* ctx, const sg_csr* A, const double* b, const double
     count_launch(ctx);
 }
 
+// SELL launch variants (for sg_csr_set_spmv_variant): count, and per
+// variant 0 = 16-bit column offsets, 1 = pipelined kernel
+int sell_variant_count() { return kNumSellCfgs; }
+int sell_variant_info(int v, int what) {
+    return what == 0 ? (int)kSellCfgs[v].dcol : (int)kSellCfgs[v].pipe;
+}
+
+template <class TV>
+int sell_cfg_of(const sg_csr* A);
+template <>
+int sell_cfg_of<double>(const sg_csr* A) { return A->sell_cfg; }
+template <>
+int sell_cfg_of<float>(const sg_csr* A) { return A->sell_cfg32; }
+
 template <class TV>
 int format_of(const sg_csr* A);
 template <>
@@ -303,22 +438,24 @@ template <class TV, class TX, class TY>
 void launch_spmv_a(sg_ctx* ctx, const sg_csr* A, const TX* x, TY* y, const double* scale,
                    const int* active) {
     if (A->nrows <= 0) return;
-    if (format_of<TV>(A) == 2 && A->sell_ok) {
-        k_spmv_sell<TV, TX, TY, 0><<<sell_grid(ctx, A->nslices), SPMV_THREADS, 0, ctx->stream>>>(
-            A->nrows, A->nslices, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, sell_vals<TV>(A), x, y,
-            scale, active, nullptr, nullptr, nullptr, nullptr);
-        SG_CUDA(cudaGetLastError());
-        count_launch(ctx);
+    const int fmt = format_of<TV>(A);
+    if (fmt >= 2 && A->sell_ok && (fmt == 2 || A->sl_dcol.p)) {
+        // the tuned launch variant of this format (default: first of the format)
+        int cfg = sell_cfg_of<TV>(A);
+        if (cfg < 0 || kSellCfgs[cfg].dcol != (fmt == 3)) cfg = fmt == 3 ? 3 : 0;
+        launch_sell<TV, TX, TY>(ctx, A, cfg, x, y, scale, active);
     } else {
         launch_spmv<TV, TX, TY>(ctx, A->nrows, A->rp.p, A->ci.p, csr_vals<TV>(A), x, y, scale,
                                 active);
     }
 }
 
-// Autotuner: times CSR and SELL on A (5 launches each after a warm-up) and
-// keeps the faster, separately for the FP64 values and for the FP32 copy.
-// Both formats give the same bits, so the choice never changes a result.  A
-// format set by the caller (sg_csr_set_format) is left alone.
+// Autotuner: times CSR and the SELL launch variants (int32 or 16-bit column
+// offsets, 4 or 6 resident blocks per SM, 8 to 24 blocks per SM in the grid)
+// on A (5 launches each after a warm-up) and keeps the fastest, separately
+// for the FP64 values and for the FP32 copy.  All formats give the same bits, so the
+// choice never changes a result.  A format set by the caller
+// (sg_csr_set_format) is left alone.
 void spmv_autotune(sg_ctx* ctx, sg_csr* A) {
     if (A->format_user) return;
     const bool need64 = A->format == 0;
@@ -347,28 +484,50 @@ void spmv_autotune(sg_ctx* ctx, sg_csr* A) {
         xb.alloc(A->ncols);
         yb.alloc(A->nrows);
         xb.zero(ctx->stream);
-        float t[3] = {0, 0, 0};
-        for (int f = 1; f <= 2; ++f) {
-            A->format = f;
-            t[f] = time_it([&] {
-                launch_spmv_a<double, double, double>(ctx, A, xb.p, yb.p, nullptr, nullptr);
+        A->format = 1;
+        float best = time_it([&] {
+            launch_spmv_a<double, double, double>(ctx, A, xb.p, yb.p, nullptr, nullptr);
+        });
+        int bf = 1, bc = -1;
+        for (int c = 0; c < kNumSellCfgs; ++c) {
+            if (kSellCfgs[c].dcol && !A->sl_dcol.p) continue;
+            if (kSellCfgs[c].pipe && A->sell_maxw > 8) continue;
+            const float t = time_it([&] {
+                launch_sell<double, double, double>(ctx, A, c, xb.p, yb.p, nullptr, nullptr);
             });
+            if (t < best) {
+                best = t;
+                bf = kSellCfgs[c].dcol ? 3 : 2;
+                bc = c;
+            }
         }
-        A->format = t[2] < t[1] ? 2 : 1;
+        A->format = bf;
+        A->sell_cfg = bc;
     }
     if (need32 && A->sl_val32.p) {
         DBuf<float> xb, yb;
         xb.alloc(A->ncols);
         yb.alloc(A->nrows);
         xb.zero(ctx->stream);
-        float t[3] = {0, 0, 0};
-        for (int f = 1; f <= 2; ++f) {
-            A->format32 = f;
-            t[f] = time_it([&] {
-                launch_spmv_a<float, float, float>(ctx, A, xb.p, yb.p, nullptr, nullptr);
+        A->format32 = 1;
+        float best = time_it([&] {
+            launch_spmv_a<float, float, float>(ctx, A, xb.p, yb.p, nullptr, nullptr);
+        });
+        int bf = 1, bc = -1;
+        for (int c = 0; c < kNumSellCfgs; ++c) {
+            if (kSellCfgs[c].dcol && !A->sl_dcol.p) continue;
+            if (kSellCfgs[c].pipe && A->sell_maxw > 8) continue;
+            const float t = time_it([&] {
+                launch_sell<float, float, float>(ctx, A, c, xb.p, yb.p, nullptr, nullptr);
             });
+            if (t < best) {
+                best = t;
+                bf = kSellCfgs[c].dcol ? 3 : 2;
+                bc = c;
+            }
         }
-        A->format32 = t[2] < t[1] ? 2 : 1;
+        A->format32 = bf;
+        A->sell_cfg32 = bc;
     } else if (need32) {
         A->format32 = 1;
     }

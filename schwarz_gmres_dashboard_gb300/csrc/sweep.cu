@@ -416,6 +416,8 @@ void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const
 
 }  // namespace
 
+void tune_sweep_threads(sg_precond* pc);
+
 // Packs the level records of the configured factor type and picks the ring
 // depth: as deep as fits while as many subdomains as possible run at once.
 void rec_setup_device(sg_precond* pc) {
@@ -450,17 +452,6 @@ void rec_setup_device(sg_precond* pc) {
         return;
     }
     pc->rec_depth = depth;
-    // threads per CTA: subdomains whose levels hold few rows (2D stencils,
-    // small subdomains) waste most of a 512-thread block at every level;
-    // 128-thread blocks let four times as many subdomains run at once
-    {
-        long long rows = 0, levels = 0;
-        for (const SubInfo& inf : pc->h_info) {
-            rows += inf.n;
-            levels += inf.nlev_f;
-        }
-        pc->sweep_threads = (levels > 0 && rows < 96 * levels) ? 128 : SW_T;
-    }
     pc->rec_off_f_d.upload(pc->h_rec_off_f, st);
     pc->rec_off_b_d.upload(pc->h_rec_off_b, st);
     pc->rec_rows_f_d.upload(pc->h_rec_rows_f, st);
@@ -480,6 +471,66 @@ void rec_setup_device(sg_precond* pc) {
     else SG_PACK(float);
 #undef SG_PACK
     SG_CUDA(cudaGetLastError());
+    // threads per CTA: forced by opts.reserved[1], else timed.  Levels of a
+    // 3D subdomain hold ~100+ rows, those of a small 2D one ~20: a 512-thread
+    // block then idles at every level barrier, while narrower blocks let more
+    // subdomains run at once on an SM.
+    if (pc->opts.reserved[1] > 0) pc->sweep_threads = pc->opts.reserved[1];
+    else tune_sweep_threads(pc);
+}
+
+// Times the sweep (RAS mode, no coarse term, zero input) with 128, 256 and
+// 512 threads per CTA and keeps the fastest.
+void tune_sweep_threads(sg_precond* pc) {
+    sg_ctx* ctx = pc->ctx;
+    cudaStream_t st = ctx->stream;
+    const size_t n = (size_t)std::max(pc->n, 1);
+    const bool f64 = pc->opts.sweep_dtype == SG_FP64;
+    const bool bf16 = pc->opts.factor_dtype == SG_BF16;
+    DBuf<double> x64, y64;
+    DBuf<float> x32, y32;
+    if (f64) {
+        x64.alloc(n);
+        y64.alloc(n);
+        x64.zero(st);
+    } else {
+        x32.alloc(n);
+        y32.alloc(n);
+        x32.zero(st);
+    }
+    auto run = [&] {
+        if (f64) launch_tma<double, double, double, double, false>(pc, x64.p, y64.p, 0, false, nullptr);
+        else if (bf16) launch_tma<float, float, float, uint16_t, false>(pc, x32.p, y32.p, 0, false, nullptr);
+        else launch_tma<float, float, float, float, false>(pc, x32.p, y32.p, 0, false, nullptr);
+    };
+    cudaEvent_t e0, e1;
+    SG_CUDA(cudaEventCreate(&e0));
+    SG_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int best_nt = SW_T;
+    for (int nt : {512, 256, 128}) {
+        pc->sweep_threads = nt;
+        run();
+        run();
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 5; ++r) run();
+        cudaEventRecord(e1, st);
+        cudaError_t e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            SG_CUDA(e);
+        }
+        if (nt == SW_T || ms < best) {
+            best = ms;
+            best_nt = nt;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pc->sweep_threads = best_nt;
 }
 
 template <class TI, class TO>

@@ -69,8 +69,8 @@ def _irregular(n, seed):
     return HostCSR(rp, ci, v)
 
 
-@pytest.mark.parametrize("fmt", [1, 2])
-@pytest.mark.parametrize("maker", ["p3d", "varcoef", "irregular", "tiny"])
+@pytest.mark.parametrize("fmt", [1, 2, 3])
+@pytest.mark.parametrize("maker", ["p3d", "varcoef", "irregular", "tiny", "wide"])
 def test_spmv_matches_oracle(sg, oracle, maker, fmt):
     if maker == "p3d":
         A = sg.make_poisson_3d(40, 37, 23)
@@ -79,19 +79,45 @@ def test_spmv_matches_oracle(sg, oracle, maker, fmt):
     elif maker == "irregular":
         H = _irregular(5000, 3)
         A = to_sg(sg, H)
+    elif maker == "wide":
+        # 3D Laplacian whose z-neighbours lie 40,000 rows away: no 16-bit offsets
+        A = sg.make_poisson_3d(200, 200, 3)
     else:
         A = sg.make_poisson_2d(1, 3)
     x = sg.uniform(A.ncols, seed=11)
     H = HostCSR(A.row_ptr, A.col_idx, A.vals)
     try:
         A.format = fmt
-    except sg.SgError as e:  # no SELL copy (padding too large): CSR only
-        assert fmt == 2 and e.status == 8
+    except sg.SgError as e:  # no SELL copy (padding too large) or no 16-bit offsets
+        assert fmt >= 2 and e.status == 8
+        # SELL is refused for padding > 25% (irregular, the 3-row matrix);
+        # 16-bit offsets for columns more than 32767 rows away (wide)
+        assert maker in ("irregular", "tiny") or (maker == "wide" and fmt == 3)
         return
+    assert maker != "wide" or fmt != 3
     assert np.array_equal(A.spmv(x), oracle.spmv(H, x))
 
 
-@pytest.mark.parametrize("fmt", [1, 2])
+@pytest.mark.parametrize("variant", list(range(10)))
+def test_every_sell_variant_matches_oracle(sg, oracle, variant):
+    """Every launch variant the SpMV autotuner may pick (column width,
+    residency, grid, pipelined kernel) gives the reference's bits."""
+    A = sg.make_varcoef_3d(32, 32, 40, 1.0, 6.0, 9)
+    x = sg.uniform(A.ncols, seed=12)
+    A.set_spmv_variant(variant)
+    H = HostCSR(A.row_ptr, A.col_idx, A.vals)
+    assert np.array_equal(A.spmv(x), oracle.spmv(H, x))
+    # and inside a mixed-precision solve (FP32 copy, same variant)
+    b = A.spmv(sg.uniform(A.nrows, seed=13))
+    pc = sg.RASPrecond(8, 1, factor_dtype=sg.FP32, sweep_dtype=sg.FP32)
+    pc.setup(A)
+    xs = np.zeros(A.nrows)
+    r = sg.gmres(A, b, xs, pc, sg.GMRESParams(restart=30, max_iter=500, tol=1e-8,
+                                             tol_kind=sg.TOL_TRUE_REL, precision=sg.FP32))
+    assert r.converged and r.true_rel_residual <= 1e-8
+
+
+@pytest.mark.parametrize("fmt", [1, 2, 3])
 def test_solve_same_bits_in_both_formats(sg, fmt):
     """The SpMV storage is a pure performance choice: FP64 solves give the
     same bits whichever format runs."""
