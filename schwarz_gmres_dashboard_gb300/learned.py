@@ -75,10 +75,11 @@ class LearnedCorrection:
         _check(_clib.sg_learned_set_weights(self.handle, w.ctypes.data, NUM_PARAMS))
 
     def save(self, path: str) -> None:
-        np.save(path, self.weights)
+        """Raw little-endian float32 weights (the format `schwarz_solve --learned` reads)."""
+        self.weights.astype("<f4").tofile(path)
 
     def load(self, path: str) -> None:
-        self.weights = np.load(path)
+        self.weights = np.fromfile(path, dtype="<f4")
 
     # ---- training data
     def add_pair(self, M: Preconditioner, r, e) -> None:
