@@ -382,6 +382,7 @@ def run_ours(args):
                      "us_per_launch": dom["us_per_launch"],
                      "timing": "CUDA events around every apply of one eager solve"},
         "kernels": per,
+        "spmv_choice": A.spmv_choice(),
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

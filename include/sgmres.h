@@ -122,6 +122,10 @@ sg_status sg_csr_set_format(sg_csr* A, int format);
  * comparison): column width, resident blocks, grid and the software-pipelined
  * kernel; SG_ERR_UNSUPPORTED when the matrix does not allow it. */
 sg_status sg_csr_set_spmv_variant(sg_csr* A, int variant);
+/* The autotuner's choice: format and SELL launch variant (-1: default) for
+ * the FP64 values and for the FP32 copy (0 until the first solve or SpMV). */
+sg_status sg_csr_get_spmv_choice(sg_csr* A, int* format, int* variant, int* format32,
+                                 int* variant32);
 sg_status sg_csr_get_format(sg_csr* A, int* format);
 /* y = A x (CSRMatrix::spmv, src/core/sparse_matrix.h:30-37; replaces
  * DeviceCSRMatrix::spmv, src/gpu/cuda_sparse.h:53-74). FP64, same summation

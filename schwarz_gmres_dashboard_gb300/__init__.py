@@ -206,6 +206,14 @@ class CSRMatrix:
     def format(self, fmt: int) -> None:
         _check(_clib.sg_csr_set_format(self.device(), int(fmt)))
 
+    def spmv_choice(self) -> dict:
+        """The autotuner's SpMV choice for the FP64 values and the FP32 copy."""
+        f, v, f32, v32 = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        _check(_clib.sg_csr_get_spmv_choice(self.device(), C.byref(f), C.byref(v), C.byref(f32),
+                                           C.byref(v32)))
+        return {"format": f.value, "variant": v.value, "format32": f32.value,
+                "variant32": v32.value}
+
     def set_spmv_variant(self, variant: int) -> None:
         """Force one SELL launch variant of the autotuner's set (testing)."""
         _check(_clib.sg_csr_set_spmv_variant(self.device(), int(variant)))

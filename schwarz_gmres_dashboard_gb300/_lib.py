@@ -80,6 +80,7 @@ PROTOTYPES = {
     "sg_csr_set_format": (C.c_int, [_vp, C.c_int]),
     "sg_csr_get_format": (C.c_int, [_vp, _ip]),
     "sg_csr_set_spmv_variant": (C.c_int, [_vp, C.c_int]),
+    "sg_csr_get_spmv_choice": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "sg_csr_spmv": (C.c_int, [_vp, _vp, _vp, C.c_int]),
     "sg_precond_create": (C.c_int, [_vp, C.c_int, C.POINTER(PrecondOpts), C.POINTER(_vp)]),
     "sg_precond_setup": (C.c_int, [_vp, _vp]),

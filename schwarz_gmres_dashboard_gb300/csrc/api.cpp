@@ -372,6 +372,17 @@ sg_status sg_csr_set_spmv_variant(sg_csr* A, int variant) {
     });
 }
 
+sg_status sg_csr_get_spmv_choice(sg_csr* A, int* format, int* variant, int* format32,
+                                 int* variant32) {
+    return guard([&] {
+        SG_CHECK_ARG(A, "NULL argument");
+        if (format) *format = A->format;
+        if (variant) *variant = A->sell_cfg;
+        if (format32) *format32 = A->format32 ? A->format32 : A->format;
+        if (variant32) *variant32 = A->sell_cfg32;
+    });
+}
+
 sg_status sg_csr_get_format(sg_csr* A, int* format) {
     return guard([&] {
         SG_CHECK_ARG(A && format, "NULL argument");
