@@ -383,6 +383,7 @@ def run_ours(args):
                      "timing": "CUDA events around every apply of one eager solve"},
         "kernels": per,
         "spmv_choice": A.spmv_choice(),
+        "sweep_choice": pc_mixed.sweep_choice(),
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

@@ -162,6 +162,12 @@ sg_status sg_precond_get_factors(sg_precond* pc, int s, int* n_s, int* nnz_s, in
 /* Coarse operator A0 (P x P, row-major) of a two-level preconditioner as
  * built on the device (CoarseSpace::A0, src/precond/coarse_space.h:43-60). */
 sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc);
+/* The subdomain sweep the set-up chose (ILU0Precond::apply's triangular
+ * solves, src/precond/ilu0.h:54-79, run per subdomain): *sweep 0 TMA-fed
+ * level records, 1 a barrier per level, 2 sync-free, -1 none (Jacobi);
+ * *threads the threads per CTA of the TMA-fed sweep (0 otherwise).  Either
+ * pointer may be NULL. */
+sg_status sg_precond_get_sweep(sg_precond* pc, int* sweep, int* threads);
 
 /* ---- solvers ---------------------------------------------------------- */
 typedef enum sg_solver {

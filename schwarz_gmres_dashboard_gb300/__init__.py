@@ -453,6 +453,14 @@ class Preconditioner:
         _check(_clib.sg_precond_get_coarse(self.handle, a0.ctypes.data, a0.size, C.byref(nc)))
         return a0.reshape(nc.value, nc.value)
 
+    def sweep_choice(self) -> dict:
+        """The subdomain sweep chosen at set-up: kind ("tma", "level",
+        "syncfree" or "none") and threads per CTA of the TMA-fed sweep."""
+        k, t = C.c_int(0), C.c_int(0)
+        _check(_clib.sg_precond_get_sweep(self.handle, C.byref(k), C.byref(t)))
+        kinds = {0: "tma", 1: "level", 2: "syncfree", -1: "none"}
+        return {"sweep": kinds[k.value], "threads": t.value}
+
     def close(self):
         if getattr(self, "handle", None):
             _clib.sg_precond_destroy(self.handle)

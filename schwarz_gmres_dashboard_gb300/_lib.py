@@ -89,6 +89,7 @@ PROTOTYPES = {
     "sg_precond_get_decomposition": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _ip]),
     "sg_precond_get_factors": (C.c_int, [_vp, C.c_int, _ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
+    "sg_precond_get_sweep": (C.c_int, [_vp, _ip, _ip]),
     "sg_solve": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int,
                            C.POINTER(SolveParams), C.POINTER(SolveResult)]),
     "sg_solve_batched": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp, C.c_int,

@@ -626,6 +626,17 @@ sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc) {
     });
 }
 
+sg_status sg_precond_get_sweep(sg_precond* pc, int* sweep, int* threads) {
+    return guard([&] {
+        SG_CHECK_ARG(pc, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        const bool ilu = pc->kind != SG_PC_NONE && pc->kind != SG_PC_JACOBI;
+        const bool tma = ilu && pc->use_rec && pc->rec_depth > 0;
+        if (sweep) *sweep = !ilu ? -1 : (tma ? 0 : (pc->use_sf ? 2 : 1));
+        if (threads) *threads = tma ? (pc->sweep_threads > 0 ? pc->sweep_threads : 512) : 0;
+    });
+}
+
 // ------------------------------------------------------------------ solve
 sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* pc,
                    const double* b, double* x, int n, sg_mem mem, const sg_solve_params* params,

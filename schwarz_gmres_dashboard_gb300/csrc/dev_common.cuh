@@ -90,6 +90,96 @@ __device__ __forceinline__ void block_sum_multi(const T (&v)[NVMAX], int nv, dou
     __syncthreads();
 }
 
+// z = sum_q row[q] * r0[q] (the coarse term of a subdomain) summed by warp 0
+// in an order that does not depend on the block size, so every sweep variant
+// and block size gives the same bits: four lane-strided accumulators, then
+// the shuffle tree.  Call from the threads of warp 0 only.
+__device__ __forceinline__ double coarse_dot_warp0(const double* __restrict__ row,
+                                                   const double* __restrict__ r0, int nc) {
+    const int lane = threadIdx.x & 31;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int q = lane; q < nc; q += 128) {
+        a0 += row[q] * r0[q];
+        if (q + 32 < nc) a1 += row[q + 32] * r0[q + 32];
+        if (q + 64 < nc) a2 += row[q + 64] * r0[q + 64];
+        if (q + 96 < nc) a3 += row[q + 96] * r0[q + 96];
+    }
+    return warp_sum((a0 + a1) + (a2 + a3));
+}
+
+// ------------------------------------------------------- subdomain gather/scatter
+// Restriction x -> t over the n subdomain rows (t[tslot(li)] = x[dof[li]])
+// and the restricted prolongation of the owned rows (y[og[q]] =
+// t[tslot(ol[q])] (+ zc)); tslot with shift p (0: the identity).  `bs`
+// threads of the block take part; each keeps eight independent index and
+// value loads in flight, which the latency of a cold gather needs.
+constexpr int SUB_ILP = 8;
+
+template <class TS, class TI>
+__device__ __forceinline__ void gather_rows(TS* t, const TI* __restrict__ x,
+                                            const int* __restrict__ dof, int n, int bs,
+                                            int p = 0) {
+    int li = threadIdx.x;
+    for (; li + (SUB_ILP - 1) * bs < n; li += SUB_ILP * bs) {
+        int d[SUB_ILP];
+#pragma unroll
+        for (int u = 0; u < SUB_ILP; ++u) d[u] = dof[li + u * bs];
+        TI v[SUB_ILP];
+#pragma unroll
+        for (int u = 0; u < SUB_ILP; ++u) v[u] = x[d[u]];
+#pragma unroll
+        for (int u = 0; u < SUB_ILP; ++u) t[tslot(li + u * bs, p)] = Load<TS>::f(v[u]);
+    }
+    for (; li < n; li += bs) t[tslot(li, p)] = Load<TS>::f(x[dof[li]]);
+}
+
+// The coarse correction added to an owned row, in the precision of the
+// output: FP64 output adds in FP64 with the reference's rounding; FP32 output
+// adds (float)zc in FP32 (the sum is rounded to FP32 either way, and FP64
+// arithmetic per row would run on GB300's narrow FP64 pipe).
+template <class TO>
+struct CoarseAdd;
+template <>
+struct CoarseAdd<double> {
+    double z;
+    __device__ __forceinline__ explicit CoarseAdd(double zc) : z(zc) {}
+    template <class TS>
+    __device__ __forceinline__ double operator()(TS v) const { return __dadd_rn((double)v, z); }
+};
+template <>
+struct CoarseAdd<float> {
+    float z;
+    __device__ __forceinline__ explicit CoarseAdd(double zc) : z((float)zc) {}
+    template <class TS>
+    __device__ __forceinline__ float operator()(TS v) const { return Store<float>::f(v) + z; }
+};
+
+template <class TS, class TO>
+__device__ __forceinline__ void scatter_owned(const TS* t, TO* __restrict__ y,
+                                              const int* __restrict__ ol,
+                                              const int* __restrict__ og, int n_own, int coarse,
+                                              double zc, int bs, int p = 0) {
+    const CoarseAdd<TO> add(zc);
+    int q = threadIdx.x;
+    for (; q + (SUB_ILP - 1) * bs < n_own; q += SUB_ILP * bs) {
+        int l[SUB_ILP], g[SUB_ILP];
+#pragma unroll
+        for (int u = 0; u < SUB_ILP; ++u) {
+            l[u] = ol[q + u * bs];
+            g[u] = og[q + u * bs];
+        }
+#pragma unroll
+        for (int u = 0; u < SUB_ILP; ++u) {
+            const TS v = t[tslot(l[u], p)];
+            y[g[u]] = coarse ? add(v) : Store<TO>::f(v);
+        }
+    }
+    for (; q < n_own; q += bs) {
+        const TS v = t[tslot(ol[q], p)];
+        y[og[q]] = coarse ? add(v) : Store<TO>::f(v);
+    }
+}
+
 // Grid-level completion of a reduction: every block stores its nv block sums
 // (bsum, smem) into partials[block*nv + k]; the last block to arrive sums
 // them in block order (deterministic) into smem `out` and returns true.  The

@@ -157,54 +157,6 @@ k_pack(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
     }
 }
 
-// ---------------------------------------------------------------- gather / scatter
-// Restriction x -> t over the subdomain rows and restricted prolongation of
-// the owned rows, four independent index/value loads in flight per thread.
-template <class TS, class TI>
-__device__ __forceinline__ void gather_rows(TS* t, const TI* __restrict__ x,
-                                            const int* __restrict__ dof, int n) {
-    const int bs = blockDim.x;
-    int li = threadIdx.x;
-    for (; li + 3 * bs < n; li += 4 * bs) {
-        int d[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) d[u] = dof[li + u * bs];
-        TI v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = x[d[u]];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) t[li + u * bs] = Load<TS>::f(v[u]);
-    }
-    for (; li < n; li += bs) t[li] = Load<TS>::f(x[dof[li]]);
-}
-
-template <class TS, class TO>
-__device__ __forceinline__ void scatter_owned(const TS* t, TO* __restrict__ y,
-                                              const int* __restrict__ ol,
-                                              const int* __restrict__ og, int n_own, int coarse,
-                                              double zc) {
-    const int bs = blockDim.x;
-    int q = threadIdx.x;
-    for (; q + 3 * bs < n_own; q += 4 * bs) {
-        int l[4], g[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            l[u] = ol[q + u * bs];
-            g[u] = og[q + u * bs];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (coarse) y[g[u]] = Store<TO>::f(__dadd_rn((double)t[l[u]], zc));
-            else y[g[u]] = Store<TO>::f(t[l[u]]);
-        }
-    }
-    for (; q < n_own; q += bs) {
-        const int li = ol[q];
-        if (coarse) y[og[q]] = Store<TO>::f(__dadd_rn((double)t[li], zc));
-        else y[og[q]] = Store<TO>::f(t[li]);
-    }
-}
-
 // ---------------------------------------------------------------- sweeps
 // One triangular sweep of a subdomain held in shared memory `t`.  Rows of a
 // level are independent; a __syncthreads separates levels.  The factor
@@ -312,7 +264,6 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
         const int* __restrict__ sub_on) {
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double s_red[SWEEP_T / 32];
     __shared__ double s_zc;
     const int s = order[blockIdx.x];
     if (sub_on && !sub_on[s]) return;  // subdomain not needed by this apply
@@ -321,21 +272,15 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
     TS* t = use_smem ? reinterpret_cast<TS*>(smraw) : gscratch + inf.row_off + s;
     const int* dof = dofs + inf.row_off;
     // restriction R_s x (gather with overlap)
-    gather_rows<TS>(t, x, dof, n);
+    gather_rows<TS>(t, x, dof, n, blockDim.x);
     if (threadIdx.x == 0) t[n] = (TS)0;
     if (coarse) {
         // z0_s = (A0^{-1} r0)_s, scaled by the part's coarse basis value
-        double acc = 0.0;
-        const double* row = a0inv + (size_t)s * nc;
-        for (int q = threadIdx.x; q < nc; q += blockDim.x) acc += row[q] * r0[q];
-        acc = warp_sum(acc);
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double z = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) z += s_red[w];
-            s_zc = inf.cscale * z;
+        if (threadIdx.x < 32) {
+            const double z = coarse_dot_warp0(a0inv + (size_t)s * nc, r0, nc);
+            if (threadIdx.x == 0) s_zc = inf.cscale * z;
         }
+        __syncthreads();
     }
     __syncthreads();
     // forward sweep (unit lower triangle), then backward sweep (upper
@@ -350,7 +295,7 @@ k_sweep(const SubInfo* __restrict__ info, const int* __restrict__ order,
         // restricted prolongation: owned rows only (src/precond/ras.h:64-68)
         const int* ol = ownloc + inf.own_off;
         const int* og = owned_glob + inf.own_off;
-        scatter_owned<TS, TO>(t, y, ol, og, inf.n_own, coarse, zc);
+        scatter_owned<TS, TO>(t, y, ol, og, inf.n_own, coarse, zc, blockDim.x);
     } else {
         // additive prolongation of every row (src/precond/asm.h:138-142)
         for (int li = threadIdx.x; li < n; li += blockDim.x)
@@ -466,7 +411,6 @@ k_sweep_sf(const SubInfo* __restrict__ info, const int* __restrict__ order,
            const int* __restrict__ active, const int* __restrict__ sub_on) {
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double s_red[SWEEP_T / 32];
     __shared__ double s_zc;
     const int s = order[blockIdx.x];
     if (sub_on && !sub_on[s]) return;  // subdomain not needed by this apply
@@ -476,24 +420,18 @@ k_sweep_sf(const SubInfo* __restrict__ info, const int* __restrict__ order,
     volatile unsigned char* fl =
         smraw + (((size_t)(n + 1) * sizeof(TS) + 15) & ~(size_t)15);
     const int* dof = dofs + inf.row_off;
-    gather_rows<TS>(t, x, dof, n);
+    gather_rows<TS>(t, x, dof, n, blockDim.x);
     for (int li = threadIdx.x; li < n; li += blockDim.x) fl[li] = 0;
     if (threadIdx.x == 0) {
         t[n] = (TS)0;  // padded entries read this zero
         fl[n] = 2;
     }
     if (coarse) {
-        double acc = 0.0;
-        const double* row = a0inv + (size_t)s * nc;
-        for (int q = threadIdx.x; q < nc; q += blockDim.x) acc += row[q] * r0[q];
-        acc = warp_sum(acc);
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double z = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) z += s_red[w];
-            s_zc = inf.cscale * z;
+        if (threadIdx.x < 32) {
+            const double z = coarse_dot_warp0(a0inv + (size_t)s * nc, r0, nc);
+            if (threadIdx.x == 0) s_zc = inf.cscale * z;
         }
+        __syncthreads();
     }
     __syncthreads();
     sweep_sf<TS, TF, TC, false, EXACT>(t, fl, n, perm_f + inf.row_off, lcol + inf.fl_off,
@@ -506,7 +444,7 @@ k_sweep_sf(const SubInfo* __restrict__ info, const int* __restrict__ order,
     if (mode == 0) {
         const int* ol = ownloc + inf.own_off;
         const int* og = owned_glob + inf.own_off;
-        scatter_owned<TS, TO>(t, y, ol, og, inf.n_own, coarse, zc);
+        scatter_owned<TS, TO>(t, y, ol, og, inf.n_own, coarse, zc, blockDim.x);
     } else {
         for (int li = threadIdx.x; li < n; li += blockDim.x)
             atomicAdd(&y[dof[li]], Store<TO>::f(t[li]));

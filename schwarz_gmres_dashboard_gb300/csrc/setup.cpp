@@ -44,6 +44,59 @@ static int levels_upper(int n, const int* rp, const int* ci, const int* dg, int*
 }
 
 // rows sorted by level (stable): perm[p] = row, ptr[l] = first position of level l
+// Bank-conflict cost of the TMA sweep's loads of the subdomain vector t under
+// the slot layout tslot(., p): per level, each warp (32 consecutive rows)
+// loads t[r] and t[c_k] for k < w (padding columns read t[n]); a load costs
+// the largest number of distinct slots that share a bank (4-byte banks,
+// `words` banks per element).  Sums over both sweeps.
+static long long sweep_bank_cost(int n, const int* lrp, const int* lci, const int* ldg,
+                                 const int* perm_f, const int* ptr_f, int nlf,
+                                 const int* perm_b, const int* ptr_b, int nlb, int wl, int wu,
+                                 int p, int words) {
+    long long cost = 0;
+    int slots[32], cnt[32];
+    auto load_cost = [&](int m) {
+        // distinct slots per bank group
+        std::sort(slots, slots + m);
+        for (int b = 0; b < 32; ++b) cnt[b] = 0;
+        int mx = 0;
+        for (int i = 0; i < m; ++i) {
+            if (i > 0 && slots[i] == slots[i - 1]) continue;
+            const int b = (int)(((long long)slots[i] * words) % 32) / words;
+            mx = std::max(mx, ++cnt[b]);
+        }
+        return mx;
+    };
+    for (int pass = 0; pass < 2; ++pass) {
+        const int* perm = pass ? perm_b : perm_f;
+        const int* ptr = pass ? ptr_b : ptr_f;
+        const int nl = pass ? nlb : nlf, w = pass ? wu : wl;
+        for (int l = 0; l < nl; ++l) {
+            for (int q0 = ptr[l]; q0 < ptr[l + 1]; q0 += 32) {
+                const int m = std::min(32, ptr[l + 1] - q0);
+                for (int i = 0; i < m; ++i) slots[i] = tslot(perm[q0 + i], p);
+                cost += load_cost(m);
+                for (int k = 0; k < w; ++k) {
+                    for (int i = 0; i < m; ++i) {
+                        const int r = perm[q0 + i];
+                        int col = n;
+                        if (pass == 0) {
+                            const int e = lrp[r] + k;
+                            if (e < lrp[r + 1] && lci[e] < r) col = lci[e];
+                        } else {
+                            const int e = ldg[r] + 1 + k;
+                            if (e < lrp[r + 1]) col = lci[e];
+                        }
+                        slots[i] = tslot(col, p);
+                    }
+                    cost += load_cost(m);
+                }
+            }
+        }
+    }
+    return cost;
+}
+
 static void level_order(int n, const int* lev, int nlev, std::vector<int>& perm,
                         std::vector<int>& ptr) {
     ptr.assign(nlev + 1, 0);
@@ -133,7 +186,7 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
     std::vector<int> perm_f_all(pc->sub.size()), perm_b_all(pc->sub.size());
     std::vector<int> loc(n, -1);
     long long fl_total = 0, fu_total = 0;
-    int max_n = 0;
+    int max_n = 0, t_len = 0;
     std::vector<int> perm, ptr;
     for (int s = 0; s < nparts; ++s) {
         const int off = pc->sub_ptr[s];
@@ -192,6 +245,27 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
         level_order(ns, up, nlb, perm, ptr);
         std::copy(perm.begin(), perm.end(), perm_b_all.begin() + off);
         pc->h_lev_ptr_b.insert(pc->h_lev_ptr_b.end(), ptr.begin(), ptr.end());
+        // slot layout of the TMA-fed sweep: the cheapest of none / one pad
+        // word per 32 / per 16 rows under the bank model (slots stay 16-bit)
+        {
+            const int words = pc->opts.sweep_dtype == SG_FP64 ? 2 : 1;
+            const int* dgl = pc->ldiag.data() + off;
+            const int* pf = perm_f_all.data() + off;
+            const int* pff = pc->h_lev_ptr_f.data() + inf.lev_off_f;
+            const int* pfb = pc->h_lev_ptr_b.data() + inf.lev_off_b;
+            inf.tshift = 0;
+            long long best = -1;
+            for (int p : {0, 5, 4}) {
+                if (tslot(ns, p) > 65535) continue;
+                const long long c = sweep_bank_cost(ns, lrp, lci, dgl, pf, pff, nlf, perm.data(),
+                                                    pfb, nlb, wl, wu, p, words);
+                if (best < 0 || c < best) {
+                    best = c;
+                    inf.tshift = p;
+                }
+            }
+        }
+        t_len = std::max(t_len, tslot(ns, inf.tshift) + 1);
         inf.fl_off = fl_total;
         inf.fu_off = fu_total;
         fl_total += (long long)wl * ns;
@@ -205,6 +279,7 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
     pc->fl_total = fl_total > 0 ? fl_total : 1;
     pc->fu_total = fu_total > 0 ? fu_total : 1;
     pc->max_n = max_n;
+    pc->t_len = t_len;
     pc->total_rows = (long long)pc->sub.size();
     pc->wide_cols = max_n > 65534;
     if (pc->wide_cols) {

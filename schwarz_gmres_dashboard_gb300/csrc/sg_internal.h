@@ -213,7 +213,13 @@ struct SubInfo {
     int csr_row_off;        // offset into the local CSR row_ptr array (n+1 per sub)
     long long csr_nz_off;   // offset into the local CSR entries
     double cscale;          // 1/sqrt(|owned|) (two-level)
+    int tshift;             // TMA sweep: row r sits in shared slot r + (r >> tshift) (0: r)
 };
+
+// Shared-memory slot of subdomain row r in the TMA-fed sweep: one unused word
+// every 2^p rows (p = 0: none), chosen per subdomain so that the rows of a
+// level -- a fixed stride apart in a box subdomain -- fall in distinct banks.
+__host__ __device__ __forceinline__ int tslot(int r, int p) { return p ? r + (r >> p) : r; }
 
 }  // namespace sg
 
@@ -238,6 +244,7 @@ struct sg_precond {
     bool wide_cols = false;  // subdomains above 65534 rows use 32-bit local indices
     long long fl_total = 0, fu_total = 0;
     int max_n = 0;
+    int t_len = 0;       // TMA sweep: largest tslot(n_s, tshift_s) + 1
     int max_levels = 0;  // largest nlev_f + nlev_b of a subdomain
     long long total_rows = 0;
     bool use_smem = true;

@@ -8,14 +8,17 @@
 // separates levels.
 //
 // A level's factor data is one contiguous, 16-byte-aligned record
-//   [row index u16 x C][column u16 x C x w][value x C x w](diagonal x C)
-// (C = rows rounded up to 8).  Thread 0 streams the records into a ring of D
-// shared-memory stages with cp.async.bulk, D levels ahead of the level being
-// computed, each stage tracked by an mbarrier (expect_tx / complete_tx).  So
-// a level costs shared-memory latency plus one barrier instead of a
-// global-memory round trip.  Every mbarrier wait is bounded (about one second
-// of clock cycles); on expiry the CTA records an error word, waits (bounded
-// again) for the copies it issued, and returns without touching the output.
+//   [row slot u16 x C][column slot u16 x C x w][value x C x w](diagonal x C)
+// (C = rows rounded up to 8; a slot is the row's place in the shared-memory
+// vector, tslot, whose per-subdomain padding keeps the rows of a level in
+// distinct banks).  The block's last thread streams the records into a ring
+// of D shared-memory stages with cp.async.bulk, D levels ahead of the level
+// being computed, each stage tracked by an mbarrier (expect_tx /
+// complete_tx).  So a level costs shared-memory latency plus one barrier
+// instead of a global-memory round trip.  Every mbarrier wait is bounded
+// (about one second of clock cycles); on expiry the CTA records an error
+// word, waits (bounded again) for the copies it issued, and returns without
+// touching the output.
 #include "dev_common.cuh"
 #include "kernels.h"
 
@@ -98,6 +101,132 @@ __device__ __forceinline__ uint16_t to_factor<uint16_t>(double v) {
     return __bfloat16_as_ushort(__float2bfloat16_rn((float)v));
 }
 
+// ---- shared-memory accesses by 32-bit shared-window address.  The level
+// loop's row updates are chains of dependent shared-memory loads; explicit
+// 32-bit addressing keeps the address arithmetic between them short.
+__device__ __forceinline__ uint32_t lds_u16(uint32_t a) {
+    uint16_t v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(a) : "memory");
+    return v;
+}
+template <class T>
+__device__ __forceinline__ T lds(uint32_t a);
+template <>
+__device__ __forceinline__ float lds<float>(uint32_t a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ double lds<double>(uint32_t a) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ uint16_t lds<uint16_t>(uint32_t a) {
+    return (uint16_t)lds_u16(a);
+}
+__device__ __forceinline__ void sts(uint32_t a, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ void sts(uint32_t a, double v) {
+    asm volatile("st.shared.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+
+// The rows of one level record with W nonzeros per row (W fixed: the 5-, 7-
+// and 9-point stencils give 2, 3 and 4).  Record at shared address R:
+//   rows u16[C] | columns u16[W][C] | values TF[W][C] | (diagonal TF[C]).
+// A row computes acc = t[r]; acc -= v_k t[c_k] for k = 0..W-1 in order;
+// backward: acc /= d -- every load of the row issued before the first
+// multiply-add.  Row and column entries are shared-memory slots of t
+// (tslot); padding entries hold the slot of row n, where t is 0, and value 0.
+template <int W, bool BACK, class TS, class TF, bool EXACT>
+__device__ __forceinline__ void level_rows_w(uint32_t tb, uint32_t R, int C, int c, int nthreads) {
+    constexpr uint32_t SF = sizeof(TF), ST = sizeof(TS);
+    const uint32_t cstride = 2u * (uint32_t)C;
+    const uint32_t vbase = R + cstride * (uint32_t)(1 + W);
+    const uint32_t vstride = SF * (uint32_t)C;
+    for (int q = threadIdx.x; q < c; q += nthreads) {
+        const uint32_t rq = R + 2u * (uint32_t)q;
+        const uint32_t vq = vbase + SF * (uint32_t)q;
+        const uint32_t r = lds_u16(rq);
+        uint32_t ck[W];
+        TF vk[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) ck[k] = lds_u16(rq + cstride * (uint32_t)(k + 1));
+#pragma unroll
+        for (int k = 0; k < W; ++k) vk[k] = lds<TF>(vq + vstride * (uint32_t)k);
+        TF dg{};
+        if (BACK) dg = lds<TF>(vq + vstride * (uint32_t)W);
+        TS acc = lds<TS>(tb + ST * r);
+        TS xk[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) xk[k] = lds<TS>(tb + ST * ck[k]);
+#pragma unroll
+        for (int k = 0; k < W; ++k) acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vk[k]), xk[k]);
+        if (BACK) acc = acc / Load<TS>::f(dg);
+        sts(tb + ST * r, acc);
+    }
+}
+
+// Any width w: the same row computation through generic pointers, the loads
+// of four nonzeros at a time.
+template <class TS, class TF, bool EXACT>
+__device__ __forceinline__ void level_rows_any(TS* t, const unsigned char* R, int C, int c,
+                                               int w, bool back, int nthreads) {
+    const uint16_t* rr = reinterpret_cast<const uint16_t*>(R);
+    const uint16_t* cc = rr + C;
+    const TF* vv = reinterpret_cast<const TF*>(cc + (size_t)C * w);
+    for (int q = threadIdx.x; q < c; q += nthreads) {
+        const int r = rr[q];
+        TS acc = t[r];
+        for (int k0 = 0; k0 < w; k0 += 4) {
+            int ci[4];
+            TF vi[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int o = (k0 + u < w ? k0 + u : k0) * C + q;
+                ci[u] = cc[o];
+                vi[u] = vv[o];
+            }
+            TS xi[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xi[u] = t[ci[u]];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (k0 + u < w) acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vi[u]), xi[u]);
+        }
+        if (back) acc = acc / Load<TS>::f(vv[w * C + q]);
+        t[r] = acc;
+    }
+}
+
+// One level: the fixed-width row code for w = 2, 3, 4, else the generic one
+// (t / t_s: the subdomain vector as generic pointer / shared address; R /
+// R_s: the level record likewise).
+template <class TS, class TF, bool EXACT>
+__device__ __forceinline__ void level_rows(TS* t, uint32_t t_s, const unsigned char* R,
+                                           uint32_t R_s, int C, int c, int w, bool back,
+                                           int nthreads) {
+    switch (w) {
+    case 2:
+        if (back) level_rows_w<2, true, TS, TF, EXACT>(t_s, R_s, C, c, nthreads);
+        else level_rows_w<2, false, TS, TF, EXACT>(t_s, R_s, C, c, nthreads);
+        return;
+    case 3:
+        if (back) level_rows_w<3, true, TS, TF, EXACT>(t_s, R_s, C, c, nthreads);
+        else level_rows_w<3, false, TS, TF, EXACT>(t_s, R_s, C, c, nthreads);
+        return;
+    case 4:
+        if (back) level_rows_w<4, true, TS, TF, EXACT>(t_s, R_s, C, c, nthreads);
+        else level_rows_w<4, false, TS, TF, EXACT>(t_s, R_s, C, c, nthreads);
+        return;
+    default:
+        level_rows_any<TS, TF, EXACT>(t, R, C, c, w, back, nthreads);
+    }
+}
+
 // Factored local CSR (FP64, reference layout) -> level records of type TF.
 template <class TF>
 __global__ void __launch_bounds__(256)
@@ -124,11 +253,11 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
             int k = 0;
             if (q < c) {
                 const int r = perm_f[inf.row_off + p0 + q];
-                rr[q] = (uint16_t)r;
+                rr[q] = (uint16_t)tslot(r, inf.tshift);
                 for (int e = rp[r]; e < rp[r + 1] && k < inf.wl; ++e) {
                     const int col = ci[e];
                     if (col >= r) break;
-                    cc[(size_t)k * C + q] = (uint16_t)col;
+                    cc[(size_t)k * C + q] = (uint16_t)tslot(col, inf.tshift);
                     vv[(size_t)k * C + q] = to_factor<TF>(v[e]);
                     ++k;
                 }
@@ -136,7 +265,7 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
                 rr[q] = 0;
             }
             for (; k < inf.wl; ++k) {
-                cc[(size_t)k * C + q] = (uint16_t)inf.n;
+                cc[(size_t)k * C + q] = (uint16_t)tslot(inf.n, inf.tshift);
                 vv[(size_t)k * C + q] = to_factor<TF>(0.0);
             }
         }
@@ -153,9 +282,9 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
             int k = 0;
             if (q < c) {
                 const int r = perm_b[inf.row_off + p0 + q];
-                rr[q] = (uint16_t)r;
+                rr[q] = (uint16_t)tslot(r, inf.tshift);
                 for (int e = dg[r] + 1; e < rp[r + 1] && k < inf.wu; ++e) {
-                    cc[(size_t)k * C + q] = (uint16_t)ci[e];
+                    cc[(size_t)k * C + q] = (uint16_t)tslot(ci[e], inf.tshift);
                     vv[(size_t)k * C + q] = to_factor<TF>(v[e]);
                     ++k;
                 }
@@ -165,7 +294,7 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
                 dd[q] = to_factor<TF>(1.0);
             }
             for (; k < inf.wu; ++k) {
-                cc[(size_t)k * C + q] = (uint16_t)inf.n;
+                cc[(size_t)k * C + q] = (uint16_t)tslot(inf.n, inf.tshift);
                 vv[(size_t)k * C + q] = to_factor<TF>(0.0);
             }
         }
@@ -190,7 +319,7 @@ struct RecArgs {
     int nc;
     int depth;
     int stage_bytes;
-    int max_n;
+    int t_len;       // elements of the subdomain vector region (largest tslot(n) + 1)
     int max_levels;  // largest nlev_f + nlev_b over the subdomains
     int* err;
     const int* sub_on;  // optional per-subdomain switch (0: the subdomain is skipped)
@@ -198,16 +327,15 @@ struct RecArgs {
 
 // mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
 template <class TI, class TO, class TS, class TF, bool EXACT>
-__global__ void __launch_bounds__(SW_T, 1)
+__global__ void __launch_bounds__(SW_T, 2)
 k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, int coarse,
             const int* __restrict__ active) {
     if (active && *active == 0) return;
     extern __shared__ __align__(128) unsigned char smraw[];
-    __shared__ double s_red[SW_T / 32];
     __shared__ double s_zc;
-    __shared__ int s_fail;
     const int D = a.depth;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // D x 8 B
+    const int NC = (int)blockDim.x;
     unsigned char* stages = smraw + 128;                               // D x stage_bytes
     TS* t = reinterpret_cast<TS*>(stages + (size_t)D * a.stage_bytes);  // n + 1
     const int s = a.order[blockIdx.x];
@@ -219,7 +347,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     // per-level metadata of both sweeps, staged once: rows, padded rows,
     // record offset (so the level loop touches global memory only through TMA)
     long long* m_off = reinterpret_cast<long long*>(
-        reinterpret_cast<unsigned char*>(t) + (((size_t)(a.max_n + 1) * sizeof(TS) + 15) & ~(size_t)15));
+        reinterpret_cast<unsigned char*>(t) + (((size_t)a.t_len * sizeof(TS) + 15) & ~(size_t)15));
     int* m_c = reinterpret_cast<int*>(m_off + a.max_levels);
     int* m_C = m_c + a.max_levels;
     for (int g = threadIdx.x; g < T; g += blockDim.x) {
@@ -235,90 +363,79 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             m_off[g] = a.off_b[i];
         }
     }
-    if (threadIdx.x == 0) s_fail = 0;
     __syncthreads();
 
     const uint32_t bytes_f = (uint32_t)(2 + inf.wl * (2 + sf));
     const uint32_t bytes_b = (uint32_t)(2 + inf.wu * (2 + sf) + sf);
-    auto issue = [&](int g) {
+    // copy level g's record into ring stage st (= g mod D)
+    auto issue = [&](int g, int st) {
         const uint32_t bytes = (uint32_t)m_C[g] * (g < nf ? bytes_f : bytes_b);
-        const int st = g % D;
         const uint32_t bar = smem_u32(&bars[st]);
         mbar_expect_tx(bar, bytes);
         bulk_g2s(smem_u32(stages + (size_t)st * a.stage_bytes), a.rec + m_off[g], bytes, bar);
     };
 
     // the producer is the block's last thread: levels rarely have rows for
-    // it, so issuing the next copy overlaps the other threads' work
+    // it, so issuing the next copy overlaps the other threads' work (a
+    // separate producer warp, signalled through per-stage "empty" mbarriers,
+    // measured slower at every block size)
     const bool producer = threadIdx.x == blockDim.x - 1;
     if (producer) {
         for (int i = 0; i < D; ++i) mbar_init(smem_u32(&bars[i]), 1);
         fence_mbar_init();
         fence_proxy_async();
         const int pre = T < D ? T : D;
-        for (int g = 0; g < pre; ++g) issue(g);
+        for (int g = 0; g < pre; ++g) issue(g, g);
     }
-    // gather while the first records are in flight (four loads in flight)
+    // gather while the first records are in flight
     const int* dof = a.dofs + inf.row_off;
-    {
-        const int bs = blockDim.x;
-        int li = threadIdx.x;
-        for (; li + 3 * bs < n; li += 4 * bs) {
-            int d[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) d[u] = dof[li + u * bs];
-            TI v[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = x[d[u]];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) t[li + u * bs] = Load<TS>::f(v[u]);
-        }
-        for (; li < n; li += bs) t[li] = Load<TS>::f(x[dof[li]]);
-    }
-    if (threadIdx.x == 0) t[n] = (TS)0;
+    const int tp = inf.tshift;
+    gather_rows<TS>(t, x, dof, n, NC, tp);
+    if (threadIdx.x == 0) t[tslot(n, tp)] = (TS)0;
     if (coarse) {
-        double acc = 0.0;
-        const double* row = a.a0inv + (size_t)s * a.nc;
-        for (int q = threadIdx.x; q < a.nc; q += blockDim.x) acc += row[q] * a.r0[q];
-        acc = warp_sum(acc);
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double z = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) z += s_red[w];
-            s_zc = inf.cscale * z;
+        if (threadIdx.x < 32) {
+            const double z = coarse_dot_warp0(a.a0inv + (size_t)s * a.nc, a.r0, a.nc);
+            if (threadIdx.x == 0) s_zc = inf.cscale * z;
         }
+        __syncthreads();
     }
     __syncthreads();
 
+    // The level loop is the latency chain of the sweep: ring stage and phase
+    // advance without divisions, the next level's row counts load while this
+    // level computes, a failed wait travels in the level barrier itself, and
+    // every thread observes the ring's mbarriers (acquiring the bulk copies)
+    // K = D/2 levels at a time: the copy of level g + K - 1 was issued after
+    // the barrier of level g + K - 1 - D < g, so it is in flight already.
+    const int K = D / 2 > 1 ? D / 2 : 1;
+    const uint32_t stages_s = smem_u32(stages), t_s = smem_u32(t);
+    int st = 0, grp = 0;
+    uint32_t ph = 0;
+    int c = T > 0 ? m_c[0] : 0, C = T > 0 ? m_C[0] : 0;
     for (int g = 0; g < T; ++g) {
-        const int st = g % D;
-        // every thread observes the phase itself (acquires the bulk copy); a
-        // thread whose wait expires computes nothing and raises the flag
-        const bool ok = mbar_wait(smem_u32(&bars[st]), (uint32_t)((g / D) & 1), WAIT_CYCLES);
-        if (ok) {
-            const unsigned char* R = stages + (size_t)st * a.stage_bytes;
-            const bool back = g >= nf;
-            const int c = m_c[g];
-            const int C = m_C[g];
-            const int w = back ? inf.wu : inf.wl;
-            const uint16_t* rr = reinterpret_cast<const uint16_t*>(R);
-            const uint16_t* cc = rr + C;
-            const TF* vv = reinterpret_cast<const TF*>(cc + (size_t)C * w);
-            for (int q = threadIdx.x; q < c; q += blockDim.x) {
-                const int r = rr[q];
-                TS acc = t[r];
-                for (int k = 0; k < w; ++k)
-                    acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vv[(size_t)k * C + q]),
-                                             t[cc[(size_t)k * C + q]]);
-                if (back) acc = acc / Load<TS>::f(vv[(size_t)w * C + q]);
-                t[r] = acc;
+        // a thread whose wait expires computes nothing and fails the barrier
+        bool ok = true;
+        if (grp == 0) {
+            grp = T - g < K ? T - g : K;
+            int s2 = st;
+            uint32_t p2 = ph;
+            for (int h = 0; h < grp && ok; ++h) {
+                ok = mbar_wait(smem_u32(&bars[s2]), p2, WAIT_CYCLES);
+                if (++s2 == D) {
+                    s2 = 0;
+                    p2 ^= 1u;
+                }
             }
-        } else {
-            s_fail = 1;
         }
-        __syncthreads();
-        if (s_fail) {
+        --grp;
+        const int cn = g + 1 < T ? m_c[g + 1] : 0, Cn = g + 1 < T ? m_C[g + 1] : 0;
+        if (ok) {
+            const bool back = g >= nf;
+            const uint32_t off = (uint32_t)st * (uint32_t)a.stage_bytes;
+            level_rows<TS, TF, EXACT>(t, t_s, stages + off, stages_s + off, C, c,
+                                      back ? inf.wu : inf.wl, back, NC);
+        }
+        if (__syncthreads_or(ok ? 0 : 1)) {
             // a record never arrived: report, drain what was issued, leave y alone
             if (producer) {
                 atomicExch(a.err, 1);
@@ -328,42 +445,29 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             }
             return;
         }
+        // stage st is free again: refill it with level g + D
         if (producer && g + D < T) {
             fence_proxy_async();
-            issue(g + D);
+            issue(g + D, st);
+        }
+        c = cn;
+        C = Cn;
+        if (++st == D) {
+            st = 0;
+            ph ^= 1u;
         }
     }
 
     const double zc = coarse ? s_zc : 0.0;
     if (mode == 0) {
-        const int* ol = a.ownloc + inf.own_off;
-        const int* og = a.owned + inf.own_off;
-        const int bs = blockDim.x;
-        int q = threadIdx.x;
-        for (; q + 3 * bs < inf.n_own; q += 4 * bs) {
-            int l[4], g[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                l[u] = ol[q + u * bs];
-                g[u] = og[q + u * bs];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (coarse) y[g[u]] = Store<TO>::f(__dadd_rn((double)t[l[u]], zc));
-                else y[g[u]] = Store<TO>::f(t[l[u]]);
-            }
-        }
-        for (; q < inf.n_own; q += bs) {
-            const int li = ol[q];
-            if (coarse) y[og[q]] = Store<TO>::f(__dadd_rn((double)t[li], zc));
-            else y[og[q]] = Store<TO>::f(t[li]);
-        }
+        scatter_owned<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
+                              coarse, zc, NC, tp);
     } else {
-        for (int li = threadIdx.x; li < n; li += blockDim.x)
-            atomicAdd(&y[dof[li]], Store<TO>::f(t[li]));
+        for (int li = threadIdx.x; li < n; li += NC)
+            atomicAdd(&y[dof[li]], Store<TO>::f(t[tslot(li, tp)]));
         if (coarse) {
             const int* og = a.owned + inf.own_off;
-            for (int q = threadIdx.x; q < inf.n_own; q += blockDim.x)
+            for (int q = threadIdx.x; q < inf.n_own; q += NC)
                 atomicAdd(&y[og[q]], Store<TO>::f(zc));
         }
     }
@@ -388,7 +492,7 @@ RecArgs rec_args(sg_precond* pc) {
     a.nc = pc->nc;
     a.depth = pc->rec_depth;
     a.stage_bytes = (int)pc->rec_stage_bytes;
-    a.max_n = pc->max_n;
+    a.t_len = pc->t_len;
     a.max_levels = pc->max_levels;
     a.err = pc->err_d.p;
     a.sub_on = pc->sub_on;
@@ -397,7 +501,7 @@ RecArgs rec_args(sg_precond* pc) {
 
 size_t sweep_smem(const sg_precond* pc, int depth) {
     const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
-    const size_t tbytes = ((size_t)(pc->max_n + 1) * ts + 15) & ~(size_t)15;
+    const size_t tbytes = ((size_t)pc->t_len * ts + 15) & ~(size_t)15;
     return 128 + (size_t)depth * (size_t)pc->rec_stage_bytes + tbytes +
            (size_t)pc->max_levels * 16;
 }
@@ -405,9 +509,9 @@ size_t sweep_smem(const sg_precond* pc, int depth) {
 template <class TI, class TO, class TS, class TF, bool EXACT>
 void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active) {
     const size_t smem = sweep_smem(pc, pc->rec_depth);
+    const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
     SG_CUDA(cudaFuncSetAttribute(k_sweep_tma<TI, TO, TS, TF, EXACT>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
     k_sweep_tma<TI, TO, TS, TF, EXACT><<<pc->nparts, nt, smem, pc->ctx->stream>>>(
         rec_args(pc), x, y, mode, coarse ? 1 : 0, active);
     SG_CUDA(cudaGetLastError());
@@ -475,8 +579,11 @@ void rec_setup_device(sg_precond* pc) {
     // 3D subdomain hold ~100+ rows, those of a small 2D one ~20: a 512-thread
     // block then idles at every level barrier, while narrower blocks let more
     // subdomains run at once on an SM.
-    if (pc->opts.reserved[1] > 0) pc->sweep_threads = pc->opts.reserved[1];
-    else tune_sweep_threads(pc);
+    if (pc->opts.reserved[1] > 0) {
+        pc->sweep_threads = pc->opts.reserved[1];
+    } else {
+        tune_sweep_threads(pc);
+    }
 }
 
 // Times the sweep (RAS mode, no coarse term, zero input) with 128, 256 and
@@ -523,7 +630,7 @@ void tune_sweep_threads(sg_precond* pc) {
             cudaEventDestroy(e1);
             SG_CUDA(e);
         }
-        if (nt == SW_T || ms < best) {
+        if (nt == 512 || ms < best) {
             best = ms;
             best_nt = nt;
         }
