@@ -70,6 +70,8 @@ __device__ __forceinline__ T warp_sum(T v) {
 
 // Sum `nv` per-thread values over the block into smem out[0..nv).  `red` is
 // smem scratch of (blockDim.x/32) * nv doubles.  Fixed order: deterministic.
+// The in-warp tree runs in T (FP32 values stay off GB300's narrow FP64
+// pipe); the warp sums are combined in FP64.
 template <int NVMAX, class T>
 __device__ __forceinline__ void block_sum_multi(const T (&v)[NVMAX], int nv, double* red,
                                                 double* out) {
@@ -77,7 +79,7 @@ __device__ __forceinline__ void block_sum_multi(const T (&v)[NVMAX], int nv, dou
 #pragma unroll
     for (int k = 0; k < NVMAX; ++k) {
         if (k < nv) {
-            double s = warp_sum((double)v[k]);
+            const double s = (double)warp_sum(v[k]);
             if (lane == 0) red[warp * nv + k] = s;
         }
     }

@@ -148,14 +148,15 @@ __device__ __forceinline__ TV dotv(const TV (&a)[Vec<TV>::N], const TV (&b)[Vec<
     return s;
 }
 
-// per-warp accumulators -> block sums bs[k] (k < kc), fixed order
+// per-warp accumulators -> block sums bs[k] (k < kc), fixed order; the warp
+// tree runs in the basis precision, its result is kept in FP64
 template <class TV>
 __device__ __forceinline__ void warp_split_sums(const TV (&acc)[KPW], int kc, double* bs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < KPW; ++q) {
         const int k = warp + KW * q;
-        const double v = warp_sum((double)acc[q]);
+        const double v = (double)warp_sum(acc[q]);
         if (lane == 0 && k < kc) bs[k] = v;
     }
     __syncthreads();
@@ -387,7 +388,7 @@ k_upd_norm(const TV* __restrict__ raw, size_t ldv, int n, int j, int m, TV* __re
     }
     __shared__ double red[KT / 32];
     __shared__ double bs[1], tot[1];
-    double v1[1] = {(double)ss};
+    TV v1[1] = {ss};
     block_sum_multi<1>(v1, 1, red, bs);
     if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0)
         arnoldi_finalize(st, j, m, tot[0], hist, hist_cap);
@@ -399,14 +400,14 @@ __global__ void __launch_bounds__(KT)
 k_cycle_init(const TV* __restrict__ raw0, int n, SolveState* st, int m, int flexible,
              double* partials, unsigned* counter) {
     if (st->done) return;
-    double ss = 0.0;
+    TV ss = (TV)0;  // per-thread sum in the basis precision
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double t = (double)raw0[i];
+        const TV t = raw0[i];
         ss += t * t;
     }
     __shared__ double red[KT / 32];
     __shared__ double bs[1], tot[1];
-    double v1[1] = {ss};
+    TV v1[1] = {ss};
     block_sum_multi<1>(v1, 1, red, bs);
     if (!last_block_reduce(partials, counter, bs, 1, tot)) return;
     const int ld = m + 1;

@@ -607,7 +607,9 @@ k_restrict(const int* __restrict__ owned_ptr, const int* __restrict__ owned,
     if (active && *active == 0) return;
     __shared__ double red[32];
     const int s = blockIdx.x;
-    // four independent gathers in flight per thread, summed in a fixed order
+    // four independent gathers in flight per thread, summed in a fixed order;
+    // the per-thread and in-warp sums run in the input precision, the warp
+    // sums are combined in FP64
     TI a[4] = {(TI)0, (TI)0, (TI)0, (TI)0};
     const int q0 = owned_ptr[s], q1 = owned_ptr[s + 1];
     int q = q0 + threadIdx.x;
@@ -616,8 +618,7 @@ k_restrict(const int* __restrict__ owned_ptr, const int* __restrict__ owned,
         for (int u = 0; u < 4; ++u) a[u] += x[owned[q + u * blockDim.x]];
     }
     for (; q < q1; q += blockDim.x) a[0] += x[owned[q]];
-    double acc = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
-    acc = warp_sum(acc);
+    const double acc = (double)warp_sum((a[0] + a[1]) + (a[2] + a[3]));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
