@@ -200,12 +200,48 @@ __device__ __forceinline__ bool last_block_reduce(double* partials, unsigned* co
     __threadfence();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nb = gridDim.x;
-    for (int k = warp; k < nv; k += nw) {
-        double s = 0.0;
-#pragma unroll 8
-        for (int b = lane; b < nb; b += 32) s += __ldcg(&partials[(size_t)b * nv + k]);
-        s = warp_sum(s);
-        if (lane == 0) out[k] = s;
+    // per lane the partials are added in block order, as a plain loop would;
+    // the loads run ahead: sixteen per lane for one value per warp, else
+    // four values k = k0 + nw * kk per warp with four partials each
+    if (nv <= nw) {
+        if (warp < nv) {
+            double s = 0.0;
+            for (int b0 = lane; b0 < nb; b0 += 32 * 16) {
+                double v[16];
+#pragma unroll
+                for (int r = 0; r < 16; ++r) {
+                    const int b = b0 + 32 * r;
+                    v[r] = b < nb ? __ldcg(&partials[(size_t)b * nv + warp]) : 0.0;
+                }
+#pragma unroll
+                for (int r = 0; r < 16; ++r)
+                    if (b0 + 32 * r < nb) s += v[r];
+            }
+            s = warp_sum(s);
+            if (lane == 0) out[warp] = s;
+        }
+    } else for (int k0 = warp; k0 < nv; k0 += 4 * nw) {
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int b0 = lane; b0 < nb; b0 += 32 * 4) {
+            double v[4][4];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int b = b0 + 32 * r, k = k0 + nw * kk;
+                    v[kk][r] = (b < nb && k < nv) ? __ldcg(&partials[(size_t)b * nv + k]) : 0.0;
+                }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (b0 + 32 * r < nb) s[kk] += v[kk][r];
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            const double t = warp_sum(s[kk]);
+            if (lane == 0 && k0 + nw * kk < nv) out[k0 + nw * kk] = t;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) *counter = 0u;

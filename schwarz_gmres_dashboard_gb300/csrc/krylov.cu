@@ -134,11 +134,18 @@ __device__ __forceinline__ void vstore<float>(float* p, const float (&o)[4]) {
 }
 
 // ---- pass A (and generic second dots): s_k = raw_{k0+k} . w for k < kc.
-// The kc <= 32 vectors are split over the 8 warps of a block (vector k is
-// handled by warp k % 8), so a thread keeps at most 4 accumulators; a row
-// tile is 32 lanes x one 16-byte vector of elements.
+// A row tile is 32 lanes x one 16-byte vector of elements.  The kc <= 32
+// vectors of a launch are spread over a group of nwg warps that share a tile
+// (vector k is held by warp k % nwg of the group, so a thread keeps at most 4
+// accumulators); the block's 8 / nwg groups walk different tiles, so a step
+// with few vectors still keeps every warp loading.
 constexpr int KW = KT / 32;  // warps per block
 constexpr int KPW = 4;       // basis vectors per warp
+
+// warps per tile group: the fewest that hold kc vectors at KPW per warp
+__device__ __forceinline__ int warps_per_tile(int kc) {
+    return kc <= KPW ? 1 : (kc <= 2 * KPW ? 2 : (kc <= 4 * KPW ? 4 : 8));
+}
 
 template <class TV>
 __device__ __forceinline__ TV dotv(const TV (&a)[Vec<TV>::N], const TV (&b)[Vec<TV>::N]) {
@@ -148,18 +155,38 @@ __device__ __forceinline__ TV dotv(const TV (&a)[Vec<TV>::N], const TV (&b)[Vec<
     return s;
 }
 
-// per-warp accumulators -> block sums bs[k] (k < kc), fixed order; the warp
-// tree runs in the basis precision, its result is kept in FP64
+// per-warp accumulators -> block sums bs[k] (k < kc): the warp trees run in
+// the basis precision, the groups' sums of vector k are added in FP64 in
+// group order (fixed: deterministic)
 template <class TV>
-__device__ __forceinline__ void warp_split_sums(const TV (&acc)[KPW], int kc, double* bs) {
+__device__ __forceinline__ void group_sums(const TV (&acc)[KPW], int kc, int nwg, double* bs) {
+    __shared__ double red[KW][KPW];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < KPW; ++q) {
-        const int k = warp + KW * q;
         const double v = (double)warp_sum(acc[q]);
-        if (lane == 0 && k < kc) bs[k] = v;
+        if (lane == 0) red[warp][q] = v;
     }
     __syncthreads();
+    if ((int)threadIdx.x < kc) {
+        const int k = threadIdx.x, slot = k % nwg, q = k / nwg;
+        double v = red[slot][q];
+        for (int g = 1; g < KW / nwg; ++g) v += red[g * nwg + slot][q];
+        bs[k] = v;
+    }
+    __syncthreads();
+}
+
+// barrier among the nwg >= 2 warps of tile group grp < 4 (named barrier
+// 1 + grp; immediate ids keep the block's barrier count at five)
+__device__ __forceinline__ void group_sync(int grp, int nwg) {
+    const int cnt = nwg * 32;
+    switch (grp) {
+    case 0: asm volatile("bar.sync 1, %0;" ::"r"(cnt) : "memory"); break;
+    case 1: asm volatile("bar.sync 2, %0;" ::"r"(cnt) : "memory"); break;
+    case 2: asm volatile("bar.sync 3, %0;" ::"r"(cnt) : "memory"); break;
+    default: asm volatile("bar.sync 4, %0;" ::"r"(cnt) : "memory"); break;
+    }
 }
 
 template <class TV>
@@ -169,17 +196,19 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
     if (!st->cycle_active) return;
     constexpr int VN = Vec<TV>::N;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwg = warps_per_tile(kc), ngrp = KW / nwg;
+    const int grp = warp / nwg, slot = warp % nwg;
     TV acc[KPW];
 #pragma unroll
     for (int q = 0; q < KPW; ++q) acc[q] = (TV)0;
     const int nvec = n / VN;
-    for (int u = blockIdx.x * 32 + lane; u < nvec + 31; u += gridDim.x * 32) {
-        if (u >= nvec) break;
+    const int stride = gridDim.x * ngrp * 32;
+    for (int u = (blockIdx.x * ngrp + grp) * 32 + lane; u < nvec; u += stride) {
         TV wv[VN];
         vload<TV>(w + (size_t)u * VN, wv);
 #pragma unroll
         for (int q = 0; q < KPW; ++q) {
-            const int k = warp + KW * q;
+            const int k = slot + nwg * q;
             if (k < kc) {
                 TV vv[VN];
                 vload<TV>(raw + (size_t)(k0 + k) * ldv + (size_t)u * VN, vv);
@@ -187,18 +216,18 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
             }
         }
     }
-    if (blockIdx.x == 0) {  // elements past the last full vector
+    if (blockIdx.x == 0 && grp == 0) {  // elements past the last full vector
         const int i = nvec * VN + lane;
         if (lane < n - nvec * VN) {
 #pragma unroll
             for (int q = 0; q < KPW; ++q) {
-                const int k = warp + KW * q;
+                const int k = slot + nwg * q;
                 if (k < kc) acc[q] += raw[(size_t)(k0 + k) * ldv + i] * w[i];
             }
         }
     }
     __shared__ double bs[KW * KPW], tot[KW * KPW];
-    warp_split_sums<TV>(acc, kc, bs);
+    group_sums<TV>(acc, kc, nwg, bs);
     if (last_block_reduce(partials, counter, bs, kc, tot)) {
         for (int k = threadIdx.x; k < kc; k += blockDim.x) {
             const double h = st->vscale[k0 + k] * tot[k];
@@ -209,9 +238,12 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
 }
 
 // ---- pass B fused (nk <= 32): w' = w - sum_k c_k raw_k ; s2_k = raw_k . w'.
-// Each warp forms the update of its own vectors for the tile; the 8 partial
-// updates meet in shared memory (summed in warp order), every warp rebuilds
-// w' from them and dots it with the vector values it still holds.
+// Each warp of a tile group forms the update of its own vectors for the
+// tile.  A one-warp group holds every vector: w' = w - share directly.  In a
+// larger group the shares meet in shared memory, the group's threads each
+// form w' = w - (sum of the shares, in warp order) for some elements of the
+// tile (and store them), and every warp dots w' with the vector values it
+// still holds.
 template <class TV>
 __global__ void __launch_bounds__(KT)
 k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict__ w,
@@ -220,9 +252,12 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
     constexpr int VN = Vec<TV>::N;
     constexpr int TE = 32 * VN;  // elements of a tile
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwg = warps_per_tile(nk), ngrp = KW / nwg;
+    const int grp = warp / nwg, slot = warp % nwg;
+    const int gsz = nwg * 32, gt = slot * 32 + lane;  // threads of the group, rank
     __shared__ TV cf[KW * KPW];
     __shared__ TV upd[KW][TE];
-    __shared__ TV wsh[TE];
+    __shared__ TV wsh[KW / 2][TE];
     for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
     __syncthreads();
     TV acc[KPW];
@@ -231,16 +266,16 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
     const int nvec = n / VN;
     const int ntiles = (nvec + 31) / 32;
     const int nfull = nvec * VN;  // elements covered by whole vectors
-    // registers of the current tile and of the next one (loaded ahead); the
-    // first TE threads also hold one element of w each
-    TV vv[KPW][VN], nv[KPW][VN];
-    TV wt = (TV)0, nwt = (TV)0;
-    auto load_tile = [&](int tile, TV (&v)[KPW][VN], TV& we) {
+    // registers of the current tile and of the next one (loaded ahead): the
+    // warp's vector values, and the w elements this thread turns into w'
+    // (its lanes' elements in a one-warp group; else elements gt + r * gsz)
+    TV vv[KPW][VN], nv[KPW][VN], we[VN], nwe[VN];
+    auto load_tile = [&](int tile, TV (&v)[KPW][VN], TV (&wl)[VN]) {
         const int u = tile * 32 + lane;
         const bool ok = u < nvec;
 #pragma unroll
         for (int q = 0; q < KPW; ++q) {
-            const int k = warp + KW * q;
+            const int k = slot + nwg * q;
             if (k < nk && ok) {
                 vload<TV>(raw + (size_t)k * ldv + (size_t)u * VN, v[q]);
             } else {
@@ -248,52 +283,79 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
                 for (int e = 0; e < VN; ++e) v[q][e] = (TV)0;
             }
         }
-        const int i = tile * TE + threadIdx.x;
-        we = (threadIdx.x < TE && i < nfull) ? w[i] : (TV)0;
+        if (nwg == 1) {
+            if (ok) {
+                vload<TV>(w + (size_t)u * VN, wl);
+            } else {
+#pragma unroll
+                for (int e = 0; e < VN; ++e) wl[e] = (TV)0;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < VN; ++r) {
+                const int t = gt + r * gsz, i = tile * TE + t;
+                wl[r] = (t < TE && i < nfull) ? w[i] : (TV)0;
+            }
+        }
     };
-    int tile = blockIdx.x;
-    if (tile < ntiles) load_tile(tile, vv, wt);
-    for (; tile < ntiles; tile += gridDim.x) {
-        const int next = tile + gridDim.x;
-        if (next < ntiles) load_tile(next, nv, nwt);
-        // this warp's share of the update for the tile
+    const int gstride = gridDim.x * ngrp;
+    int tile = blockIdx.x * ngrp + grp;
+    if (tile < ntiles) load_tile(tile, vv, we);
+    for (; tile < ntiles; tile += gstride) {
+        const int next = tile + gstride;
+        if (next < ntiles) load_tile(next, nv, nwe);
+        // this warp's share of the update for its lanes' elements
         TV part[VN];
 #pragma unroll
         for (int e = 0; e < VN; ++e) part[e] = (TV)0;
 #pragma unroll
         for (int q = 0; q < KPW; ++q) {
-            const int k = warp + KW * q;
+            const int k = slot + nwg * q;
             if (k < nk) {
 #pragma unroll
                 for (int e = 0; e < VN; ++e) part[e] += cf[k] * vv[q][e];
             }
         }
+        TV wn[VN];
+        if (nwg == 1) {
 #pragma unroll
-        for (int e = 0; e < VN; ++e) upd[warp][lane * VN + e] = part[e];
-        __syncthreads();
-        // w' = w - (sum of the 8 shares, in warp order), once per element
-        if (threadIdx.x < TE) {
-            const int i = tile * TE + threadIdx.x;
-            TV sum = (TV)0;
+            for (int e = 0; e < VN; ++e) wn[e] = we[e] - ((TV)0 + part[e]);
+            const int u = tile * 32 + lane;
+            if (u < nvec) vstore<TV>(w + (size_t)u * VN, wn);
+        } else {
 #pragma unroll
-            for (int g = 0; g < KW; ++g) sum += upd[g][threadIdx.x];
-            const TV wn = wt - sum;
-            wsh[threadIdx.x] = wn;
-            if (i < nfull) w[i] = wn;
+            for (int e = 0; e < VN; ++e) upd[warp][lane * VN + e] = part[e];
+            group_sync(grp, nwg);
+            // w' = w - (sum of the shares, in warp order), once per element
+#pragma unroll
+            for (int r = 0; r < VN; ++r) {
+                const int t = gt + r * gsz;
+                if (t < TE) {
+                    TV sum = (TV)0;
+                    for (int g = 0; g < nwg; ++g) sum += upd[grp * nwg + g][t];
+                    const TV x = we[r] - sum;
+                    wsh[grp][t] = x;
+                    const int i = tile * TE + t;
+                    if (i < nfull) w[i] = x;
+                }
+            }
+            group_sync(grp, nwg);
+#pragma unroll
+            for (int e = 0; e < VN; ++e) wn[e] = wsh[grp][lane * VN + e];
         }
-        __syncthreads();
 #pragma unroll
         for (int q = 0; q < KPW; ++q) {
             TV d = (TV)0;
 #pragma unroll
-            for (int e = 0; e < VN; ++e) d += vv[q][e] * wsh[lane * VN + e];
+            for (int e = 0; e < VN; ++e) d += vv[q][e] * wn[e];
             acc[q] += d;
         }
 #pragma unroll
         for (int q = 0; q < KPW; ++q)
 #pragma unroll
             for (int e = 0; e < VN; ++e) vv[q][e] = nv[q][e];
-        wt = nwt;
+#pragma unroll
+        for (int e = 0; e < VN; ++e) we[e] = nwe[e];
     }
     if (blockIdx.x == 0 && warp == 0) {  // tail elements: one warp, serial over k
         const int i = nfull + lane;
@@ -304,18 +366,18 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
         }
     }
     __syncthreads();
-    if (blockIdx.x == 0) {
+    if (blockIdx.x == 0 && grp == 0) {
         const int i = nfull + lane;
         if (lane < n - nfull) {
 #pragma unroll
             for (int q = 0; q < KPW; ++q) {
-                const int k = warp + KW * q;
+                const int k = slot + nwg * q;
                 if (k < nk) acc[q] += raw[(size_t)k * ldv + i] * w[i];
             }
         }
     }
     __shared__ double bs[KW * KPW], tot[KW * KPW];
-    warp_split_sums<TV>(acc, nk, bs);
+    group_sums<TV>(acc, nk, nwg, bs);
     if (last_block_reduce(partials, counter, bs, nk, tot)) {
         for (int k = threadIdx.x; k < nk; k += blockDim.x) {
             const double h = st->vscale[k] * tot[k];
