@@ -95,6 +95,12 @@ sg_status sg_ctx_synchronize(sg_ctx* ctx);
 /* Kernels launched through this context so far (a CUDA-graph launch adds
  * the kernel nodes it replays).  No counterpart in the reference. */
 sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count);
+/* Restart cycles captured as a CUDA graph so far.  A solve reuses the
+ * previous capture when the matrix, preconditioner (and its learned stage),
+ * vectors, restart length and precision are the same objects in the same
+ * state; a re-set-up, format change or new buffer captures again.  No
+ * counterpart in the reference. */
+sg_status sg_ctx_get_capture_count(sg_ctx* ctx, long long* count);
 /* Kernel-class timers: with timing on, solves that run without a CUDA graph
  * record a CUDA event pair on the context stream around every kernel class:
  * kind 0 Krylov SpMV, 1 FP64 residual, 2 preconditioner, 3 orthogonalisation

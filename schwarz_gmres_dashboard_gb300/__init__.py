@@ -90,6 +90,14 @@ class Context:
         _check(_clib.sg_ctx_get_launch_count(self.handle, C.byref(c)))
         return int(c.value)
 
+    @property
+    def capture_count(self) -> int:
+        """Restart cycles captured as CUDA graphs so far (a solve reuses the
+        previous capture while its inputs are unchanged)."""
+        c = C.c_longlong(0)
+        _check(_clib.sg_ctx_get_capture_count(self.handle, C.byref(c)))
+        return int(c.value)
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             _clib.sg_ctx_destroy(self.handle)

@@ -72,6 +72,7 @@ PROTOTYPES = {
     "sg_ctx_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "sg_ctx_synchronize": (C.c_int, [_vp]),
     "sg_ctx_get_launch_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "sg_ctx_get_capture_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     "sg_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
     "sg_ctx_get_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "sg_csr_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int,

@@ -2,6 +2,7 @@
 // entry point validates its arguments, runs on the context's device and
 // stream, and turns internal failures into an sg_status plus a thread-local
 // message.
+#include <atomic>
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -12,6 +13,13 @@
 
 #include "kernels.h"
 #include "sg_internal.h"
+
+namespace sg {
+uint64_t next_object_gen() {
+    static std::atomic<uint64_t> g{0};
+    return ++g;
+}
+}  // namespace sg
 
 namespace sg {
 
@@ -247,6 +255,13 @@ sg_status sg_ctx_get_launch_count(sg_ctx* ctx, long long* count) {
     });
 }
 
+sg_status sg_ctx_get_capture_count(sg_ctx* ctx, long long* count) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && count, "NULL argument");
+        *count = ctx->captures;
+    });
+}
+
 sg_status sg_ctx_set_timing(sg_ctx* ctx, int on) {
     return guard([&] {
         SG_CHECK_ARG(ctx, "ctx is NULL");
@@ -289,6 +304,7 @@ sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* r
         SG_CHECK_ARG(nnz == 0 || (col_idx && vals), "col_idx/vals are NULL");
         use_device(ctx);
         auto* A = new sg_csr();
+        A->gen = next_object_gen();
         try {
             A->ctx = ctx;
             A->nrows = nrows;
@@ -430,6 +446,7 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
         *out = nullptr;
         SG_CHECK_ARG(kind >= SG_PC_NONE && kind <= SG_PC_TWOLEVEL_RAS, "unknown kind %d", (int)kind);
         auto* pc = new sg_precond();
+        pc->gen = next_object_gen();
         pc->ctx = ctx;
         pc->kind = kind;
         if (opts) pc->opts = *opts;
@@ -482,6 +499,7 @@ sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
         SG_CHECK_ARG(A->ctx == pc->ctx, "matrix and preconditioner belong to different contexts");
         use_device(pc->ctx);
         pc->is_setup = false;
+        pc->gen = next_object_gen();
         pc->n = A->nrows;
         if (pc->kind == SG_PC_NONE) {
             pc->is_setup = true;

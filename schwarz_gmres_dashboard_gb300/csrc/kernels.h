@@ -78,6 +78,7 @@ void learned_apply(sg_learned* L, const TI* x, TO* y, int n, const int* active);
 void learned_begin(sg_learned* L, SolveState* st);
 void learned_monitor(sg_learned* L, SolveState* st);
 void learned_detach(sg_learned* L);
+uint64_t learned_gen(const sg_learned* L);  // changes when the stage's matrix changes
 
 // ---------------------------------------------------------------- batched.cu
 // nsys independent systems (block-diagonal A, rows of system s at

@@ -635,6 +635,7 @@ __global__ void k_learned_monitor(LearnedCtl* ctl, const SolveState* st) {
 // ============================================================ host side
 struct LearnedImpl {
     sg_ctx* ctx = nullptr;
+    uint64_t gen = 0;  // object generation, renewed by sg_learned_set_matrix
     int nx = 0, ny = 0, nz = 0, cx = 0, cy = 0, cz = 0;
     int nc = 0;  // coarse cells
     const sg_csr* A = nullptr;
@@ -931,6 +932,8 @@ void learned_detach(sg_learned* L) {
     if (L) L->attached = nullptr;
 }
 
+uint64_t learned_gen(const sg_learned* L) { return L ? L->gen : 0; }
+
 void learned_begin(sg_learned* L, SolveState* st) {
     check_ready(L);
     k_learned_begin<<<1, 1, 0, L->ctx->stream>>>(L->ctl.p, st, L->on ? 1 : 0);
@@ -1009,6 +1012,7 @@ sg_status sg_learned_create(sg_ctx* ctx, int nx, int ny, int nz, sg_learned** ou
         SG_CHECK_ARG((long long)nx * ny * nz < (1ll << 31), "grid too large");
         SG_CUDA(cudaSetDevice(ctx->device));
         auto* L = new sg_learned();
+        L->gen = next_object_gen();
         try {
             L->ctx = ctx;
             L->nx = nx; L->ny = ny; L->nz = nz;
@@ -1070,7 +1074,10 @@ sg_status sg_learned_destroy(sg_learned* L) {
     return lguard([&] {
         if (!L) return;
         cudaSetDevice(L->ctx->device);
-        if (L->attached) L->attached->learned = nullptr;
+        if (L->attached) {
+            L->attached->learned = nullptr;
+            L->attached->gen = next_object_gen();
+        }
         delete L;
     });
 }
@@ -1078,6 +1085,7 @@ sg_status sg_learned_destroy(sg_learned* L) {
 sg_status sg_learned_set_matrix(sg_learned* L, const sg_csr* A) {
     return lguard([&] {
         SG_CHECK_ARG(L && A, "NULL argument");
+        L->gen = next_object_gen();
         SG_CHECK_ARG(A->ctx == L->ctx, "matrix belongs to a different context");
         SG_CHECK_ARG(A->nrows == A->ncols &&
                          (long long)L->nx * L->ny * L->nz == (long long)A->nrows,
@@ -1495,6 +1503,7 @@ sg_status sg_learned_get_state(sg_learned* L, int* enabled, int* fallback_cycle,
 sg_status sg_precond_set_learned(sg_precond* pc, sg_learned* L, double stagnation) {
     return lguard([&] {
         SG_CHECK_ARG(pc, "NULL argument");
+        pc->gen = next_object_gen();
         if (!L) {
             if (pc->learned) pc->learned->attached = nullptr;
             pc->learned = nullptr;
@@ -1508,7 +1517,10 @@ sg_status sg_precond_set_learned(sg_precond* pc, sg_learned* L, double stagnatio
         if (pc->is_setup)
             SG_CHECK_ARG(pc->n == L->A->nrows, "preconditioner size %d != grid size %d", pc->n,
                          L->A->nrows);
-        if (L->attached && L->attached != pc) L->attached->learned = nullptr;
+        if (L->attached && L->attached != pc) {
+            L->attached->learned = nullptr;
+            L->attached->gen = next_object_gen();
+        }
         if (pc->learned && pc->learned != L) pc->learned->attached = nullptr;
         L->attached = pc;
         pc->learned = L;

@@ -106,13 +106,35 @@ struct BatchWork;  // workspace of the batched solver (batched.cu)
 void destroy_batch_work(BatchWork* w);
 
 // Per-context solve workspace (grown on demand, reused across solves).
+// Everything a captured restart cycle bakes in: object identities and
+// generations (a generation changes whenever an object's device buffers or
+// launch choices may have changed), buffer addresses and sizes.  Compared
+// bytewise, so instances are zeroed before their fields are set.
+struct GraphKey {
+    const void* A;
+    uint64_t agen;
+    int afmt, afmt32, acfg, acfg32;
+    const void* aval32;
+    const void* pc;
+    uint64_t pgen;
+    const void* L;
+    uint64_t lgen;
+    const void *b, *x;
+    int n, m, flexible, fp32;
+    size_t ldv;
+    const void *V, *Z, *t, *r64, *st, *hist;
+    int hist_cap;
+};
+
 struct SolveWork {
     DBuf<SolveState> st;
     DBuf<double> r64, b64, x64;  // residual; staging of host b / x
     DBuf<double> V64, Z64, t64;  // Krylov basis, FGMRES directions, SpMV output
     DBuf<float> V32, Z32, t32;
     SolveState* h_st = nullptr;  // pinned mirror of the state
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;  // the last captured restart cycle
+    GraphKey gkey{};                  // what it was captured for
+    long long graph_nodes = 0;        // its kernel launches
     ~SolveWork();
 };
 
@@ -145,6 +167,7 @@ struct sg_ctx {
     // kernels launched by this context (graph launches add their kernel nodes)
     long long launches = 0;
     long long captured = 0;
+    long long captures = 0;  // restart cycles captured as CUDA graphs
     bool capturing = false;
 };
 
@@ -163,6 +186,9 @@ struct ClassTimer {
 };
 // adds the elapsed times of completed pairs (call after a stream sync)
 void collect_timers(sg_ctx* ctx);
+// process-wide increasing generation numbers of matrices, preconditioners and
+// learned stages (a recycled address never repeats a generation)
+uint64_t next_object_gen();
 inline void count_launch(sg_ctx* ctx) {
     if (ctx->capturing) ctx->captured++;
     else ctx->launches++;
@@ -171,6 +197,7 @@ inline void count_launch(sg_ctx* ctx) {
 
 struct sg_csr {
     sg_ctx* ctx = nullptr;
+    uint64_t gen = 0;  // object generation (sg::next_object_gen)
     int nrows = 0, ncols = 0, nnz = 0;
     bool sorted = true;  // column indices nondecreasing within each row
     std::vector<int> h_rp, h_ci;
@@ -225,6 +252,7 @@ __host__ __device__ __forceinline__ int tslot(int r, int p) { return p ? r + (r 
 
 struct sg_precond {
     sg_ctx* ctx = nullptr;
+    uint64_t gen = 0;  // renewed by every set-up and learned-stage change
     int kind = SG_PC_NONE;
     sg_precond_opts opts{};
     bool is_setup = false;

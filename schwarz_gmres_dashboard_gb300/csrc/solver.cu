@@ -225,31 +225,72 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     const bool use_graph = prm.use_graph != 0 && !done_at_start && prm.max_iter > 0;
     cudaGraphExec_t exec = nullptr;
     if (use_graph) {
-        cudaGraph_t g = nullptr;
-        SG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
-        ctx->capturing = true;
-        ctx->captured = 0;
-        try {
-            if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
-            else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
-        } catch (...) {
+        // the restart cycle is captured once and reused while nothing it
+        // bakes in has changed (same operator, preconditioner, vectors, sizes)
+        GraphKey key;
+        std::memset(&key, 0, sizeof(key));
+        key.A = A;
+        key.agen = A->gen;
+        key.afmt = A->format;
+        key.afmt32 = A->format32;
+        key.acfg = A->sell_cfg;
+        key.acfg32 = A->sell_cfg32;
+        key.aval32 = A->val32.p;
+        key.pc = pc;
+        key.pgen = pc ? pc->gen : 0;
+        key.L = pc ? pc->learned : nullptr;
+        key.lgen = pc && pc->learned ? learned_gen(pc->learned) : 0;
+        key.b = b;
+        key.x = x;
+        key.n = n;
+        key.m = m;
+        key.flexible = flexible ? 1 : 0;
+        key.fp32 = fp32 ? 1 : 0;
+        key.ldv = ldv;
+        key.V = fp32 ? (const void*)w->V32.p : (const void*)w->V64.p;
+        key.Z = fp32 ? (const void*)w->Z32.p : (const void*)w->Z64.p;
+        key.t = fp32 ? (const void*)w->t32.p : (const void*)w->t64.p;
+        key.r64 = w->r64.p;
+        key.st = w->st.p;
+        key.hist = ctx->hist_d;
+        key.hist_cap = ctx->hist_cap;
+        if (!(w->graph && std::memcmp(&key, &w->gkey, sizeof(key)) == 0)) {
+            if (w->graph) {
+                cudaGraphExecDestroy(w->graph);
+                w->graph = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            SG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+            ctx->capturing = true;
+            ctx->captured = 0;
+            try {
+                if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
+                else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
+            } catch (...) {
+                ctx->capturing = false;
+                cudaStreamEndCapture(ctx->stream, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
             ctx->capturing = false;
-            cudaStreamEndCapture(ctx->stream, &g);
-            if (g) cudaGraphDestroy(g);
-            throw;
+            SG_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+            cudaGraphExec_t ge = nullptr;
+            cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            SG_CUDA(e);
+            w->graph = ge;
+            w->gkey = key;
+            ctx->captures++;
+            w->graph_nodes = ctx->captured;
         }
-        ctx->capturing = false;
-        SG_CUDA(cudaStreamEndCapture(ctx->stream, &g));
-        cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
-        cudaGraphDestroy(g);
-        SG_CUDA(e);
+        exec = w->graph;
     }
     int cycles = 0;
     try {
         while (!done_at_start && cycles < prm.max_iter) {
             if (use_graph) {
                 SG_CUDA(cudaGraphLaunch(exec, ctx->stream));
-                ctx->launches += ctx->captured;
+                ctx->launches += w->graph_nodes;
             }
             else if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
             else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
@@ -260,10 +301,11 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
             if (hs->done) break;
         }
     } catch (...) {
-        if (exec) cudaGraphExecDestroy(exec);
+        // a failed solve drops the cached cycle
+        if (w->graph) cudaGraphExecDestroy(w->graph);
+        w->graph = nullptr;
         throw;
     }
-    if (exec) cudaGraphExecDestroy(exec);
     // the state now holds the FP64 true residual of the returned x
     SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(cudaStreamSynchronize(ctx->stream));
