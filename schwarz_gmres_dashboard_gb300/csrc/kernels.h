@@ -32,10 +32,12 @@ void launch_bnorm(sg_ctx* ctx, const double* v, int n, SolveState* st);
 template <class TV>
 void launch_cycle_init(sg_ctx* ctx, const TV* raw0, int n, SolveState* st, int m, bool flexible);
 // One CGS2 Arnoldi step on raw[j+1] against raw[0..j] (with the Givens
-// update of the least-squares problem done by the last block).
+// update of the least-squares problem done by the last block); lagged: the
+// two-pass variant with the second projection carried to the next step
+// (st->lagged must be set for the whole solve, m < SG_LAGM).
 template <class TV>
 void launch_cgs2(sg_ctx* ctx, TV* raw, size_t ldv, int n, int j, int m, SolveState* st,
-                 bool flexible);
+                 bool lagged);
 // y = H^{-1} g (k x k upper triangle) by one thread.
 void launch_backsolve(sg_ctx* ctx, SolveState* st, int m);
 // x += sum_k y_k * vscale_k * basis_k  (k < st->kcount)

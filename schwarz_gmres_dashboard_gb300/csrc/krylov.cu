@@ -189,10 +189,84 @@ __device__ __forceinline__ void group_sync(int grp, int nwg) {
     }
 }
 
+// ---- lagged CGS2 (left-preconditioned FP32 GMRES, restart < SG_LAGM).
+// Step j orthogonalises z = B (vscale_j raw_j), where the stored raw_j still
+// lacks its second projection: v_j = T(j,j) raw_j - sum_{k<j} c_k v_k.  By
+// linearity B v_j = z - V_j g with g = H(0..j, 0..j-1) c (the Arnoldi relation
+// B v_k = V H(:,k)), so the projections of z give the Hessenberg column after
+// subtracting g, and the orthogonalised vector is the same.  Two passes:
+//   A  d = S^T z over the stored vectors; p = T^T d; hsum = p - g;
+//      update coefficients on the stored vectors u = T p
+//   B  w' = z - S u; r = S^T w'; ||w'||^2; then h2 = T^T r, the column is
+//      hsum + h2, ||w''||^2 = ||w'||^2 - ||h2||^2 (Pythagoras), and w' is
+//      stored as raw_{j+1} with its pending correction c = h2 / ||w''||.
+// In exact arithmetic this is CGS2; the stored vectors are never rewritten.
+
+// pass A epilogue (all threads of the last block; d = tot[0..j])
+__device__ void lagged_pass_a(SolveState* st, int j, const double* d) {
+    __shared__ double p_s[SG_LAGM];
+    const double* T = st->lagT;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        double s = 0.0;
+        for (int l = 0; l <= i; ++l) s += T[l + i * SG_LAGM] * d[l];
+        p_s[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        double g = 0.0;
+        for (int k = (i > 0 ? i - 1 : 0); k < j; ++k) g += st->lagH[i + k * SG_LAGM] * st->lagc[k];
+        st->h[i] = p_s[i];
+        st->hsum[i] = p_s[i] - g;
+        double u = 0.0;
+        for (int k = i; k <= j; ++k) u += T[i + k * SG_LAGM] * p_s[k];
+        st->cfu[i] = u;
+    }
+}
+
+// pass B epilogue (all threads of the last block; r = tot[0..j], ss = ||w'||^2)
+__device__ void lagged_pass_b(SolveState* st, int j, int m, const double* r, double ss,
+                              double* hist, int hist_cap) {
+    __shared__ double h2_s[SG_LAGM];
+    __shared__ int s_ok;
+    double* T = st->lagT;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        double s = 0.0;
+        for (int l = 0; l <= i; ++l) s += T[l + i * SG_LAGM] * r[l];
+        h2_s[i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double nrm2 = ss;
+        for (int i = 0; i <= j; ++i) {
+            nrm2 -= h2_s[i] * h2_s[i];
+            st->hsum[i] += h2_s[i];
+            st->lagH[i + j * SG_LAGM] = st->hsum[i];
+        }
+        if (!(nrm2 > 0.0)) nrm2 = isfinite(nrm2) ? 0.0 : nrm2;
+        st->lagH[j + 1 + j * SG_LAGM] = sqrt(nrm2);
+        arnoldi_finalize(st, j, m, nrm2, hist, hist_cap);
+        // the pending correction of the new stored vector
+        s_ok = (!st->breakdown && st->cycle_active && j + 1 < SG_LAGM) ? 1 : 0;
+        if (s_ok) {
+            const double vs = st->vscale[j + 1];
+            for (int k = 0; k <= j; ++k) st->lagc[k] = h2_s[k] * vs;
+            T[(j + 1) + (j + 1) * SG_LAGM] = vs;
+        }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    // T(:, j+1) = T(j+1,j+1) e_{j+1} - T(:, 0..j) c
+    for (int l = threadIdx.x; l <= j; l += blockDim.x) {
+        double s = 0.0;
+        for (int k = l; k <= j; ++k) s += T[l + k * SG_LAGM] * st->lagc[k];
+        T[l + (j + 1) * SG_LAGM] = -s;
+    }
+}
+
 template <class TV>
 __global__ void __launch_bounds__(KT)
 k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* __restrict__ w,
-       SolveState* st, int second, double* partials, unsigned* counter) {
+       SolveState* st, int second, int lagged, double* partials, unsigned* counter) {
     if (!st->cycle_active) return;
     constexpr int VN = Vec<TV>::N;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -229,6 +303,10 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
     __shared__ double bs[KW * KPW], tot[KW * KPW];
     group_sums<TV>(acc, kc, nwg, bs);
     if (last_block_reduce(partials, counter, bs, kc, tot)) {
+        if (lagged) {
+            lagged_pass_a(st, kc - 1, tot);
+            return;
+        }
         for (int k = threadIdx.x; k < kc; k += blockDim.x) {
             const double h = st->vscale[k0 + k] * tot[k];
             st->h[k0 + k] = h;
@@ -247,7 +325,8 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
 template <class TV>
 __global__ void __launch_bounds__(KT)
 k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict__ w,
-           SolveState* st, double* partials, unsigned* counter) {
+           SolveState* st, double* partials, unsigned* counter, int lagged, int m,
+           double* hist, int hist_cap) {
     if (!st->cycle_active) return;
     constexpr int VN = Vec<TV>::N;
     constexpr int TE = 32 * VN;  // elements of a tile
@@ -258,8 +337,10 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
     __shared__ TV cf[KW * KPW];
     __shared__ TV upd[KW][TE];
     __shared__ TV wsh[KW / 2][TE];
-    for (int k = threadIdx.x; k < nk; k += blockDim.x) cf[k] = (TV)(st->h[k] * st->vscale[k]);
+    for (int k = threadIdx.x; k < nk; k += blockDim.x)
+        cf[k] = lagged ? (TV)st->cfu[k] : (TV)(st->h[k] * st->vscale[k]);
     __syncthreads();
+    TV ss = (TV)0;  // ||w'||^2 (lagged): slot 0 of each group counts its elements
     TV acc[KPW];
 #pragma unroll
     for (int q = 0; q < KPW; ++q) acc[q] = (TV)0;
@@ -322,6 +403,8 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
             for (int e = 0; e < VN; ++e) wn[e] = we[e] - ((TV)0 + part[e]);
             const int u = tile * 32 + lane;
             if (u < nvec) vstore<TV>(w + (size_t)u * VN, wn);
+#pragma unroll
+            for (int e = 0; e < VN; ++e) ss += wn[e] * wn[e];
         } else {
 #pragma unroll
             for (int e = 0; e < VN; ++e) upd[warp][lane * VN + e] = part[e];
@@ -342,6 +425,10 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
             group_sync(grp, nwg);
 #pragma unroll
             for (int e = 0; e < VN; ++e) wn[e] = wsh[grp][lane * VN + e];
+            if (slot == 0) {
+#pragma unroll
+                for (int e = 0; e < VN; ++e) ss += wn[e] * wn[e];
+            }
         }
 #pragma unroll
         for (int q = 0; q < KPW; ++q) {
@@ -363,6 +450,7 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
             TV wi = w[i];
             for (int k = 0; k < nk; ++k) wi -= cf[k] * raw[(size_t)k * ldv + i];
             w[i] = wi;
+            ss += wi * wi;
         }
     }
     __syncthreads();
@@ -376,8 +464,24 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
             }
         }
     }
-    __shared__ double bs[KW * KPW], tot[KW * KPW];
+    __shared__ double bs[KW * KPW + 1], tot[KW * KPW + 1];
     group_sums<TV>(acc, nk, nwg, bs);
+    if (lagged) {
+        // block sum of ||w'||^2 next to the dots
+        __shared__ double red_ss[KW];
+        const double v = (double)warp_sum(ss);
+        if (lane == 0) red_ss[warp] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = red_ss[0];
+            for (int g = 1; g < KW; ++g) t += red_ss[g];
+            bs[nk] = t;
+        }
+        __syncthreads();
+        if (last_block_reduce(partials, counter, bs, nk + 1, tot))
+            lagged_pass_b(st, nk - 1, m, tot, tot[nk], hist, hist_cap);
+        return;
+    }
     if (last_block_reduce(partials, counter, bs, nk, tot)) {
         for (int k = threadIdx.x; k < nk; k += blockDim.x) {
             const double h = st->vscale[k] * tot[k];
@@ -501,6 +605,7 @@ k_cycle_init(const TV* __restrict__ raw0, int n, SolveState* st, int m, int flex
         return;
     }
     st->vscale[0] = 1.0 / beta;
+    st->lagT[0] = 1.0 / beta;  // lagged CGS2: v_0 = raw_0 / beta
     st->g[0] = beta;
     st->est_scale = flexible ? 1.0 : st->rnorm / beta;
     st->cycle_active = 1;
@@ -516,6 +621,14 @@ __global__ void k_backsolve(SolveState* st, int m) {
         for (int l = i + 1; l < k; ++l) yi -= st->H[i + l * ld] * st->y[l];
         st->y[i] = yi / st->H[i + i * ld];
     }
+    // lagged CGS2: V y = S (T y), coefficients on the stored vectors
+    if (st->lagged) {
+        for (int i = 0; i < k; ++i) {
+            double u = 0.0;
+            for (int l = i; l < k; ++l) u += st->lagT[i + l * SG_LAGM] * st->y[l];
+            st->cfu[i] = u;
+        }
+    }
 }
 
 template <class TV>
@@ -527,7 +640,8 @@ k_update_x(const TV* __restrict__ basis, size_t ldv, int n, double* __restrict__
     // the correction d = V y is formed in the basis precision (FP32 for the
     // mixed solver: the inner solve's precision) and added to x in FP64
     __shared__ TV cf[SG_MMAX];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) cf[i] = (TV)(st->y[i] * st->vscale[i]);
+    for (int i = threadIdx.x; i < k; i += blockDim.x)
+        cf[i] = st->lagged ? (TV)st->cfu[i] : (TV)(st->y[i] * st->vscale[i]);
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         TV d = (TV)0;
@@ -597,11 +711,11 @@ void launch_cycle_init(sg_ctx* ctx, const TV* raw0, int n, SolveState* st, int m
 
 template <class TV>
 static void dots_any(sg_ctx* ctx, const TV* raw, size_t ldv, int n, int nk, const TV* w,
-                     SolveState* st, int second) {
+                     SolveState* st, int second, int lagged = 0) {
     for (int k0 = 0; k0 < nk; k0 += KW * KPW) {
         const int kc = nk - k0 < KW * KPW ? nk - k0 : KW * KPW;
         k_dots<TV><<<kgrid(ctx, (n + 3) / 4 * 8, 4), KT, 0, ctx->stream>>>(
-            raw, ldv, n, k0, kc, w, st, second, ctx->partials.p, ctx->counter.p);
+            raw, ldv, n, k0, kc, w, st, second, lagged, ctx->partials.p, ctx->counter.p);
         SG_CUDA(cudaGetLastError());
         count_launch(ctx);
     }
@@ -609,16 +723,26 @@ static void dots_any(sg_ctx* ctx, const TV* raw, size_t ldv, int n, int nk, cons
 
 template <class TV>
 void launch_cgs2(sg_ctx* ctx, TV* raw, size_t ldv, int n, int j, int m, SolveState* st,
-                 bool flexible) {
-    (void)flexible;
+                 bool lagged) {
     const int nk = j + 1;
     TV* w = raw + (size_t)(j + 1) * ldv;
+    if (lagged) {
+        // two passes (see lagged_pass_a / lagged_pass_b); m < SG_LAGM <= 32
+        if (m >= SG_LAGM || nk > KW * KPW) fail(SG_ERR_INTERNAL, "lagged CGS2 needs m < %d", SG_LAGM);
+        dots_any<TV>(ctx, raw, ldv, n, nk, w, st, 0, 1);
+        k_upd_dots<TV><<<kgrid(ctx, (n + 3) / 4 * 8, 3), KT, 0, ctx->stream>>>(
+            raw, ldv, n, nk, w, st, ctx->partials.p, ctx->counter.p, 1, m, ctx->hist_d,
+            ctx->hist_cap);
+        SG_CUDA(cudaGetLastError());
+        count_launch(ctx);
+        return;
+    }
     // pass A
     dots_any<TV>(ctx, raw, ldv, n, nk, w, st, 0);
     // pass B
     if (nk <= KW * KPW) {
         k_upd_dots<TV><<<kgrid(ctx, (n + 3) / 4 * 8, 3), KT, 0, ctx->stream>>>(
-            raw, ldv, n, nk, w, st, ctx->partials.p, ctx->counter.p);
+            raw, ldv, n, nk, w, st, ctx->partials.p, ctx->counter.p, 0, m, nullptr, 0);
         SG_CUDA(cudaGetLastError());
         count_launch(ctx);
     } else {

@@ -69,6 +69,8 @@ struct DBuf {
 // --------------------------------------------------------------- solver state
 // Restart lengths up to SG_MMAX are supported.
 constexpr int SG_MMAX = 128;
+// restart lengths below SG_LAGM use the lagged CGS2 in the FP32 GMRES cycle
+constexpr int SG_LAGM = 32;
 
 // Device-resident Arnoldi / Givens state of one solve (FP64 throughout).
 struct SolveState {
@@ -100,6 +102,15 @@ struct SolveState {
     double hsum[SG_MMAX + 1];           // h1 + h2 of the current column
     double vscale[SG_MMAX + 1];         // basis vector k is stored as raw_k; v_k = vscale[k]*raw_k
     double y[SG_MMAX];
+    // lagged CGS2 (left-preconditioned FP32 GMRES, restart < SG_LAGM): the
+    // stored basis vectors raw_l relate to the orthonormal ones through an
+    // upper triangular T, v_i = sum_{l<=i} T(l,i) raw_l; the newest stored
+    // vector still lacks its second projection, held in lagc
+    int lagged;
+    double lagT[SG_LAGM * SG_LAGM];  // T(l,i) at l + i*SG_LAGM
+    double lagH[SG_LAGM * SG_LAGM];  // unrotated Hessenberg, H(i,k) at i + k*SG_LAGM
+    double lagc[SG_LAGM];            // v_j = T(j,j) raw_j - sum_{k<j} lagc[k] v_k
+    double cfu[SG_LAGM];             // update coefficients on the stored vectors
 };
 
 struct BatchWork;  // workspace of the batched solver (batched.cu)

@@ -93,6 +93,11 @@ void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int*
     }
 }
 
+// The lagged two-pass CGS2 serves the FP32 left-preconditioned cycle with a
+// restart below SG_LAGM: it relies on the operator being linear (B v_k =
+// V H(:,k)), which FGMRES's possibly nonlinear preconditioner does not give.
+bool use_lagged(bool fp32, bool flexible, int m) { return fp32 && !flexible && m < SG_LAGM; }
+
 // One restart cycle as a launch sequence on ctx->stream.
 template <class TV>
 void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b, double* x,
@@ -138,7 +143,8 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
             launch_spmv_a<TV, TV, TV>(ctx, A, zj, wj, &st->vscale[j], active);
         }
         ClassTimer tm(ctx, TK_ORTHO);
-        launch_cgs2<TV>(ctx, V, ldv, n, j, m, st, flexible);
+        launch_cgs2<TV>(ctx, V, ldv, n, j, m, st,
+                        use_lagged(sizeof(TV) == sizeof(float), flexible, m));
     }
     {
         ClassTimer tm(ctx, TK_UPDATE);
@@ -212,6 +218,7 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     hs->max_iter = prm.max_iter;
     hs->tol = prm.tol;
     hs->tol_kind = prm.tol_kind;
+    hs->lagged = use_lagged(fp32, flexible, m) ? 1 : 0;
     const auto t0 = std::chrono::high_resolution_clock::now();
     SG_CUDA(cudaMemcpyAsync(w->st.p, hs, sizeof(SolveState), cudaMemcpyHostToDevice, ctx->stream));
     launch_bnorm(ctx, b, n, w->st.p);
