@@ -611,39 +611,95 @@ k_cycle_init(const TV* __restrict__ raw0, int n, SolveState* st, int m, int flex
     st->cycle_active = 1;
 }
 
+// y = H^{-1} g on the k x k upper triangle of the rotated Hessenberg
+// (src/core/gmres.cpp:131-137).  Up to SG_LAGM columns one warp solves it in
+// shared memory column by column (y_i, then every lane updates its rows);
+// longer triangles use one thread.  Lagged CGS2: also the coefficients on
+// the stored vectors, cfu = T y.
 __global__ void k_backsolve(SolveState* st, int m) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0) return;
     const int k = st->kcount;
     const int ld = m + 1;
-    // src/core/gmres.cpp:131-137
-    for (int i = k - 1; i >= 0; --i) {
-        double yi = st->g[i];
-        for (int l = i + 1; l < k; ++l) yi -= st->H[i + l * ld] * st->y[l];
-        st->y[i] = yi / st->H[i + i * ld];
-    }
-    // lagged CGS2: V y = S (T y), coefficients on the stored vectors
-    if (st->lagged) {
-        for (int i = 0; i < k; ++i) {
-            double u = 0.0;
-            for (int l = i; l < k; ++l) u += st->lagT[i + l * SG_LAGM] * st->y[l];
-            st->cfu[i] = u;
+    const int lane = threadIdx.x;
+    if (k > SG_LAGM) {
+        if (lane != 0) return;
+        for (int i = k - 1; i >= 0; --i) {
+            double yi = st->g[i];
+            for (int l = i + 1; l < k; ++l) yi -= st->H[i + l * ld] * st->y[l];
+            st->y[i] = yi / st->H[i + i * ld];
         }
+        return;
+    }
+    __shared__ double Hs[SG_LAGM][SG_LAGM + 1];
+    __shared__ double gs[SG_LAGM], ys[SG_LAGM];
+    for (int idx = lane; idx < k * k; idx += blockDim.x) {
+        const int i = idx % k, l = idx / k;
+        Hs[i][l] = i <= l ? st->H[i + l * ld] : 0.0;
+    }
+    for (int i = lane; i < k; i += blockDim.x) gs[i] = st->g[i];
+    __syncwarp();
+    for (int i = k - 1; i >= 0; --i) {
+        const double yi = gs[i] / Hs[i][i];
+        if (lane == 0) ys[i] = yi;
+        for (int t = lane; t < i; t += blockDim.x) gs[t] -= Hs[t][i] * yi;
+        __syncwarp();
+    }
+    for (int i = lane; i < k; i += blockDim.x) st->y[i] = ys[i];
+    if (!st->lagged) return;
+    // V y = S (T y): coefficients on the stored vectors
+    for (int idx = lane; idx < k * k; idx += blockDim.x) {
+        const int i = idx % k, l = idx / k;
+        Hs[i][l] = i <= l ? st->lagT[i + l * SG_LAGM] : 0.0;
+    }
+    __syncwarp();
+    for (int i = lane; i < k; i += blockDim.x) {
+        double u = 0.0;
+        for (int l = i; l < k; ++l) u += Hs[i][l] * ys[l];
+        st->cfu[i] = u;
     }
 }
 
+// x += V y: the correction is formed in the basis precision (FP32 for the
+// mixed solver: the inner solve's precision) and added to x in FP64.  A
+// thread takes one 16-byte vector of elements and four basis vectors' loads
+// at a time; per element the terms are summed in basis order.
 template <class TV>
 __global__ void __launch_bounds__(KT)
 k_update_x(const TV* __restrict__ basis, size_t ldv, int n, double* __restrict__ x,
            SolveState* st) {
     const int k = st->kcount;
     if (k <= 0) return;
-    // the correction d = V y is formed in the basis precision (FP32 for the
-    // mixed solver: the inner solve's precision) and added to x in FP64
+    constexpr int VN = Vec<TV>::N;
     __shared__ TV cf[SG_MMAX];
     for (int i = threadIdx.x; i < k; i += blockDim.x)
         cf[i] = st->lagged ? (TV)st->cfu[i] : (TV)(st->y[i] * st->vscale[i]);
     __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int nvec = n / VN;
+    const int stride = gridDim.x * blockDim.x;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nvec; u += stride) {
+        TV d[VN];
+#pragma unroll
+        for (int e = 0; e < VN; ++e) d[e] = (TV)0;
+        int q = 0;
+        for (; q + 4 <= k; q += 4) {
+            TV a[4][VN];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) vload<TV>(basis + (size_t)(q + r) * ldv + (size_t)u * VN, a[r]);
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int e = 0; e < VN; ++e) d[e] += cf[q + r] * a[r][e];
+        }
+        for (; q < k; ++q) {
+            TV a[VN];
+            vload<TV>(basis + (size_t)q * ldv + (size_t)u * VN, a);
+#pragma unroll
+            for (int e = 0; e < VN; ++e) d[e] += cf[q] * a[e];
+        }
+#pragma unroll
+        for (int e = 0; e < VN; ++e) x[(size_t)u * VN + e] += (double)d[e];
+    }
+    for (int i = nvec * VN + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         TV d = (TV)0;
         for (int q = 0; q < k; ++q) d += cf[q] * basis[(size_t)q * ldv + i];
         x[i] += (double)d;

@@ -67,9 +67,12 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
     using VV = typename VecT<TV>::V;
     using VI = typename VecT<TV>::I;
     __shared__ TV buf[SPMV_WARPS][CAP];
+    // MODE 1 keeps values and gathered x apart, for fused multiply-adds
+    __shared__ TV xbuf_all[MODE == 1 ? SPMV_WARPS : 1][MODE == 1 ? CAP : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = gridDim.x * SPMV_WARPS;
     TV* wbuf = buf[warp];
+    TV* xbuf = xbuf_all[MODE == 1 ? warp : 0];
     double ss = 0.0;
     const TV sc = (MODE == 0 && scale) ? (TV)(*scale) : (TV)1;
     for (int tile = blockIdx.x * SPMV_WARPS + warp; tile * 32 < n; tile += nwarps) {
@@ -95,12 +98,25 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
 #pragma unroll
                 for (int q = 0; q < VN; ++q) {
                     const int e = e0 + q;
-                    if (e >= ws && e < we) wbuf[e - ws] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+                    if (e >= ws && e < we) {
+                        if (MODE == 1) {
+                            wbuf[e - ws] = v[q];
+                            xbuf[e - ws] = (TV)__ldg(&x[c[q]]);
+                        } else {
+                            wbuf[e - ws] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+                        }
+                    }
                 }
             }
             __syncwarp();
             const int lo = max(rs, ws), hi = min(re, we);
-            for (int e = lo; e < hi; ++e) sum = padd(sum, wbuf[e - ws]);
+            if (MODE == 1) {
+                // the solver's FP64 true residual: fused multiply-adds in
+                // entry order, the same bits as the SELL kernel
+                for (int e = lo; e < hi; ++e) sum = fma(wbuf[e - ws], xbuf[e - ws], sum);
+            } else {
+                for (int e = lo; e < hi; ++e) sum = padd(sum, wbuf[e - ws]);
+            }
             __syncwarp();
         }
         if (r < n) {
@@ -146,8 +162,9 @@ __device__ __forceinline__ int sell_col(const int16_t* col, long long e, int r) 
 }
 
 // SELL-32 SpMV: a warp per slice of 32 rows, a lane per row; every load of
-// a step k is one contiguous 32-element segment.  Same per-row order and
-// rounding as the CSR kernel (padding adds exact zeros at the end of a row).
+// a step k is one contiguous 32-element segment.  MODE 0: same per-row order
+// and rounding as the CSR kernel (padding adds exact zeros at the end of a
+// row); MODE 1 (the solver's true residual) fuses each product into the sum.
 // TC = int: absolute columns; TC = int16_t: column - row (banded matrices
 // such as grid stencils), 6 instead of 8 bytes per FP32 entry.
 template <class TV, class TX, class TY, int MODE, class TC = int, int MINB = 4>
@@ -181,10 +198,18 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
             TV p[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q)
-                if (k + q < w) p[q] = pmul(v[q], (TV)__ldg(&x[c[q]]));
+                if (k + q < w) p[q] = (TV)__ldg(&x[c[q]]);
+            if (MODE == 1) {
+                // the solver's FP64 true residual: fused multiply-adds in
+                // entry order (one FP64 instruction per entry instead of two)
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (k + q < w) sum = padd(sum, p[q]);
+                for (int q = 0; q < 8; ++q)
+                    if (k + q < w) sum = fma(v[q], p[q], sum);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (k + q < w) sum = padd(sum, pmul(v[q], p[q]));
+            }
         }
         const int r = sl * 32 + lane;
         if (r < n) {
