@@ -72,7 +72,11 @@ typedef struct sg_precond_opts {
                          from global memory, 4 the sync-free sweep (per-row
                          ready flags); reserved[1]: threads per CTA of the
                          TMA-fed sweep (128, 256 or 512; 0 = the fastest,
-                         timed at set-up); other entries must be 0 */
+                         timed at set-up); reserved[2]: two-level
+                         preconditioners compute the coarse restriction
+                         inside the TMA-fed sweep when all subdomains' CTAs
+                         fit on the GPU at once (0), or in a kernel of its
+                         own (1; same results); other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;

@@ -382,7 +382,7 @@ class Preconditioner:
     def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
                  ctx: Context | None = None, generic_sweep: bool = False,
-                 sweep: str = "tma", sweep_threads: int = 0):
+                 sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True):
         # sweep variant (testing/comparison): "tma" (default: TMA-fed level
         # records), "level" (factors read from global memory), "syncfree"
         if generic_sweep:
@@ -403,6 +403,9 @@ class Preconditioner:
         opts.reserved[0] = {"tma": 0, "level": 1, "syncfree": 4}[self.sweep]
         # threads per CTA of the TMA-fed sweep (0: timed at set-up)
         opts.reserved[1] = int(sweep_threads)
+        # two-level: coarse restriction inside the TMA-fed sweep when all the
+        # subdomains' CTAs fit at once (False: a kernel of its own; same bits)
+        opts.reserved[2] = 0 if fuse_restrict else 1
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),

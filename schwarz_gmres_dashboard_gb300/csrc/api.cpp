@@ -461,6 +461,10 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             delete pc;
             fail(SG_ERR_INVALID_ARG, "sweep threads (reserved[1]) must be 0, 128, 256 or 512");
         }
+        if (pc->opts.reserved[2] != 0 && pc->opts.reserved[2] != 1) {
+            delete pc;
+            fail(SG_ERR_INVALID_ARG, "restriction placement (reserved[2]) must be 0 or 1");
+        }
         const int sd = pc->opts.sweep_dtype, fd = pc->opts.factor_dtype;
         const bool ok = (sd == SG_FP64 && fd == SG_FP64) ||
                         (sd == SG_FP32 && (fd == SG_FP32 || fd == SG_BF16));

@@ -96,17 +96,67 @@ __device__ __forceinline__ void block_sum_multi(const T (&v)[NVMAX], int nv, dou
 // in an order that does not depend on the block size, so every sweep variant
 // and block size gives the same bits: four lane-strided accumulators, then
 // the shuffle tree.  Call from the threads of warp 0 only.
+// (r0 through L2 when other blocks of the same launch wrote it)
+template <bool CG = false>
 __device__ __forceinline__ double coarse_dot_warp0(const double* __restrict__ row,
                                                    const double* __restrict__ r0, int nc) {
     const int lane = threadIdx.x & 31;
+    auto ld = [&](int q) { return CG ? __ldcg(&r0[q]) : r0[q]; };
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     for (int q = lane; q < nc; q += 128) {
-        a0 += row[q] * r0[q];
-        if (q + 32 < nc) a1 += row[q + 32] * r0[q + 32];
-        if (q + 64 < nc) a2 += row[q + 64] * r0[q + 64];
-        if (q + 96 < nc) a3 += row[q + 96] * r0[q + 96];
+        a0 += row[q] * ld(q);
+        if (q + 32 < nc) a1 += row[q + 32] * ld(q + 32);
+        if (q + 64 < nc) a2 += row[q + 64] * ld(q + 64);
+        if (q + 96 < nc) a3 += row[q + 96] * ld(q + 96);
     }
     return warp_sum((a0 + a1) + (a2 + a3));
+}
+
+// --------------------------------------------------------- coarse restriction
+// sum_q x[owned[q]] over one subdomain's owned rows, in an order that does
+// not depend on the block size: chunks of RC_CHUNK positions, each summed by
+// one warp (lane l takes positions l, l+32, ... of the chunk into four
+// accumulators in the input precision, combined pairwise, then the shuffle
+// tree; FP64 from the warp sum on), chunk sums added in chunk order.  Every
+// thread of the block calls it; the result is valid in thread 0.  red:
+// shared scratch of RC_MAXCH doubles.
+constexpr int RC_CHUNK = 1024;
+constexpr int RC_MAXCH = 64;
+
+template <class TI>
+__device__ __forceinline__ double restrict_chunks(const int* __restrict__ owned,
+                                                  const TI* __restrict__ x, int n_own,
+                                                  double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nch = (n_own + RC_CHUNK - 1) / RC_CHUNK;
+    double total = 0.0;
+    for (int c0 = 0; c0 < nch; c0 += RC_MAXCH) {
+        const int cend = nch < c0 + RC_MAXCH ? nch : c0 + RC_MAXCH;
+        for (int c = c0 + warp; c < cend; c += nw) {
+            const int p0 = c * RC_CHUNK;
+            TI a[4] = {(TI)0, (TI)0, (TI)0, (TI)0};
+            for (int i0 = 0; i0 < RC_CHUNK / 32; i0 += 8) {
+                int idx[8];
+                TI v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int p = p0 + lane + 32 * (i0 + u);
+                    idx[u] = p < n_own ? owned[p] : -1;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = idx[u] >= 0 ? x[idx[u]] : (TI)0;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) a[u & 3] += v[u];
+            }
+            const double sum = (double)warp_sum((a[0] + a[1]) + (a[2] + a[3]));
+            if (lane == 0) red[c - c0] = sum;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int c = c0; c < cend; ++c) total += red[c - c0];
+        __syncthreads();
+    }
+    return total;
 }
 
 // ------------------------------------------------------- subdomain gather/scatter

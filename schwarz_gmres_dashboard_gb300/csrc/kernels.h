@@ -71,6 +71,8 @@ template <class TI, class TO>
 bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
                const int* active);
 int sweep_error(sg_precond* pc);
+// the TMA sweep computes the coarse restriction itself (no k_restrict launch)
+bool sweep_fuses_restrict(const sg_precond* pc);
 // ---------------------------------------------------------------- learned.cu
 // y += learned correction of the preconditioned vector y = M x (x: the
 // vector M was applied to; n: its length, checked against the stage's grid)

@@ -605,27 +605,11 @@ k_restrict(const int* __restrict__ owned_ptr, const int* __restrict__ owned,
            const double* __restrict__ cscale, const TI* __restrict__ x, double* r0,
            const int* __restrict__ active) {
     if (active && *active == 0) return;
-    __shared__ double red[32];
+    __shared__ double red[RC_MAXCH];
     const int s = blockIdx.x;
-    // four independent gathers in flight per thread, summed in a fixed order;
-    // the per-thread and in-warp sums run in the input precision, the warp
-    // sums are combined in FP64
-    TI a[4] = {(TI)0, (TI)0, (TI)0, (TI)0};
     const int q0 = owned_ptr[s], q1 = owned_ptr[s + 1];
-    int q = q0 + threadIdx.x;
-    for (; q + 3 * (int)blockDim.x < q1; q += 4 * blockDim.x) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] += x[owned[q + u * blockDim.x]];
-    }
-    for (; q < q1; q += blockDim.x) a[0] += x[owned[q]];
-    const double acc = (double)warp_sum((a[0] + a[1]) + (a[2] + a[3]));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double z = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) z += red[w];
-        r0[s] = cscale[s] * z;
-    }
+    const double z = restrict_chunks<TI>(owned + q0, x, q1 - q0, red);
+    if (threadIdx.x == 0) r0[s] = cscale[s] * z;
 }
 
 template <class T>
@@ -886,10 +870,12 @@ void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active,
     if (coarse) {
         if (!pc->owned_ptr_d.p || !pc->owned_d.p || !pc->cscale_d.p || !pc->r0.p)
             fail(SG_ERR_INTERNAL, "coarse-space device buffers missing");
-        k_restrict<TI><<<pc->nc, 1024, 0, ctx->stream>>>(pc->owned_ptr_d.p, pc->owned_d.p,
-                                                        pc->cscale_d.p, x, pc->r0.p, active);
-        SG_CUDA(cudaGetLastError());
-        count_launch(ctx);
+        if (!sweep_fuses_restrict(pc)) {
+            k_restrict<TI><<<pc->nc, 1024, 0, ctx->stream>>>(pc->owned_ptr_d.p, pc->owned_d.p,
+                                                            pc->cscale_d.p, x, pc->r0.p, active);
+            SG_CUDA(cudaGetLastError());
+            count_launch(ctx);
+        }
     }
     if (asm_mode) SG_CUDA(cudaMemsetAsync(y, 0, sizeof(TO) * (size_t)n, ctx->stream));
     if (sweep_tma<TI, TO>(pc, x, y, asm_mode ? 1 : 0, coarse, exact, active)) return;

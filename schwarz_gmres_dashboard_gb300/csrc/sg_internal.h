@@ -293,6 +293,8 @@ struct sg_precond {
     bool use_sf = false;   // sync-free sweep (per-row ready flags)
     int rec_depth = 0;               // ring stages in shared memory
     int sweep_threads = 0;           // threads per CTA of the TMA-fed sweep
+    bool fuse_restrict = false;      // two-level: restriction inside the sweep (all CTAs resident)
+    sg::DBuf<unsigned> coarse_sync;  // its arrival / departure counters
     long long rec_stage_bytes = 0;   // largest record
     long long rec_total = 0;
     std::vector<long long> h_rec_off_f, h_rec_off_b;  // byte offset per level

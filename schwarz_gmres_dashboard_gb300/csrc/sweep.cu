@@ -280,7 +280,19 @@ struct RecArgs {
     int max_levels;  // largest nlev_f + nlev_b over the subdomains
     int* err;
     const int* sub_on;  // optional per-subdomain switch (0: the subdomain is skipped)
+    // coarse restriction fused into the sweep (cooperative launch, all blocks
+    // resident): each block writes r0[s] and counts itself in sync[0]; sync[1]
+    // counts the blocks done with r0 (the last one resets both)
+    int fuse;
+    double* r0w;
+    unsigned* sync;
 };
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 // mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
 template <class TI, class TO, class TS, class TF, bool EXACT>
@@ -290,6 +302,8 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     if (active && *active == 0) return;
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ double s_zc;
+    __shared__ double s_red[RC_MAXCH];
+    __shared__ int s_ok;
     const int D = a.depth;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // D x 8 B
     const int NC = (int)blockDim.x;
@@ -349,12 +363,23 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     const int tp = inf.tshift;
     gather_rows<TS>(t, x, dof, n, NC, tp);
     if (threadIdx.x == 0) t[tslot(n, tp)] = (TS)0;
-    if (coarse) {
-        if (threadIdx.x < 32) {
-            const double z = coarse_dot_warp0(a.a0inv + (size_t)s * a.nc, a.r0, a.nc);
-            if (threadIdx.x == 0) s_zc = inf.cscale * z;
+    if (coarse && a.fuse && (int)blockIdx.x >= (int)gridDim.x / 2) {
+        // coarse restrictions (the order of k_restrict), published for the
+        // other blocks before the level loop.  Blocks run largest subdomain
+        // first, so the second half -- the smaller subdomains, with slack --
+        // computes its own and its mirror block's, and the critical first
+        // half computes none.
+        const int mirror = (int)gridDim.x - 1 - (int)blockIdx.x;
+        for (int pass = 0; pass < (mirror == (int)blockIdx.x ? 1 : 2); ++pass) {
+            const int sr = pass == 0 ? s : a.order[mirror];
+            const SubInfo ir = pass == 0 ? inf : a.info[sr];
+            const double z = restrict_chunks<TI>(a.owned + ir.own_off, x, ir.n_own, s_red);
+            if (threadIdx.x == 0) {
+                a.r0w[sr] = ir.cscale * z;
+                __threadfence();
+                atomicAdd(&a.sync[0], 1u);
+            }
         }
-        __syncthreads();
     }
     __syncthreads();
 
@@ -415,6 +440,43 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
         }
     }
 
+    if (coarse) {
+        if (a.fuse) {
+            // every block published its restriction before its level loop;
+            // all blocks are resident (cooperative launch), so this bounded
+            // wait ends as soon as the slowest block got there
+            if (threadIdx.x == 0) {
+                const long long t0 = clock64();
+                int ok = 1;
+                while (ld_acquire(&a.sync[0]) < gridDim.x) {
+                    if (clock64() - t0 > WAIT_CYCLES) {
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+                s_ok = ok;
+            }
+            __syncthreads();
+            if (!s_ok) {
+                if (threadIdx.x == 0) atomicExch(a.err, 1);
+                return;
+            }
+        }
+        if (threadIdx.x < 32) {
+            const double z = a.fuse ? coarse_dot_warp0<true>(a.a0inv + (size_t)s * a.nc, a.r0, a.nc)
+                                    : coarse_dot_warp0<false>(a.a0inv + (size_t)s * a.nc, a.r0, a.nc);
+            if (threadIdx.x == 0) {
+                s_zc = inf.cscale * z;
+                // the last block done with r0 resets the counters
+                if (a.fuse && atomicAdd(&a.sync[1], 1u) == gridDim.x - 1) {
+                    a.sync[0] = 0u;
+                    a.sync[1] = 0u;
+                }
+            }
+        }
+        __syncthreads();
+    }
     const double zc = coarse ? s_zc : 0.0;
     if (mode == 0) {
         scatter_owned<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
@@ -430,8 +492,11 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
 }
 
-RecArgs rec_args(sg_precond* pc) {
+RecArgs rec_args(sg_precond* pc, bool fuse) {
     RecArgs a;
+    a.fuse = fuse ? 1 : 0;
+    a.r0w = pc->r0.p;
+    a.sync = pc->coarse_sync.p;
     a.info = pc->info.p;
     a.order = pc->order.p;
     a.dofs = pc->dofs.p;
@@ -464,13 +529,31 @@ size_t sweep_smem(const sg_precond* pc, int depth) {
 }
 
 template <class TI, class TO, class TS, class TF, bool EXACT>
-void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active) {
+void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active,
+                bool fuse = false) {
     const size_t smem = sweep_smem(pc, pc->rec_depth);
     const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
-    SG_CUDA(cudaFuncSetAttribute(k_sweep_tma<TI, TO, TS, TF, EXACT>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_sweep_tma<TI, TO, TS, TF, EXACT><<<pc->nparts, nt, smem, pc->ctx->stream>>>(
-        rec_args(pc), x, y, mode, coarse ? 1 : 0, active);
+    auto kern = k_sweep_tma<TI, TO, TS, TF, EXACT>;
+    SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RecArgs a = rec_args(pc, fuse);
+    const int coarse_i = coarse ? 1 : 0;
+    if (fuse) {
+        // the blocks wait for one another's restriction: co-residency is
+        // guaranteed by the cooperative launch (checked at set-up)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(pc->nparts);
+        cfg.blockDim = dim3(nt);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = pc->ctx->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        SG_CUDA(cudaLaunchKernelEx(&cfg, kern, a, x, y, mode, coarse_i, active));
+    } else {
+        kern<<<pc->nparts, nt, smem, pc->ctx->stream>>>(a, x, y, mode, coarse_i, active);
+    }
     SG_CUDA(cudaGetLastError());
     count_launch(pc->ctx);
 }
@@ -541,6 +624,35 @@ void rec_setup_device(sg_precond* pc) {
     } else {
         tune_sweep_threads(pc);
     }
+    // two-level: the coarse restriction runs inside the sweep when every
+    // subdomain's CTA can be resident at once (a cooperative launch)
+    pc->fuse_restrict = false;
+    if (pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS) {
+        const size_t smem = sweep_smem(pc, pc->rec_depth);
+        const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
+        int coop = 0, per_sm = 0;
+        SG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+        auto occupancy = [&](auto kern) {
+            SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+            SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
+        };
+        if (pc->opts.sweep_dtype == SG_FP64)
+            occupancy(k_sweep_tma<double, double, double, double, false>);
+        else if (pc->opts.factor_dtype == SG_BF16)
+            occupancy(k_sweep_tma<float, float, float, uint16_t, false>);
+        else
+            occupancy(k_sweep_tma<float, float, float, float, false>);
+        if (coop && (long long)per_sm * ctx->num_sms >= pc->nparts && pc->opts.reserved[2] == 0) {
+            pc->coarse_sync.alloc(2);
+            pc->coarse_sync.zero(st);
+            pc->fuse_restrict = true;
+        }
+    }
+}
+
+bool sweep_fuses_restrict(const sg_precond* pc) {
+    return pc->use_rec && pc->rec_depth > 0 && pc->fuse_restrict && !pc->sub_on;
 }
 
 // Times the sweep (RAS mode, no coarse term, zero input) with 128, 256 and
@@ -601,13 +713,14 @@ template <class TI, class TO>
 bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
                const int* active) {
     if (!pc->use_rec || pc->rec_depth == 0) return false;
+    const bool fuse = coarse && sweep_fuses_restrict(pc);
     if (pc->opts.sweep_dtype == SG_FP64) {
-        if (exact) launch_tma<TI, TO, double, double, true>(pc, x, y, mode, coarse, active);
-        else launch_tma<TI, TO, double, double, false>(pc, x, y, mode, coarse, active);
+        if (exact) launch_tma<TI, TO, double, double, true>(pc, x, y, mode, coarse, active, fuse);
+        else launch_tma<TI, TO, double, double, false>(pc, x, y, mode, coarse, active, fuse);
     } else if (pc->opts.factor_dtype == SG_BF16) {
-        launch_tma<TI, TO, float, uint16_t, false>(pc, x, y, mode, coarse, active);
+        launch_tma<TI, TO, float, uint16_t, false>(pc, x, y, mode, coarse, active, fuse);
     } else {
-        launch_tma<TI, TO, float, float, false>(pc, x, y, mode, coarse, active);
+        launch_tma<TI, TO, float, float, false>(pc, x, y, mode, coarse, active, fuse);
     }
     return true;
 }
@@ -617,6 +730,12 @@ int sweep_error(sg_precond* pc) {
     int e = 0;
     SG_CUDA(cudaMemcpyAsync(&e, pc->err_d.p, sizeof(int), cudaMemcpyDeviceToHost, pc->ctx->stream));
     SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
+    // a sweep that gave up may have left the fused restriction's counters
+    // mid-count: clear them with the error word
+    if (e && pc->coarse_sync.p) {
+        pc->coarse_sync.zero(pc->ctx->stream);
+        SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
+    }
     return e;
 }
 

@@ -522,3 +522,36 @@ def test_use_before_setup_and_bad_csr(sg):
     with pytest.raises(sg.SgError) as e:
         bad.upload()
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("kind", [sg_kind for sg_kind in ("twolevel_ras", "twolevel_asm")])
+@pytest.mark.parametrize("dt", ["fp64", "bf16"])
+def test_fused_restriction_same_bits(sg, kind, dt):
+    """The coarse restriction computed inside the TMA-fed sweep (cooperative
+    launch) and in a kernel of its own sum in the same order: the apply and a
+    whole solve give the same bits either way."""
+    A = sg.make_varcoef_3d(24, 20, 22, 1.0, 5.0, 6)
+    part = sg.partition_boxes(24, 20, 22, 12, 0.1, 2)
+    x = sg.uniform(A.nrows, seed=10)
+    b = A.spmv(x)
+    fdt = sg.FP64 if dt == "fp64" else sg.BF16
+    sdt = sg.FP64 if dt == "fp64" else sg.FP32
+    ft = sg.FineLevelType.RAS if kind == "twolevel_ras" else sg.FineLevelType.ASM
+    ys, xs = [], []
+    for fuse in (True, False):
+        pc = sg.TwoLevelSchwarzPrecond(12, 1, ft, part, fdt, sdt, fuse_restrict=fuse)
+        pc.setup(A)
+        ys.append(pc.apply(x))
+        if kind == "twolevel_ras":
+            xx = np.zeros(A.nrows)
+            r = sg.gmres(A, b, xx, pc, sg.GMRESParams(
+                restart=30, max_iter=2000, tol=1e-9, tol_kind=sg.TOL_TRUE_REL,
+                precision=sg.FP32 if dt == "bf16" else sg.FP64))
+            assert r.converged
+            xs.append(xx)
+    if kind == "twolevel_ras":
+        assert np.array_equal(ys[0], ys[1])
+        assert np.array_equal(xs[0], xs[1])
+    else:
+        # ASM adds overlapping rows atomically: order of the adds may differ
+        assert rel(ys[0], ys[1]) <= 1e-12 if dt == "fp64" else rel(ys[0], ys[1]) <= 1e-6
