@@ -32,6 +32,13 @@ __device__ __forceinline__ float bf16_to_f(uint16_t b) {
     return __uint_as_float(((unsigned)b) << 16);
 }
 
+// The backward sweep's division by the diagonal: FP64 divides (the
+// reference's rounding); FP32 multiplies by the reciprocal, which depends
+// only on the diagonal (loaded early), so it leaves the row's dependency
+// chain -- one multiply instead of a division on it.
+__device__ __forceinline__ double div_diag(double acc, double d) { return acc / d; }
+__device__ __forceinline__ float div_diag(float acc, float d) { return acc * (1.0f / d); }
+
 template <class TS>
 struct Load;
 template <>

@@ -181,7 +181,7 @@ __device__ __forceinline__ void sweep_levels(TS* t, int n, int nlev, const int* 
                 TS acc = t[r];
                 for (int k = 0; k < w; ++k)
                     acc = msub(acc, Load<TS>::f(val[(size_t)k * n + p]), t[col[(size_t)k * n + p]]);
-                if (BACK) acc = acc / Load<TS>::f(diag[p]);
+                if (BACK) acc = div_diag(acc, Load<TS>::f(diag[p]));
                 t[r] = acc;
             }
             __syncthreads();
@@ -233,7 +233,7 @@ __device__ __forceinline__ void sweep_levels(TS* t, int n, int nlev, const int* 
 #pragma unroll
             for (int k = 0; k < SWEEP_WP; ++k)
                 if (k < w) acc = msub(acc, vc[k], t[cc[k]]);
-            if (BACK) acc = acc / dc;
+            if (BACK) acc = div_diag(acc, dc);
             t[rc] = acc;
         }
         // rows of this level beyond the first pass
@@ -242,7 +242,7 @@ __device__ __forceinline__ void sweep_levels(TS* t, int n, int nlev, const int* 
             TS acc = t[rr];
             for (int k = 0; k < w; ++k)
                 acc = msub(acc, Load<TS>::f(val[(size_t)k * n + q]), t[col[(size_t)k * n + q]]);
-            if (BACK) acc = acc / Load<TS>::f(diag[q]);
+            if (BACK) acc = div_diag(acc, Load<TS>::f(diag[q]));
             t[rr] = acc;
         }
         __syncthreads();
@@ -351,7 +351,7 @@ __device__ __forceinline__ void sweep_sf(TS* t, volatile unsigned char* fl, int 
                 wait_row(c);
                 acc = sf_sub<TS, EXACT>(acc, v, t[c]);
             }
-            if (BACK) acc = acc / Load<TS>::f(diag[p]);
+            if (BACK) acc = div_diag(acc, Load<TS>::f(diag[p]));
             t[r] = acc;
             __threadfence_block();
             fl[r] = epoch;
@@ -391,7 +391,7 @@ __device__ __forceinline__ void sweep_sf(TS* t, volatile unsigned char* fl, int 
                 acc = sf_sub<TS, EXACT>(acc, vc[k], t[cc[k]]);
             }
         }
-        if (BACK) acc = acc / dc;
+        if (BACK) acc = div_diag(acc, dc);
         t[rc] = acc;
         __threadfence_block();
         fl[rc] = epoch;

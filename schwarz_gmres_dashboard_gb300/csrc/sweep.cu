@@ -122,7 +122,7 @@ __device__ __forceinline__ void level_rows_w(uint32_t tb, uint32_t R, int C, int
         for (int k = 0; k < W; ++k) xk[k] = lds<TS>(tb + ST * ck[k]);
 #pragma unroll
         for (int k = 0; k < W; ++k) acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vk[k]), xk[k]);
-        if (BACK) acc = acc / Load<TS>::f(dg);
+        if (BACK) acc = div_diag(acc, Load<TS>::f(dg));
         sts(tb + ST * r, acc);
     }
 }
@@ -154,7 +154,7 @@ __device__ __forceinline__ void level_rows_any(TS* t, const unsigned char* R, in
             for (int u = 0; u < 4; ++u)
                 if (k0 + u < w) acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(vi[u]), xi[u]);
         }
-        if (back) acc = acc / Load<TS>::f(vv[w * C + q]);
+        if (back) acc = div_diag(acc, Load<TS>::f(vv[w * C + q]));
         t[r] = acc;
     }
 }
