@@ -291,7 +291,9 @@ struct sg_precond {
     // record [rows | columns | values (| diagonal)], rows padded to 8
     bool use_rec = false;
     bool use_sf = false;   // sync-free sweep (per-row ready flags)
-    int rec_depth = 0;               // ring stages in shared memory
+    int rec_depth = 0;               // ring buffers in shared memory (0: no TMA-fed sweep)
+    int rec_glev = 1;                // consecutive levels per buffer (one bulk copy)
+    long long rec_gbytes = 0;        // buffer size: the largest group of rec_glev records
     int sweep_threads = 0;           // threads per CTA of the TMA-fed sweep
     bool fuse_restrict = false;      // two-level: restriction inside the sweep (all CTAs resident)
     sg::DBuf<unsigned> coarse_sync;  // its arrival / departure counters

@@ -11,14 +11,18 @@
 //   [row slot u16 x C][column slot u16 x C x w][value x C x w](diagonal x C)
 // (C = rows rounded up to 8; a slot is the row's place in the shared-memory
 // vector, tslot, whose per-subdomain padding keeps the rows of a level in
-// distinct banks).  The block's last thread streams the records into a ring
-// of D shared-memory stages with cp.async.bulk, D levels ahead of the level
-// being computed, each stage tracked by an mbarrier (expect_tx /
-// complete_tx).  So a level costs shared-memory latency plus one barrier
-// instead of a global-memory round trip.  Every mbarrier wait is bounded
+// distinct banks).  A subdomain's records are contiguous (forward levels,
+// then backward), so the ring holds groups of K consecutive records: the
+// block's last thread copies a whole group into one of NB shared-memory
+// buffers with one cp.async.bulk, tracked by one mbarrier, NB - 1 groups
+// ahead of the group being computed.  So a level costs shared-memory latency
+// plus one barrier instead of a global-memory round trip, and the copy issue
+// and the waits are paid once per K levels.  Every mbarrier wait is bounded
 // (about one second of clock cycles); on expiry the CTA records an error
 // word, waits (bounded again) for the copies it issued, and returns without
 // touching the output.
+#include <algorithm>
+
 #include "dev_common.cuh"
 #include "kernels.h"
 #include "tma.cuh"
@@ -274,8 +278,9 @@ struct RecArgs {
     const double* a0inv;
     const double* r0;
     int nc;
-    int depth;
-    int stage_bytes;
+    int nbuf;     // record buffers in the ring
+    int glev;     // consecutive levels per buffer
+    int gbytes;   // buffer size
     int t_len;       // elements of the subdomain vector region (largest tslot(n) + 1)
     int max_levels;  // largest nlev_f + nlev_b over the subdomains
     int* err;
@@ -304,11 +309,11 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     __shared__ double s_zc;
     __shared__ double s_red[RC_MAXCH];
     __shared__ int s_ok;
-    const int D = a.depth;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // D x 8 B
+    const int NB = a.nbuf, K = a.glev;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // NB x 8 B
     const int NC = (int)blockDim.x;
-    unsigned char* stages = smraw + 128;                               // D x stage_bytes
-    TS* t = reinterpret_cast<TS*>(stages + (size_t)D * a.stage_bytes);  // n + 1
+    unsigned char* bufs = smraw + 128;                                 // NB x gbytes
+    TS* t = reinterpret_cast<TS*>(bufs + (size_t)NB * a.gbytes);       // t_len
     const int s = a.order[blockIdx.x];
     if (a.sub_on && !a.sub_on[s]) return;  // subdomain not needed by this apply
     const SubInfo inf = a.info[s];
@@ -338,25 +343,28 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
 
     const uint32_t bytes_f = (uint32_t)(2 + inf.wl * (2 + sf));
     const uint32_t bytes_b = (uint32_t)(2 + inf.wu * (2 + sf) + sf);
-    // copy level g's record into ring stage st (= g mod D)
-    auto issue = [&](int g, int st) {
-        const uint32_t bytes = (uint32_t)m_C[g] * (g < nf ? bytes_f : bytes_b);
-        const uint32_t bar = smem_u32(&bars[st]);
+    const int ngrp = (T + K - 1) / K;
+    // copy the records of group q (levels qK .. qK+K-1, contiguous) into
+    // buffer b with one bulk copy
+    auto issue = [&](int q, int b) {
+        const int g0 = q * K, g1 = (g0 + K < T ? g0 + K : T) - 1;
+        const uint32_t bytes = (uint32_t)(m_off[g1] - m_off[g0]) +
+                               (uint32_t)m_C[g1] * (g1 < nf ? bytes_f : bytes_b);
+        const uint32_t bar = smem_u32(&bars[b]);
         mbar_expect_tx(bar, bytes);
-        bulk_g2s(smem_u32(stages + (size_t)st * a.stage_bytes), a.rec + m_off[g], bytes, bar);
+        bulk_g2s(smem_u32(bufs + (size_t)b * a.gbytes), a.rec + m_off[g0], bytes, bar);
     };
 
     // the producer is the block's last thread: levels rarely have rows for
     // it, so issuing the next copy overlaps the other threads' work (a
-    // separate producer warp, signalled through per-stage "empty" mbarriers,
-    // measured slower at every block size)
+    // separate producer warp, signalled through per-buffer "empty"
+    // mbarriers, measured slower at every block size)
     const bool producer = threadIdx.x == blockDim.x - 1;
     if (producer) {
-        for (int i = 0; i < D; ++i) mbar_init(smem_u32(&bars[i]), 1);
+        for (int i = 0; i < NB; ++i) mbar_init(smem_u32(&bars[i]), 1);
         fence_mbar_init();
         fence_proxy_async();
-        const int pre = T < D ? T : D;
-        for (int g = 0; g < pre; ++g) issue(g, g);
+        for (int q = 0; q < ngrp && q < NB; ++q) issue(q, q);
     }
     // gather while the first records are in flight
     const int* dof = a.dofs + inf.row_off;
@@ -383,61 +391,66 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
     __syncthreads();
 
-    // The level loop is the latency chain of the sweep: ring stage and phase
-    // advance without divisions, the next level's row counts load while this
-    // level computes, a failed wait travels in the level barrier itself, and
-    // every thread observes the ring's mbarriers (acquiring the bulk copies)
-    // K = D/2 levels at a time: the copy of level g + K - 1 was issued after
-    // the barrier of level g + K - 1 - D < g, so it is in flight already.
-    const int K = D / 2 > 1 ? D / 2 : 1;
-    const uint32_t stages_s = smem_u32(stages), t_s = smem_u32(t);
-    int st = 0, grp = 0;
+    // The level loop is the latency chain of the sweep.  Per level: the rows,
+    // then one barrier.  Per group of K levels: every thread observes the
+    // buffer's mbarrier (acquiring the bulk copy) at the first level, a
+    // failed wait travels in that level's barrier, and after the group's last
+    // level the producer refills the buffer with group q + NB.  Buffer and
+    // phase advance without divisions; the next level's row counts load while
+    // this level computes.
+    const uint32_t bufs_s = smem_u32(bufs), t_s = smem_u32(t);
+    int q = 0, b = 0, gstart = 0, gend = T < K ? T : K;
     uint32_t ph = 0;
     int c = T > 0 ? m_c[0] : 0, C = T > 0 ? m_C[0] : 0;
+    long long base_off = T > 0 ? m_off[0] : 0;
     for (int g = 0; g < T; ++g) {
-        // a thread whose wait expires computes nothing and fails the barrier
         bool ok = true;
-        if (grp == 0) {
-            grp = T - g < K ? T - g : K;
-            int s2 = st;
-            uint32_t p2 = ph;
-            for (int h = 0; h < grp && ok; ++h) {
-                ok = mbar_wait(smem_u32(&bars[s2]), p2, WAIT_CYCLES);
-                if (++s2 == D) {
-                    s2 = 0;
-                    p2 ^= 1u;
-                }
-            }
-        }
-        --grp;
+        if (g == gstart) ok = mbar_wait(smem_u32(&bars[b]), ph, WAIT_CYCLES);
         const int cn = g + 1 < T ? m_c[g + 1] : 0, Cn = g + 1 < T ? m_C[g + 1] : 0;
         if (ok) {
             const bool back = g >= nf;
-            const uint32_t off = (uint32_t)st * (uint32_t)a.stage_bytes;
-            level_rows<TS, TF, EXACT>(t, t_s, stages + off, stages_s + off, C, c,
+            const uint32_t off = (uint32_t)b * (uint32_t)a.gbytes + (uint32_t)(m_off[g] - base_off);
+            level_rows<TS, TF, EXACT>(t, t_s, bufs + off, bufs_s + off, C, c,
                                       back ? inf.wu : inf.wl, back, NC);
         }
-        if (__syncthreads_or(ok ? 0 : 1)) {
-            // a record never arrived: report, drain what was issued, leave y alone
-            if (producer) {
-                atomicExch(a.err, 1);
-                const int last = (g + D < T ? g + D : T);
-                for (int h = g + 1; h < last; ++h)
-                    mbar_wait(smem_u32(&bars[h % D]), (uint32_t)((h / D) & 1), WAIT_CYCLES / 8);
+        if (g == gstart) {
+            if (__syncthreads_or(ok ? 0 : 1)) {
+                // a record group never arrived: report, drain what was
+                // issued, leave y alone
+                if (producer) {
+                    atomicExch(a.err, 1);
+                    int b2 = b;
+                    uint32_t p2 = ph;
+                    for (int h = q; h < ngrp && h < q + NB; ++h) {
+                        mbar_wait(smem_u32(&bars[b2]), p2, WAIT_CYCLES / 8);
+                        if (++b2 == NB) {
+                            b2 = 0;
+                            p2 ^= 1u;
+                        }
+                    }
+                }
+                return;
             }
-            return;
+        } else {
+            __syncthreads();
         }
-        // stage st is free again: refill it with level g + D
-        if (producer && g + D < T) {
-            fence_proxy_async();
-            issue(g + D, st);
+        if (g + 1 == gend) {
+            // buffer b is free again: refill it with group q + NB
+            if (producer && q + NB < ngrp) {
+                fence_proxy_async();
+                issue(q + NB, b);
+            }
+            ++q;
+            if (++b == NB) {
+                b = 0;
+                ph ^= 1u;
+            }
+            gstart = gend;
+            gend = gstart + K < T ? gstart + K : T;
+            if (gstart < T) base_off = m_off[gstart];
         }
         c = cn;
         C = Cn;
-        if (++st == D) {
-            st = 0;
-            ph ^= 1u;
-        }
     }
 
     if (coarse) {
@@ -512,8 +525,9 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     a.a0inv = pc->a0inv.p;
     a.r0 = pc->r0.p;
     a.nc = pc->nc;
-    a.depth = pc->rec_depth;
-    a.stage_bytes = (int)pc->rec_stage_bytes;
+    a.nbuf = pc->rec_depth;
+    a.glev = pc->rec_glev;
+    a.gbytes = (int)pc->rec_gbytes;
     a.t_len = pc->t_len;
     a.max_levels = pc->max_levels;
     a.err = pc->err_d.p;
@@ -521,17 +535,21 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     return a;
 }
 
-size_t sweep_smem(const sg_precond* pc, int depth) {
+// dynamic shared memory of the sweep: mbarriers, nbuf record buffers of
+// gbytes, the subdomain vector, per-level metadata
+size_t sweep_smem_for(const sg_precond* pc, int nbuf, long long gbytes) {
     const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
     const size_t tbytes = ((size_t)pc->t_len * ts + 15) & ~(size_t)15;
-    return 128 + (size_t)depth * (size_t)pc->rec_stage_bytes + tbytes +
-           (size_t)pc->max_levels * 16;
+    return 128 + (size_t)nbuf * (size_t)gbytes + tbytes + (size_t)pc->max_levels * 16;
+}
+size_t sweep_smem(const sg_precond* pc) {
+    return sweep_smem_for(pc, pc->rec_depth, pc->rec_gbytes);
 }
 
 template <class TI, class TO, class TS, class TF, bool EXACT>
 void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active,
                 bool fuse = false) {
-    const size_t smem = sweep_smem(pc, pc->rec_depth);
+    const size_t smem = sweep_smem(pc);
     const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
     auto kern = k_sweep_tma<TI, TO, TS, TF, EXACT>;
     SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -562,8 +580,37 @@ void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const
 
 void tune_sweep_threads(sg_precond* pc);
 
-// Packs the level records of the configured factor type and picks the ring
-// depth: as deep as fits while as many subdomains as possible run at once.
+// Largest byte span of K consecutive level records of one subdomain (its
+// forward then backward records are contiguous in the packed array).
+static long long rec_group_max(const sg_precond* pc, int K) {
+    const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
+                         : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
+    long long mx = 0;
+    std::vector<long long> offs;
+    for (int s = 0; s < pc->nparts; ++s) {
+        const SubInfo& inf = pc->h_info[s];
+        const int T = inf.nlev_f + inf.nlev_b;
+        if (T == 0) continue;
+        offs.assign((size_t)T + 1, 0);
+        for (int l = 0; l < inf.nlev_f; ++l) offs[l] = pc->h_rec_off_f[inf.lev_off_f + l];
+        for (int l = 0; l < inf.nlev_b; ++l)
+            offs[inf.nlev_f + l] = pc->h_rec_off_b[inf.lev_off_b + l];
+        const long long last_rows = inf.nlev_b > 0
+                                        ? pc->h_rec_rows_b[inf.lev_off_b + inf.nlev_b - 1]
+                                        : pc->h_rec_rows_f[inf.lev_off_f + inf.nlev_f - 1];
+        const long long last_bytes = inf.nlev_b > 0 ? last_rows * (2 + inf.wu * (2 + sf) + sf)
+                                                    : last_rows * (2 + inf.wl * (2 + sf));
+        offs[T] = offs[T - 1] + last_bytes;
+        for (int g0 = 0; g0 < T; g0 += K) {
+            const int g1 = g0 + K < T ? g0 + K : T;
+            mx = std::max(mx, offs[g1] - offs[g0]);
+        }
+    }
+    return mx;
+}
+
+// Packs the level records of the configured factor type and sizes the
+// record ring so that as many subdomains as possible run at once.
 void rec_setup_device(sg_precond* pc) {
     if (!pc->use_rec) return;
     sg_ctx* ctx = pc->ctx;
@@ -579,23 +626,39 @@ void rec_setup_device(sg_precond* pc) {
     const int static_smem = 1024;  // reduction scratch and the like
     // CTAs per SM needed to keep every subdomain resident at once
     const int want = (pc->nparts + ctx->num_sms - 1) / ctx->num_sms;
-    int depth = 0;
-    for (int per_sm = want < 1 ? 1 : want; per_sm >= 1 && depth == 0; --per_sm) {
+    // ring: nbuf buffers, each holding K consecutive level records (a
+    // subdomain's records are contiguous: forward levels, then backward), so
+    // one bulk copy and one mbarrier serve K levels.  Prefer K*(nbuf-1)
+    // levels of lead (up to 8), then larger K, under the CTAs-per-SM budget.
+    int nbuf = 0, glev = 1;
+    long long gbytes = 0;
+    for (int per_sm = want < 1 ? 1 : want; per_sm >= 1 && nbuf == 0; --per_sm) {
         const long long budget = (long long)sm_smem / per_sm - static_smem - 1024;
-        for (int d : {8, 6, 4, 3, 2}) {
-            const long long need = (long long)sweep_smem(pc, d);
-            if (need <= budget && need <= max_smem - static_smem) {
-                depth = d;
-                break;
+        int best = -1;
+        for (int K : {8, 6, 4, 3, 2, 1}) {
+            const long long g = (rec_group_max(pc, K) + 127) & ~127ll;
+            for (int nb : {3, 2}) {
+                const long long need = (long long)sweep_smem_for(pc, nb, g);
+                if (need > budget || need > max_smem - static_smem) continue;
+                const int lead = (nb - 1) * K;
+                const int score = (lead < 8 ? lead : 8) * 10 + K;
+                if (score > best) {
+                    best = score;
+                    nbuf = nb;
+                    glev = K;
+                    gbytes = g;
+                }
             }
         }
     }
     // an mbarrier transaction count stays below 2^20 bytes
-    if (depth == 0 || pc->rec_stage_bytes >= (1 << 20) || (pc->opts.reserved[0] & 1)) {
+    if (nbuf == 0 || gbytes >= (1 << 20) || (pc->opts.reserved[0] & 1)) {
         pc->use_rec = false;
         return;
     }
-    pc->rec_depth = depth;
+    pc->rec_depth = nbuf;
+    pc->rec_glev = glev;
+    pc->rec_gbytes = gbytes;
     pc->rec_off_f_d.upload(pc->h_rec_off_f, st);
     pc->rec_off_b_d.upload(pc->h_rec_off_b, st);
     pc->rec_rows_f_d.upload(pc->h_rec_rows_f, st);
@@ -628,7 +691,7 @@ void rec_setup_device(sg_precond* pc) {
     // subdomain's CTA can be resident at once (a cooperative launch)
     pc->fuse_restrict = false;
     if (pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS) {
-        const size_t smem = sweep_smem(pc, pc->rec_depth);
+        const size_t smem = sweep_smem(pc);
         const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
         int coop = 0, per_sm = 0;
         SG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
