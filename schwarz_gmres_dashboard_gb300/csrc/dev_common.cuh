@@ -174,20 +174,20 @@ __device__ __forceinline__ double restrict_chunks(const int* __restrict__ owned,
 // value loads in flight, which the latency of a cold gather needs.
 constexpr int SUB_ILP = 8;
 
-template <class TS, class TI>
+template <class TS, class TI, int ILP = SUB_ILP>
 __device__ __forceinline__ void gather_rows(TS* t, const TI* __restrict__ x,
                                             const int* __restrict__ dof, int n, int bs,
                                             int p = 0) {
     int li = threadIdx.x;
-    for (; li + (SUB_ILP - 1) * bs < n; li += SUB_ILP * bs) {
-        int d[SUB_ILP];
+    for (; li + (ILP - 1) * bs < n; li += ILP * bs) {
+        int d[ILP];
 #pragma unroll
-        for (int u = 0; u < SUB_ILP; ++u) d[u] = dof[li + u * bs];
-        TI v[SUB_ILP];
+        for (int u = 0; u < ILP; ++u) d[u] = dof[li + u * bs];
+        TI v[ILP];
 #pragma unroll
-        for (int u = 0; u < SUB_ILP; ++u) v[u] = x[d[u]];
+        for (int u = 0; u < ILP; ++u) v[u] = x[d[u]];
 #pragma unroll
-        for (int u = 0; u < SUB_ILP; ++u) t[tslot(li + u * bs, p)] = Load<TS>::f(v[u]);
+        for (int u = 0; u < ILP; ++u) t[tslot(li + u * bs, p)] = Load<TS>::f(v[u]);
     }
     for (; li < n; li += bs) t[tslot(li, p)] = Load<TS>::f(x[dof[li]]);
 }

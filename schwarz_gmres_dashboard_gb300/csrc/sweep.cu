@@ -401,15 +401,25 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     const uint32_t bufs_s = smem_u32(bufs), t_s = smem_u32(t);
     int q = 0, b = 0, gstart = 0, gend = T < K ? T : K;
     uint32_t ph = 0;
+    // level g's rows (c), padded rows (C) and record offset in its buffer
+    // (roff) are in registers; the next level's load during this level and
+    // are used after its barrier, so no shared-memory load heads a level
     int c = T > 0 ? m_c[0] : 0, C = T > 0 ? m_C[0] : 0;
     long long base_off = T > 0 ? m_off[0] : 0;
+    uint32_t roff = 0;
     for (int g = 0; g < T; ++g) {
         bool ok = true;
         if (g == gstart) ok = mbar_wait(smem_u32(&bars[b]), ph, WAIT_CYCLES);
-        const int cn = g + 1 < T ? m_c[g + 1] : 0, Cn = g + 1 < T ? m_C[g + 1] : 0;
+        int cn = 0, Cn = 0;
+        long long on = 0;
+        if (g + 1 < T) {
+            cn = m_c[g + 1];
+            Cn = m_C[g + 1];
+            on = m_off[g + 1];
+        }
         if (ok) {
             const bool back = g >= nf;
-            const uint32_t off = (uint32_t)b * (uint32_t)a.gbytes + (uint32_t)(m_off[g] - base_off);
+            const uint32_t off = (uint32_t)b * (uint32_t)a.gbytes + roff;
             level_rows<TS, TF, EXACT>(t, t_s, bufs + off, bufs_s + off, C, c,
                                       back ? inf.wu : inf.wl, back, NC);
         }
@@ -447,8 +457,9 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             }
             gstart = gend;
             gend = gstart + K < T ? gstart + K : T;
-            if (gstart < T) base_off = m_off[gstart];
+            base_off = on;  // the next level opens the new group
         }
+        roff = (uint32_t)(on - base_off);
         c = cn;
         C = Cn;
     }
