@@ -46,16 +46,30 @@ __device__ void rot_apply(double c, double s, double& h1, double& h2) {
     h2 = t2;
 }
 
-// Completes Arnoldi step j once ||w''||^2 is known (thread 0 of the last block).
+// Completes Arnoldi step j once ||w''||^2 is known (all threads of the last block).
 __device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double* hist,
                                  int hist_cap) {
+    // the column, the earlier rotations and g(j..j+1) come to shared memory
+    // with every thread; thread 0 then runs the serial part from there
+    __shared__ double hc[SG_MMAX + 2], csv[SG_MMAX], snv[SG_MMAX], gv[2];
     const int ld = m + 1;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) hc[i] = st->hsum[i];
+    for (int i = threadIdx.x; i < j; i += blockDim.x) {
+        csv[i] = st->cs[i];
+        snv[i] = st->sn[i];
+    }
+    if (threadIdx.x == 0) {
+        gv[0] = st->g[j];
+        gv[1] = st->g[j + 1];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     const double nrm = sqrt(ss);
     double* Hc = st->H + (size_t)j * ld;
-    for (int i = 0; i <= j; ++i) Hc[i] = st->hsum[i];
-    Hc[j + 1] = nrm;
+    hc[j + 1] = nrm;
     if (!(nrm >= 1e-30)) {
         // breakdown (src/core/gmres.cpp:297-300): this column is used as is
+        for (int i = 0; i <= j + 1; ++i) Hc[i] = hc[i];
         if (!isfinite(nrm)) {
             st->nonfinite = 1;
             st->done = 1;
@@ -66,11 +80,17 @@ __device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double
         return;
     }
     st->vscale[j + 1] = 1.0 / nrm;
-    for (int i = 0; i < j; ++i) rot_apply(st->cs[i], st->sn[i], Hc[i], Hc[i + 1]);
-    rot_compute(st->cs[j], st->sn[j], Hc[j], Hc[j + 1]);
-    rot_apply(st->cs[j], st->sn[j], Hc[j], Hc[j + 1]);
-    rot_apply(st->cs[j], st->sn[j], st->g[j], st->g[j + 1]);
-    const double res = fabs(st->g[j + 1]);
+    for (int i = 0; i < j; ++i) rot_apply(csv[i], snv[i], hc[i], hc[i + 1]);
+    double c, sn;
+    rot_compute(c, sn, hc[j], hc[j + 1]);
+    rot_apply(c, sn, hc[j], hc[j + 1]);
+    rot_apply(c, sn, gv[0], gv[1]);
+    st->cs[j] = c;
+    st->sn[j] = sn;
+    st->g[j] = gv[0];
+    st->g[j + 1] = gv[1];
+    for (int i = 0; i <= j + 1; ++i) Hc[i] = hc[i];
+    const double res = fabs(gv[1]);
     if (hist && st->hist_len < hist_cap) hist[st->hist_len] = res;
     st->hist_len++;
     st->last_res = res;
@@ -202,64 +222,89 @@ __device__ __forceinline__ void group_sync(int grp, int nwg) {
 //      stored as raw_{j+1} with its pending correction c = h2 / ||w''||.
 // In exact arithmetic this is CGS2; the stored vectors are never rewritten.
 
-// pass A epilogue (all threads of the last block; d = tot[0..j])
+// the leading n x n block of the column-major SG_LAGM matrix M into
+// shared memory (upper triangle only when `upper`)
+__device__ __forceinline__ void stage_lag(double (*dst)[SG_LAGM + 1], const double* M, int n,
+                                          int ncol, bool upper) {
+    for (int idx = threadIdx.x; idx < n * ncol; idx += blockDim.x) {
+        const int i = idx % n, k = idx / n;
+        dst[i][k] = (!upper || i <= k) ? M[i + k * SG_LAGM] : 0.0;
+    }
+}
+
+// pass A epilogue (all threads of the last block; d = tot[0..j]): p = T^T d,
+// hsum = p - g, update coefficients u = T p -- from shared memory
 __device__ void lagged_pass_a(SolveState* st, int j, const double* d) {
-    __shared__ double p_s[SG_LAGM];
-    const double* T = st->lagT;
+    __shared__ double Ts[SG_LAGM][SG_LAGM + 1], Hs[SG_LAGM][SG_LAGM + 1];
+    __shared__ double cs[SG_LAGM], p_s[SG_LAGM];
+    const int n1 = j + 1;
+    stage_lag(Ts, st->lagT, n1, n1, true);
+    stage_lag(Hs, st->lagH, n1, j, false);
+    for (int i = threadIdx.x; i < j; i += blockDim.x) cs[i] = st->lagc[i];
+    __syncthreads();
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double s = 0.0;
-        for (int l = 0; l <= i; ++l) s += T[l + i * SG_LAGM] * d[l];
+        for (int l = 0; l <= i; ++l) s += Ts[l][i] * d[l];
         p_s[i] = s;
     }
     __syncthreads();
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double g = 0.0;
-        for (int k = (i > 0 ? i - 1 : 0); k < j; ++k) g += st->lagH[i + k * SG_LAGM] * st->lagc[k];
+        for (int k = (i > 0 ? i - 1 : 0); k < j; ++k) g += Hs[i][k] * cs[k];
         st->h[i] = p_s[i];
         st->hsum[i] = p_s[i] - g;
         double u = 0.0;
-        for (int k = i; k <= j; ++k) u += T[i + k * SG_LAGM] * p_s[k];
+        for (int k = i; k <= j; ++k) u += Ts[i][k] * p_s[k];
         st->cfu[i] = u;
     }
+    __syncthreads();
 }
 
 // pass B epilogue (all threads of the last block; r = tot[0..j], ss = ||w'||^2)
 __device__ void lagged_pass_b(SolveState* st, int j, int m, const double* r, double ss,
                               double* hist, int hist_cap) {
-    __shared__ double h2_s[SG_LAGM];
+    __shared__ double Ts[SG_LAGM][SG_LAGM + 1];
+    __shared__ double h2_s[SG_LAGM], c_s[SG_LAGM];
+    __shared__ double s_nrm2;
     __shared__ int s_ok;
-    double* T = st->lagT;
+    const int n1 = j + 1;
+    stage_lag(Ts, st->lagT, n1, n1, true);
+    __syncthreads();
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double s = 0.0;
-        for (int l = 0; l <= i; ++l) s += T[l + i * SG_LAGM] * r[l];
+        for (int l = 0; l <= i; ++l) s += Ts[l][i] * r[l];
         h2_s[i] = s;
+        const double hs = st->hsum[i] + s;  // the Hessenberg column
+        st->hsum[i] = hs;
+        st->lagH[i + j * SG_LAGM] = hs;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double nrm2 = ss;
-        for (int i = 0; i <= j; ++i) {
-            nrm2 -= h2_s[i] * h2_s[i];
-            st->hsum[i] += h2_s[i];
-            st->lagH[i + j * SG_LAGM] = st->hsum[i];
-        }
+        for (int i = 0; i <= j; ++i) nrm2 -= h2_s[i] * h2_s[i];
         if (!(nrm2 > 0.0)) nrm2 = isfinite(nrm2) ? 0.0 : nrm2;
         st->lagH[j + 1 + j * SG_LAGM] = sqrt(nrm2);
-        arnoldi_finalize(st, j, m, nrm2, hist, hist_cap);
-        // the pending correction of the new stored vector
-        s_ok = (!st->breakdown && st->cycle_active && j + 1 < SG_LAGM) ? 1 : 0;
-        if (s_ok) {
-            const double vs = st->vscale[j + 1];
-            for (int k = 0; k <= j; ++k) st->lagc[k] = h2_s[k] * vs;
-            T[(j + 1) + (j + 1) * SG_LAGM] = vs;
-        }
+        s_nrm2 = nrm2;
     }
     __syncthreads();
+    arnoldi_finalize(st, j, m, s_nrm2, hist, hist_cap);
+    __syncthreads();
+    // the pending correction of the new stored vector
+    if (threadIdx.x == 0) s_ok = (!st->breakdown && st->cycle_active && j + 1 < SG_LAGM) ? 1 : 0;
+    __syncthreads();
     if (!s_ok) return;
+    const double vs = st->vscale[j + 1];
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) {
+        c_s[k] = h2_s[k] * vs;
+        st->lagc[k] = c_s[k];
+    }
+    if (threadIdx.x == 0) st->lagT[(j + 1) + (j + 1) * SG_LAGM] = vs;
+    __syncthreads();
     // T(:, j+1) = T(j+1,j+1) e_{j+1} - T(:, 0..j) c
     for (int l = threadIdx.x; l <= j; l += blockDim.x) {
         double s = 0.0;
-        for (int k = l; k <= j; ++k) s += T[l + k * SG_LAGM] * st->lagc[k];
-        T[l + (j + 1) * SG_LAGM] = -s;
+        for (int k = l; k <= j; ++k) s += Ts[l][k] * c_s[k];
+        st->lagT[l + (j + 1) * SG_LAGM] = -s;
     }
 }
 
@@ -556,7 +601,7 @@ k_upd_norm(const TV* __restrict__ raw, size_t ldv, int n, int j, int m, TV* __re
     __shared__ double bs[1], tot[1];
     TV v1[1] = {ss};
     block_sum_multi<1>(v1, 1, red, bs);
-    if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0)
+    if (last_block_reduce(partials, counter, bs, 1, tot))
         arnoldi_finalize(st, j, m, tot[0], hist, hist_cap);
 }
 
