@@ -396,7 +396,10 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
     // warp's vector values, and the w elements this thread turns into w'
     // (its lanes' elements in a one-warp group; else elements gt + r * gsz)
     TV vv[KPW][VN], nv[KPW][VN], we[VN], nwe[VN];
-    auto load_tile = [&](int tile, TV (&v)[KPW][VN], TV (&wl)[VN]) {
+    // tiles are walked in reverse: pass A (k_dots) has just streamed the
+    // basis in ascending order, so its last tiles are still in L2
+    auto load_tile = [&](int tile_l, TV (&v)[KPW][VN], TV (&wl)[VN]) {
+        const int tile = ntiles - 1 - tile_l;
         const int u = tile * 32 + lane;
         const bool ok = u < nvec;
 #pragma unroll
@@ -443,10 +446,11 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
             }
         }
         TV wn[VN];
+        const int ptile = ntiles - 1 - tile;  // the physical tile
         if (nwg == 1) {
 #pragma unroll
             for (int e = 0; e < VN; ++e) wn[e] = we[e] - ((TV)0 + part[e]);
-            const int u = tile * 32 + lane;
+            const int u = ptile * 32 + lane;
             if (u < nvec) vstore<TV>(w + (size_t)u * VN, wn);
 #pragma unroll
             for (int e = 0; e < VN; ++e) ss += wn[e] * wn[e];
@@ -463,7 +467,7 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
                     for (int g = 0; g < nwg; ++g) sum += upd[grp * nwg + g][t];
                     const TV x = we[r] - sum;
                     wsh[grp][t] = x;
-                    const int i = tile * TE + t;
+                    const int i = ptile * TE + t;
                     if (i < nfull) w[i] = x;
                 }
             }
