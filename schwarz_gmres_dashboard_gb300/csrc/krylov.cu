@@ -134,12 +134,12 @@ template <class T>
 __device__ __forceinline__ void vload(const T* p, T (&o)[Vec<T>::N]);
 template <>
 __device__ __forceinline__ void vload<double>(const double* p, double (&o)[2]) {
-    const double2 v = *reinterpret_cast<const double2*>(p);
+    const double2 v = ld_stream(reinterpret_cast<const double2*>(p));
     o[0] = v.x; o[1] = v.y;
 }
 template <>
 __device__ __forceinline__ void vload<float>(const float* p, float (&o)[4]) {
-    const float4 v = *reinterpret_cast<const float4*>(p);
+    const float4 v = ld_stream(reinterpret_cast<const float4*>(p));
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
 }
 template <class T>

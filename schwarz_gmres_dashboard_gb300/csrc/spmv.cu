@@ -156,9 +156,11 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
 }
 
 // column of SELL entry: absolute int32, or a 16-bit offset from the row
-__device__ __forceinline__ int sell_col(const int* col, long long e, int) { return __ldg(&col[e]); }
+__device__ __forceinline__ int sell_col(const int* col, long long e, int) {
+    return ldg_stream(&col[e]);
+}
 __device__ __forceinline__ int sell_col(const int16_t* col, long long e, int r) {
-    return r + (int)__ldg(&col[e]);
+    return r + (int)ldg_stream(&col[e]);
 }
 
 // SELL-32 SpMV: a warp per slice of 32 rows, a lane per row; every load of
@@ -191,7 +193,7 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 if (k + q < w) {
-                    v[q] = __ldg(&val[base + (long long)(k + q) * 32]);
+                    v[q] = ldg_stream(&val[base + (long long)(k + q) * 32]);
                     c[q] = sell_col(col, base + (long long)(k + q) * 32, row);
                 }
             }
@@ -273,7 +275,7 @@ k_spmv_sell_pipe(int n, int nslices, const long long* __restrict__ sptr,
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             if (q < ww) {
-                vv[q] = __ldg(&val[base + (long long)q * 32]);
+                vv[q] = ldg_stream(&val[base + (long long)q * 32]);
                 cc[q] = sell_col(col, base + (long long)q * 32, row);
             }
         }
