@@ -107,6 +107,38 @@ __device__ __forceinline__ int16_t ldg_stream(const int16_t* p) {
     asm("ld.global.nc.L1::no_allocate.L2::256B.u16 %0, [%1];" : "=h"(v) : "l"(p));
     return (int16_t)v;
 }
+// The same loads with an L2 cache policy (policy_evict_first(): data read
+// once per solve step, which should not displace vectors that the next
+// kernels re-read).
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float ldg_stream(const float* p, uint64_t pol) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.f32 %0, [%1], %2;"
+        : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ldg_stream(const double* p, uint64_t pol) {
+    double v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.f64 %0, [%1], %2;"
+        : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int ldg_stream(const int* p, uint64_t pol) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.s32 %0, [%1], %2;"
+        : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int16_t ldg_stream(const int16_t* p, uint64_t pol) {
+    unsigned short v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.u16 %0, [%1], %2;"
+        : "=h"(v) : "l"(p), "l"(pol));
+    return (int16_t)v;
+}
 
 // ----------------------------------------------------------------- reductions
 template <class T>

@@ -156,11 +156,11 @@ k_spmv_csr(int n, const int* __restrict__ rp, const int* __restrict__ ci,
 }
 
 // column of SELL entry: absolute int32, or a 16-bit offset from the row
-__device__ __forceinline__ int sell_col(const int* col, long long e, int) {
-    return ldg_stream(&col[e]);
+__device__ __forceinline__ int sell_col(const int* col, long long e, int, uint64_t pol) {
+    return ldg_stream(&col[e], pol);
 }
-__device__ __forceinline__ int sell_col(const int16_t* col, long long e, int r) {
-    return r + (int)ldg_stream(&col[e]);
+__device__ __forceinline__ int sell_col(const int16_t* col, long long e, int r, uint64_t pol) {
+    return r + (int)ldg_stream(&col[e], pol);
 }
 
 // SELL-32 SpMV: a warp per slice of 32 rows, a lane per row; every load of
@@ -177,6 +177,7 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
             const double* __restrict__ b, double* partials, unsigned* counter, SolveState* st) {
     if (active && *active == 0) return;
     const int lane = threadIdx.x & 31;
+    const uint64_t pol = policy_evict_first();  // the matrix streams past the basis
     const int nwarps = gridDim.x * SPMV_WARPS;
     double ss = 0.0;
     const TV sc = (MODE == 0 && scale) ? (TV)(*scale) : (TV)1;
@@ -193,8 +194,8 @@ k_spmv_sell(int n, int nslices, const long long* __restrict__ sptr, const int* _
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 if (k + q < w) {
-                    v[q] = ldg_stream(&val[base + (long long)(k + q) * 32]);
-                    c[q] = sell_col(col, base + (long long)(k + q) * 32, row);
+                    v[q] = ldg_stream(&val[base + (long long)(k + q) * 32], pol);
+                    c[q] = sell_col(col, base + (long long)(k + q) * 32, row, pol);
                 }
             }
             TV p[8];
@@ -262,6 +263,7 @@ k_spmv_sell_pipe(int n, int nslices, const long long* __restrict__ sptr,
                  const double* __restrict__ scale, const int* __restrict__ active) {
     if (active && *active == 0) return;
     const int lane = threadIdx.x & 31;
+    const uint64_t pol = policy_evict_first();
     const int nwarps = gridDim.x * SPMV_WARPS;
     const TV sc = scale ? (TV)(*scale) : (TV)1;
     int sl = blockIdx.x * SPMV_WARPS + (threadIdx.x >> 5);
@@ -275,8 +277,8 @@ k_spmv_sell_pipe(int n, int nslices, const long long* __restrict__ sptr,
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             if (q < ww) {
-                vv[q] = ldg_stream(&val[base + (long long)q * 32]);
-                cc[q] = sell_col(col, base + (long long)q * 32, row);
+                vv[q] = ldg_stream(&val[base + (long long)q * 32], pol);
+                cc[q] = sell_col(col, base + (long long)q * 32, row, pol);
             }
         }
     };

@@ -352,7 +352,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
                                (uint32_t)m_C[g1] * (g1 < nf ? bytes_f : bytes_b);
         const uint32_t bar = smem_u32(&bars[b]);
         mbar_expect_tx(bar, bytes);
-        bulk_g2s(smem_u32(bufs + (size_t)b * a.gbytes), a.rec + m_off[g0], bytes, bar);
+        bulk_g2s_stream(smem_u32(bufs + (size_t)b * a.gbytes), a.rec + m_off[g0], bytes, bar);
     };
 
     // the producer is the block's last thread: levels rarely have rows for
