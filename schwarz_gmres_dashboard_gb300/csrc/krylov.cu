@@ -22,7 +22,8 @@ namespace sg {
 
 namespace {
 
-constexpr int KT = 256;  // threads of the Krylov kernels
+constexpr int KT = 256;    // threads of the Krylov kernels
+constexpr int BS_T = 256;  // threads of the back substitution (loads; one warp solves)
 
 // Givens rotation of src/core/gmres.cpp:9-30
 __device__ void rot_compute(double& c, double& s, double a, double b) {
@@ -615,9 +616,17 @@ __global__ void __launch_bounds__(KT)
 k_cycle_init(const TV* __restrict__ raw0, int n, SolveState* st, int m, int flexible,
              double* partials, unsigned* counter) {
     if (st->done) return;
+    constexpr int VN = Vec<TV>::N;
     TV ss = (TV)0;  // per-thread sum in the basis precision
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const TV t = raw0[i];
+    const int nvec = n / VN;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nvec; u += gridDim.x * blockDim.x) {
+        TV v[VN];
+        vload<TV>(raw0 + (size_t)u * VN, v);
+#pragma unroll
+        for (int e = 0; e < VN; ++e) ss += v[e] * v[e];
+    }
+    if (blockIdx.x == 0 && (int)threadIdx.x < n - nvec * VN) {
+        const TV t = raw0[nvec * VN + threadIdx.x];
         ss += t * t;
     }
     __shared__ double red[KT / 32];
@@ -665,13 +674,13 @@ k_cycle_init(const TV* __restrict__ raw0, int n, SolveState* st, int m, int flex
 // shared memory column by column (y_i, then every lane updates its rows);
 // longer triangles use one thread.  Lagged CGS2: also the coefficients on
 // the stored vectors, cfu = T y.
-__global__ void k_backsolve(SolveState* st, int m) {
+__global__ void __launch_bounds__(BS_T) k_backsolve(SolveState* st, int m) {
     if (blockIdx.x != 0) return;
     const int k = st->kcount;
     const int ld = m + 1;
-    const int lane = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (k > SG_LAGM) {
-        if (lane != 0) return;
+        if (tid != 0) return;
         for (int i = k - 1; i >= 0; --i) {
             double yi = st->g[i];
             for (int l = i + 1; l < k; ++l) yi -= st->H[i + l * ld] * st->y[l];
@@ -679,31 +688,33 @@ __global__ void k_backsolve(SolveState* st, int m) {
         }
         return;
     }
-    __shared__ double Hs[SG_LAGM][SG_LAGM + 1];
+    // the whole block loads R (and T) with independent loads; one warp then
+    // solves, the block forms T y
+    __shared__ double Hs[SG_LAGM][SG_LAGM + 1], Ts[SG_LAGM][SG_LAGM + 1];
     __shared__ double gs[SG_LAGM], ys[SG_LAGM];
-    for (int idx = lane; idx < k * k; idx += blockDim.x) {
+    const bool lagged = st->lagged != 0;
+    for (int idx = tid; idx < k * k; idx += blockDim.x) {
         const int i = idx % k, l = idx / k;
         Hs[i][l] = i <= l ? st->H[i + l * ld] : 0.0;
+        if (lagged) Ts[i][l] = i <= l ? st->lagT[i + l * SG_LAGM] : 0.0;
     }
-    for (int i = lane; i < k; i += blockDim.x) gs[i] = st->g[i];
-    __syncwarp();
-    for (int i = k - 1; i >= 0; --i) {
-        const double yi = gs[i] / Hs[i][i];
-        if (lane == 0) ys[i] = yi;
-        for (int t = lane; t < i; t += blockDim.x) gs[t] -= Hs[t][i] * yi;
-        __syncwarp();
+    for (int i = tid; i < k; i += blockDim.x) gs[i] = st->g[i];
+    __syncthreads();
+    if (tid < 32) {
+        for (int i = k - 1; i >= 0; --i) {
+            const double yi = gs[i] / Hs[i][i];
+            if (lane == 0) ys[i] = yi;
+            for (int t = lane; t < i; t += 32) gs[t] -= Hs[t][i] * yi;
+            __syncwarp();
+        }
     }
-    for (int i = lane; i < k; i += blockDim.x) st->y[i] = ys[i];
-    if (!st->lagged) return;
+    __syncthreads();
+    for (int i = tid; i < k; i += blockDim.x) st->y[i] = ys[i];
+    if (!lagged) return;
     // V y = S (T y): coefficients on the stored vectors
-    for (int idx = lane; idx < k * k; idx += blockDim.x) {
-        const int i = idx % k, l = idx / k;
-        Hs[i][l] = i <= l ? st->lagT[i + l * SG_LAGM] : 0.0;
-    }
-    __syncwarp();
-    for (int i = lane; i < k; i += blockDim.x) {
+    for (int i = tid; i < k; i += blockDim.x) {
         double u = 0.0;
-        for (int l = i; l < k; ++l) u += Hs[i][l] * ys[l];
+        for (int l = i; l < k; ++l) u += Ts[i][l] * ys[l];
         st->cfu[i] = u;
     }
 }
@@ -808,8 +819,8 @@ int kgrid(sg_ctx* ctx, int n, int per_sm) {
 
 template <class TV>
 void launch_cycle_init(sg_ctx* ctx, const TV* raw0, int n, SolveState* st, int m, bool flexible) {
-    k_cycle_init<TV><<<kgrid(ctx, n, 2), KT, 0, ctx->stream>>>(raw0, n, st, m, flexible ? 1 : 0,
-                                                               ctx->partials.p, ctx->counter.p);
+    k_cycle_init<TV><<<kgrid(ctx, (n + 3) / 4, 4), KT, 0, ctx->stream>>>(
+        raw0, n, st, m, flexible ? 1 : 0, ctx->partials.p, ctx->counter.p);
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
 }
@@ -864,7 +875,7 @@ void launch_cgs2(sg_ctx* ctx, TV* raw, size_t ldv, int n, int j, int m, SolveSta
 }
 
 void launch_backsolve(sg_ctx* ctx, SolveState* st, int m) {
-    k_backsolve<<<1, 32, 0, ctx->stream>>>(st, m);
+    k_backsolve<<<1, BS_T, 0, ctx->stream>>>(st, m);
     SG_CUDA(cudaGetLastError());
     count_launch(ctx);
 }
