@@ -47,24 +47,41 @@ __device__ void rot_apply(double c, double s, double& h1, double& h2) {
     h2 = t2;
 }
 
-// Completes Arnoldi step j once ||w''||^2 is known (all threads of the last block).
-__device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double* hist,
-                                 int hist_cap) {
-    // the column, the earlier rotations and g(j..j+1) come to shared memory
-    // with every thread; thread 0 then runs the serial part from there
-    __shared__ double hc[SG_MMAX + 2], csv[SG_MMAX], snv[SG_MMAX], gv[2];
-    const int ld = m + 1;
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) hc[i] = st->hsum[i];
+// State the serial end of an Arnoldi step reads, brought to shared memory
+// (and, for thread 0, registers) in one round of loads: the column h(0..j),
+// the earlier rotations, g(j..j+1) and the stopping-test scalars.
+struct FinalizeIn {
+    double hc[SG_MMAX + 2], csv[SG_MMAX], snv[SG_MMAX], gv[2];
+    double tol, bnorm, est_scale;
+    int tol_kind, hist_len, total_iter;
+};
+
+// all threads of the block: loads everything but hc (the caller's column)
+__device__ __forceinline__ void finalize_load(FinalizeIn& f, const SolveState* st, int j) {
     for (int i = threadIdx.x; i < j; i += blockDim.x) {
-        csv[i] = st->cs[i];
-        snv[i] = st->sn[i];
+        f.csv[i] = st->cs[i];
+        f.snv[i] = st->sn[i];
     }
     if (threadIdx.x == 0) {
-        gv[0] = st->g[j];
-        gv[1] = st->g[j + 1];
+        f.gv[0] = st->g[j];
+        f.gv[1] = st->g[j + 1];
+        f.tol = st->tol;
+        f.bnorm = st->bnorm;
+        f.est_scale = st->est_scale;
+        f.tol_kind = st->tol_kind;
+        f.hist_len = st->hist_len;
+        f.total_iter = st->total_iter;
     }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
+}
+
+// Thread 0: completes Arnoldi step j from f (hc[0..j] holds the column) and
+// ss = ||w''||^2: normalisation, Givens rotations, residual estimate and
+// stopping test.  Returns the new vector's scale 1/||w''|| when the cycle
+// goes on, 0 when it stops here (breakdown, convergence, last step).
+__device__ double finalize_core(SolveState* st, FinalizeIn& f, int j, int m, double ss,
+                                double* hist, int hist_cap) {
+    const int ld = m + 1;
+    double* hc = f.hc;
     const double nrm = sqrt(ss);
     double* Hc = st->H + (size_t)j * ld;
     hc[j + 1] = nrm;
@@ -78,36 +95,37 @@ __device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double
         st->breakdown = 1;
         st->kcount = j + 1;
         st->cycle_active = 0;
-        return;
+        return 0.0;
     }
-    st->vscale[j + 1] = 1.0 / nrm;
-    for (int i = 0; i < j; ++i) rot_apply(csv[i], snv[i], hc[i], hc[i + 1]);
+    const double vs = 1.0 / nrm;
+    st->vscale[j + 1] = vs;
+    for (int i = 0; i < j; ++i) rot_apply(f.csv[i], f.snv[i], hc[i], hc[i + 1]);
     double c, sn;
     rot_compute(c, sn, hc[j], hc[j + 1]);
     rot_apply(c, sn, hc[j], hc[j + 1]);
-    rot_apply(c, sn, gv[0], gv[1]);
+    rot_apply(c, sn, f.gv[0], f.gv[1]);
     st->cs[j] = c;
     st->sn[j] = sn;
-    st->g[j] = gv[0];
-    st->g[j + 1] = gv[1];
+    st->g[j] = f.gv[0];
+    st->g[j + 1] = f.gv[1];
     for (int i = 0; i <= j + 1; ++i) Hc[i] = hc[i];
-    const double res = fabs(gv[1]);
-    if (hist && st->hist_len < hist_cap) hist[st->hist_len] = res;
-    st->hist_len++;
+    const double res = fabs(f.gv[1]);
+    if (hist && f.hist_len < hist_cap) hist[f.hist_len] = res;
+    st->hist_len = f.hist_len + 1;
     st->last_res = res;
-    st->total_iter++;
+    st->total_iter = f.total_iter + 1;
     st->kcount = j + 1;
     st->j = j + 1;
     bool stop = false;
-    if (st->tol_kind == SG_TOL_REF_ABS) {
-        if (res < st->tol) {
+    if (f.tol_kind == SG_TOL_REF_ABS) {
+        if (res < f.tol) {
             st->converged = 1;
             st->done = 1;
             stop = true;
         }
-    } else if (st->tol_kind == SG_TOL_TRUE_REL) {
+    } else if (f.tol_kind == SG_TOL_TRUE_REL) {
         // estimated true residual; the restart verifies it in FP64
-        if (res * st->est_scale <= 0.5 * st->tol * st->bnorm) stop = true;
+        if (res * f.est_scale <= 0.5 * f.tol * f.bnorm) stop = true;
     }
     if (!isfinite(res)) {
         st->nonfinite = 1;
@@ -115,7 +133,22 @@ __device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double
         stop = true;
     }
     if (j + 1 >= m) stop = true;
-    if (stop) st->cycle_active = 0;
+    if (stop) {
+        st->cycle_active = 0;
+        return 0.0;
+    }
+    return vs;
+}
+
+// Completes Arnoldi step j once ||w''||^2 is known (all threads of the last
+// block; the column is hsum(0..j)).
+__device__ void arnoldi_finalize(SolveState* st, int j, int m, double ss, double* hist,
+                                 int hist_cap) {
+    __shared__ FinalizeIn f;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) f.hc[i] = st->hsum[i];
+    finalize_load(f, st, j);
+    __syncthreads();
+    if (threadIdx.x == 0) finalize_core(st, f, j, m, ss, hist, hist_cap);
 }
 
 template <class T>
@@ -261,21 +294,27 @@ __device__ void lagged_pass_a(SolveState* st, int j, const double* d) {
     __syncthreads();
 }
 
-// pass B epilogue (all threads of the last block; r = tot[0..j], ss = ||w'||^2)
+// pass B epilogue (all threads of the last block; r = tot[0..j], ss = ||w'||^2).
+// Everything it reads from the state loads in one round (T, the column's
+// pass A part, the rotations, g, the stopping-test scalars); the step's end
+// runs on thread 0 from shared memory.
 __device__ void lagged_pass_b(SolveState* st, int j, int m, const double* r, double ss,
                               double* hist, int hist_cap) {
     __shared__ double Ts[SG_LAGM][SG_LAGM + 1];
     __shared__ double h2_s[SG_LAGM], c_s[SG_LAGM];
-    __shared__ double s_nrm2;
-    __shared__ int s_ok;
+    __shared__ FinalizeIn f;
+    __shared__ double s_vs;
     const int n1 = j + 1;
     stage_lag(Ts, st->lagT, n1, n1, true);
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) f.hc[i] = st->hsum[i];
+    finalize_load(f, st, j);
     __syncthreads();
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double s = 0.0;
         for (int l = 0; l <= i; ++l) s += Ts[l][i] * r[l];
         h2_s[i] = s;
-        const double hs = st->hsum[i] + s;  // the Hessenberg column
+        const double hs = f.hc[i] + s;  // the Hessenberg column
+        f.hc[i] = hs;
         st->hsum[i] = hs;
         st->lagH[i + j * SG_LAGM] = hs;
     }
@@ -285,16 +324,13 @@ __device__ void lagged_pass_b(SolveState* st, int j, int m, const double* r, dou
         for (int i = 0; i <= j; ++i) nrm2 -= h2_s[i] * h2_s[i];
         if (!(nrm2 > 0.0)) nrm2 = isfinite(nrm2) ? 0.0 : nrm2;
         st->lagH[j + 1 + j * SG_LAGM] = sqrt(nrm2);
-        s_nrm2 = nrm2;
+        const double vs = finalize_core(st, f, j, m, nrm2, hist, hist_cap);
+        s_vs = j + 1 < SG_LAGM ? vs : 0.0;
     }
     __syncthreads();
-    arnoldi_finalize(st, j, m, s_nrm2, hist, hist_cap);
-    __syncthreads();
     // the pending correction of the new stored vector
-    if (threadIdx.x == 0) s_ok = (!st->breakdown && st->cycle_active && j + 1 < SG_LAGM) ? 1 : 0;
-    __syncthreads();
-    if (!s_ok) return;
-    const double vs = st->vscale[j + 1];
+    const double vs = s_vs;
+    if (vs == 0.0) return;
     for (int k = threadIdx.x; k <= j; k += blockDim.x) {
         c_s[k] = h2_s[k] * vs;
         st->lagc[k] = c_s[k];
