@@ -317,8 +317,16 @@ __device__ __forceinline__ void scatter_owned(const TS* t, TO* __restrict__ y,
 // them in block order (deterministic) into smem `out` and returns true.  The
 // arrival counter is reset by the last block, so consecutive kernels on one
 // stream can share it.  No block waits for another.
+struct NoPrefetch {
+    __device__ __forceinline__ void operator()() const {}
+};
+// prefetch: run by the last block before it loads the partials (loads of
+// what its epilogue needs, so both rounds of loads are in flight together;
+// the results are visible to the block when this returns true)
+template <class Prefetch = NoPrefetch>
 __device__ __forceinline__ bool last_block_reduce(double* partials, unsigned* counter,
-                                                  const double* bsum, int nv, double* out) {
+                                                  const double* bsum, int nv, double* out,
+                                                  Prefetch prefetch = Prefetch()) {
     __shared__ unsigned s_ticket;
     for (int k = threadIdx.x; k < nv; k += blockDim.x)
         partials[(size_t)blockIdx.x * nv + k] = bsum[k];
@@ -328,6 +336,7 @@ __device__ __forceinline__ bool last_block_reduce(double* partials, unsigned* co
     __syncthreads();
     if (s_ticket != gridDim.x - 1) return false;
     __threadfence();
+    prefetch();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nb = gridDim.x;
     // per lane the partials are added in block order, as a plain loop would;

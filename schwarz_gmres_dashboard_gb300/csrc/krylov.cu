@@ -266,16 +266,26 @@ __device__ __forceinline__ void stage_lag(double (*dst)[SG_LAGM + 1], const doub
     }
 }
 
-// pass A epilogue (all threads of the last block; d = tot[0..j]): p = T^T d,
-// hsum = p - g, update coefficients u = T p -- from shared memory
-__device__ void lagged_pass_a(SolveState* st, int j, const double* d) {
-    __shared__ double Ts[SG_LAGM][SG_LAGM + 1], Hs[SG_LAGM][SG_LAGM + 1];
-    __shared__ double cs[SG_LAGM], p_s[SG_LAGM];
+// what the pass A epilogue reads from the state (T, the lagged Hessenberg
+// block, the pending correction), loaded by the last block with its partials
+struct LagAIn {
+    double Ts[SG_LAGM][SG_LAGM + 1], Hs[SG_LAGM][SG_LAGM + 1];
+    double cs[SG_LAGM];
+};
+__device__ __forceinline__ void lagged_a_load(LagAIn& in, const SolveState* st, int j) {
     const int n1 = j + 1;
-    stage_lag(Ts, st->lagT, n1, n1, true);
-    stage_lag(Hs, st->lagH, n1, j, false);
-    for (int i = threadIdx.x; i < j; i += blockDim.x) cs[i] = st->lagc[i];
-    __syncthreads();
+    stage_lag(in.Ts, st->lagT, n1, n1, true);
+    stage_lag(in.Hs, st->lagH, n1, j, false);
+    for (int i = threadIdx.x; i < j; i += blockDim.x) in.cs[i] = st->lagc[i];
+}
+
+// pass A epilogue (all threads of the last block; d = tot[0..j], `in` loaded
+// and visible): p = T^T d, hsum = p - g, update coefficients u = T p
+__device__ void lagged_pass_a(SolveState* st, int j, const double* d, const LagAIn& in) {
+    __shared__ double p_s[SG_LAGM];
+    const auto& Ts = in.Ts;
+    const auto& Hs = in.Hs;
+    const double* cs = in.cs;
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double s = 0.0;
         for (int l = 0; l <= i; ++l) s += Ts[l][i] * d[l];
@@ -294,21 +304,28 @@ __device__ void lagged_pass_a(SolveState* st, int j, const double* d) {
     __syncthreads();
 }
 
-// pass B epilogue (all threads of the last block; r = tot[0..j], ss = ||w'||^2).
-// Everything it reads from the state loads in one round (T, the column's
-// pass A part, the rotations, g, the stopping-test scalars); the step's end
-// runs on thread 0 from shared memory.
-__device__ void lagged_pass_b(SolveState* st, int j, int m, const double* r, double ss,
-                              double* hist, int hist_cap) {
-    __shared__ double Ts[SG_LAGM][SG_LAGM + 1];
-    __shared__ double h2_s[SG_LAGM], c_s[SG_LAGM];
-    __shared__ FinalizeIn f;
-    __shared__ double s_vs;
+// pass B epilogue (all threads of the last block; r = tot[0..j], ss =
+// ||w'||^2).  Everything it reads from the state (T, the column's pass A
+// part, the rotations, g, the stopping-test scalars) is loaded by
+// lagged_b_load with the partials; the step's end runs on thread 0 from
+// shared memory.
+struct LagBIn {
+    double Ts[SG_LAGM][SG_LAGM + 1];
+    FinalizeIn f;
+};
+__device__ __forceinline__ void lagged_b_load(LagBIn& in, const SolveState* st, int j) {
     const int n1 = j + 1;
-    stage_lag(Ts, st->lagT, n1, n1, true);
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) f.hc[i] = st->hsum[i];
-    finalize_load(f, st, j);
-    __syncthreads();
+    stage_lag(in.Ts, st->lagT, n1, n1, true);
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) in.f.hc[i] = st->hsum[i];
+    finalize_load(in.f, st, j);
+}
+
+__device__ void lagged_pass_b(SolveState* st, int j, int m, const double* r, double ss,
+                              double* hist, int hist_cap, LagBIn& in) {
+    __shared__ double h2_s[SG_LAGM], c_s[SG_LAGM];
+    __shared__ double s_vs;
+    const auto& Ts = in.Ts;
+    FinalizeIn& f = in.f;
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double s = 0.0;
         for (int l = 0; l <= i; ++l) s += Ts[l][i] * r[l];
@@ -383,10 +400,13 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
         }
     }
     __shared__ double bs[KW * KPW], tot[KW * KPW];
+    __shared__ LagAIn lag_in;
     group_sums<TV>(acc, kc, nwg, bs);
-    if (last_block_reduce(partials, counter, bs, kc, tot)) {
+    if (last_block_reduce(partials, counter, bs, kc, tot, [&] {
+            if (lagged) lagged_a_load(lag_in, st, kc - 1);
+        })) {
         if (lagged) {
-            lagged_pass_a(st, kc - 1, tot);
+            lagged_pass_a(st, kc - 1, tot, lag_in);
             return;
         }
         for (int k = threadIdx.x; k < kc; k += blockDim.x) {
@@ -564,8 +584,10 @@ k_upd_dots(const TV* __restrict__ raw, size_t ldv, int n, int nk, TV* __restrict
             bs[nk] = t;
         }
         __syncthreads();
-        if (last_block_reduce(partials, counter, bs, nk + 1, tot))
-            lagged_pass_b(st, nk - 1, m, tot, tot[nk], hist, hist_cap);
+        __shared__ LagBIn lag_in;
+        if (last_block_reduce(partials, counter, bs, nk + 1, tot,
+                              [&] { lagged_b_load(lag_in, st, nk - 1); }))
+            lagged_pass_b(st, nk - 1, m, tot, tot[nk], hist, hist_cap, lag_in);
         return;
     }
     if (last_block_reduce(partials, counter, bs, nk, tot)) {
