@@ -298,7 +298,8 @@ def run_ours(args):
     per = {}
     model = {
         "spmv": ("spmv_fp32 (SELL/CSR, autotuned)", spmv_bytes(n, nnz, 4, 4)),
-        "precond": ("two_level_ras_apply (k_restrict + k_sweep_tma, BF16 factors, FP32 sweep)",
+        "precond": ("two_level_ras_apply (k_sweep_tma with the coarse restriction fused, "
+                    "BF16 factors, FP32 sweep)",
                     apply_bytes(n, n_loc, nnz_loc, NPARTS, 2, 4)),
         "residual": ("residual_fp64", spmv_bytes(n, nnz, 8, 8) + 2 * n * 8),
     }
