@@ -200,7 +200,7 @@ k_b_cycle_init(BatchDev B, const TV* __restrict__ raw0) {
     const int len = B.clen[c];
     TV ssv = (TV)0;
     for (int q = threadIdx.x; q < len; q += BT) {
-        const TV t = raw0[off + q];
+        const TV t = ld_stream(&raw0[off + q]);
         ssv += t * t;
     }
     const double ss = warp_sum((double)ssv);
@@ -272,12 +272,13 @@ k_b_dots(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
     const int len = B.clen[c];
     const TV* w = V + (size_t)(j + 1) * ldv + off;
     // per-thread products and sums in the basis precision (FP64 arithmetic
-    // is scarce on this GPU), warp and block sums in FP64
+    // is scarce on this GPU), warp and block sums in FP64; the vectors are
+    // streamed (256-byte L2 fetches)
     TV wv[BRPT];
 #pragma unroll
     for (int q = 0; q < BRPT; ++q) {
         const int row = threadIdx.x + q * BT;
-        wv[q] = row < len ? w[row] : (TV)0;
+        wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
     }
     for (int k = 0; k <= j; ++k) {
         const TV* vk = V + (size_t)k * ldv + off;
@@ -285,7 +286,7 @@ k_b_dots(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
 #pragma unroll
         for (int q = 0; q < BRPT; ++q) {
             const int row = threadIdx.x + q * BT;
-            if (row < len) acc += vk[row] * wv[q];
+            if (row < len) acc += ld_stream(&vk[row]) * wv[q];
         }
         const double a = warp_sum((double)acc);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = a;
@@ -319,7 +320,7 @@ k_b_upd_dots(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
 #pragma unroll
     for (int q = 0; q < BRPT; ++q) {
         const int row = threadIdx.x + q * BT;
-        wv[q] = row < len ? w[row] : (TV)0;
+        wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
     }
     for (int k = 0; k <= j; ++k) {
         const TV* vk = V + (size_t)k * ldv + off;
@@ -327,7 +328,7 @@ k_b_upd_dots(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
 #pragma unroll
         for (int q = 0; q < BRPT; ++q) {
             const int row = threadIdx.x + q * BT;
-            if (row < len) wv[q] -= ck * vk[row];
+            if (row < len) wv[q] -= ck * ld_stream(&vk[row]);
         }
     }
 #pragma unroll
@@ -377,7 +378,7 @@ k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
 #pragma unroll
     for (int q = 0; q < BRPT; ++q) {
         const int row = threadIdx.x + q * BT;
-        wv[q] = row < len ? w[row] : (TV)0;
+        wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
     }
     for (int k = 0; k <= j; ++k) {
         const TV* vk = V + (size_t)k * ldv + off;
@@ -385,7 +386,7 @@ k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
 #pragma unroll
         for (int q = 0; q < BRPT; ++q) {
             const int row = threadIdx.x + q * BT;
-            if (row < len) wv[q] -= ck * vk[row];
+            if (row < len) wv[q] -= ck * ld_stream(&vk[row]);
         }
     }
     TV ssv = (TV)0;
@@ -492,7 +493,7 @@ k_b_update_x(BatchDev B, const TV* __restrict__ V, size_t ldv, const int* __rest
         const int k = B.kcount[inst];
         const TV* cf = ycoef<TV>(B) + (size_t)inst * m;
         TV d = (TV)0;
-        for (int i = 0; i < k; ++i) d += cf[i] * V[(size_t)i * ldv + q];
+        for (int i = 0; i < k; ++i) d += cf[i] * ld_stream(&V[(size_t)i * ldv + q]);
         x[q] += (double)d;
     }
 }

@@ -87,6 +87,16 @@ __device__ __forceinline__ double2 ld_stream(const double2* p) {
                  : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ float ld_stream(const float* p) {
+    float v;
+    asm volatile("ld.global.L1::no_allocate.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ double ld_stream(const double* p) {
+    double v;
+    asm volatile("ld.global.L1::no_allocate.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ float ldg_stream(const float* p) {
     float v;
     asm("ld.global.nc.L1::no_allocate.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
