@@ -259,6 +259,68 @@ k_b_spmv(BatchDev B, const int* __restrict__ rp, const int* __restrict__ ci,
     }
 }
 
+// red[warp][k] = warp sums of raw_k . wv (k <= j) for a chunk: four
+// vectors' loads in flight at a time; per vector the products are summed
+// over the thread's rows in row order, then across the warp
+constexpr int BKG = 4;
+template <class TV>
+__device__ __forceinline__ void chunk_dots(const TV* V, size_t ldv, long long off, int len, int j,
+                                           const TV (&wv)[BRPT], double (*red)[BLD]) {
+    for (int k0 = 0; k0 <= j; k0 += BKG) {
+        TV a[BKG][BRPT];
+#pragma unroll
+        for (int kk = 0; kk < BKG; ++kk) {
+            const TV* vk = V + (size_t)(k0 + kk) * ldv + off;
+#pragma unroll
+            for (int q = 0; q < BRPT; ++q) {
+                const int row = threadIdx.x + q * BT;
+                a[kk][q] = (k0 + kk <= j && row < len) ? ld_stream(&vk[row]) : (TV)0;
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < BKG; ++kk) {
+            if (k0 + kk > j) break;
+            TV acc = (TV)0;
+#pragma unroll
+            for (int q = 0; q < BRPT; ++q) {
+                const int row = threadIdx.x + q * BT;
+                if (row < len) acc += a[kk][q] * wv[q];
+            }
+            const double v = warp_sum((double)acc);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k0 + kk] = v;
+        }
+    }
+}
+
+// wv -= sum_{k <= j} cf[k] raw_k over a chunk, k in order, four vectors'
+// loads in flight at a time
+template <class TV>
+__device__ __forceinline__ void chunk_update(const TV* V, size_t ldv, long long off, int len, int j,
+                                             const TV* cf, TV (&wv)[BRPT]) {
+    for (int k0 = 0; k0 <= j; k0 += BKG) {
+        TV a[BKG][BRPT];
+#pragma unroll
+        for (int kk = 0; kk < BKG; ++kk) {
+            const TV* vk = V + (size_t)(k0 + kk) * ldv + off;
+#pragma unroll
+            for (int q = 0; q < BRPT; ++q) {
+                const int row = threadIdx.x + q * BT;
+                a[kk][q] = (k0 + kk <= j && row < len) ? ld_stream(&vk[row]) : (TV)0;
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < BKG; ++kk) {
+            if (k0 + kk > j) break;
+            const TV ck = cf[k0 + kk];
+#pragma unroll
+            for (int q = 0; q < BRPT; ++q) {
+                const int row = threadIdx.x + q * BT;
+                if (row < len) wv[q] -= ck * a[kk][q];
+            }
+        }
+    }
+}
+
 // ---- CGS2 pass A: h1_k = vscale_k (raw_k . w), k <= j
 template <class TV>
 __global__ void __launch_bounds__(BT)
@@ -280,17 +342,7 @@ k_b_dots(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
         const int row = threadIdx.x + q * BT;
         wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
     }
-    for (int k = 0; k <= j; ++k) {
-        const TV* vk = V + (size_t)k * ldv + off;
-        TV acc = (TV)0;
-#pragma unroll
-        for (int q = 0; q < BRPT; ++q) {
-            const int row = threadIdx.x + q * BT;
-            if (row < len) acc += ld_stream(&vk[row]) * wv[q];
-        }
-        const double a = warp_sum((double)acc);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = a;
-    }
+    chunk_dots<TV>(V, ldv, off, len, j, wv, red);
     __syncthreads();
     if (!seg_reduce(B, c, inst, red, j + 1, bsum, tot)) return;
     const int ld = B.m + 1;
@@ -322,31 +374,13 @@ k_b_upd_dots(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
         const int row = threadIdx.x + q * BT;
         wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
     }
-    for (int k = 0; k <= j; ++k) {
-        const TV* vk = V + (size_t)k * ldv + off;
-        const TV ck = cf[k];
-#pragma unroll
-        for (int q = 0; q < BRPT; ++q) {
-            const int row = threadIdx.x + q * BT;
-            if (row < len) wv[q] -= ck * ld_stream(&vk[row]);
-        }
-    }
+    chunk_update<TV>(V, ldv, off, len, j, cf, wv);
 #pragma unroll
     for (int q = 0; q < BRPT; ++q) {
         const int row = threadIdx.x + q * BT;
         if (row < len) w[row] = wv[q];
     }
-    for (int k = 0; k <= j; ++k) {
-        const TV* vk = V + (size_t)k * ldv + off;
-        TV acc = (TV)0;
-#pragma unroll
-        for (int q = 0; q < BRPT; ++q) {
-            const int row = threadIdx.x + q * BT;
-            if (row < len) acc += vk[row] * wv[q];
-        }
-        const double a = warp_sum((double)acc);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = a;
-    }
+    chunk_dots<TV>(V, ldv, off, len, j, wv, red);
     __syncthreads();
     if (!seg_reduce(B, c, inst, red, j + 1, bsum, tot)) return;
     for (int k = threadIdx.x; k <= j; k += BT) {
@@ -380,15 +414,7 @@ k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
         const int row = threadIdx.x + q * BT;
         wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
     }
-    for (int k = 0; k <= j; ++k) {
-        const TV* vk = V + (size_t)k * ldv + off;
-        const TV ck = cf[k];
-#pragma unroll
-        for (int q = 0; q < BRPT; ++q) {
-            const int row = threadIdx.x + q * BT;
-            if (row < len) wv[q] -= ck * ld_stream(&vk[row]);
-        }
-    }
+    chunk_update<TV>(V, ldv, off, len, j, cf, wv);
     TV ssv = (TV)0;
 #pragma unroll
     for (int q = 0; q < BRPT; ++q) {
