@@ -1,0 +1,37 @@
+"""The reference arm of bench.py on the CPU: one JSON line with the keys the
+bench contract asks for, on a 16^3 version of the cfg3 workload (the oracle
+port runs the reference's algorithm; no GPU is involved)."""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line(sg, oracle):
+    out = subprocess.run(
+        [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--grid", "16",
+         "--steps", "1", "--warmup", "3"],
+        cwd=ROOT, capture_output=True, text=True, timeout=600, check=True)
+    lines = [ln for ln in out.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, out.stdout
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+                "impl", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference"
+    assert d["unit"] == "s" and d["higher_is_better"] is False
+    assert d["warmup"] >= 3 and d["steps"] == 1
+    assert d["value"] > 0 and d["config"]["n"] == 16 ** 3
+    assert "16^3" in d["config"]["workload"]
+    # the oracle reaches the target residual within the cycles it ran
+    assert d["cycles_to_rtol"] is not None and d["cycles_to_rtol"] >= 1
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0
+    assert e2e["d2h_bytes_per_step"] == 0
