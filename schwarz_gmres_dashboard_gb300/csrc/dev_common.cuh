@@ -73,8 +73,7 @@ struct Store<float> {
 // next step's data) instead of single sectors, and L1 keeps no copy.
 // Measured on a 268 MB read: 5.8 TB/s against 4.9 TB/s with plain 16-byte
 // loads.  ld_stream is coherent (safe on data the kernel itself writes
-// later); ldg_stream takes the read-only path (data no thread writes during
-// the kernel).
+// later).
 __device__ __forceinline__ float4 ld_stream(const float4* p) {
     float4 v;
     asm volatile("ld.global.L1::no_allocate.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];"
@@ -97,29 +96,10 @@ __device__ __forceinline__ double ld_stream(const double* p) {
     asm volatile("ld.global.L1::no_allocate.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ float ldg_stream(const float* p) {
-    float v;
-    asm("ld.global.nc.L1::no_allocate.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ double ldg_stream(const double* p) {
-    double v;
-    asm("ld.global.nc.L1::no_allocate.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ int ldg_stream(const int* p) {
-    int v;
-    asm("ld.global.nc.L1::no_allocate.L2::256B.s32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ int16_t ldg_stream(const int16_t* p) {
-    unsigned short v;
-    asm("ld.global.nc.L1::no_allocate.L2::256B.u16 %0, [%1];" : "=h"(v) : "l"(p));
-    return (int16_t)v;
-}
-// The same loads with an L2 cache policy (policy_evict_first(): data read
-// once per solve step, which should not displace vectors that the next
-// kernels re-read).
+
+// Read-only streaming loads (data no thread writes during the kernel) with
+// an L2 cache policy; policy_evict_first() marks data read once per solve
+// step, which should not displace vectors that the next kernels re-read.
 __device__ __forceinline__ uint64_t policy_evict_first() {
     uint64_t pol;
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
