@@ -35,3 +35,17 @@ def test_reference_arm_prints_one_contract_line(sg, oracle):
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0
     assert e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_under_torchrun_prints_once(sg, oracle):
+    """Launched as the multi-GPU bench is (torchrun, two ranks), rank 0 alone
+    runs the reference arm and prints; the other rank exits 0 without work."""
+    out = subprocess.run(
+        [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+         "--master-addr", "127.0.0.1", "--master-port", "29531", os.path.join(ROOT, "bench.py"),
+         "--impl", "reference", "--grid", "16", "--steps", "1", "--warmup", "3", "--gpus", "2"],
+        cwd=ROOT, capture_output=True, text=True, timeout=600, check=True)
+    lines = [ln for ln in out.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1, out.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2
