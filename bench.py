@@ -39,7 +39,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -73,6 +72,27 @@ def make_problem(sg, seed_offset=0):
     return A, part, xs
 
 
+def make_problem_oracle(orc, seed_offset=0):
+    """The same inputs from the oracle's restatement of the generators (bit
+    for bit the package's), for the reference arm, which loads nothing else."""
+    A = orc.varcoef3d(N_GRID, N_GRID, N_GRID, 1.0, 8.0, 0 + seed_offset)
+    part = orc.partition_boxes(N_GRID, N_GRID, N_GRID, NPARTS, SPREAD, 1)
+    xs = orc.uniform(A.nrows, 2 + seed_offset)
+    return A, part, xs
+
+
+def cfg3_config(n, nnz, world):
+    """The workload both arms report (identical dicts)."""
+    return {
+        "workload": WORKLOAD,
+        "n": n, "nnz": nnz, "nparts": NPARTS, "overlap": OVERLAP, "restart": RESTART,
+        "rtol": RTOL, "partition": f"boxes, seeded uneven cuts (spread {SPREAD})",
+        "rhs": "b = A x*, x* ~ U[-1,1] (seed 2), x0 = 0",
+        "l2": "working set > L2 (no flush)",
+        "parallelism": f"replicas x{world}",
+    }
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -82,17 +102,20 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(name):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/<name>."""
-    p = os.path.join(ROOT, "profiles", name)
+def dram_traffic(kernel, workload):
+    """DRAM bytes (read + write) per launch of `kernel` on `workload`, from the
+    committed list of ncu captures (profiles/dram_traffic.txt: one line per
+    capture, `kernel | workload | bytes per launch | sweep build | command`).
+    Returns (bytes, source line) or (None, reason)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     try:
         for line in open(p):
-            m = re.match(r"\s*traffic_bytes_per_launch:\s*([0-9.eE+]+)", line)
-            if m:
-                return float(m.group(1))
+            f = [x.strip() for x in line.split("|")]
+            if len(f) >= 5 and f[0] == kernel and f[1] == workload:
+                return float(f[2]), f"ncu capture: {f[4]} (build: {f[3]})"
     except OSError:
         pass
-    return None
+    return None, "no ncu capture of this kernel and workload is recorded"
 
 
 def local_sizes(sg, A, part, nparts, overlap):
@@ -270,8 +293,13 @@ def run_ours(args):
     with Clocks(local) as clk:
         ms_mixed, res_mixed, launches = timed(pc_mixed, p_mixed, args.steps, args.warmup)
     x_mixed = xd.cpu().numpy()
-    ms_fp64, res_fp64, _ = timed(pc_fp64, p_fp64, max(1, min(args.steps, 3)), 1)
+    nfp = max(1, min(args.steps, 3))
+    ms_fp64, res_fp64, _ = timed(pc_fp64, p_fp64, nfp, 1)
     x_fp64 = xd.cpu().numpy()
+    # the FP64 solver with the classic three-pass CGS2 (the mixed and the FP64
+    # solvers above both use the two-pass lagged form)
+    p_fp64c = sg.GMRESParams(**{**p_fp64.__dict__, "ortho": 1})
+    ms_fp64c, res_fp64c, _ = timed(pc_fp64, p_fp64c, nfp, 1)
 
     # e2e through the C ABI with host buffers (copies inside the timed region)
     bh = b.copy()
@@ -286,57 +314,46 @@ def run_ours(args):
             e2e.append(t1 - t0)
     e2e_s = statistics.mean(e2e)
 
-    # kernel classes of one eager mixed solve (CUDA events on the launching
-    # stream), and the FP64 SpMV of the operator alone
+    # kernel classes of one eager mixed and one eager FP64 solve (CUDA events
+    # on the launching stream, no host synchronisation between launches)
     nnz = A.nnz()
     peak, peak_kind = peaks()
-    p_eager = sg.GMRESParams(restart=RESTART, max_iter=20000, tol=RTOL,
-                             tol_kind=sg.TOL_TRUE_REL, precision=sg.FP32, use_graph=False)
+    p_eager = sg.GMRESParams(**{**p_mixed.__dict__, "use_graph": False})
     classes, res_eager = class_breakdown(ctx, lambda: device_solve(pc_mixed, p_eager))
+    p_eager64 = sg.GMRESParams(**{**p_fp64.__dict__, "use_graph": False})
+    classes64, res_eager64 = class_breakdown(ctx, lambda: device_solve(pc_fp64, p_eager64))
     n_loc, nnz_loc = local_sizes(sg, A, part, NPARTS, OVERLAP)
-    it = res_eager.iterations
-    per = {}
-    model = {
-        "spmv": ("spmv_fp32 (SELL/CSR, autotuned)", spmv_bytes(n, nnz, 4, 4)),
-        "precond": ("two_level_ras_apply (k_sweep_tma with the coarse restriction fused, "
-                    "BF16 factors, FP32 sweep)",
-                    apply_bytes(n, n_loc, nnz_loc, NPARTS, 2, 4)),
-        "residual": ("residual_fp64", spmv_bytes(n, nnz, 8, 8) + 2 * n * 8),
-    }
-    for name, (ms, cnt) in classes.items():
-        if cnt == 0:
-            continue
-        entry = {"ms": ms, "launches": cnt, "us_per_launch": ms * 1e3 / cnt}
-        if name in model:
-            kname, byt = model[name]
-            entry.update({"kernel": kname, "algorithmic_bytes": byt,
-                          "achieved_gbs": byt / (ms / cnt / 1e3) / 1e9})
-            entry["frac"] = entry["achieved_gbs"] / peak
-        if name == "ortho":
-            byt = cgs2_bytes(n, 4, it, RESTART)
-            entry.update({"kernel": "lagged cgs2 passes (k_dots, k_upd_dots) per step",
-                          "algorithmic_bytes_total": byt,
-                          "achieved_gbs": byt / (ms / 1e3) / 1e9})
-            entry["frac"] = entry["achieved_gbs"] / peak
-        per[name] = entry
+
+    def per_class(cls, it, w, wf, what):
+        model = {
+            "spmv": (f"spmv_{what} (SELL/CSR, autotuned)", spmv_bytes(n, nnz, w, w)),
+            "precond": (f"two_level_ras_apply (k_sweep_tma with the coarse restriction fused, "
+                        f"{'BF16' if wf == 2 else 'FP64'} factors, {what.upper()} sweep)",
+                        apply_bytes(n, n_loc, nnz_loc, NPARTS, wf, w)),
+            "residual": ("residual_fp64", spmv_bytes(n, nnz, 8, 8) + 2 * n * 8),
+        }
+        per = {}
+        for name, (ms, cnt) in cls.items():
+            if cnt == 0:
+                continue
+            entry = {"ms": ms, "launches": cnt, "us_per_launch": ms * 1e3 / cnt}
+            if name in model:
+                kname, byt = model[name]
+                entry.update({"kernel": kname, "algorithmic_bytes": byt,
+                              "achieved_gbs": byt / (ms / cnt / 1e3) / 1e9})
+                entry["frac"] = entry["achieved_gbs"] / peak
+            if name == "ortho":
+                byt = cgs2_bytes(n, w, it, RESTART)
+                entry.update({"kernel": "lagged cgs2 passes (k_dots, k_upd_dots) per step",
+                              "algorithmic_bytes_total": byt,
+                              "achieved_gbs": byt / (ms / 1e3) / 1e9})
+                entry["frac"] = entry["achieved_gbs"] / peak
+            per[name] = entry
+        return per
+
+    per = per_class(classes, res_eager.iterations, 4, 2, "fp32")
+    per64 = per_class(classes64, res_eager64.iterations, 8, 8, "fp64")
     dom = per["precond"]
-    yd = torch.empty_like(bd)
-    for _ in range(3):
-        A.spmv(bd, yd)
-    reps = 50
-    s0 = torch.cuda.Event(enable_timing=True)
-    s1 = torch.cuda.Event(enable_timing=True)
-    s0.record(stream)
-    for _ in range(reps):
-        A.spmv(bd, yd)
-    s1.record(stream)
-    torch.cuda.synchronize()
-    spmv64_s = s0.elapsed_time(s1) / 1e3 / reps
-    per["spmv_fp64_alone"] = {"kernel": "spmv_fp64 (sg_csr_spmv, reference summation order)",
-                              "us_per_launch": spmv64_s * 1e6,
-                              "algorithmic_bytes": spmv_bytes(n, nnz, 8, 8),
-                              "achieved_gbs": spmv_bytes(n, nnz, 8, 8) / spmv64_s / 1e9}
-    per["spmv_fp64_alone"]["frac"] = per["spmv_fp64_alone"]["achieved_gbs"] / peak
 
     if rank != 0:
         return
@@ -346,8 +363,14 @@ def run_ours(args):
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        cpu = cpu_baseline_sample(A, part, b, rf.iterations)
+        cpu, x_ref = cpu_baseline_solve(A, part, b)
+        if x_ref is not None:
+            nr = np.linalg.norm(x_ref)
+            cpu["rel_err_vs_reference_fp64"] = {
+                "mixed": float(np.linalg.norm(x_mixed - x_ref) / nr),
+                "fp64_gpu": float(np.linalg.norm(x_fp64 - x_ref) / nr)}
 
+    traffic, traffic_src = dram_traffic("k_sweep_tma", f"varcoef{N_GRID}_mixed")
     line = {
         "metric": METRIC,
         "value": ms_mixed / 1e3,
@@ -361,14 +384,9 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "fp32+bf16 inner / f64 outer",
         "data": "synthetic: seeded Gaussian random field coefficients, x* ~ U[-1,1]",
-        "config": {
-            "workload": WORKLOAD,
-            "n": n, "nnz": nnz, "nparts": NPARTS, "overlap": OVERLAP, "restart": RESTART,
-            "rtol": RTOL, "partition": f"boxes, seeded uneven cuts (spread {SPREAD})",
-            "l2": "working set > L2 (no flush)",
-            "solver": "GMRES(30) left-preconditioned, FP32 Krylov cycle from FP64 residual",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": cfg3_config(n, nnz, world),
+        "solver": "GMRES(30) left-preconditioned, FP32 Krylov cycle (lagged two-pass CGS2) "
+                  "from the FP64 true residual; FP32 sweeps over BF16 ILU(0) factors",
         "iterations": rm.iterations,
         "cycles": rm.cycles,
         "true_rel_residual": rm.true_rel_residual,
@@ -376,19 +394,26 @@ def run_ours(args):
         "rel_err_vs_xstar": relerr_vs_xstar,
         "solves_per_s": 1e3 / ms_mixed,
         "fp64_gpu": {"value": ms_fp64 / 1e3, "unit": "s", "iterations": rf.iterations,
-                     "true_rel_residual": rf.true_rel_residual},
+                     "true_rel_residual": rf.true_rel_residual,
+                     "ortho": "lagged two-pass CGS2"},
+        "fp64_gpu_classic_cgs2": {"value": ms_fp64c / 1e3, "unit": "s",
+                                  "iterations": res_fp64c[-1].iterations,
+                                  "true_rel_residual": res_fp64c[-1].true_rel_residual,
+                                  "ortho": "classic three-pass CGS2"},
         "speedup_vs_fp64_gpu": ms_fp64 / ms_mixed,
+        "speedup_vs_fp64_gpu_classic_cgs2": ms_fp64c / ms_mixed,
         "setup_s": {"mixed": setup_mixed, "fp64": setup_fp64},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * n * 8,
                 "d2h_bytes_per_step": n * 8},
         "roofline": {"kernel": dom["kernel"], "bound": "hbm",
                      "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": dom["achieved_gbs"] / peak, "peak_source": peak_kind,
-                     "traffic": profile_traffic("two_level_ras_apply_varcoef128_mixed.md"),
+                     "traffic": traffic, "traffic_source": traffic_src,
                      "algorithmic_bytes": dom["algorithmic_bytes"],
                      "us_per_launch": dom["us_per_launch"],
                      "timing": "CUDA events around every apply of one eager solve"},
         "kernels": per,
+        "kernels_fp64_solve": per64,
         "spmv_choice": A.spmv_choice(),
         "sweep_choice": pc_mixed.sweep_choice(),
         "gpu_launches": launches,
@@ -399,25 +424,31 @@ def run_ours(args):
     print(json.dumps(line))
 
 
-def cpu_baseline_sample(A, part, b, iterations):
-    """The oracle on one restart cycle (30 Arnoldi steps) of the same workload
-    with all host threads; scaled to the FP64 GPU solver's iteration count."""
+def cpu_baseline_solve(A, part, b):
+    """The oracle (the reference's algorithm, OpenMP subdomain loop, sparse
+    restatement of the dense coarse space) solving the same system to the
+    same FP64 true relative residual with all host threads: its wall time is
+    the CPU baseline and its x the reference FP64 solution every GPU result
+    is compared with."""
     try:
         from oracle.oracle import Oracle
         orc = Oracle()
         threads = os.cpu_count() or 1
         orc.set_threads(threads)
-        pc = orc.precond("twolevel_ras", A, NPARTS, OVERLAP, part)
         t0 = time.perf_counter()
-        orc.gmres(A, b, np.zeros(A.nrows), pc, restart=RESTART, max_iter=RESTART, tol=0.0)
-        dt = time.perf_counter() - t0
-        return {"value": dt / RESTART * iterations, "unit": "s", "cores": threads, "kind": "port",
-                "sample": f"one GMRES(30) restart cycle (30 iterations) of the oracle two-level "
-                          f"RAS solve, {dt:.2f} s, scaled to the {iterations} iterations the "
-                          f"FP64 solver needs"}
+        pc = orc.precond("twolevel_ras", A, NPARTS, OVERLAP, part)
+        t1 = time.perf_counter()
+        x, its, cycles, rel = orc.solve_true_rel(A, b, pc, RESTART, RTOL, max_cycles=60)
+        t2 = time.perf_counter()
+        return ({"value": t2 - t1, "unit": "s", "cores": threads, "kind": "port",
+                 "setup_s": t1 - t0, "iterations": its, "cycles": cycles,
+                 "true_rel_residual": rel,
+                 "sample": f"the whole solve: {cycles} GMRES(30) restart cycles of the oracle "
+                           f"two-level RAS solve to FP64 true relative residual {rel:.2e} "
+                           f"({its} iterations; set-up {t1 - t0:.2f} s not included)"}, x)
     except Exception as e:  # the baseline is reported, never required
-        return {"value": None, "unit": "s", "cores": os.cpu_count(), "kind": "port",
-                "sample": f"failed: {e}"}
+        return ({"value": None, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                 "sample": f"failed: {e}"}, None)
 
 
 # ---------------------------------------------------------------- learned workload
@@ -855,21 +886,25 @@ def cpu_baseline_batched(prob, Bh, sample=8):
 
 # ---------------------------------------------------------------- reference arm
 def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle port (the
+    reference's GMRES and two-level RAS restated in C, OpenMP subdomain
+    loop, sparse restatement of its dense coarse space) on the same inputs,
+    built by the oracle's restatement of the generators -- nothing of the
+    package is loaded.  A step is one GMRES(30) restart cycle of the harness
+    (tol 0, warm start, FP64 true residual checked between cycles); value =
+    mean cycle time x the cycles the harness needs to reach 1e-8."""
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    import schwarz_gmres_dashboard_gb300 as sg  # host generators only
     from oracle.oracle import Oracle
 
-    A, part, xs = make_problem(sg)
     orc = Oracle()
+    A, part, xs = make_problem_oracle(orc)
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
     b = orc.spmv(A, xs)
     bn = np.linalg.norm(b)
     pc = orc.precond("twolevel_ras", A, NPARTS, OVERLAP, part)
-    # cycles of the oracle harness (GMRES(30), tol 0, warm start, FP64 true
-    # residual checked between cycles); a step is one cycle
     x = np.zeros(A.nrows)
     cycle_times = []
     cycles_needed = None
@@ -895,7 +930,9 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": sec_cycle * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded Gaussian random field coefficients, x* ~ U[-1,1]",
-        "config": {"workload": WORKLOAD, "n": A.nrows, "nnz": A.nnz()},
+        "config": cfg3_config(A.nrows, A.nnz(), world),
+        "solver": "GMRES(30) left-preconditioned, all FP64 (the reference's gmres(), "
+                  "src/core/gmres.cpp:34-160), two-level RAS with ILU(0) subdomain solves",
         "impl": "reference",
         "cycles_to_rtol": cycles_needed,
         "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",

@@ -179,6 +179,18 @@ sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc);
  * pointer may be NULL. */
 sg_status sg_precond_get_sweep(sg_precond* pc, int* sweep, int* threads);
 
+/* Test hook of the bounded device waits (no counterpart in the reference).
+ * mode 1: the TMA-fed sweep copies no subdomain's first level-record group,
+ * so every CTA's first record wait runs out after ~1 ms; mode 2: no CTA
+ * counts its coarse restriction, so the wait of the sweep's fused
+ * restriction runs out after ~1 ms (two-level preconditioners whose sweep
+ * computes the restriction itself).  Either way each CTA drains the copies
+ * it did issue and returns without writing y; sg_precond_apply and sg_solve
+ * then return SG_ERR_DEVICE_TIMEOUT, and the error state is cleared for the
+ * next call.  mode 0 restores the normal waits (~1 s budget).
+ * SG_ERR_UNSUPPORTED when this set-up has no such wait. */
+sg_status sg_precond_set_wait_test(sg_precond* pc, int mode);
+
 /* ---- solvers ---------------------------------------------------------- */
 typedef enum sg_solver {
     SG_GMRES = 0, /* left preconditioned, src/core/gmres.cpp:34-160 */
@@ -209,7 +221,13 @@ typedef struct sg_solve_params {
     int use_graph;   /* 1: launch each restart cycle as a CUDA graph */
     double* history; /* optional host array receiving |g_{j+1}| per iteration */
     int history_cap;
-    int reserved[8];
+    /* orthogonalisation of the Arnoldi step (the reference uses modified
+     * Gram-Schmidt, src/core/gmres.cpp:288-292): 0 = CGS2 in the fewest
+     * streaming passes -- two (second projection deferred by one step) when
+     * the cycle's operator is linear (GMRES, restart < 32), else three;
+     * 1 = classic CGS2, three passes per step */
+    int ortho;
+    int reserved[7];
 } sg_solve_params;
 
 typedef struct sg_solve_result {
@@ -268,10 +286,11 @@ sg_status sg_scale(sg_ctx* ctx, double alpha, double* x, int n, sg_mem mem);
 
 /* ---- allocation-free dot product -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory when they need a reduction -- code running while its stream is
- * captured into a CUDA graph (no cudaMalloc/cudaFree during capture), plug-ins
- * inside an application that owns all device memory through its own pool,
- * real-time loops that cannot pay cudaFree's device-wide synchronisation.
+ * memory when they need a reduction: plug-ins hosted by an application that
+ * owns all device memory through its own pool and forbids raw cudaMalloc,
+ * and real-time loops that cannot pay cudaMalloc's latency or cudaFree's
+ * device-wide synchronisation.  (sg_dot takes its scratch from an sg_ctx,
+ * whose creation allocates.)
  * Computes *result = dot(x, y) like sg_dot, but takes its per-block partial
  * sums from a fixed 64 KiB array inside the library instead of a context,
  * needs no sg_ctx, and calls no allocator.  x, y and result are device
@@ -280,8 +299,9 @@ sg_status sg_scale(sg_ctx* ctx, double alpha, double* x, int n, sg_mem mem);
  * Limits: n <= SG_DOT_NOALLOC_MAX_N, else SG_ERR_INVALID_ARG and nothing runs.
  * All calls on a device share the array: calls whose kernels overlap on the
  * GPU race and return wrong sums.  The first call on a device (with that
- * device current) looks up the array's address; make it before any stream
- * capture. */
+ * device current) looks up the array's device address and keeps it for the
+ * life of the process; make that first call before any stream capture, and
+ * do not call the function again after cudaDeviceReset on that device. */
 #define SG_DOT_NOALLOC_MAX_N 33554432
 sg_status sg_dot_noalloc(const double* x, const double* y, int n, double* result, void* stream);
 

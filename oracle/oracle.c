@@ -14,6 +14,7 @@
 #include "oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -769,4 +770,182 @@ int orc_poisson3d(int nx, int ny, int nz_, int* rp, int* ci, double* v) {
 #undef PUT
     if (rp) rp[nxy * nz_] = nz;
     return nz;
+}
+
+/* ------------------------------------------------------------------------
+ * Benchmark inputs (no reference counterpart).  The project generates its
+ * 3D variable-coefficient operator, uneven box partitions and uniform
+ * vectors itself (the package's sg_gen_varcoef3d, sg_partition_boxes,
+ * sg_gen_uniform); they are restated here so that the CPU baseline builds
+ * the same problem without loading the package.  tests/test_oracle_inputs.py
+ * checks them against the package bit for bit.  Compiled like the rest of
+ * this file with -ffp-contract=off, as the package's host code is.
+ * ---------------------------------------------------------------------- */
+static uint64_t orc_next64(uint64_t* state) {
+    /* SplitMix64 (Steele, Lea, Flood 2014) */
+    uint64_t z = (*state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double orc_unit(uint64_t* state) {
+    return (double)(orc_next64(state) >> 11) * (1.0 / 9007199254740992.0); /* 2^-53 */
+}
+
+void orc_uniform(uint64_t seed, int n, double lo, double hi, double* out) {
+    uint64_t st = seed;
+    for (int i = 0; i < n; ++i) out[i] = lo + (hi - lo) * orc_unit(&st);
+}
+
+/* Recursive coordinate bisection into nparts boxes: a box of k parts is cut
+ * across its longest axis (x, then y, then z on ties) at the fraction
+ * k1/k * (1 + spread * (2u - 1)) of its length (k1 = k/2, u uniform from the
+ * seeded stream, one draw per cut), clamped to leave both halves non-empty;
+ * the lower half takes parts [base, base+k1) and is cut next (depth first). */
+int orc_partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed,
+                        int* part) {
+    if (nx <= 0 || ny <= 0 || nz <= 0 || nparts < 1) return 1;
+    typedef struct { int lo[3], hi[3], k, base; } box_t;
+    box_t* todo = (box_t*)malloc(sizeof(box_t) * (size_t)(2 * nparts + 2));
+    if (!todo) return 3;
+    int top = 0;
+    box_t root = {{0, 0, 0}, {nx, ny, nz}, nparts, 0};
+    todo[top++] = root;
+    uint64_t st = seed;
+    while (top > 0) {
+        box_t bx = todo[--top];
+        if (bx.k == 1) {
+            for (int z = bx.lo[2]; z < bx.hi[2]; ++z)
+                for (int y = bx.lo[1]; y < bx.hi[1]; ++y)
+                    for (int x = bx.lo[0]; x < bx.hi[0]; ++x)
+                        part[((size_t)z * ny + y) * nx + x] = bx.base;
+            continue;
+        }
+        int ax = 0;
+        for (int d = 1; d < 3; ++d)
+            if (bx.hi[d] - bx.lo[d] > bx.hi[ax] - bx.lo[ax]) ax = d;
+        const int len = bx.hi[ax] - bx.lo[ax];
+        if (len < 2) {
+            free(todo);
+            return 2;
+        }
+        const int k1 = bx.k / 2;
+        const double frac = (double)k1 / bx.k * (1.0 + spread * (2.0 * orc_unit(&st) - 1.0));
+        long cut = lround(frac * len);
+        if (cut < 1) cut = 1;
+        if (cut > len - 1) cut = len - 1;
+        box_t lower = bx, upper = bx;
+        lower.k = k1;
+        lower.hi[ax] = bx.lo[ax] + (int)cut;
+        upper.k = bx.k - k1;
+        upper.base = bx.base + k1;
+        upper.lo[ax] = bx.lo[ax] + (int)cut;
+        todo[top++] = upper;
+        todo[top++] = lower;
+    }
+    free(todo);
+    return 0;
+}
+
+/* ln k of the benchmark's coefficient field, then k = exp(sigma * g):
+ * g is Gaussian white noise (Box-Muller on the seeded stream, two values per
+ * pair of draws) on the grid padded by R = ceil(3 corr / sqrt 2) cells per
+ * side, smoothed by the separable kernel exp(-d^2 / corr^2) along x, y and z
+ * in turn, then standardised to zero mean and unit sample variance. */
+static double* orc_coef_field(int nx, int ny, int nz, double sigma, double corr, uint64_t seed) {
+    const int R = (int)fmax(1.0, ceil(3.0 * (corr / sqrt(2.0))));
+    const int W = 2 * R + 1;
+    double* ker = (double*)malloc(sizeof(double) * (size_t)W);
+    for (int d = -R; d <= R; ++d) ker[d + R] = exp(-(double)d * d / (corr * corr));
+    const size_t px = (size_t)nx + 2 * R, py = (size_t)ny + 2 * R, pz = (size_t)nz + 2 * R;
+    const size_t npad = px * py * pz, n = (size_t)nx * ny * nz;
+    double* noise = (double*)malloc(sizeof(double) * npad);
+    uint64_t st = seed;
+    const double two_pi = 6.283185307179586232; /* 2 * M_PI, as the double product */
+    for (size_t i = 0; i < npad; i += 2) {
+        const double u1 = 1.0 - orc_unit(&st), u2 = orc_unit(&st);
+        const double rad = sqrt(-2.0 * log(u1));
+        noise[i] = rad * cos(two_pi * u2);
+        if (i + 1 < npad) noise[i + 1] = rad * sin(two_pi * u2);
+    }
+    /* smooth along x (padded y, z kept), then y, then z */
+    double* sx = (double*)malloc(sizeof(double) * (size_t)nx * py * pz);
+    for (size_t z = 0; z < pz; ++z)
+        for (size_t y = 0; y < py; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const double* src = noise + (z * py + y) * px + x;
+                double acc = 0.0;
+                for (int d = 0; d < W; ++d) acc += ker[d] * src[d];
+                sx[(z * py + y) * nx + x] = acc;
+            }
+    free(noise);
+    double* sy = (double*)malloc(sizeof(double) * (size_t)nx * ny * pz);
+    for (size_t z = 0; z < pz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                double acc = 0.0;
+                for (int d = 0; d < W; ++d) acc += ker[d] * sx[(z * py + y + d) * nx + x];
+                sy[(z * ny + y) * nx + x] = acc;
+            }
+    free(sx);
+    double* g = (double*)malloc(sizeof(double) * n);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                double acc = 0.0;
+                for (int d = 0; d < W; ++d)
+                    acc += ker[d] * sy[(((size_t)z + d) * ny + y) * nx + x];
+                g[((size_t)z * ny + y) * nx + x] = acc;
+            }
+    free(sy);
+    free(ker);
+    double mean = 0.0;
+    for (size_t i = 0; i < n; ++i) mean += g[i];
+    mean /= (double)n;
+    double var = 0.0;
+    for (size_t i = 0; i < n; ++i) var += (g[i] - mean) * (g[i] - mean);
+    var /= (double)n;
+    const double inv = var > 0 ? 1.0 / sqrt(var) : 1.0;
+    for (size_t i = 0; i < n; ++i) g[i] = exp(sigma * (g[i] - mean) * inv);
+    return g;
+}
+
+/* -div(k grad u), 7-point, Dirichlet: the coupling across an interior face
+ * is the harmonic mean 2 k_a k_b / (k_a + k_b) of the two cells, a boundary
+ * face couples to the zero boundary value with the cell's own k, and the
+ * diagonal is the sum of the six face coefficients (added -z, -y, -x, +x,
+ * +y, +z).  Rows and columns in make_poisson_3d's order
+ * (src/mesh/poisson.h:42-74).  Returns nnz; rp == NULL only sizes. */
+int orc_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t seed, int* rp,
+                  int* ci, double* v) {
+    if (!rp) return orc_poisson3d(nx, ny, nz, NULL, NULL, NULL);
+    double* k = orc_coef_field(nx, ny, nz, sigma, corr, seed);
+    const int nxy = nx * ny;
+    int e = 0;
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix) {
+                const int c = iz * nxy + iy * nx + ix;
+                const double kc = k[c];
+#define ORC_FACE(nb) (2.0 * kc * k[nb] / (kc + k[nb]))
+                const double f[6] = {iz > 0 ? ORC_FACE(c - nxy) : kc,
+                                     iy > 0 ? ORC_FACE(c - nx) : kc,
+                                     ix > 0 ? ORC_FACE(c - 1) : kc,
+                                     ix < nx - 1 ? ORC_FACE(c + 1) : kc,
+                                     iy < ny - 1 ? ORC_FACE(c + nx) : kc,
+                                     iz < nz - 1 ? ORC_FACE(c + nxy) : kc};
+#undef ORC_FACE
+                const double diag = f[0] + f[1] + f[2] + f[3] + f[4] + f[5];
+                rp[c] = e;
+                if (iz > 0) { ci[e] = c - nxy; v[e++] = -f[0]; }
+                if (iy > 0) { ci[e] = c - nx; v[e++] = -f[1]; }
+                if (ix > 0) { ci[e] = c - 1; v[e++] = -f[2]; }
+                ci[e] = c; v[e++] = diag;
+                if (ix < nx - 1) { ci[e] = c + 1; v[e++] = -f[3]; }
+                if (iy < ny - 1) { ci[e] = c + nx; v[e++] = -f[4]; }
+                if (iz < nz - 1) { ci[e] = c + nxy; v[e++] = -f[5]; }
+            }
+    rp[nxy * nz] = e;
+    free(k);
+    return e;
 }

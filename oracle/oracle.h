@@ -21,6 +21,8 @@
 #ifndef SG_ORACLE_H
 #define SG_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -99,6 +101,17 @@ int orc_fgmres(int n, const int* rp, const int* ci, const double* v, const doubl
  * NULL on the sizing call. */
 int orc_poisson2d(int nx, int ny, int* rp, int* ci, double* v);
 int orc_poisson3d(int nx, int ny, int nz, int* rp, int* ci, double* v);
+
+/* Benchmark inputs the project generates (no reference counterpart),
+ * restated from the package so the CPU baseline needs nothing else:
+ * uniform vectors (SplitMix64, (u >> 11) * 2^-53), uneven box partitions
+ * (returns 0 on success) and the 3D variable-coefficient 7-point operator
+ * k = exp(sigma g) (returns nnz; rp == NULL only sizes). */
+void orc_uniform(uint64_t seed, int n, double lo, double hi, double* out);
+int orc_partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed,
+                        int* part);
+int orc_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t seed, int* rp,
+                  int* ci, double* v);
 
 #ifdef __cplusplus
 }

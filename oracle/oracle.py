@@ -92,6 +92,13 @@ class Oracle(_Lib):
         L.orc_poisson3d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                     C.c_void_p]
         L.orc_poisson3d.restype = C.c_int
+        L.orc_uniform.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, _f64p]
+        L.orc_partition_boxes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                          C.c_uint64, _i32p]
+        L.orc_partition_boxes.restype = C.c_int
+        L.orc_varcoef3d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_varcoef3d.restype = C.c_int
 
     # -- threads
     def set_threads(self, n: int) -> None:
@@ -187,6 +194,67 @@ class Oracle(_Lib):
         v = np.empty(nz, np.float64)
         self.lib.orc_poisson3d(nx, ny, nz_, rp.ctypes.data, ci.ctypes.data, v.ctypes.data)
         return rp, ci, v
+
+
+    # -- benchmark inputs (the project's generators, restated)
+    def uniform(self, n, seed, lo=-1.0, hi=1.0):
+        out = np.empty(n, np.float64)
+        self.lib.orc_uniform(seed, n, lo, hi, out)
+        return out
+
+    def partition_boxes(self, nx, ny, nz, nparts, spread, seed):
+        part = np.empty(nx * ny * nz, np.int32)
+        rc = self.lib.orc_partition_boxes(nx, ny, nz, nparts, spread, seed, part)
+        if rc:
+            raise ValueError(f"orc_partition_boxes failed ({rc})")
+        return part
+
+    def varcoef3d(self, nx, ny, nz, sigma, corr, seed):
+        nnz = self.lib.orc_varcoef3d(nx, ny, nz, sigma, corr, seed, None, None, None)
+        rp = np.empty(nx * ny * nz + 1, np.int32)
+        ci = np.empty(nnz, np.int32)
+        v = np.empty(nnz, np.float64)
+        self.lib.orc_varcoef3d(nx, ny, nz, sigma, corr, seed, rp.ctypes.data, ci.ctypes.data,
+                               v.ctypes.data)
+        return HostMatrix(rp, ci, v)
+
+    def solve_true_rel(self, A, b, pc, restart, rtol, fgmres=False, max_cycles=400,
+                       on_cycle=None):
+        """The oracle harness for an FP64 true-relative-residual target: the
+        reference's GMRES (or FGMRES) one restart cycle at a time (tol 0,
+        max_iter = restart, warm start through x) until ||b - A x|| / ||b||
+        <= rtol, checked in FP64 between cycles.  Returns (x, iterations,
+        cycles, relative residual)."""
+        x = np.zeros(A.nrows)
+        bn = np.linalg.norm(b)
+        its = cycles = 0
+        rel = 1.0
+        fn = self.fgmres if fgmres else self.gmres
+        for _ in range(max_cycles):
+            r = fn(A, b, x, pc, restart=restart, max_iter=restart, tol=0.0)
+            x = r["x"]
+            its += r["iterations"]
+            cycles += 1
+            rel = float(np.linalg.norm(b - self.spmv(A, x)) / bn)
+            if on_cycle:
+                on_cycle(cycles, rel)
+            if rel <= rtol:
+                break
+        return x, its, cycles, rel
+
+
+class HostMatrix:
+    """A CSR matrix in host memory (int32 row_ptr / col_idx, FP64 values),
+    the layout of src/core/sparse_matrix.h:13-18."""
+
+    def __init__(self, row_ptr, col_idx, vals):
+        self.row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+        self.col_idx = np.ascontiguousarray(col_idx, np.int32)
+        self.vals = np.ascontiguousarray(vals, np.float64)
+        self.nrows = self.ncols = len(self.row_ptr) - 1
+
+    def nnz(self) -> int:
+        return int(self.row_ptr[-1])
 
 
 class OraclePC:

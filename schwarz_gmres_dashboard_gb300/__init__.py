@@ -472,6 +472,13 @@ class Preconditioner:
         kinds = {0: "tma", 1: "level", 2: "syncfree", -1: "none"}
         return {"sweep": kinds[k.value], "threads": t.value}
 
+    def set_wait_test(self, mode: int) -> None:
+        """Test hook of the bounded device waits: 1 makes every sweep CTA's
+        first record wait run out, 2 the fused coarse restriction's wait
+        (~1 ms each; applies and solves then raise SgError with
+        SG_ERR_DEVICE_TIMEOUT); 0 restores the normal waits."""
+        _check(_clib.sg_precond_set_wait_test(self.handle, int(mode)))
+
     def close(self):
         if getattr(self, "handle", None):
             _clib.sg_precond_destroy(self.handle)
@@ -545,6 +552,9 @@ class GMRESParams:
     tol_kind: int = TOL_REF_ABS
     precision: int = FP64
     use_graph: bool = True
+    # 0: CGS2 in the fewest passes (two for linear GMRES cycles, restart < 32);
+    # 1: classic three-pass CGS2
+    ortho: int = 0
 
 
 @dataclass
@@ -576,6 +586,7 @@ def _solve(solver: int, A: CSRMatrix, b, x, M: Optional[Preconditioner],
     p.tol_kind = params.tol_kind
     p.precision = params.precision
     p.use_graph = 1 if params.use_graph else 0
+    p.ortho = params.ortho
     hist = None
     if history:
         cap = max(params.max_iter, 0) + params.restart + 1

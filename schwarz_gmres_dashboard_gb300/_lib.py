@@ -43,8 +43,8 @@ class PrecondOpts(C.Structure):
 class SolveParams(C.Structure):
     _fields_ = [("restart", C.c_int), ("max_iter", C.c_int), ("tol", C.c_double),
                 ("tol_kind", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int),
-                ("history", C.c_void_p), ("history_cap", C.c_int),
-                ("reserved", C.c_int * 8)]
+                ("history", C.c_void_p), ("history_cap", C.c_int), ("ortho", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class BatchResult(C.Structure):
@@ -91,6 +91,7 @@ PROTOTYPES = {
     "sg_precond_get_factors": (C.c_int, [_vp, C.c_int, _ip, _ip, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "sg_precond_get_sweep": (C.c_int, [_vp, _ip, _ip]),
+    "sg_precond_set_wait_test": (C.c_int, [_vp, C.c_int]),
     "sg_solve": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int,
                            C.POINTER(SolveParams), C.POINTER(SolveResult)]),
     "sg_solve_batched": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp, C.c_int,

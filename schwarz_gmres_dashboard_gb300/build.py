@@ -22,7 +22,10 @@ LIB = os.path.join(BUILD, "libsgmres.so")
 CLI = os.path.join(BUILD, "schwarz_solve")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+# host code without contracted multiply-adds: the generators and the host
+# set-up give the same bits on x86-64 and aarch64 (where FMA is always there)
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+          "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def _nvcc() -> str:
@@ -51,6 +54,14 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [0.0])
+    # objects compiled with other flags are stale too
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join(ARCH + COMMON)
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        for o in glob.glob(os.path.join(BUILD, "*.o")):
+            os.remove(o)
+        with open(stamp, "w") as f:
+            f.write(flags)
     objs, todo = [], []
     for s in srcs:
         o = os.path.join(BUILD, os.path.basename(s) + ".o")

@@ -572,6 +572,22 @@ sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg
     });
 }
 
+sg_status sg_precond_set_wait_test(sg_precond* pc, int mode) {
+    return guard([&] {
+        SG_CHECK_ARG(pc, "NULL argument");
+        SG_CHECK_ARG(mode >= 0 && mode <= 2, "wait test mode must be 0, 1 or 2 (got %d)", mode);
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        if (!sweep_wait_test_supported(pc, mode))
+            fail(SG_ERR_UNSUPPORTED, mode == 2 ? "the sweep of this set-up does not compute the "
+                                                 "coarse restriction itself"
+                                               : "this set-up has no TMA-fed sweep");
+        if (pc->wait_test != mode) {
+            pc->wait_test = mode;
+            pc->gen = next_object_gen();  // a captured cycle holds the old launch arguments
+        }
+    });
+}
+
 sg_status sg_precond_destroy(sg_precond* pc) {
     return guard([&] {
         if (!pc) return;

@@ -70,7 +70,10 @@ void rec_setup_device(sg_precond* pc);
 template <class TI, class TO>
 bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
                const int* active);
+// reads the sweeps' error word (0: none) and clears it
 int sweep_error(sg_precond* pc);
+// whether sg_precond_set_wait_test's mode applies to this set-up
+bool sweep_wait_test_supported(const sg_precond* pc, int mode);
 // the TMA sweep computes the coarse restriction itself (no k_restrict launch)
 bool sweep_fuses_restrict(const sg_precond* pc);
 // ---------------------------------------------------------------- learned.cu

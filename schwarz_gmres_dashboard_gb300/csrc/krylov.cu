@@ -243,7 +243,7 @@ __device__ __forceinline__ void group_sync(int grp, int nwg) {
     }
 }
 
-// ---- lagged CGS2 (left-preconditioned FP32 GMRES, restart < SG_LAGM).
+// ---- lagged CGS2 (left-preconditioned GMRES, FP32 or FP64 basis, restart < SG_LAGM).
 // Step j orthogonalises z = B (vscale_j raw_j), where the stored raw_j still
 // lacks its second projection: v_j = T(j,j) raw_j - sum_{k<j} c_k v_k.  By
 // linearity B v_j = z - V_j g with g = H(0..j, 0..j-1) c (the Arnoldi relation

@@ -2,14 +2,10 @@
 //
 // Why it exists: some callers of this library cannot allocate device memory
 // at the moment they need a reduction.
-//  * Code that runs while its stream is being captured into a CUDA graph:
-//    cudaMalloc and cudaFree are not allowed during a global-mode capture
-//    (and would invalidate it), yet the capture still needs every scratch
-//    buffer of the captured kernels to exist.
 //  * Plug-ins hosted by an application that owns all device memory through
 //    its own pool and forbids raw cudaMalloc/cudaFree once it has started.
-//  * Real-time loops that cannot afford the implicit device-wide
-//    synchronisation of cudaFree.
+//  * Real-time loops that cannot afford cudaMalloc's latency or the
+//    implicit device-wide synchronisation of cudaFree.
 // sg_dot needs scratch for its per-block partial sums and takes it from an
 // sg_ctx, whose creation allocates.  sg_dot_noalloc runs the same kernel with
 // that scratch in a fixed array compiled into this library instead.
@@ -26,8 +22,10 @@
 //    kernels overlap on the GPU (different streams, or host threads calling
 //    concurrently) race on the array and give wrong results: serialise them.
 //  * The first call on a device, with that device current, looks up the
-//    array's device address (cudaGetSymbolAddress) and caches it; make that
-//    first call before any stream capture begins.
+//    array's device address (cudaGetSymbolAddress) and caches it for the
+//    life of the process; make that first call before any stream capture
+//    begins.  cudaDeviceReset destroys the context the cached address
+//    belongs to: do not call sg_dot_noalloc on that device afterwards.
 #include <mutex>
 
 #include "dev_common.cuh"

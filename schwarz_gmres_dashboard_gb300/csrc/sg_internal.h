@@ -69,7 +69,7 @@ struct DBuf {
 // --------------------------------------------------------------- solver state
 // Restart lengths up to SG_MMAX are supported.
 constexpr int SG_MMAX = 128;
-// restart lengths below SG_LAGM use the lagged CGS2 in the FP32 GMRES cycle
+// restart lengths below SG_LAGM use the lagged CGS2 in the GMRES cycle
 constexpr int SG_LAGM = 32;
 
 // Device-resident Arnoldi / Givens state of one solve (FP64 throughout).
@@ -87,6 +87,7 @@ struct SolveState {
     int nonfinite;
     int hist_len;
     int cycles;
+    int sweep_err;     // the preconditioner's sweep error word, copied after every cycle
     double tol;
     double bnorm;      // ||b||
     double rnorm;      // ||b - A x|| at the current cycle start (FP64)
@@ -102,7 +103,7 @@ struct SolveState {
     double hsum[SG_MMAX + 1];           // h1 + h2 of the current column
     double vscale[SG_MMAX + 1];         // basis vector k is stored as raw_k; v_k = vscale[k]*raw_k
     double y[SG_MMAX];
-    // lagged CGS2 (left-preconditioned FP32 GMRES, restart < SG_LAGM): the
+    // lagged CGS2 (left-preconditioned GMRES, restart < SG_LAGM): the
     // stored basis vectors raw_l relate to the orthonormal ones through an
     // upper triangular T, v_i = sum_{l<=i} T(l,i) raw_l; the newest stored
     // vector still lacks its second projection, held in lagc
@@ -131,7 +132,7 @@ struct GraphKey {
     const void* L;
     uint64_t lgen;
     const void *b, *x;
-    int n, m, flexible, fp32;
+    int n, m, flexible, fp32, lagged;
     size_t ldv;
     const void *V, *Z, *t, *r64, *st, *hist;
     int hist_cap;
@@ -321,6 +322,7 @@ struct sg_precond {
     sg::DBuf<int> rec_rows_f_d, rec_rows_b_d;
     sg::DBuf<unsigned char> rec_d;
     sg::DBuf<int> err_d;  // device error word of the sweeps (bounded waits)
+    int wait_test = 0;     // sg_precond_set_wait_test mode (0: normal)
     sg::DBuf<double> gscratch64;
     sg::DBuf<float> gscratch32;
     // ---- coarse space

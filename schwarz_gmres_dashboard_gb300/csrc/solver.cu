@@ -93,15 +93,16 @@ void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int*
     }
 }
 
-// The lagged two-pass CGS2 serves the FP32 left-preconditioned cycle with a
-// restart below SG_LAGM: it relies on the operator being linear (B v_k =
+// The lagged two-pass CGS2 serves the left-preconditioned cycle (FP32 or
+// FP64 basis) with a restart below SG_LAGM unless the caller asks for the
+// classic three passes: it relies on the operator being linear (B v_k =
 // V H(:,k)), which FGMRES's possibly nonlinear preconditioner does not give.
-bool use_lagged(bool fp32, bool flexible, int m) { return fp32 && !flexible && m < SG_LAGM; }
+bool use_lagged(bool flexible, int m, int ortho) { return ortho == 0 && !flexible && m < SG_LAGM; }
 
 // One restart cycle as a launch sequence on ctx->stream.
 template <class TV>
 void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b, double* x,
-                   int m, bool flexible, size_t ldv) {
+                   int m, bool flexible, bool lagged, size_t ldv) {
     SolveWork* w = ctx->work;
     SolveState* st = w->st.p;
     const int n = A->nrows;
@@ -143,8 +144,7 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
             launch_spmv_a<TV, TV, TV>(ctx, A, zj, wj, &st->vscale[j], active);
         }
         ClassTimer tm(ctx, TK_ORTHO);
-        launch_cgs2<TV>(ctx, V, ldv, n, j, m, st,
-                        use_lagged(sizeof(TV) == sizeof(float), flexible, m));
+        launch_cgs2<TV>(ctx, V, ldv, n, j, m, st, lagged);
     }
     {
         ClassTimer tm(ctx, TK_UPDATE);
@@ -178,8 +178,10 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
                  "solve precision must be SG_FP64 or SG_FP32");
     SG_CHECK_ARG(prm.tol_kind >= SG_TOL_REF_ABS && prm.tol_kind <= SG_TOL_TRUE_REL,
                  "unknown tol_kind %d", prm.tol_kind);
+    SG_CHECK_ARG(prm.ortho == 0 || prm.ortho == 1, "ortho must be 0 or 1 (got %d)", prm.ortho);
     const bool flexible = solver == SG_FGMRES;
     const bool fp32 = prm.precision == SG_FP32;
+    const bool lagged = use_lagged(flexible, m, prm.ortho);
     if (!ctx->work) ctx->work = new SolveWork();
     SolveWork* w = ctx->work;
     // basis stride: a multiple of 32 elements plus 32, so consecutive basis
@@ -218,7 +220,7 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     hs->max_iter = prm.max_iter;
     hs->tol = prm.tol;
     hs->tol_kind = prm.tol_kind;
-    hs->lagged = use_lagged(fp32, flexible, m) ? 1 : 0;
+    hs->lagged = lagged ? 1 : 0;
     const auto t0 = std::chrono::high_resolution_clock::now();
     SG_CUDA(cudaMemcpyAsync(w->st.p, hs, sizeof(SolveState), cudaMemcpyHostToDevice, ctx->stream));
     launch_bnorm(ctx, b, n, w->st.p);
@@ -253,6 +255,7 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
         key.m = m;
         key.flexible = flexible ? 1 : 0;
         key.fp32 = fp32 ? 1 : 0;
+        key.lagged = lagged ? 1 : 0;
         key.ldv = ldv;
         key.V = fp32 ? (const void*)w->V32.p : (const void*)w->V64.p;
         key.Z = fp32 ? (const void*)w->Z32.p : (const void*)w->Z64.p;
@@ -271,8 +274,8 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
             ctx->capturing = true;
             ctx->captured = 0;
             try {
-                if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
-                else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
+                if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, lagged, ldv);
+                else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, lagged, ldv);
             } catch (...) {
                 ctx->capturing = false;
                 cudaStreamEndCapture(ctx->stream, &g);
@@ -299,13 +302,18 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
                 SG_CUDA(cudaGraphLaunch(exec, ctx->stream));
                 ctx->launches += w->graph_nodes;
             }
-            else if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, ldv);
-            else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, ldv);
+            else if (fp32) enqueue_cycle<float>(ctx, A, pc, b, x, m, flexible, lagged, ldv);
+            else enqueue_cycle<double>(ctx, A, pc, b, x, m, flexible, lagged, ldv);
             ++cycles;
+            // a sweep that gave up on a bounded wait ends the solve (its
+            // output was not written, so later cycles would be meaningless)
+            if (pc && pc->err_d.p)
+                SG_CUDA(cudaMemcpyAsync(&w->st.p->sweep_err, pc->err_d.p, sizeof(int),
+                                        cudaMemcpyDeviceToDevice, ctx->stream));
             SG_CUDA(cudaMemcpyAsync(hs, w->st.p, ctl_bytes, cudaMemcpyDeviceToHost, ctx->stream));
             SG_CUDA(cudaStreamSynchronize(ctx->stream));
             if (ctx->timing) collect_timers(ctx);
-            if (hs->done) break;
+            if (hs->done || hs->sweep_err) break;
         }
     } catch (...) {
         // a failed solve drops the cached cycle

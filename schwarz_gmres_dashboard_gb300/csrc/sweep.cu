@@ -291,6 +291,11 @@ struct RecArgs {
     int fuse;
     double* r0w;
     unsigned* sync;
+    // bounded waits: cycle budget of the record and restriction waits, and
+    // the test mode that makes one of them run out without any fault
+    // (1: no record group 0 is copied; 2: no restriction is counted)
+    long long wait_budget;
+    int wait_test;
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -364,7 +369,8 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
         for (int i = 0; i < NB; ++i) mbar_init(smem_u32(&bars[i]), 1);
         fence_mbar_init();
         fence_proxy_async();
-        for (int q = 0; q < ngrp && q < NB; ++q) issue(q, q);
+        for (int q = 0; q < ngrp && q < NB; ++q)
+            if (!(a.wait_test == 1 && q == 0)) issue(q, q);
     }
     // gather while the first records are in flight
     const int* dof = a.dofs + inf.row_off;
@@ -385,7 +391,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             if (threadIdx.x == 0) {
                 a.r0w[sr] = ir.cscale * z;
                 __threadfence();
-                atomicAdd(&a.sync[0], 1u);
+                if (a.wait_test != 2) atomicAdd(&a.sync[0], 1u);
             }
         }
     }
@@ -409,7 +415,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     uint32_t roff = 0;
     for (int g = 0; g < T; ++g) {
         bool ok = true;
-        if (g == gstart) ok = mbar_wait(smem_u32(&bars[b]), ph, WAIT_CYCLES);
+        if (g == gstart) ok = mbar_wait(smem_u32(&bars[b]), ph, a.wait_budget);
         int cn = 0, Cn = 0;
         long long on = 0;
         if (g + 1 < T) {
@@ -425,19 +431,25 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
         }
         if (g == gstart) {
             if (__syncthreads_or(ok ? 0 : 1)) {
-                // a record group never arrived: report, drain what was
-                // issued, leave y alone
+                // a record group did not arrive in time: report, drain the
+                // copies that were issued (groups q .. q+NB-1; the earlier
+                // ones have landed), leave y alone.  Each drain wait has the
+                // full budget; if one still gives up, the block leaves with
+                // that copy outstanding -- accepted only because such a copy
+                // never arrives at all -- and the error word says 2.
                 if (producer) {
-                    atomicExch(a.err, 1);
+                    int code = 1;
                     int b2 = b;
                     uint32_t p2 = ph;
                     for (int h = q; h < ngrp && h < q + NB; ++h) {
-                        mbar_wait(smem_u32(&bars[b2]), p2, WAIT_CYCLES / 8);
+                        const bool issued = !(a.wait_test == 1 && h == 0);
+                        if (issued && !mbar_wait(smem_u32(&bars[b2]), p2, WAIT_CYCLES)) code = 2;
                         if (++b2 == NB) {
                             b2 = 0;
                             p2 ^= 1u;
                         }
                     }
+                    atomicMax(a.err, code);
                 }
                 return;
             }
@@ -473,7 +485,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
                 const long long t0 = clock64();
                 int ok = 1;
                 while (ld_acquire(&a.sync[0]) < gridDim.x) {
-                    if (clock64() - t0 > WAIT_CYCLES) {
+                    if (clock64() - t0 > a.wait_budget) {
                         ok = 0;
                         break;
                     }
@@ -483,7 +495,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             }
             __syncthreads();
             if (!s_ok) {
-                if (threadIdx.x == 0) atomicExch(a.err, 1);
+                if (threadIdx.x == 0) atomicMax(a.err, 1);
                 return;
             }
         }
@@ -543,6 +555,8 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     a.max_levels = pc->max_levels;
     a.err = pc->err_d.p;
     a.sub_on = pc->sub_on;
+    a.wait_test = pc->wait_test;
+    a.wait_budget = pc->wait_test ? WAIT_TEST_CYCLES : WAIT_CYCLES;
     return a;
 }
 
@@ -804,13 +818,22 @@ int sweep_error(sg_precond* pc) {
     int e = 0;
     SG_CUDA(cudaMemcpyAsync(&e, pc->err_d.p, sizeof(int), cudaMemcpyDeviceToHost, pc->ctx->stream));
     SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
-    // a sweep that gave up may have left the fused restriction's counters
-    // mid-count: clear them with the error word
-    if (e && pc->coarse_sync.p) {
-        pc->coarse_sync.zero(pc->ctx->stream);
+    // reported once: clear the error word, and the fused restriction's
+    // counters, which a sweep that gave up may have left mid-count, so the
+    // next apply starts clean
+    if (e) {
+        pc->err_d.zero(pc->ctx->stream);
+        if (pc->coarse_sync.p) pc->coarse_sync.zero(pc->ctx->stream);
         SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
     }
     return e;
+}
+
+bool sweep_wait_test_supported(const sg_precond* pc, int mode) {
+    if (mode == 0) return true;
+    if (!pc->use_rec || pc->rec_depth == 0) return false;
+    if (mode == 1) return true;
+    return mode == 2 && sweep_fuses_restrict(pc);
 }
 
 template bool sweep_tma<double, double>(sg_precond*, const double*, double*, int, bool, bool,

@@ -9,6 +9,8 @@
 namespace sg {
 
 constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
+// the budget of the waits a wait test makes run out (~1 ms)
+constexpr long long WAIT_TEST_CYCLES = 2000000ll;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);

@@ -1,11 +1,13 @@
-"""The lagged two-pass CGS2 of the FP32 GMRES cycle (restart < 32).
+"""The lagged two-pass CGS2 of the GMRES cycle (restart < 32, FP32 or FP64
+basis).
 
 Each Arnoldi step defers the second projection of its new basis vector to the
 next step and corrects that step's Hessenberg column through the Arnoldi
 relation; in exact arithmetic it is CGS2.  The residual estimates of the
-first cycle must therefore follow the FP64 solver's (classic CGS2) to FP32
-accuracy, and the FP32 solve with a restart of 31 (lagged) must behave like
-one of 32 (classic).
+first cycle must therefore follow the classic three-pass CGS2 of the FP64
+solver (ortho=1) to FP32 accuracy for the FP32 basis and to near FP64
+accuracy for the FP64 basis, and the FP32 solve with a restart of 31 (lagged)
+must behave like one of 32 (classic).
 """
 from __future__ import annotations
 
@@ -31,7 +33,8 @@ def test_first_cycle_residual_estimates_match_fp64(sg):
         A, b, pc = _setup(sg, 32, 8, sd)
         x = np.zeros(A.nrows)
         r = sg.gmres(A, b, x, pc, sg.GMRESParams(restart=30, max_iter=30, tol=1e-30,
-                                                  tol_kind=sg.TOL_REF_ABS, precision=prec))
+                                                  tol_kind=sg.TOL_REF_ABS, precision=prec,
+                                                  ortho=1 if prec == sg.FP64 else 0))
         hist[prec] = np.asarray(r.residual_history)
     h64, h32 = hist[sg.FP64], hist[sg.FP32]
     assert len(h64) == len(h32) == 30
@@ -39,6 +42,35 @@ def test_first_cycle_residual_estimates_match_fp64(sg):
     # inner cycle works on the preconditioned residual, like the FP64 one)
     rel = np.abs(h32 / h32[0] - h64 / h64[0]) / (h64 / h64[0])
     assert rel[:20].max() <= 2e-3, rel
+
+
+def test_fp64_lagged_matches_classic(sg):
+    A, b, pc = _setup(sg, 32, 8, sg.FP64)
+    hist, xs = {}, {}
+    for ortho in (0, 1):
+        x = np.zeros(A.nrows)
+        r = sg.gmres(A, b, x, pc, sg.GMRESParams(restart=30, max_iter=30, tol=1e-30,
+                                                  tol_kind=sg.TOL_REF_ABS, precision=sg.FP64,
+                                                  ortho=ortho))
+        hist[ortho] = np.asarray(r.residual_history)
+        xs[ortho] = x
+    h0, h1 = hist[0], hist[1]
+    assert len(h0) == len(h1) == 30
+    # the same Krylov space to FP64 rounding: estimates agree to 1e-12 of the
+    # starting norm, and to 1e-6 relative even after they have fallen far
+    assert (np.abs(h0 - h1) / h1[0]).max() <= 1e-12
+    assert (np.abs(h0 - h1) / h1).max() <= 1e-6
+    assert np.linalg.norm(xs[0] - xs[1]) <= 1e-8 * np.linalg.norm(xs[1])
+    # and both solvers reach the target with the same iteration count (+-1)
+    its = []
+    for ortho in (0, 1):
+        x = np.zeros(A.nrows)
+        r = sg.gmres(A, b, x, pc, sg.GMRESParams(restart=30, max_iter=3000, tol=1e-8,
+                                                  tol_kind=sg.TOL_TRUE_REL, precision=sg.FP64,
+                                                  ortho=ortho))
+        assert r.converged and r.true_rel_residual <= 1e-8
+        its.append(r.iterations)
+    assert abs(its[0] - its[1]) <= 1, its
 
 
 @pytest.mark.parametrize("restart", [31, 32])

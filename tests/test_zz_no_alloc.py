@@ -1,11 +1,10 @@
 """sg_dot_noalloc: the dot product for callers that cannot allocate device memory.
 
-Who needs it: code that runs while its stream is being captured into a CUDA
-graph (cudaMalloc/cudaFree are not allowed during capture), plug-ins inside an
-application that owns all device memory through its own pool, and real-time
-loops that cannot pay cudaFree's device-wide synchronisation.  sg_dot takes
-its reduction scratch from a context, which allocates; sg_dot_noalloc keeps
-that scratch in a fixed array inside the library.
+Who needs it: plug-ins inside an application that owns all device memory
+through its own pool and forbids raw cudaMalloc, and real-time loops that
+cannot pay cudaMalloc's latency or cudaFree's device-wide synchronisation.
+sg_dot takes its reduction scratch from a context, which allocates;
+sg_dot_noalloc keeps that scratch in a fixed array inside the library.
 
 The test calls the entry point through the C ABI (ctypes) twice in a row,
 on different sizes (the second call finds the first call's partial sums still
@@ -13,7 +12,9 @@ in the shared array), and checks each result against sg_dot -- the existing
 entry point -- within the dot-product tolerance the other tests use
 (1e-14 relative to sum |x_i y_i|: the two kernels add the same terms in
 different block orders).  The device buffers come from torch; the entry point
-itself allocates nothing.
+itself allocates nothing, which the test checks through the device's free
+memory around calls made after the first one (the first call on a device may
+load the library's device code, which the driver allocates for).
 """
 from __future__ import annotations
 
@@ -46,6 +47,30 @@ def test_dot_noalloc_matches_sg_dot_on_two_calls(sg):
         got = float(out.item())
         ref = sg.dot(xd, yd)  # the existing entry point (context scratch)
         assert abs(got - ref) <= 1e-14 * float(np.abs(x * y).sum()), (got, ref)
+
+
+def test_dot_noalloc_allocates_nothing(sg):
+    torch = pytest.importorskip("torch")
+    from schwarz_gmres_dashboard_gb300 import _lib
+
+    lib = _lib.load()
+    n = 4_000_037
+    xd = torch.from_numpy(sg.uniform(n, seed=7)).cuda()
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    args = (C.c_void_p(xd.data_ptr()), C.c_void_p(xd.data_ptr()), n)
+    assert lib.sg_dot_noalloc(*args, C.c_void_p(out.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_allocated()
+    for i in (1, 2):
+        st = lib.sg_dot_noalloc(*args, C.c_void_p(out.data_ptr() + 8 * i), None)
+        assert st == 0, lib.sg_last_error().decode()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert torch.cuda.memory_allocated() == alloc0
+    v = out.cpu().numpy()
+    assert v[0] == v[1] == v[2]  # same inputs, same order: same bits
 
 
 def test_dot_noalloc_rejects_sizes_beyond_its_scratch(sg):
