@@ -386,6 +386,38 @@ sg_status sg_learned_get_state(sg_learned* L, int* enabled, int* fallback_cycle,
  * serves one preconditioner at a time. */
 sg_status sg_precond_set_learned(sg_precond* pc, sg_learned* L, double stagnation);
 
+/* ---- file formats (host side, no device work) ------------------------- */
+/* read_matrix_market (src/io/matrix_market.h:14-92), same reading rules:
+ * '%' comment lines mentioning "symmetric" mirror every off-diagonal entry,
+ * "pattern" reads entries as 1.0; duplicates are kept; rows and columns end
+ * up ascending (duplicates in file order).  Blank lines are skipped; an
+ * index outside the declared size is SG_ERR_INVALID_ARG.  Call with
+ * row_ptr == NULL for the sizes, then with arrays of nrows+1 / cap / cap
+ * entries (cap >= nnz). */
+sg_status sg_read_matrix_market(const char* path, int* nrows, int* ncols, int* nnz, int* row_ptr,
+                                int* col_idx, double* vals, int cap);
+/* ConvergenceMetrics (src/analysis/convergence_analysis.h:15-65) of a
+ * residual history: rate_k = (r_k / r_0)^(1/k), the mean of the last (up to)
+ * 20 rates, and the first 20-iteration window with a relative reduction
+ * below 1e-3 (-1: none).  rates (optional) receives len values. */
+typedef struct sg_convergence {
+    int iterations;
+    int converged;
+    int stagnation_start;
+    int reserved;
+    double initial_residual;
+    double final_residual;
+    double asymptotic_rate;
+} sg_convergence;
+sg_status sg_convergence_metrics(const double* history, int len, int converged,
+                                 sg_convergence* out, double* rates);
+/* Appends the record ConvergenceMetrics::write_jsonl writes
+ * (convergence_analysis.h:69-93; the CLI's <output>.conv.jsonl, src/main.cpp:
+ * 251-258): same keys, order and 6-significant-digit numbers. */
+sg_status sg_write_convergence_jsonl(const char* path, const char* matrix, const char* precond,
+                                     int nparts, int overlap, const double* history, int len,
+                                     int converged);
+
 /* ---- problem generators and partitions (host side, deterministic) ----- */
 /* make_poisson_2d / make_poisson_3d (src/mesh/poisson.h:10-74).  Call with
  * NULL arrays to get nnz, then with arrays of n+1 / nnz / nnz entries. */

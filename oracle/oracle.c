@@ -949,3 +949,260 @@ int orc_varcoef3d(int nx, int ny, int nz, double sigma, double corr, uint64_t se
     free(k);
     return e;
 }
+
+/* ------------------------------------------------------------------------
+ * BiCGSTAB with right preconditioning (src/core/bicgstab.h:57-204), in the
+ * reference's operation order.  Returns the converged flag; iters, res_norm
+ * and the history of ||r|| (or ||s|| on an early exit) as the reference's
+ * GMRESResult holds them.
+ * ---------------------------------------------------------------------- */
+int orc_bicgstab(int n, const int* rp, const int* ci, const double* v, const double* b,
+                 double* x, const orc_pc* pc, int max_iter, double tol, int* iters,
+                 double* res_norm, double* hist, int hist_cap, int* hist_len) {
+    const size_t bytes = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    double *r = malloc(bytes), *rh = malloc(bytes), *p = calloc((size_t)(n > 0 ? n : 1), 8),
+           *vv = calloc((size_t)(n > 0 ? n : 1), 8), *y = malloc(bytes), *z = malloc(bytes),
+           *s = malloc(bytes), *t = malloc(bytes), *tmp = malloc(bytes);
+    int nh = 0, conv = 0, it_out = 0;
+    double res = 0.0;
+#define O_HIST(val) do { if (hist && nh < hist_cap) hist[nh] = (val); ++nh; } while (0)
+#define O_PREC(in, out) do { if (pc) orc_pc_apply(pc, in, out, n); \
+                             else memcpy(out, in, sizeof(double) * (size_t)n); } while (0)
+    orc_spmv(n, rp, ci, v, x, tmp); /* bicgstab.h:76-78 */
+    for (int i = 0; i < n; ++i) r[i] = b[i] - tmp[i];
+    memcpy(rh, r, sizeof(double) * (size_t)n);
+    const double r0 = o_norm2(r, n);
+    if (r0 < 1e-14) { /* :83-88 */
+        conv = 1;
+        res = r0;
+        goto done;
+    }
+    double rho = 1.0, alpha = 1.0, omega = 1.0, rho_prev;
+    for (int iter = 1; iter <= max_iter; ++iter) {
+        rho_prev = rho;
+        rho = o_dot(rh, r, n);
+        if (fabs(rho) < 1e-300) { /* :101-107 */
+            it_out = iter;
+            res = o_norm2(r, n);
+            conv = 0;
+            break;
+        }
+        if (iter == 1) {
+            memcpy(p, r, sizeof(double) * (size_t)n);
+        } else {
+            const double beta = (rho / rho_prev) * (alpha / omega);
+            for (int i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * vv[i]);
+        }
+        O_PREC(p, y);
+        orc_spmv(n, rp, ci, v, y, vv);
+        const double rhv = o_dot(rh, vv, n);
+        if (fabs(rhv) < 1e-300) { /* :125-130 */
+            it_out = iter;
+            res = o_norm2(r, n);
+            conv = 0;
+            break;
+        }
+        alpha = rho / rhv;
+        for (int i = 0; i < n; ++i) s[i] = r[i] - alpha * vv[i];
+        const double sn = o_norm2(s, n);
+        if (sn < tol * r0) { /* :140-148 lucky exit after the half step */
+            for (int i = 0; i < n; ++i) x[i] += alpha * y[i];
+            it_out = iter;
+            res = sn;
+            conv = 1;
+            O_HIST(sn);
+            break;
+        }
+        O_PREC(s, z);
+        orc_spmv(n, rp, ci, v, z, t);
+        const double tt = o_dot(t, t, n);
+        if (tt < 1e-300) { /* :158-165 */
+            for (int i = 0; i < n; ++i) x[i] += alpha * y[i];
+            it_out = iter;
+            res = sn;
+            conv = sn < tol * r0;
+            break;
+        }
+        omega = o_dot(t, s, n) / tt;
+        for (int i = 0; i < n; ++i) x[i] += alpha * y[i] + omega * z[i];
+        for (int i = 0; i < n; ++i) r[i] = s[i] - omega * t[i];
+        const double rn = o_norm2(r, n);
+        O_HIST(rn);
+        it_out = iter;
+        res = rn;
+        conv = 0;
+        if (rn < tol * r0) { /* :181-186 */
+            conv = 1;
+            break;
+        }
+        if (fabs(omega) < 1e-300) break; /* :188-194 stagnation */
+    }
+done:
+#undef O_HIST
+#undef O_PREC
+    *iters = it_out;
+    *res_norm = res;
+    if (hist_len) *hist_len = nh;
+    free(r); free(rh); free(p); free(vv); free(y); free(z); free(s); free(t); free(tmp);
+    return conv;
+}
+
+/* ------------------------------------------------------------------------
+ * Analysis tools (src/analysis/condition_estimator.h:94-191,
+ * src/analysis/spectral_analysis.h:30-97).
+ * ---------------------------------------------------------------------- */
+/* the reference's start vector: a 32-bit LCG (x <- 1664525 x + 1013904223)
+ * read as a signed int / 2^31, normalised (condition_estimator.h:107-117) */
+static void o_lcg_unit(int n, unsigned seed, double* v, int guard_tiny) {
+    unsigned st = seed;
+    double nrm = 0.0;
+    for (int i = 0; i < n; ++i) {
+        st = st * 1664525u + 1013904223u;
+        v[i] = (double)(int)st / 2147483648.0;
+        nrm += v[i] * v[i];
+    }
+    nrm = sqrt(nrm);
+    if (guard_tiny && nrm < 1e-14) nrm = 1.0;
+    for (int i = 0; i < n; ++i) v[i] /= nrm;
+}
+
+static int o_cmp_double(const void* a, const void* b) {
+    const double x = *(const double*)a, y = *(const double*)b;
+    return (x > y) - (x < y);
+}
+
+/* eigenvalues of the symmetric tridiagonal (d, e) by implicit QL with the
+ * Wilkinson shift, as tridiag_eigs_ql (condition_estimator.h:42-88) runs it
+ * (including its handling of an exactly zero rotation radius); sorted */
+static void o_tridiag_eigs(double* d, double* e, int n) {
+    const int max_iter = 100 * n;
+    for (int l = 0; l < n; ++l) {
+        int m, iter = 0;
+        do {
+            for (m = l; m < n - 1; ++m) {
+                const double off = fabs(d[m]) + fabs(d[m + 1]);
+                if (fabs(e[m]) <= 1e-14 * off) break;
+            }
+            if (m == l) break;
+            if (++iter > max_iter) break;
+            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double r = hypot(g, 1.0);
+            g = d[m] - d[l] + e[l] / (g + copysign(r, g));
+            double s = 1.0, c = 1.0, p = 0.0;
+            for (int i = m - 1; i >= l; --i) {
+                const double f = s * e[i];
+                const double bb = c * e[i];
+                r = hypot(f, g);
+                e[i + 1] = r;
+                if (r == 0.0) {
+                    d[i + 1] -= p;
+                    e[m] = 0.0;
+                    break;
+                }
+                s = f / r;
+                c = g / r;
+                g = d[i + 1] - p;
+                r = (d[i] - g) * s + 2.0 * c * bb;
+                p = s * r;
+                d[i + 1] = g + p;
+                g = c * r - bb;
+            }
+            d[l] -= p;
+            e[l] = g;
+            e[m] = 0.0;
+        } while (m != l);
+    }
+    qsort(d, (size_t)n, sizeof(double), o_cmp_double);
+}
+
+/* estimate_condition: k Lanczos steps on M^{-1}A (A when pc is NULL or of
+ * kind NONE), extreme Ritz values of the tridiagonal.  out: lambda_min,
+ * lambda_max, kappa; iout: steps, valid.  Returns the steps (0: no estimate). */
+int orc_condition(int n, const int* rp, const int* ci, const double* v, const orc_pc* pc, int k,
+                  unsigned seed, double* out, int* iout) {
+    out[0] = out[1] = out[2] = 0.0;
+    iout[0] = iout[1] = 0;
+    if (k > n) k = n;
+    if (k < 2) return 0;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    double *vc = malloc(bytes), *vp = calloc((size_t)n, 8), *w = malloc(bytes), *z = malloc(bytes);
+    double* al = malloc(sizeof(double) * (size_t)k);
+    double* be = calloc((size_t)k + 1, sizeof(double));
+    o_lcg_unit(n, seed, vc, 1);
+    int na = 0, nb = 0;
+    double beta = 0.0;
+    for (int j = 0; j < k; ++j) {
+        orc_spmv(n, rp, ci, v, vc, w);
+        if (pc) orc_pc_apply(pc, w, z, n);
+        else memcpy(z, w, bytes);
+        const double alpha = o_dot(vc, z, n);
+        al[na++] = alpha;
+        for (int i = 0; i < n; ++i) z[i] -= alpha * vc[i] + beta * vp[i];
+        const double bn = o_norm2(z, n);
+        if (bn < 1e-10 * (1.0 + fabs(alpha))) break;
+        if (j < k - 1) {
+            be[nb++] = bn;
+            memcpy(vp, vc, bytes);
+            beta = bn;
+            const double inv = 1.0 / bn;
+            for (int i = 0; i < n; ++i) vc[i] = z[i] * inv;
+        }
+    }
+    int steps = 0;
+    int finite = 1;
+    for (int i = 0; i < na; ++i) finite &= isfinite(al[i]) != 0;
+    for (int i = 0; i < nb; ++i) finite &= isfinite(be[i]) != 0;
+    if (na >= 2 && finite) {
+        for (int i = nb; i < na; ++i) be[i] = 0.0;
+        o_tridiag_eigs(al, be, na);
+        int lo = -1, hi = -1;
+        for (int i = 0; i < na; ++i)
+            if (isfinite(al[i])) {
+                if (lo < 0) lo = i;
+                hi = i;
+            }
+        if (lo >= 0) {
+            out[0] = al[lo];
+            out[1] = al[hi];
+            out[2] = fabs(al[lo]) > 1e-14 ? al[hi] / al[lo] : 1e30;
+            iout[0] = steps = na;
+            iout[1] = al[lo] > 0.0;
+        }
+    }
+    free(vc); free(vp); free(w); free(z); free(al); free(be);
+    return steps;
+}
+
+/* estimate_spectral_radius: power iteration on E = I - M^{-1}A, stopping
+ * when the Rayleigh quotient changes by < tol (1 + |mu|); reports |mu| of
+ * the step before the last, as the reference does.  out: rho; iout: steps,
+ * rho < 1. */
+void orc_spectral(int n, const int* rp, const int* ci, const double* v, const orc_pc* pc,
+                  int max_iter, double tol, unsigned seed, double* out, int* iout) {
+    const size_t bytes = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    double *vv = malloc(bytes), *w = malloc(bytes), *z = malloc(bytes);
+    o_lcg_unit(n, seed, vv, 0);
+    double mu_prev = 0.0;
+    int steps = 0;
+    for (int it = 0; it < max_iter; ++it) {
+        orc_spmv(n, rp, ci, v, vv, w);
+        if (pc) orc_pc_apply(pc, w, z, n);
+        else memcpy(z, w, bytes);
+        for (int i = 0; i < n; ++i) w[i] = vv[i] - z[i];
+        double mu = o_dot(vv, w, n);
+        const double en = o_norm2(w, n);
+        if (en < 1e-14) {
+            steps = it + 1;
+            mu = 0.0;
+            break;
+        }
+        for (int i = 0; i < n; ++i) vv[i] = w[i] / en;
+        steps = it + 1;
+        if (fabs(mu - mu_prev) < tol * (1.0 + fabs(mu))) break;
+        mu_prev = mu;
+    }
+    out[0] = fabs(mu_prev);
+    iout[0] = steps;
+    iout[1] = out[0] < 1.0;
+    free(vv); free(w); free(z);
+}

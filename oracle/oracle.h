@@ -102,6 +102,20 @@ int orc_fgmres(int n, const int* rp, const int* ci, const double* v, const doubl
 int orc_poisson2d(int nx, int ny, int* rp, int* ci, double* v);
 int orc_poisson3d(int nx, int ny, int nz, int* rp, int* ci, double* v);
 
+/* BiCGSTAB, right preconditioned (src/core/bicgstab.h:57-204); pc may be
+ * NULL.  Returns the converged flag. */
+int orc_bicgstab(int n, const int* rp, const int* ci, const double* v, const double* b,
+                 double* x, const orc_pc* pc, int max_iter, double tol, int* iters,
+                 double* res_norm, double* hist, int hist_cap, int* hist_len);
+/* estimate_condition (src/analysis/condition_estimator.h:94-191): out =
+ * lambda_min, lambda_max, kappa; iout = Lanczos steps, valid. */
+int orc_condition(int n, const int* rp, const int* ci, const double* v, const orc_pc* pc, int k,
+                  unsigned seed, double* out, int* iout);
+/* estimate_spectral_radius (src/analysis/spectral_analysis.h:30-97): out =
+ * rho(I - M^{-1}A); iout = power iterations, rho < 1. */
+void orc_spectral(int n, const int* rp, const int* ci, const double* v, const orc_pc* pc,
+                  int max_iter, double tol, unsigned seed, double* out, int* iout);
+
 /* Benchmark inputs the project generates (no reference counterpart),
  * restated from the package so the CPU baseline needs nothing else:
  * uniform vectors (SplitMix64, (u >> 11) * 2^-53), uneven box partitions

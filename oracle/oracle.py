@@ -92,6 +92,16 @@ class Oracle(_Lib):
         L.orc_poisson3d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                     C.c_void_p]
         L.orc_poisson3d.restype = C.c_int
+        L.orc_bicgstab.argtypes = [C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.c_void_p,
+                                   C.c_int, C.c_double, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_double), C.c_void_p, C.c_int,
+                                   C.POINTER(C.c_int)]
+        L.orc_bicgstab.restype = C.c_int
+        L.orc_condition.argtypes = [C.c_int, _i32p, _i32p, _f64p, C.c_void_p, C.c_int, C.c_uint,
+                                    _f64p, _i32p]
+        L.orc_condition.restype = C.c_int
+        L.orc_spectral.argtypes = [C.c_int, _i32p, _i32p, _f64p, C.c_void_p, C.c_int, C.c_double,
+                                   C.c_uint, _f64p, _i32p]
         L.orc_uniform.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, _f64p]
         L.orc_partition_boxes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                           C.c_uint64, _i32p]
@@ -178,6 +188,38 @@ class Oracle(_Lib):
 
     def fgmres(self, A, b, x0, pc=None, restart=30, max_iter=1000, tol=1e-10, hist_cap=0):
         return self._solve(self.lib.orc_fgmres, A, b, x0, pc, restart, max_iter, tol, hist_cap)
+
+    def bicgstab(self, A, b, x0, pc=None, max_iter=1000, tol=1e-10, hist_cap=0):
+        rp, ci, v = _csr_args(A)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.array(x0, dtype=np.float64, copy=True)
+        it, res, hl = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        hist = np.zeros(max(hist_cap, 1))
+        conv = self.lib.orc_bicgstab(A.nrows, rp, ci, v, b, x,
+                                     pc.handle if pc is not None else None, max_iter, tol,
+                                     C.byref(it), C.byref(res),
+                                     hist.ctypes.data if hist_cap else None, hist_cap,
+                                     C.byref(hl))
+        return dict(x=x, converged=bool(conv), iterations=it.value, residual_norm=res.value,
+                    history=hist[: min(hl.value, hist_cap)].copy(), history_len=hl.value)
+
+    def condition(self, A, pc=None, k=80, seed=42):
+        rp, ci, v = _csr_args(A)
+        out = np.zeros(3)
+        iout = np.zeros(2, np.int32)
+        self.lib.orc_condition(A.nrows, rp, ci, v, pc.handle if pc is not None else None, k,
+                               seed, out, iout)
+        return dict(lambda_min=out[0], lambda_max=out[1], kappa=out[2],
+                    lanczos_steps=int(iout[0]), valid=bool(iout[1]))
+
+    def spectral(self, A, pc=None, max_iter=200, tol=1e-6, seed=123):
+        rp, ci, v = _csr_args(A)
+        out = np.zeros(1)
+        iout = np.zeros(2, np.int32)
+        self.lib.orc_spectral(A.nrows, rp, ci, v, pc.handle if pc is not None else None,
+                              max_iter, tol, seed, out, iout)
+        return dict(spectral_radius=out[0], power_iters=int(iout[0]),
+                    convergence_ok=bool(iout[1]))
 
     def poisson2d(self, nx, ny):
         nz = self.lib.orc_poisson2d(nx, ny, None, None, None)
@@ -337,6 +379,19 @@ class Reference(_Lib):
                            C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
                            C.POINTER(C.c_int)]
             fn.restype = C.c_int
+        L.ref_bicgstab.argtypes = [C.c_void_p, _f64p, _f64p, C.c_int, C.c_double,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p,
+                                   C.c_int, C.POINTER(C.c_int)]
+        L.ref_bicgstab.restype = C.c_int
+        L.ref_read_mm.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_int]
+        L.ref_read_mm.restype = C.c_int
+        L.ref_conv_metrics.argtypes = [_f64p, C.c_int, C.c_int, _f64p, _i32p, C.c_void_p]
+        L.ref_conv_write.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int,
+                                     _f64p, C.c_int, C.c_int]
+        L.ref_condition.argtypes = [C.c_void_p, C.c_int, C.c_uint, _f64p, _i32p]
+        L.ref_spectral.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_uint, _f64p, _i32p]
 
     def set_partition(self, part, nparts):
         part = np.ascontiguousarray(part, dtype=np.int32)
@@ -410,6 +465,72 @@ class Reference(_Lib):
 
     def fgmres(self, A, b, x0, pc=None, restart=30, max_iter=1000, tol=1e-10, hist_cap=0):
         return self._solve(self.lib.ref_fgmres, A, b, x0, pc, restart, max_iter, tol, hist_cap)
+
+
+def _ref_methods(cls):
+    def read_mm(self, path):
+        nr, nc, nz = C.c_int(0), C.c_int(0), C.c_int(0)
+        if self.lib.ref_read_mm(path.encode(), C.byref(nr), C.byref(nc), C.byref(nz), None,
+                                None, None, 0):
+            raise RuntimeError("reference read_matrix_market threw")
+        rp = np.empty(nr.value + 1, np.int32)
+        ci = np.empty(max(nz.value, 1), np.int32)
+        v = np.empty(max(nz.value, 1))
+        self.lib.ref_read_mm(path.encode(), C.byref(nr), C.byref(nc), C.byref(nz),
+                             rp.ctypes.data, ci.ctypes.data, v.ctypes.data, ci.size)
+        return nr.value, nc.value, rp, ci[: nz.value], v[: nz.value]
+
+    def conv_metrics(self, hist, converged):
+        h = np.ascontiguousarray(hist, np.float64)
+        d = np.zeros(3)
+        i = np.zeros(2, np.int32)
+        rates = np.zeros(max(len(h), 1))
+        self.lib.ref_conv_metrics(h, len(h), int(converged), d, i, rates.ctypes.data)
+        return dict(initial_residual=d[0], final_residual=d[1], asymptotic_rate=d[2],
+                    iterations=int(i[0]), stagnation_start=int(i[1]), rates=rates[: len(h)])
+
+    def conv_write(self, path, matrix, precond, nparts, overlap, hist, converged):
+        h = np.ascontiguousarray(hist, np.float64)
+        self.lib.ref_conv_write(path.encode(), matrix.encode(), precond.encode(), nparts,
+                                overlap, h, len(h), int(converged))
+
+    def bicgstab(self, A, b, x0, pc=None, max_iter=1000, tol=1e-10, hist_cap=0):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.array(x0, dtype=np.float64, copy=True)
+        it, res, hl = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        hist = np.zeros(max(hist_cap, 1))
+        if pc is None:
+            pc = RefPC(self, "none", A, 1, 0, None)
+        conv = self.lib.ref_bicgstab(pc.handle, b, x, max_iter, tol, C.byref(it), C.byref(res),
+                                     hist.ctypes.data if hist_cap else None, hist_cap,
+                                     C.byref(hl))
+        return dict(x=x, converged=bool(conv), iterations=it.value, residual_norm=res.value,
+                    history=hist[: min(hl.value, hist_cap)].copy(), history_len=hl.value)
+
+    def condition(self, A, pc=None, k=80, seed=42):
+        if pc is None:
+            pc = RefPC(self, "none", A, 1, 0, None)
+        out = np.zeros(3)
+        iout = np.zeros(2, np.int32)
+        self.lib.ref_condition(pc.handle, k, seed, out, iout)
+        return dict(lambda_min=out[0], lambda_max=out[1], kappa=out[2],
+                    lanczos_steps=int(iout[0]), valid=bool(iout[1]))
+
+    def spectral(self, A, pc=None, max_iter=200, tol=1e-6, seed=123):
+        if pc is None:
+            pc = RefPC(self, "none", A, 1, 0, None)
+        out = np.zeros(1)
+        iout = np.zeros(2, np.int32)
+        self.lib.ref_spectral(pc.handle, max_iter, tol, seed, out, iout)
+        return dict(spectral_radius=out[0], power_iters=int(iout[0]),
+                    convergence_ok=bool(iout[1]))
+
+    for f in (read_mm, conv_metrics, conv_write, bicgstab, condition, spectral):
+        setattr(cls, f.__name__, f)
+    return cls
+
+
+Reference = _ref_methods(Reference)
 
 
 class RefPC:

@@ -16,6 +16,11 @@
 #include "precond/ras.h"
 #include "precond/two_level_schwarz.h"
 #include "decomp/domain_decomp.h"
+#include "core/bicgstab.h"
+#include "io/matrix_market.h"
+#include "analysis/convergence_analysis.h"
+#include "analysis/condition_estimator.h"
+#include "analysis/spectral_analysis.h"
 
 #include <cstring>
 #include <exception>
@@ -215,6 +220,85 @@ int ref_fgmres(void* hp, const double* b, double* x, int restart, int max_iter, 
                int* iters, double* res, double* hist, int hist_cap, int* hist_len) {
     return run_solver(true, hp, b, x, restart, max_iter, tol, iters, res, hist, hist_cap,
                       hist_len);
+}
+
+// ---- I/O, the adjacent solver and the analysis tools on the same boundary
+int ref_read_mm(const char* path, int* nrows, int* ncols, int* nnz, int* rp, int* ci, double* v,
+                int cap) {
+    try {
+        CSRMatrix A = read_matrix_market(path);
+        *nrows = A.nrows;
+        *ncols = A.ncols;
+        *nnz = A.nnz();
+        if (rp) {
+            if (cap < A.nnz()) return -2;
+            std::memcpy(rp, A.row_ptr.data(), sizeof(int) * (A.nrows + 1));
+            std::memcpy(ci, A.col_idx.data(), sizeof(int) * A.nnz());
+            std::memcpy(v, A.vals.data(), sizeof(double) * A.nnz());
+        }
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// dout: initial, final, asymptotic rate; iout: iterations, stagnation start
+void ref_conv_metrics(const double* hist, int len, int conv, double* dout, int* iout,
+                      double* rates) {
+    std::vector<double> h(hist, hist + len);
+    ConvergenceMetrics m = analyze_convergence(h, conv != 0);
+    dout[0] = m.initial_residual;
+    dout[1] = m.final_residual;
+    dout[2] = m.asymptotic_rate;
+    iout[0] = m.iterations;
+    iout[1] = m.stagnation_start;
+    if (rates)
+        for (int i = 0; i < (int)m.rates.size(); ++i) rates[i] = m.rates[i];
+}
+
+void ref_conv_write(const char* path, const char* matrix, const char* precond, int nparts,
+                    int overlap, const double* hist, int len, int conv) {
+    std::vector<double> h(hist, hist + len);
+    analyze_convergence(h, conv != 0).write_jsonl(path, matrix, precond, nparts, overlap);
+}
+
+int ref_bicgstab(void* hp, const double* b, double* x, int max_iter, double tol, int* iters,
+                 double* res, double* hist, int hist_cap, int* hist_len) {
+    auto* h = static_cast<RefPC*>(hp);
+    int n = h->A.nrows;
+    std::vector<double> bb(b, b + n), xx(x, x + n);
+    GMRESParams p;
+    p.max_iter = max_iter;
+    p.tol = tol;
+    GMRESResult r = bicgstab(h->A, bb, xx, h->pc.get(), p);
+    std::memcpy(x, xx.data(), sizeof(double) * n);
+    *iters = r.iterations;
+    *res = r.residual_norm;
+    int nh = static_cast<int>(r.residual_history.size());
+    if (hist)
+        for (int i = 0; i < nh && i < hist_cap; ++i) hist[i] = r.residual_history[i];
+    if (hist_len) *hist_len = nh;
+    return r.converged ? 1 : 0;
+}
+
+// out: lambda_min, lambda_max, kappa; iout: Lanczos steps, valid
+void ref_condition(void* hp, int k, unsigned seed, double* out, int* iout) {
+    auto* h = static_cast<RefPC*>(hp);
+    ConditionEstimate e = estimate_condition(h->A, h->pc.get(), k, seed);
+    out[0] = e.lambda_min;
+    out[1] = e.lambda_max;
+    out[2] = e.kappa;
+    iout[0] = e.lanczos_steps;
+    iout[1] = e.valid ? 1 : 0;
+}
+
+// out: spectral radius; iout: power iterations, convergence_ok
+void ref_spectral(void* hp, int max_iter, double tol, unsigned seed, double* out, int* iout) {
+    auto* h = static_cast<RefPC*>(hp);
+    SpectralResult r = estimate_spectral_radius(h->A, h->pc.get(), max_iter, tol, seed);
+    out[0] = r.spectral_radius;
+    iout[0] = r.power_iters;
+    iout[1] = r.convergence_ok ? 1 : 0;
 }
 
 }  // extern "C"

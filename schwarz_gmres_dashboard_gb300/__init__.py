@@ -30,6 +30,7 @@ _clib = L.load()
 
 __all__ = [
     "SgError", "Context", "default_context", "CSRMatrix", "make_identity", "make_poisson_2d",
+    "read_matrix_market", "convergence_metrics", "write_convergence_jsonl",
     "make_poisson_3d", "make_varcoef_3d", "uniform", "partition_graph", "partition_boxes",
     "schwarz_structure", "dot", "norm2", "axpy", "scale",
     "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
@@ -280,6 +281,44 @@ def uniform(n: int, seed: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
     _check(_clib.sg_gen_uniform(C.c_uint64(seed), n, C.c_double(lo), C.c_double(hi),
                                out.ctypes.data))
     return out
+
+
+def read_matrix_market(path: str) -> CSRMatrix:
+    """read_matrix_market (src/io/matrix_market.h:14-92): the same reading
+    rules (symmetric mirrored, pattern read as 1.0, duplicates kept)."""
+    nr, nc, nz = C.c_int(0), C.c_int(0), C.c_int(0)
+    _check(_clib.sg_read_matrix_market(path.encode(), C.byref(nr), C.byref(nc), C.byref(nz),
+                                       None, None, None, 0))
+    rp = np.empty(nr.value + 1, np.int32)
+    ci = np.empty(max(nz.value, 1), np.int32)
+    v = np.empty(max(nz.value, 1), np.float64)
+    _check(_clib.sg_read_matrix_market(path.encode(), C.byref(nr), C.byref(nc), C.byref(nz),
+                                       rp.ctypes.data, ci.ctypes.data, v.ctypes.data, ci.size))
+    return CSRMatrix(nr.value, nc.value, rp, ci[: nz.value], v[: nz.value])
+
+
+def convergence_metrics(history, converged: bool) -> dict:
+    """ConvergenceMetrics (src/analysis/convergence_analysis.h:15-65) of a
+    residual history."""
+    h = np.ascontiguousarray(history, np.float64)
+    out = L.Convergence()
+    rates = np.zeros(max(h.size, 1))
+    _check(_clib.sg_convergence_metrics(h.ctypes.data, h.size, int(bool(converged)),
+                                        C.byref(out), rates.ctypes.data))
+    return dict(iterations=out.iterations, converged=bool(out.converged),
+                stagnation_start=out.stagnation_start, initial_residual=out.initial_residual,
+                final_residual=out.final_residual, asymptotic_rate=out.asymptotic_rate,
+                rates=rates[: h.size])
+
+
+def write_convergence_jsonl(path: str, matrix: str, precond: str, nparts: int, overlap: int,
+                            history, converged: bool) -> None:
+    """Appends the <output>.conv.jsonl record of the reference CLI
+    (src/analysis/convergence_analysis.h:69-93)."""
+    h = np.ascontiguousarray(history, np.float64)
+    _check(_clib.sg_write_convergence_jsonl(path.encode(), matrix.encode(), precond.encode(),
+                                            nparts, overlap, h.ctypes.data, h.size,
+                                            int(bool(converged))))
 
 
 def partition_graph(A: CSRMatrix, nparts: int) -> np.ndarray:

@@ -52,6 +52,12 @@ class BatchResult(C.Structure):
                 ("status", C.c_int), ("true_rel_residual", C.c_double)]
 
 
+class Convergence(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("stagnation_start", C.c_int),
+                ("reserved", C.c_int), ("initial_residual", C.c_double),
+                ("final_residual", C.c_double), ("asymptotic_rate", C.c_double)]
+
+
 class SolveResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("cycles", C.c_int), ("converged", C.c_int),
                 ("history_len", C.c_int), ("residual_norm", C.c_double),
@@ -92,6 +98,10 @@ PROTOTYPES = {
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "sg_precond_get_sweep": (C.c_int, [_vp, _ip, _ip]),
     "sg_precond_set_wait_test": (C.c_int, [_vp, C.c_int]),
+    "sg_read_matrix_market": (C.c_int, [C.c_char_p, _ip, _ip, _ip, _vp, _vp, _vp, C.c_int]),
+    "sg_convergence_metrics": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "sg_write_convergence_jsonl": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int,
+                                             C.c_int, _vp, C.c_int, C.c_int]),
     "sg_solve": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int,
                            C.POINTER(SolveParams), C.POINTER(SolveResult)]),
     "sg_solve_batched": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp, C.c_int,

@@ -69,62 +69,16 @@ static void usage() {
                  "  --output <file.jsonl>    Append metrics to JSONL file\n";
 }
 
-// Matrix Market reader with the semantics of src/io/matrix_market.h:14-92
-// (symmetric entries mirrored, pattern files read as 1.0, entries sorted by
-// row then column, duplicates kept).
-static CSRMatrix read_matrix_market(const std::string& filename) {
-    std::ifstream in(filename);
-    if (!in.is_open()) throw std::runtime_error("Cannot open file: " + filename);
-    std::string line;
-    bool symmetric = false, pattern = false;
-    while (std::getline(in, line)) {
-        if (!line.empty() && line[0] == '%') {
-            if (line.find("symmetric") != std::string::npos) symmetric = true;
-            if (line.find("pattern") != std::string::npos) pattern = true;
-            continue;
-        }
-        break;
-    }
+// Matrix Market input: the library's reader (sg_read_matrix_market), which
+// follows the reference reader's rules (src/io/matrix_market.h:14-92).
+static CSRMatrix read_matrix_market(const std::string& path) {
     int nrows = 0, ncols = 0, nnz = 0;
-    {
-        std::istringstream iss(line);
-        iss >> nrows >> ncols >> nnz;
-    }
-    struct T {
-        int r, c;
-        double v;
-    };
-    std::vector<T> e;
-    e.reserve(symmetric ? 2 * (size_t)nnz : (size_t)nnz);
-    for (int k = 0; k < nnz; ++k) {
-        if (!std::getline(in, line)) throw std::runtime_error("Premature end of file");
-        std::istringstream iss(line);
-        int r, c;
-        double v = 1.0;
-        iss >> r >> c;
-        if (!pattern) iss >> v;
-        --r;
-        --c;
-        e.push_back({r, c, v});
-        if (symmetric && r != c) e.push_back({c, r, v});
-    }
-    std::sort(e.begin(), e.end(), [](const T& a, const T& b) {
-        return a.r < b.r || (a.r == b.r && a.c < b.c);
-    });
+    detail::check(sg_read_matrix_market(path.c_str(), &nrows, &ncols, &nnz, nullptr, nullptr,
+                                        nullptr, 0));
     CSRMatrix A;
-    A.nrows = nrows;
-    A.ncols = ncols;
-    A.row_ptr.assign(nrows + 1, 0);
-    A.col_idx.resize(e.size());
-    A.vals.resize(e.size());
-    for (auto& t : e) A.row_ptr[t.r + 1]++;
-    for (int i = 0; i < nrows; ++i) A.row_ptr[i + 1] += A.row_ptr[i];
-    std::vector<int> pos(A.row_ptr.begin(), A.row_ptr.end());
-    for (auto& t : e) {
-        const int p = pos[t.r]++;
-        A.col_idx[p] = t.c;
-        A.vals[p] = t.v;
-    }
+    A.resize(nrows, ncols, nnz);
+    detail::check(sg_read_matrix_market(path.c_str(), &nrows, &ncols, &nnz, A.row_ptr.data(),
+                                        A.col_idx.data(), A.vals.data(), nnz));
     return A;
 }
 
