@@ -194,7 +194,12 @@ sg_status sg_precond_set_wait_test(sg_precond* pc, int mode);
 /* ---- solvers ---------------------------------------------------------- */
 typedef enum sg_solver {
     SG_GMRES = 0, /* left preconditioned, src/core/gmres.cpp:34-160 */
-    SG_FGMRES = 1 /* right preconditioned storing V and Z, src/core/fgmres.cpp:28-144 */
+    SG_FGMRES = 1, /* right preconditioned storing V and Z, src/core/fgmres.cpp:28-144 */
+    /* right preconditioned BiCGSTAB, src/core/bicgstab.h:57-204 (FP64; restart
+     * is unused; SG_TOL_REF_ABS is the reference rule ||r|| < tol ||r0|| on the
+     * recursive residual; the true-residual kinds restart from the current x
+     * while ||b - A x|| / ||b|| > tol and iterations remain) */
+    SG_BICGSTAB = 2
 } sg_solver;
 
 typedef enum sg_tol_kind {
@@ -271,6 +276,34 @@ sg_status sg_solve_batched(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsy
                            const int* sys_row_ptr, int nrhs, const double* b, double* x,
                            sg_mem mem, const sg_solve_params* params, sg_batch_result* results,
                            double* time_s);
+
+/* ---- analysis (the reference CLI's --analyze, src/main.cpp:213-224) ---- */
+/* ConditionEstimate (src/analysis/condition_estimator.h:32-38). */
+typedef struct sg_condition_estimate {
+    double lambda_min;
+    double lambda_max;
+    double kappa;      /* lambda_max / lambda_min (1e30 when |lambda_min| <= 1e-14) */
+    int lanczos_steps; /* 0: no estimate */
+    int valid;         /* lambda_min > 0 (meaningful for an SPD operator) */
+} sg_condition_estimate;
+/* estimate_condition (condition_estimator.h:94-191): k Lanczos steps on
+ * M^{-1}A (A when pc is NULL) from the reference's seeded start vector, the
+ * extreme eigenvalues of the tridiagonal.  k <= 1024. */
+sg_status sg_estimate_condition(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int k,
+                                unsigned seed, sg_condition_estimate* out);
+/* SpectralResult (src/analysis/spectral_analysis.h:21-27). */
+typedef struct sg_spectral_result {
+    double spectral_radius; /* rho(I - M^{-1}A) */
+    int power_iters;
+    int convergence_ok;     /* rho < 1 */
+} sg_spectral_result;
+/* estimate_spectral_radius (spectral_analysis.h:30-97): power iteration on
+ * I - M^{-1}A until the Rayleigh quotient changes by less than
+ * tol (1 + |mu|); eigenvector (optional host array [n]) receives the last
+ * normalised iterate. */
+sg_status sg_estimate_spectral_radius(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int max_iter,
+                                      double tol, unsigned seed, double* eigenvector,
+                                      sg_spectral_result* out);
 
 /* ---- BLAS-1 (src/core/vector.h:11-44) --------------------------------- */
 /* dot (vector.h:11-16), FP64, deterministic order (block partial sums added

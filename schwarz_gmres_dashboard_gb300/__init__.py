@@ -30,7 +30,8 @@ _clib = L.load()
 
 __all__ = [
     "SgError", "Context", "default_context", "CSRMatrix", "make_identity", "make_poisson_2d",
-    "read_matrix_market", "convergence_metrics", "write_convergence_jsonl",
+    "read_matrix_market", "convergence_metrics", "write_convergence_jsonl", "bicgstab",
+    "estimate_condition", "estimate_spectral_radius",
     "make_poisson_3d", "make_varcoef_3d", "uniform", "partition_graph", "partition_boxes",
     "schwarz_structure", "dot", "norm2", "axpy", "scale",
     "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
@@ -654,6 +655,46 @@ def fgmres(A: CSRMatrix, b, x, M: Optional[Preconditioner] = None,
            params: Optional[GMRESParams] = None) -> GMRESResult:
     """FGMRES(m), right preconditioning (src/core/fgmres.h:42-47)."""
     return _solve(L.FGMRES, A, b, x, M, params)
+
+
+def bicgstab(A: CSRMatrix, b, x, M: Optional[Preconditioner] = None,
+             params: Optional[GMRESParams] = None) -> GMRESResult:
+    """BiCGSTAB, right preconditioning (src/core/bicgstab.h:57-204), FP64.
+    params.restart is unused; the reference rule (TOL_REF_ABS) stops on
+    ||r|| < tol ||r0||."""
+    return _solve(L.BICGSTAB, A, b, x, M, params)
+
+
+def estimate_condition(A: CSRMatrix, M: Optional[Preconditioner] = None, k: int = 80,
+                       seed: int = 42) -> dict:
+    """estimate_condition (src/analysis/condition_estimator.h:94-191): k
+    Lanczos steps on M^{-1}A on the GPU; extreme Ritz values and kappa."""
+    ctx = M.ctx if M is not None else default_context()
+    out = L.ConditionEstimate()
+    _check(_clib.sg_estimate_condition(ctx.handle, A.device(ctx),
+                                       M.handle if M is not None else None, k, seed,
+                                       C.byref(out)))
+    return dict(lambda_min=out.lambda_min, lambda_max=out.lambda_max, kappa=out.kappa,
+                lanczos_steps=out.lanczos_steps, valid=bool(out.valid))
+
+
+def estimate_spectral_radius(A: CSRMatrix, M: Optional[Preconditioner] = None,
+                             max_iter: int = 200, tol: float = 1e-6, seed: int = 123,
+                             eigenvector: bool = False) -> dict:
+    """estimate_spectral_radius (src/analysis/spectral_analysis.h:30-97):
+    power iteration on I - M^{-1}A on the GPU."""
+    ctx = M.ctx if M is not None else default_context()
+    out = L.SpectralResult()
+    ev = np.zeros(A.nrows) if eigenvector else None
+    _check(_clib.sg_estimate_spectral_radius(ctx.handle, A.device(ctx),
+                                             M.handle if M is not None else None, max_iter,
+                                             tol, seed, ev.ctypes.data if ev is not None else None,
+                                             C.byref(out)))
+    res = dict(spectral_radius=out.spectral_radius, power_iters=out.power_iters,
+               convergence_ok=bool(out.convergence_ok))
+    if ev is not None:
+        res["eigenvector"] = ev
+    return res
 
 
 from .learned import LearnedCorrection, collect_pairs  # noqa: E402  (uses the names above)

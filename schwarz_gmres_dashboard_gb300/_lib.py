@@ -19,7 +19,7 @@ STATUS = {0: "SG_OK", 1: "SG_ERR_INVALID_ARG", 2: "SG_ERR_CUDA", 3: "SG_ERR_OOM"
 
 MEM_HOST, MEM_DEVICE = 0, 1
 FP64, FP32, BF16 = 0, 1, 2
-GMRES, FGMRES = 0, 1
+GMRES, FGMRES, BICGSTAB = 0, 1, 2
 TOL_REF_ABS, TOL_TRUE_REL_CYCLE, TOL_TRUE_REL = 0, 1, 2
 PC_KINDS = {"none": 0, "jacobi": 1, "ilu0": 2, "asm": 3, "ras": 4,
             "twolevel_asm": 5, "twolevel_ras": 6}
@@ -56,6 +56,16 @@ class Convergence(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("stagnation_start", C.c_int),
                 ("reserved", C.c_int), ("initial_residual", C.c_double),
                 ("final_residual", C.c_double), ("asymptotic_rate", C.c_double)]
+
+
+class ConditionEstimate(C.Structure):
+    _fields_ = [("lambda_min", C.c_double), ("lambda_max", C.c_double), ("kappa", C.c_double),
+                ("lanczos_steps", C.c_int), ("valid", C.c_int)]
+
+
+class SpectralResult(C.Structure):
+    _fields_ = [("spectral_radius", C.c_double), ("power_iters", C.c_int),
+                ("convergence_ok", C.c_int)]
 
 
 class SolveResult(C.Structure):
@@ -98,6 +108,10 @@ PROTOTYPES = {
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "sg_precond_get_sweep": (C.c_int, [_vp, _ip, _ip]),
     "sg_precond_set_wait_test": (C.c_int, [_vp, C.c_int]),
+    "sg_estimate_condition": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_uint,
+                                        C.POINTER(ConditionEstimate)]),
+    "sg_estimate_spectral_radius": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_double, C.c_uint, _vp,
+                                              C.POINTER(SpectralResult)]),
     "sg_read_matrix_market": (C.c_int, [C.c_char_p, _ip, _ip, _ip, _vp, _vp, _vp, C.c_int]),
     "sg_convergence_metrics": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "sg_write_convergence_jsonl": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int,

@@ -684,7 +684,8 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
         SG_CHECK_ARG(A->ctx == ctx, "matrix belongs to a different context");
         SG_CHECK_ARG(A->nrows == A->ncols, "the solvers need a square matrix");
         SG_CHECK_ARG(n == A->nrows, "n (%d) != matrix rows (%d)", n, A->nrows);
-        SG_CHECK_ARG(solver == SG_GMRES || solver == SG_FGMRES, "unknown solver %d", (int)solver);
+        SG_CHECK_ARG(solver == SG_GMRES || solver == SG_FGMRES || solver == SG_BICGSTAB,
+                     "unknown solver %d", (int)solver);
         if (pc) {
             SG_CHECK_ARG(pc->ctx == ctx, "preconditioner belongs to a different context");
             if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
@@ -726,7 +727,8 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
                 }
             }
         } cb{ctx, x, dx, n, mem == SG_MEM_HOST};
-        solve_device(ctx, solver, A, pc, db, dx, prm, result);
+        if (solver == SG_BICGSTAB) solve_bicgstab_device(ctx, A, pc, db, dx, prm, result);
+        else solve_device(ctx, solver, A, pc, db, dx, prm, result);
     });
 }
 
@@ -785,6 +787,41 @@ void check_vec_args(sg_ctx* ctx, int n, sg_mem mem) {
     SG_CHECK_ARG(mem == SG_MEM_HOST || mem == SG_MEM_DEVICE, "bad memory kind");
 }
 }  // namespace
+
+// ------------------------------------------------------------------ analysis
+namespace {
+void check_analysis_args(sg_ctx* ctx, const sg_csr* A, sg_precond* pc) {
+    SG_CHECK_ARG(ctx && A, "NULL argument");
+    SG_CHECK_ARG(A->ctx == ctx, "matrix belongs to a different context");
+    SG_CHECK_ARG(A->nrows == A->ncols, "the analysis needs a square matrix");
+    if (pc) {
+        SG_CHECK_ARG(pc->ctx == ctx, "preconditioner belongs to a different context");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        SG_CHECK_ARG(pc->n == A->nrows, "preconditioner was set up for n=%d", pc->n);
+    }
+}
+}  // namespace
+
+sg_status sg_estimate_condition(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int k,
+                                unsigned seed, sg_condition_estimate* out) {
+    return guard([&] {
+        check_analysis_args(ctx, A, pc);
+        SG_CHECK_ARG(out, "NULL argument");
+        use_device(ctx);
+        estimate_condition_device(ctx, A, pc, k, seed, out);
+    });
+}
+
+sg_status sg_estimate_spectral_radius(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int max_iter,
+                                      double tol, unsigned seed, double* eigenvector,
+                                      sg_spectral_result* out) {
+    return guard([&] {
+        check_analysis_args(ctx, A, pc);
+        SG_CHECK_ARG(out, "NULL argument");
+        use_device(ctx);
+        estimate_spectral_device(ctx, A, pc, max_iter, tol, seed, eigenvector, out);
+    });
+}
 
 sg_status sg_dot(sg_ctx* ctx, const double* x, const double* y, int n, sg_mem mem,
                  double* result) {

@@ -57,6 +57,19 @@ void launch_dot_scratch(cudaStream_t stream, const double* x, const double* y, i
 // cycle bookkeeping after the update: cycles++, out-of-iterations test
 void launch_cycle_end(sg_ctx* ctx, SolveState* st);
 
+// ---------------------------------------------------------------- bicgstab.cu
+// BiCGSTAB (src/core/bicgstab.h:57-204) on device vectors b, x (x0 on entry)
+void solve_bicgstab_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b,
+                           double* x, const sg_solve_params& prm, sg_solve_result* res);
+// ---------------------------------------------------------------- analysis.cu
+// Lanczos estimate of the extreme eigenvalues of M^{-1}A and power iteration
+// on I - M^{-1}A (src/analysis/condition_estimator.h, spectral_analysis.h)
+void estimate_condition_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int k,
+                               unsigned seed, sg_condition_estimate* out);
+void estimate_spectral_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int max_iter,
+                              double tol, unsigned seed, double* eigvec_host,
+                              sg_spectral_result* out);
+
 // ---------------------------------------------------------------- schwarz.cu
 void precond_setup_device(sg_precond* pc, const sg_csr* A);
 // exact: FP64 sweeps round each product and difference (reference bits);
