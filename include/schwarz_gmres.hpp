@@ -10,14 +10,29 @@
 //   TwoLevelSchwarzPrecond    src/precond/two_level_schwarz.h:21-75
 //   GMRESParams/GMRESResult   src/core/gmres.h:12-24
 //   gmres / fgmres            src/core/gmres.h:28-33, src/core/fgmres.h:42-47
+//   FlexApply / fgmres_flex   src/core/fgmres.h:37, :50-55
+//   bicgstab                  src/core/bicgstab.h:57-204
 //   make_poisson_2d/3d        src/mesh/poisson.h:10-74
+//   read_matrix_market        src/io/matrix_market.h:14-92
+//   ConvergenceMetrics /      src/analysis/convergence_analysis.h:15-123
+//     analyze_convergence
+//   ConditionEstimate /       src/analysis/condition_estimator.h:32-191
+//     estimate_condition
+//   SpectralResult /          src/analysis/spectral_analysis.h:21-97
+//     estimate_spectral_radius
 //
 // Errors surface as std::runtime_error, as in the reference.  Extra knobs
 // (partition vector, factor/sweep dtypes, precision, stopping rule) are
-// optional members with the reference's behaviour as default.  Only the GPU
-// preconditioners of this header can be passed to gmres()/fgmres().
+// optional members with the reference's behaviour as default.  The GPU
+// preconditioners of this header run on the device; any other
+// Preconditioner subclass (and fgmres_flex's FlexApply) is called on the
+// host through sg_precond_create_host, in stream order inside the solve --
+// its apply must not call CUDA.
 #pragma once
 
+#include <cstdio>
+#include <functional>
+#include <iostream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -260,11 +275,35 @@ struct GMRESParams {
 };
 
 namespace detail {
-inline GMRESResult solve(sg_solver solver, const CSRMatrix& A, const std::vector<double>& b,
-                         std::vector<double>& x, const Preconditioner* M, const GMRESParams& p) {
-    const auto* dm = dynamic_cast<const DevicePreconditioner*>(M);
-    if (M && !dm)
-        throw std::runtime_error("only the GPU preconditioners of schwarz_gmres.hpp can be used");
+// Any host-side apply (a foreign Preconditioner, a FlexApply) as a host
+// preconditioner of the library.  The C callback catches exceptions and
+// reports them through the status; solve() rethrows the message.
+struct HostApply {
+    std::function<void(const double*, double*, int)> fn;
+    std::string error;
+    static int call(void* user, const double* x, double* y, int n) {
+        auto* h = static_cast<HostApply*>(user);
+        try {
+            h->fn(x, y, n);
+            return 0;
+        } catch (const std::exception& e) {
+            h->error = e.what();
+        } catch (...) {
+            h->error = "unknown exception";
+        }
+        return 1;
+    }
+};
+struct PrecondHandle {
+    sg_precond* h = nullptr;
+    ~PrecondHandle() {
+        if (h) sg_precond_destroy(h);
+    }
+};
+
+inline GMRESResult solve_with(sg_solver solver, const CSRMatrix& A, const std::vector<double>& b,
+                              std::vector<double>& x, const DevicePreconditioner* dm,
+                              HostApply* host, const GMRESParams& p) {
     if (static_cast<int>(b.size()) != A.nrows) throw std::runtime_error("b has the wrong size");
     x.resize(A.nrows, 0.0);
     std::shared_ptr<CsrHandle> dA;
@@ -272,6 +311,12 @@ inline GMRESResult solve(sg_solver solver, const CSRMatrix& A, const std::vector
     if (!hA) {
         dA = A.device();
         hA = dA->h;
+    }
+    PrecondHandle hp;
+    sg_precond* pc = dm ? dm->handle() : nullptr;
+    if (host) {
+        check(sg_precond_create_host(context(), &HostApply::call, host, A.nrows, &hp.h));
+        pc = hp.h;
     }
     std::vector<double> hist(static_cast<size_t>(p.max_iter) + p.restart + 1);
     sg_solve_params prm{};
@@ -284,8 +329,11 @@ inline GMRESResult solve(sg_solver solver, const CSRMatrix& A, const std::vector
     prm.history = hist.data();
     prm.history_cap = static_cast<int>(hist.size());
     sg_solve_result r{};
-    check(sg_solve(context(), solver, hA, dm ? dm->handle() : nullptr, b.data(), x.data(),
-                   A.nrows, SG_MEM_HOST, &prm, &r));
+    const sg_status st = sg_solve(context(), solver, hA, pc, b.data(), x.data(), A.nrows,
+                                  SG_MEM_HOST, &prm, &r);
+    if (st == SG_ERR_CALLBACK && host && !host->error.empty())
+        throw std::runtime_error(host->error);  // what the apply threw
+    check(st);
     GMRESResult out;
     out.iterations = r.iterations;
     out.residual_norm = r.residual_norm;
@@ -296,6 +344,17 @@ inline GMRESResult solve(sg_solver solver, const CSRMatrix& A, const std::vector
     const int h = r.history_len < prm.history_cap ? r.history_len : prm.history_cap;
     out.residual_history.assign(hist.begin(), hist.begin() + h);
     return out;
+}
+
+inline GMRESResult solve(sg_solver solver, const CSRMatrix& A, const std::vector<double>& b,
+                         std::vector<double>& x, const Preconditioner* M, const GMRESParams& p) {
+    const auto* dm = dynamic_cast<const DevicePreconditioner*>(M);
+    if (M && !dm) {
+        // a Preconditioner plugin of the caller's own: applied on the host
+        HostApply host{[M](const double* in, double* out, int n) { M->apply(in, out, n); }, {}};
+        return solve_with(solver, A, b, x, nullptr, &host, p);
+    }
+    return solve_with(solver, A, b, x, dm, nullptr, p);
 }
 }  // namespace detail
 
@@ -308,6 +367,182 @@ inline GMRESResult fgmres(const CSRMatrix& A, const std::vector<double>& b,
                           std::vector<double>& x, const Preconditioner* M,
                           const GMRESParams& params = {}) {
     return detail::solve(SG_FGMRES, A, b, x, M, params);
+}
+
+// FGMRES with an arbitrary (possibly nonlinear) apply z = M(v), as
+// fgmres_flex (src/core/fgmres.h:37, :50-55); an empty FlexApply is the
+// identity.  The apply runs on the host, on the normalised basis vector.
+using FlexApply = std::function<void(const double* x, double* y, int n)>;
+inline GMRESResult fgmres_flex(const CSRMatrix& A, const std::vector<double>& b,
+                               std::vector<double>& x, FlexApply apply,
+                               const GMRESParams& params = {}) {
+    if (!apply) return detail::solve(SG_FGMRES, A, b, x, nullptr, params);
+    detail::HostApply host{std::move(apply), {}};
+    return detail::solve_with(SG_FGMRES, A, b, x, nullptr, &host, params);
+}
+
+// BiCGSTAB, right preconditioned (src/core/bicgstab.h:57-204), FP64.
+inline GMRESResult bicgstab(const CSRMatrix& A, const std::vector<double>& b,
+                            std::vector<double>& x, const Preconditioner* M,
+                            const GMRESParams& params = {}) {
+    return detail::solve(SG_BICGSTAB, A, b, x, M, params);
+}
+
+// ------------------------------------------------------------------ analysis
+struct ConditionEstimate {
+    double lambda_min = 0.0;
+    double lambda_max = 0.0;
+    double kappa = 0.0;
+    int lanczos_steps = 0;
+    bool valid = false;
+};
+
+struct SpectralResult {
+    double spectral_radius = 0.0;
+    bool convergence_ok = false;
+    int power_iters = 0;
+    std::vector<double> eigenvector;
+};
+
+namespace detail {
+// runs f(ctx, device matrix, device-or-host preconditioner)
+template <class F>
+void with_operator(const CSRMatrix& A, const Preconditioner* M, F&& f) {
+    const auto* dm = dynamic_cast<const DevicePreconditioner*>(M);
+    std::shared_ptr<CsrHandle> dA;
+    const sg_csr* hA = dm ? dm->matrix() : nullptr;
+    if (!hA) {
+        dA = A.device();
+        hA = dA->h;
+    }
+    PrecondHandle hp;
+    HostApply host{[M](const double* in, double* out, int n) { M->apply(in, out, n); }, {}};
+    sg_precond* pc = dm ? dm->handle() : nullptr;
+    if (M && !dm) {
+        check(sg_precond_create_host(context(), &HostApply::call, &host, A.nrows, &hp.h));
+        pc = hp.h;
+    }
+    const sg_status st = f(context(), hA, pc);
+    if (st == SG_ERR_CALLBACK && !host.error.empty()) throw std::runtime_error(host.error);
+    check(st);
+}
+}  // namespace detail
+
+// estimate_condition (src/analysis/condition_estimator.h:94-191): k Lanczos
+// steps on M^{-1}A (A when M is null) on the GPU.
+inline ConditionEstimate estimate_condition(const CSRMatrix& A, const Preconditioner* M,
+                                            int k = 80, unsigned int seed = 42) {
+    sg_condition_estimate e{};
+    detail::with_operator(A, M, [&](sg_ctx* c, const sg_csr* hA, sg_precond* pc) {
+        return sg_estimate_condition(c, hA, pc, k, seed, &e);
+    });
+    ConditionEstimate out;
+    out.lambda_min = e.lambda_min;
+    out.lambda_max = e.lambda_max;
+    out.kappa = e.kappa;
+    out.lanczos_steps = e.lanczos_steps;
+    out.valid = e.valid != 0;
+    return out;
+}
+
+// estimate_spectral_radius (src/analysis/spectral_analysis.h:30-97).
+inline SpectralResult estimate_spectral_radius(const CSRMatrix& A, const Preconditioner* M,
+                                               int max_iter = 200, double tol = 1e-6,
+                                               unsigned int seed = 123) {
+    sg_spectral_result r{};
+    SpectralResult out;
+    out.eigenvector.resize(A.nrows);
+    detail::with_operator(A, M, [&](sg_ctx* c, const sg_csr* hA, sg_precond* pc) {
+        return sg_estimate_spectral_radius(c, hA, pc, max_iter, tol, seed, out.eigenvector.data(),
+                                           &r);
+    });
+    out.spectral_radius = r.spectral_radius;
+    out.convergence_ok = r.convergence_ok != 0;
+    out.power_iters = r.power_iters;
+    return out;
+}
+
+inline void print_condition_estimate(const ConditionEstimate& e, const std::string& label = "") {
+    std::cout << "  Condition estimate" << (label.empty() ? "" : " (" + label + ")")
+              << " [Lanczos " << e.lanczos_steps << " steps]:\n";
+    if (!e.valid || e.lambda_min <= 0.0)
+        std::cout << "    Ritz(min) = " << e.lambda_min << "\n    Ritz(max) = " << e.lambda_max
+                  << "\n    kappa_est = " << e.kappa
+                  << "\n    (Note: M^{-1}A is non-symmetric; bounds are approximate)\n";
+    else
+        std::cout << "    lambda_min = " << e.lambda_min << "\n    lambda_max = " << e.lambda_max
+                  << "\n    kappa      = " << e.kappa << "\n";
+}
+
+inline void print_spectral_result(const SpectralResult& r, const std::string& label = "") {
+    std::cout << "  Spectral radius" << (label.empty() ? "" : " (" + label + ")")
+              << " [power iter " << r.power_iters << " steps]:\n"
+              << "    rho(I - M^{-1}A) = " << r.spectral_radius << "\n"
+              << "    Convergence cond : "
+              << (r.convergence_ok ? "SATISFIED (rho < 1)" : "VIOLATED (rho >= 1)") << "\n";
+}
+
+// ConvergenceMetrics / analyze_convergence (src/analysis/
+// convergence_analysis.h:15-123), computed by the library.
+struct ConvergenceMetrics {
+    std::vector<double> residuals;
+    std::vector<double> rates;
+    double initial_residual = 0.0;
+    double final_residual = 0.0;
+    double asymptotic_rate = 0.0;
+    int stagnation_start = -1;
+    bool converged = false;
+    int iterations = 0;
+
+    void compute(const std::vector<double>& history, bool conv) {
+        residuals = history;
+        rates.assign(history.size(), 0.0);
+        sg_convergence m{};
+        detail::check(sg_convergence_metrics(history.data(), static_cast<int>(history.size()),
+                                             conv ? 1 : 0, &m, rates.data()));
+        initial_residual = m.initial_residual;
+        final_residual = m.final_residual;
+        asymptotic_rate = m.asymptotic_rate;
+        stagnation_start = m.stagnation_start;
+        converged = m.converged != 0;
+        iterations = m.iterations;
+    }
+    // appends the <output>.conv.jsonl record
+    void write_jsonl(const std::string& path, const std::string& matrix,
+                     const std::string& precond, int nparts, int overlap) const {
+        detail::check(sg_write_convergence_jsonl(path.c_str(), matrix.c_str(), precond.c_str(),
+                                                 nparts, overlap, residuals.data(),
+                                                 static_cast<int>(residuals.size()),
+                                                 converged ? 1 : 0));
+    }
+    void print_summary() const {
+        std::cout << "  Convergence analysis:\n"
+                  << "    Initial residual : " << initial_residual << "\n"
+                  << "    Final residual   : " << final_residual << "\n"
+                  << "    Asymptotic rate  : " << asymptotic_rate << "\n";
+        if (stagnation_start >= 0)
+            std::cout << "    *** Stagnation detected at iter " << stagnation_start << " ***\n";
+        else
+            std::cout << "    No stagnation detected\n";
+    }
+};
+
+inline ConvergenceMetrics analyze_convergence(const std::vector<double>& history, bool converged) {
+    ConvergenceMetrics m;
+    m.compute(history, converged);
+    return m;
+}
+
+// read_matrix_market (src/io/matrix_market.h:14-92), the library's reader
+inline CSRMatrix read_matrix_market(const std::string& filename) {
+    int nr = 0, nc = 0, nz = 0;
+    detail::check(sg_read_matrix_market(filename.c_str(), &nr, &nc, &nz, nullptr, nullptr,
+                                        nullptr, 0));
+    CSRMatrix A;
+    A.resize(nr, nc, nz);
+    detail::check(sg_read_matrix_market(filename.c_str(), &nr, &nc, &nz, A.row_ptr.data(),
+                                        A.col_idx.data(), A.vals.data(), nz));
+    return A;
 }
 
 }  // namespace schwarz

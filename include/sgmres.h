@@ -40,7 +40,8 @@ typedef enum sg_status {
     SG_ERR_NONFINITE = 6,   /* NaN/Inf in the right-hand side or the iteration */
     SG_ERR_DEVICE_TIMEOUT = 7, /* a bounded device wait gave up */
     SG_ERR_UNSUPPORTED = 8, /* option combination not provided */
-    SG_ERR_INTERNAL = 9
+    SG_ERR_INTERNAL = 9,
+    SG_ERR_CALLBACK = 10    /* a host preconditioner function returned nonzero */
 } sg_status;
 
 typedef enum sg_mem { SG_MEM_HOST = 0, SG_MEM_DEVICE = 1 } sg_mem;
@@ -53,7 +54,8 @@ typedef enum sg_precond_kind {
     SG_PC_ASM = 3,          /* src/precond/asm.h:13-71 */
     SG_PC_RAS = 4,          /* src/precond/ras.h:16-82 */
     SG_PC_TWOLEVEL_ASM = 5, /* src/precond/two_level_schwarz.h:23-75, FineLevelType::ASM */
-    SG_PC_TWOLEVEL_RAS = 6  /* src/precond/two_level_schwarz.h:23-75, FineLevelType::RAS */
+    SG_PC_TWOLEVEL_RAS = 6, /* src/precond/two_level_schwarz.h:23-75, FineLevelType::RAS */
+    SG_PC_HOST = 7          /* a caller's host function (sg_precond_create_host only) */
 } sg_precond_kind;
 
 /* Arithmetic / storage types. */
@@ -178,6 +180,23 @@ sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc);
  * *threads the threads per CTA of the TMA-fed sweep (0 otherwise).  Either
  * pointer may be NULL. */
 sg_status sg_precond_get_sweep(sg_precond* pc, int* sweep, int* threads);
+
+/* A preconditioner that is a caller's host function: FGMRES's flexible apply
+ * (FlexApply / fgmres_flex, src/core/fgmres.h:37, src/core/fgmres.cpp:164-172)
+ * and any Preconditioner plugin that is not one of the GPU kinds
+ * (src/precond/preconditioner.h:7-20).  fn(user, x, y, n) must write all of
+ * y = M^{-1} x (host arrays of n doubles) and return 0, or nonzero to report
+ * an error (the call then returns SG_ERR_CALLBACK).  Inside sg_solve the
+ * function runs in stream order on a CUDA host-function thread (between a
+ * device-to-host and a host-to-device copy of pinned buffers, so a restart
+ * cycle with it still runs without host synchronisation and may be replayed
+ * as a CUDA graph): it must not call CUDA itself.  FGMRES applies it to the
+ * normalised basis vector, as the reference does.  The object is set up on
+ * creation (n rows) and is used with SG_GMRES, SG_FGMRES, SG_BICGSTAB,
+ * sg_precond_apply and the analysis calls; the batched solver rejects it. */
+typedef int (*sg_host_apply_fn)(void* user, const double* x, double* y, int n);
+sg_status sg_precond_create_host(sg_ctx* ctx, sg_host_apply_fn fn, void* user, int n,
+                                 sg_precond** out);
 
 /* Test hook of the bounded device waits (no counterpart in the reference).
  * mode 1: the TMA-fed sweep copies no subdomain's first level-record group,

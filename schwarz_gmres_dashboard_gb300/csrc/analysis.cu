@@ -270,6 +270,8 @@ void estimate_condition_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int
     SG_CUDA(cudaStreamSynchronize(stream));
     if (pc && sweep_error(pc))
         fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+    if (pc && host_precond_status(pc))
+        fail(SG_ERR_CALLBACK, "the host preconditioner function reported an error");
     const int m = h.steps;
     if (m < 2 || h.nonfinite) return;
     std::vector<double> d(h.alpha, h.alpha + m), e((size_t)m, 0.0);
@@ -336,6 +338,8 @@ void estimate_spectral_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int 
     SG_CUDA(cudaStreamSynchronize(stream));
     if (pc && sweep_error(pc))
         fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+    if (pc && host_precond_status(pc))
+        fail(SG_ERR_CALLBACK, "the host preconditioner function reported an error");
     out->spectral_radius = std::fabs(h.mu_prev);
     out->power_iters = h.steps;
     out->convergence_ok = out->spectral_radius < 1.0 ? 1 : 0;

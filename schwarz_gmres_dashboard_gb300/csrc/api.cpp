@@ -179,6 +179,7 @@ const char* sg_status_string(sg_status st) {
     case SG_ERR_DEVICE_TIMEOUT: return "device wait timed out";
     case SG_ERR_UNSUPPORTED: return "unsupported";
     case SG_ERR_INTERNAL: return "internal error";
+    case SG_ERR_CALLBACK: return "host callback error";
     }
     return "unknown status";
 }
@@ -502,6 +503,12 @@ sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
         SG_CHECK_ARG(pc && A, "NULL argument");
         SG_CHECK_ARG(A->ctx == pc->ctx, "matrix and preconditioner belong to different contexts");
         use_device(pc->ctx);
+        if (pc->kind == SG_PC_HOST) {
+            // a host function is set up by its owner; only the size must agree
+            SG_CHECK_ARG(A->nrows == pc->n, "the host preconditioner has %d rows, A %d", pc->n,
+                         A->nrows);
+            return;
+        }
         pc->is_setup = false;
         pc->gen = next_object_gen();
         pc->n = A->nrows;
@@ -553,6 +560,11 @@ sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg
         if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
         SG_CHECK_ARG(n == pc->n, "n (%d) does not match the set-up size (%d)", n, pc->n);
         sg_ctx* ctx = pc->ctx;
+        if (pc->kind == SG_PC_HOST && mem == SG_MEM_HOST) {
+            const int st = pc->host_fn(pc->host_user, x, y, n);
+            if (st) fail(SG_ERR_CALLBACK, "the host preconditioner function returned %d", st);
+            return;
+        }
         use_device(ctx);
         const double* dx = x;
         double* dy = y;
@@ -569,6 +581,28 @@ sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
         if (sweep_error(pc))
             fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+        if (const int hst = host_precond_status(pc))
+            fail(SG_ERR_CALLBACK, "the host preconditioner function returned %d", hst);
+    });
+}
+
+sg_status sg_precond_create_host(sg_ctx* ctx, sg_host_apply_fn fn, void* user, int n,
+                                 sg_precond** out) {
+    return guard([&] {
+        SG_CHECK_ARG(ctx && fn && out, "NULL argument");
+        SG_CHECK_ARG(n >= 1, "n must be >= 1");
+        *out = nullptr;
+        use_device(ctx);
+        auto* pc = new sg_precond();
+        try {
+            pc->gen = next_object_gen();
+            pc->ctx = ctx;
+            host_precond_init(pc, fn, user, n);
+        } catch (...) {
+            delete pc;
+            throw;
+        }
+        *out = pc;
     });
 }
 
@@ -751,6 +785,7 @@ sg_status sg_solve_batched(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsy
             if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
             SG_CHECK_ARG(pc->n == A->nrows, "preconditioner was set up for n=%d", pc->n);
             SG_CHECK_ARG(!pc->learned, "the batched solver takes no learned stage");
+            SG_CHECK_ARG(pc->kind != SG_PC_HOST, "the batched solver takes no host preconditioner");
         }
         // block-diagonal matrix and system-local subdomains: checked in
         // solve_batched_device (once per matrix / preconditioner set-up)

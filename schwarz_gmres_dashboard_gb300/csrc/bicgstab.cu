@@ -411,6 +411,10 @@ void solve_bicgstab_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const d
     }
     if (pc && sweep_error(pc))
         fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+    if (pc) {
+        const int hst = host_precond_status(pc);
+        if (hst) fail(SG_ERR_CALLBACK, "the host preconditioner function returned %d", hst);
+    }
     if (nonfinite) fail(SG_ERR_NONFINITE, "non-finite value in the right-hand side or iteration");
 }
 

@@ -4,9 +4,9 @@
 // exit code 0 iff converged (:274).  No MPI: a single process drives one GPU.
 //
 // Reference flags kept: --matrix --poisson --precond --restart --tol
-// --maxiter --fgmres --nparts --overlap --gpu (implied) --output.
-// Flags of reference features outside this solve path (--precond ilut,
-// --drop-tol, --fill-factor, --bicgstab, --analyze) are rejected with a
+// --maxiter --fgmres --bicgstab --analyze --nparts --overlap --gpu (implied)
+// --output.  Flags of the reference's ILUT preconditioner (--precond ilut,
+// --drop-tol, --fill-factor), outside this solve path, are rejected with a
 // message.  Added: --poisson3d N, --varcoef N, --precision fp64|mixed,
 // --factor fp64|fp32|bf16, --stop ref|true_rel, --partition boxes|graph,
 // --learned FILE (learned coarse stage, FGMRES), --nrhs R and --aniso-batch S
@@ -44,6 +44,7 @@ static void usage() {
                  "  --tol <val>              Convergence tolerance (default 1e-10)\n"
                  "  --maxiter <n>            Max iterations (default 1000)\n"
                  "  --fgmres                 Use Flexible GMRES (right-preconditioned)\n"
+                 "  --bicgstab               Use BiCGSTAB (Van der Vorst 1992), FP64\n"
                  "  --precision <p>          fp64 | mixed (FP32 inner Krylov, FP64 outer)\n"
                  "  --stop <rule>            ref (|g| < tol, the reference rule) | true_rel\n"
                  "\nDomain decomposition:\n"
@@ -66,20 +67,8 @@ static void usage() {
                  "\nHardware:\n"
                  "  --gpu                    accepted; every solve runs on the GPU\n"
                  "\nOutput:\n"
-                 "  --output <file.jsonl>    Append metrics to JSONL file\n";
-}
-
-// Matrix Market input: the library's reader (sg_read_matrix_market), which
-// follows the reference reader's rules (src/io/matrix_market.h:14-92).
-static CSRMatrix read_matrix_market(const std::string& path) {
-    int nrows = 0, ncols = 0, nnz = 0;
-    detail::check(sg_read_matrix_market(path.c_str(), &nrows, &ncols, &nnz, nullptr, nullptr,
-                                        nullptr, 0));
-    CSRMatrix A;
-    A.resize(nrows, ncols, nnz);
-    detail::check(sg_read_matrix_market(path.c_str(), &nrows, &ncols, &nnz, A.row_ptr.data(),
-                                        A.col_idx.data(), A.vals.data(), nnz));
-    return A;
+                 "  --output <file.jsonl>    Append metrics to JSONL file\n"
+                 "  --analyze                Run convergence / condition / spectral analysis\n";
 }
 
 // The batch of make_aniso_batch (schwarz_gmres_dashboard_gb300/batched.py):
@@ -239,6 +228,8 @@ int main(int argc, char** argv) {
     double stagnation = 0.5;
     std::string learned_file;
     bool use_fgmres = false;
+    bool use_bicgstab = false;
+    bool run_analysis = false;
     for (int i = 1; i < argc; ++i) {
         auto is = [&](const char* f) { return !std::strcmp(argv[i], f); };
         auto more = [&] { return i + 1 < argc; };
@@ -252,6 +243,8 @@ int main(int argc, char** argv) {
         else if (is("--output") && more()) output_file = argv[++i];
         else if (is("--gpu")) {
         } else if (is("--fgmres")) use_fgmres = true;
+        else if (is("--bicgstab")) use_bicgstab = true;
+        else if (is("--analyze")) run_analysis = true;
         else if (is("--poisson") && more()) poisson_n = std::atoi(argv[++i]);
         else if (is("--poisson3d") && more()) poisson3d_n = std::atoi(argv[++i]);
         else if (is("--varcoef") && more()) varcoef_n = std::atoi(argv[++i]);
@@ -265,7 +258,7 @@ int main(int argc, char** argv) {
         else if (is("--aniso-batch") && more()) aniso_batch = std::atoi(argv[++i]);
         else if (is("--autotune")) {
         }
-        else if (is("--bicgstab") || is("--analyze") || is("--drop-tol") || is("--fill-factor")) {
+        else if (is("--drop-tol") || is("--fill-factor")) {
             std::cerr << "schwarz_solve: " << argv[i]
                       << " belongs to a reference feature outside the GPU solve path\n";
             return 1;
@@ -369,12 +362,28 @@ int main(int argc, char** argv) {
             use_fgmres = true;
             std::cout << "Learned stage: " << learned_file << "\n";
         }
+        // pre-solve analysis (src/main.cpp:213-224): Lanczos condition
+        // estimates of A and M^{-1}A, power-iteration spectral radius of
+        // I - M^{-1}A, all on the GPU
+        if (run_analysis && M) {
+            std::cout << "\n--- Pre-solve analysis ---\n";
+            print_condition_estimate(estimate_condition(A, nullptr, 80), "A (unpreconditioned)");
+            print_condition_estimate(estimate_condition(A, M.get(), 80),
+                                     "M^{-1}A (preconditioned)");
+            print_spectral_result(estimate_spectral_radius(A, M.get(), 300), precond_type);
+            std::cout << "\n";
+        }
         std::vector<double> x(n, 0.0);
-        const std::string label = (use_fgmres ? "FGMRES(" : "GMRES(") +
-                                  std::to_string(params.restart) + ")";
+        if (use_bicgstab && L)
+            throw std::runtime_error("--bicgstab takes no learned stage (it needs FGMRES)");
+        const std::string label = use_bicgstab ? std::string("BiCGSTAB")
+                                               : (use_fgmres ? "FGMRES(" : "GMRES(") +
+                                                     std::to_string(params.restart) + ")";
         std::cout << "Solving with " << label << " + " << precond_type << "\n";
-        GMRESResult res = use_fgmres ? fgmres(A, b, x, M.get(), params)
-                                     : gmres(A, b, x, M.get(), params);
+        if (use_bicgstab) params.precision = SG_FP64;
+        GMRESResult res = use_bicgstab ? bicgstab(A, b, x, M.get(), params)
+                          : use_fgmres ? fgmres(A, b, x, M.get(), params)
+                                       : gmres(A, b, x, M.get(), params);
         std::cout << "  Converged: " << (res.converged ? "yes" : "no") << "\n"
                   << "  Iterations: " << res.iterations << "\n"
                   << "  Residual: " << res.residual_norm << "\n"
@@ -389,11 +398,22 @@ int main(int argc, char** argv) {
                       << (fb >= 0 ? "fell back after cycle " + std::to_string(fb) : std::string("on"))
                       << " (" << applies << " applies)\n";
         }
+        // post-solve convergence analysis and its .conv.jsonl record
+        // (src/main.cpp:251-258)
+        if (run_analysis) {
+            const ConvergenceMetrics ca = analyze_convergence(res.residual_history, res.converged);
+            ca.print_summary();
+            if (!output_file.empty())
+                ca.write_jsonl(output_file + ".conv.jsonl", matrix_file, precond_type, nparts,
+                               overlap);
+        }
         if (!output_file.empty()) {
             // the Metrics record of src/io/metrics_logger.h:28-51, plus extras
             std::ofstream out(output_file, std::ios::app);
             out << std::setprecision(6) << "{\"matrix\":\"" << matrix_file << "\","
-                << "\"method\":\"" << (use_fgmres ? "GPU_FGMRES+" : "GPU_GMRES+") << precond_type
+                << "\"method\":\""
+                << (use_bicgstab ? "GPU_BiCGSTAB+" : use_fgmres ? "GPU_FGMRES+" : "GPU_GMRES+")
+                << precond_type
                 << "\",\"n\":" << n << ",\"nnz\":" << A.nnz() << ",\"ranks\":1,\"threads\":1,"
                 << "\"gpus\":1,\"overlap\":" << overlap << ",\"restart\":" << params.restart
                 << ",\"iterations\":" << res.iterations << ",\"tol\":" << params.tol

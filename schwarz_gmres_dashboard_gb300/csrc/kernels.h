@@ -70,6 +70,18 @@ void estimate_spectral_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int 
                               double tol, unsigned seed, double* eigvec_host,
                               sg_spectral_result* out);
 
+// ---------------------------------------------------------------- host_precond.cu
+// a caller's host function as preconditioner (kind SG_PC_HOST): set-up, and
+// the stream-ordered apply (D2H copy, host function, H2D copy); `scale`
+// (device, optional) is the input's scale, applied before the function and
+// divided out after it (FGMRES directions)
+void host_precond_init(sg_precond* pc, sg_host_apply_fn fn, void* user, int n);
+template <class TI, class TO>
+void host_precond_apply(sg_precond* pc, const TI* x, TO* y, const int* active,
+                        const double* scale);
+int host_precond_status(sg_precond* pc);  // first nonzero return since the last read
+long long host_precond_calls(const sg_precond* pc);
+
 // ---------------------------------------------------------------- schwarz.cu
 void precond_setup_device(sg_precond* pc, const sg_csr* A);
 // exact: FP64 sweeps round each product and difference (reference bits);

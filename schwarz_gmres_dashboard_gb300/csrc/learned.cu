@@ -1510,7 +1510,8 @@ sg_status sg_precond_set_learned(sg_precond* pc, sg_learned* L, double stagnatio
             return;
         }
         SG_CHECK_ARG(L->ctx == pc->ctx, "learned stage belongs to a different context");
-        SG_CHECK_ARG(pc->kind >= SG_PC_ASM, "the learned stage attaches to Schwarz preconditioners");
+        SG_CHECK_ARG(pc->kind >= SG_PC_ASM && pc->kind <= SG_PC_TWOLEVEL_RAS,
+                     "the learned stage attaches to Schwarz preconditioners");
         SG_CHECK_ARG(stagnation >= 0.0 && std::isfinite(stagnation),
                      "stagnation ratio must be >= 0");
         check_ready(L);

@@ -854,6 +854,9 @@ void precond_apply_device(sg_precond* pc, const TI* x, TO* y, const int* active,
     case SG_PC_NONE:
         launch_copy<TI, TO>(ctx, x, y, n, active);
         return;
+    case SG_PC_HOST:
+        host_precond_apply<TI, TO>(pc, x, y, active, nullptr);
+        return;
     case SG_PC_JACOBI:
         if (pc->opts.sweep_dtype == SG_FP64)
             k_jacobi<TI, TO, double><<<grid, 256, 0, ctx->stream>>>(n, pc->inv_diag.p, x, y, active);

@@ -66,6 +66,27 @@ struct DBuf {
     }
 };
 
+// pinned host buffer (freed with the owner)
+template <class T>
+struct PinnedBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    void alloc(size_t count) {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (count == 0) count = 1;
+        SG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&p), count * sizeof(T)));
+        n = count;
+    }
+};
+
 // --------------------------------------------------------------- solver state
 // Restart lengths up to SG_MMAX are supported.
 constexpr int SG_MMAX = 128;
@@ -336,4 +357,16 @@ struct sg_precond {
     // optional device array [nparts]: 0 skips that subdomain's sweep (set by
     // the batched solver around its applies; NULL = every subdomain)
     const int* sub_on = nullptr;
+    // ---- host preconditioner (kind SG_PC_HOST, sg_precond_create_host): a
+    // caller's function applied in stream order between pinned copies
+    sg_host_apply_fn host_fn = nullptr;
+    void* host_user = nullptr;
+    struct HostCtl {
+        int active;    // the launch's active flag, copied before the call
+        int status;    // first nonzero return of the function (0: none)
+        double scale;  // the input vector's scale (FGMRES directions)
+        long long calls;
+    };
+    sg::PinnedBuf<double> h_in, h_out;  // n doubles each (FP32 data uses the front)
+    sg::PinnedBuf<HostCtl> h_ctl;
 };

@@ -82,10 +82,15 @@ struct Basis<float> {
     static const float* vals(const sg_csr* A) { return A->val32.p; }
 };
 
+// host_scale (FGMRES): the device scale of the stored input vector; a host
+// preconditioner function is applied to the normalised vector, as the
+// reference's FGMRES applies its FlexApply (src/core/fgmres.cpp:133-136)
 template <class TI, class TO>
-void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int* active) {
+void apply_pc(sg_ctx* ctx, sg_precond* pc, const TI* x, TO* y, int n, const int* active,
+              const double* host_scale = nullptr) {
     // inside the solver FP64 sweeps may fuse multiply-adds (exact = false)
-    if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active, false);
+    if (pc && pc->kind == SG_PC_HOST) host_precond_apply<TI, TO>(pc, x, y, active, host_scale);
+    else if (pc && pc->kind != SG_PC_NONE) precond_apply_device<TI, TO>(pc, x, y, active, false);
     else launch_copy<TI, TO>(ctx, x, y, n, active);
     if (pc && pc->learned) {
         ClassTimer tm(ctx, TK_LEARNED);
@@ -138,7 +143,7 @@ void enqueue_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const double* b
             TV* zj = Z + (size_t)j * ldv;
             {
                 ClassTimer tm(ctx, TK_PRECOND);
-                apply_pc<TV, TV>(ctx, pc, vj, zj, n, active);
+                apply_pc<TV, TV>(ctx, pc, vj, zj, n, active, &st->vscale[j]);
             }
             ClassTimer tm(ctx, TK_SPMV);
             launch_spmv_a<TV, TV, TV>(ctx, A, zj, wj, &st->vscale[j], active);
@@ -343,6 +348,10 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     }
     if (pc && sweep_error(pc))
         fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+    if (pc) {
+        const int hst = host_precond_status(pc);
+        if (hst) fail(SG_ERR_CALLBACK, "the host preconditioner function returned %d", hst);
+    }
     if (hs->nonfinite) fail(SG_ERR_NONFINITE, "non-finite value in the right-hand side or iteration");
 }
 

@@ -27,7 +27,7 @@ def _field(out, key):
 def test_cli_usage_and_rejected_flags(sg):
     r = _run()
     assert r.returncode == 1 and "Usage" in r.stderr
-    r = _run("--poisson", "8", "--bicgstab")
+    r = _run("--poisson", "8", "--drop-tol", "1e-3")
     assert r.returncode == 1 and "outside the GPU solve path" in r.stderr
 
 
@@ -94,3 +94,45 @@ def test_cli_learned_stage(sg, tmp_path):
     r = _run("--varcoef", "32", "--precond", "twolevel_ras", "--learned",
              str(tmp_path / "short.bin"))
     assert r.returncode == 2 and "float32 weights" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_matrix_market_input(sg, tmp_path):
+    """--matrix with a symmetric file (lower triangle stored): the reader
+    mirrors it, b = A * ones, and the solve converges to x = ones."""
+    A = sg.make_poisson_2d(20, 20)
+    p = tmp_path / "p.mtx"
+    rows = []
+    for i in range(A.nrows):
+        for e in range(A.row_ptr[i], A.row_ptr[i + 1]):
+            if A.col_idx[e] <= i:
+                rows.append(f"{i + 1} {A.col_idx[e] + 1} {float(A.vals[e])!r}")
+    p.write_text("%%MatrixMarket matrix coordinate real symmetric\n% Poisson 20x20\n"
+                 f"{A.nrows} {A.ncols} {len(rows)}\n" + "\n".join(rows) + "\n")
+    out = tmp_path / "m.jsonl"
+    r = _run("--matrix", str(p), "--precond", "ras", "--nparts", "4", "--output", str(out))
+    assert r.returncode == 0, r.stderr
+    assert f"n={A.nrows}  nnz={A.nnz()}" in r.stdout
+    assert _field(r.stdout, "Converged") == "yes"
+    rec = json.loads(out.read_text().splitlines()[-1])
+    assert rec["matrix"] == str(p) and rec["nnz"] == A.nnz()
+
+
+@pytest.mark.gpu
+def test_cli_bicgstab_and_analysis(sg, tmp_path):
+    """--bicgstab and --analyze: the pre-solve condition / spectral estimates
+    are printed, the solve converges, and <output>.conv.jsonl receives the
+    reference's convergence record."""
+    out = tmp_path / "b.jsonl"
+    r = _run("--poisson", "32", "--precond", "ilu0", "--bicgstab", "--analyze", "--tol", "1e-10",
+             "--output", str(out))
+    assert r.returncode == 0, r.stderr
+    assert "Solving with BiCGSTAB + ilu0" in r.stdout
+    assert "Condition estimate (A (unpreconditioned)) [Lanczos 80 steps]" in r.stdout
+    assert "rho(I - M^{-1}A)" in r.stdout and "Convergence analysis" in r.stdout
+    assert _field(r.stdout, "Converged") == "yes"
+    rec = json.loads(out.read_text().splitlines()[-1])
+    assert rec["method"] == "GPU_BiCGSTAB+ilu0"
+    conv = json.loads((tmp_path / "b.jsonl.conv.jsonl").read_text().splitlines()[-1])
+    assert conv["type"] == "convergence" and conv["converged"] is True
+    assert conv["iterations"] == len(conv["residual_history"]) > 0
