@@ -31,7 +31,7 @@ _clib = L.load()
 __all__ = [
     "SgError", "Context", "default_context", "CSRMatrix", "make_identity", "make_poisson_2d",
     "read_matrix_market", "convergence_metrics", "write_convergence_jsonl", "bicgstab",
-    "estimate_condition", "estimate_spectral_radius",
+    "estimate_condition", "estimate_spectral_radius", "HostPreconditioner",
     "make_poisson_3d", "make_varcoef_3d", "uniform", "partition_graph", "partition_boxes",
     "schwarz_structure", "dot", "norm2", "axpy", "scale",
     "Preconditioner", "NoPrecond", "JacobiPrecond", "ILU0Precond", "ASMPrecond", "RASPrecond",
@@ -531,6 +531,42 @@ class Preconditioner:
             pass
 
 
+class HostPreconditioner(Preconditioner):
+    """A Preconditioner plug-in of the caller's own (src/precond/
+    preconditioner.h:7-20), or FGMRES's flexible apply (FlexApply,
+    src/core/fgmres.h:37): fn(x, y) receives numpy views of the input and the
+    output (n doubles) and must fill y.  Inside a solve it runs in stream
+    order on a CUDA host-function thread, so it must not call into CUDA (nor
+    into this package's GPU functions).  An exception inside fn makes the
+    call raise SgError (SG_ERR_CALLBACK) carrying the message."""
+
+    kind = "host"
+
+    def __init__(self, fn, n: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.n = int(n)
+        self.fn = fn
+        self.error = None
+
+        def call(_user, x, y, m):
+            try:
+                fn(np.ctypeslib.as_array(x, (m,)), np.ctypeslib.as_array(y, (m,)))
+                return 0
+            except Exception as e:  # reported through the status
+                self.error = f"{type(e).__name__}: {e}"
+                return 1
+
+        self._cb = L.HOST_APPLY_FN(call)  # kept alive with the object
+        h = C.c_void_p()
+        _check(_clib.sg_precond_create_host(self.ctx.handle, C.cast(self._cb, C.c_void_p), None,
+                                           self.n, C.byref(h)))
+        self.handle = h
+
+    def setup(self, A: CSRMatrix) -> None:
+        if A.nrows != self.n:
+            raise ValueError("size mismatch")
+
+
 class NoPrecond(Preconditioner):
     kind = "none"
 
@@ -636,6 +672,9 @@ def _solve(solver: int, A: CSRMatrix, b, x, M: Optional[Preconditioner],
     r = L.SolveResult()
     st = _clib.sg_solve(ctx.handle, solver, dev, M.handle if M is not None else None, pb, px, n,
                        mx, C.byref(p), C.byref(r))
+    if st == L.SG_ERR_CALLBACK and getattr(M, "error", None):
+        msg, M.error = M.error, None
+        raise SgError(st, msg)
     _check(st)
     hl = min(r.history_len, hist.size) if hist is not None else 0
     return GMRESResult(iterations=r.iterations, residual_norm=r.residual_norm,

@@ -15,7 +15,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libsgmres.so")
 SG_OK = 0
 STATUS = {0: "SG_OK", 1: "SG_ERR_INVALID_ARG", 2: "SG_ERR_CUDA", 3: "SG_ERR_OOM",
           4: "SG_ERR_SINGULAR", 5: "SG_ERR_NOT_SETUP", 6: "SG_ERR_NONFINITE",
-          7: "SG_ERR_DEVICE_TIMEOUT", 8: "SG_ERR_UNSUPPORTED", 9: "SG_ERR_INTERNAL"}
+          7: "SG_ERR_DEVICE_TIMEOUT", 8: "SG_ERR_UNSUPPORTED", 9: "SG_ERR_INTERNAL",
+          10: "SG_ERR_CALLBACK"}
+SG_ERR_CALLBACK = 10
 
 MEM_HOST, MEM_DEVICE = 0, 1
 FP64, FP32, BF16 = 0, 1, 2
@@ -50,6 +52,11 @@ class SolveParams(C.Structure):
 class BatchResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("cycles", C.c_int), ("converged", C.c_int),
                 ("status", C.c_int), ("true_rel_residual", C.c_double)]
+
+
+# int fn(void* user, const double* x, double* y, int n)
+HOST_APPLY_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                            C.c_int)
 
 
 class Convergence(C.Structure):
@@ -108,6 +115,7 @@ PROTOTYPES = {
     "sg_precond_get_coarse": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "sg_precond_get_sweep": (C.c_int, [_vp, _ip, _ip]),
     "sg_precond_set_wait_test": (C.c_int, [_vp, C.c_int]),
+    "sg_precond_create_host": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
     "sg_estimate_condition": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_uint,
                                         C.POINTER(ConditionEstimate)]),
     "sg_estimate_spectral_radius": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_double, C.c_uint, _vp,

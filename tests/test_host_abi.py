@@ -40,7 +40,7 @@ def test_abi_version_and_status_strings(sg):
     from schwarz_gmres_dashboard_gb300 import _lib as L
     lib = L.load()
     assert lib.sg_abi_version() == 1
-    for st in range(10):
+    for st in range(11):
         assert lib.sg_status_string(st)
 
 
