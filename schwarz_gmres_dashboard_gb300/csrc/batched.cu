@@ -259,6 +259,55 @@ k_b_spmv(BatchDev B, const int* __restrict__ rp, const int* __restrict__ ci,
     }
 }
 
+// The same product from the SELL-32 copy of A (slices of 32 rows, entries
+// column-major within a slice: a warp's loads of values and columns are
+// coalesced), for up to four right-hand sides at once: each matrix entry is
+// read once for all of them.  Per row the products are summed in the CSR
+// order (padding adds exact zeros at the end), as k_b_spmv does.
+constexpr int BSR = 4;  // right-hand sides per pass over the matrix
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_spmv_sell(BatchDev B, const long long* __restrict__ sl_ptr, const int* __restrict__ sl_w,
+              const int* __restrict__ sl_col, const TV* __restrict__ sl_val,
+              const int* __restrict__ row_sys, int nslices, const TV* __restrict__ x,
+              TV* __restrict__ y, int j) {
+    const int lane = threadIdx.x & 31;
+    const int ld = B.m + 1;
+    const int wstride = (gridDim.x * blockDim.x) >> 5;
+    for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < nslices; sl += wstride) {
+        const long long row = (long long)sl * 32 + lane;
+        const bool in = row < B.N;
+        const int sys = in ? row_sys[row] : 0;
+        const long long base = sl_ptr[sl] + lane;
+        const int w = sl_w[sl];
+        for (int r0 = 0; r0 < B.R; r0 += BSR) {
+            bool act[BSR];
+            bool any = false;
+#pragma unroll
+            for (int u = 0; u < BSR; ++u) {
+                act[u] = in && r0 + u < B.R && B.active[(r0 + u) * B.S + sys];
+                any |= act[u];
+            }
+            if (!__any_sync(0xffffffffu, any)) continue;
+            TV acc[BSR];
+#pragma unroll
+            for (int u = 0; u < BSR; ++u) acc[u] = (TV)0;
+            for (int k = 0; k < w; ++k) {
+                const int c = __ldg(&sl_col[base + 32ll * k]);
+                const TV v = ld_stream(&sl_val[base + 32ll * k]);
+#pragma unroll
+                for (int u = 0; u < BSR; ++u)
+                    if (act[u]) acc[u] += v * x[(long long)(r0 + u) * B.N + c];
+            }
+#pragma unroll
+            for (int u = 0; u < BSR; ++u)
+                if (act[u])
+                    y[(long long)(r0 + u) * B.N + row] =
+                        (TV)((double)acc[u] * B.vscale[(size_t)((r0 + u) * B.S + sys) * ld + j]);
+        }
+    }
+}
+
 // red[warp][k] = warp sums of raw_k . wv (k <= j) for a chunk: four
 // vectors' loads in flight at a time; per vector the products are summed
 // over the thread's rows in row order, then across the warp
@@ -597,12 +646,14 @@ struct BBasis<float> {
     static DBuf<float>& V(BatchWork* w) { return w->V32; }
     static DBuf<float>& T(BatchWork* w) { return w->t32; }
     static const float* vals(const sg_csr* A) { return A->val32.p; }
+    static const float* sell_vals(const sg_csr* A) { return A->sl_val32.p; }
 };
 template <>
 struct BBasis<double> {
     static DBuf<double>& V(BatchWork* w) { return w->V64; }
     static DBuf<double>& T(BatchWork* w) { return w->t64; }
     static const double* vals(const sg_csr* A) { return A->val.p; }
+    static const double* sell_vals(const sg_csr* A) { return A->sl_val.p; }
 };
 
 template <class TV>
@@ -662,8 +713,16 @@ void enqueue_batch_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const Bat
     for (int j = 0; j < B.m; ++j) {
         {
             ClassTimer tm(ctx, TK_SPMV);
-            k_b_spmv<TV><<<bgrid(ctx, total), BT, 0, st>>>(B, A->rp.p, A->ci.p, val, w->row_sys.p,
-                                                           V + (size_t)j * ldv, t, j);
+            const TV* sval = BBasis<TV>::sell_vals(A);
+            if (A->sell_ok && sval) {
+                k_b_spmv_sell<TV><<<bgrid(ctx, (long long)A->nslices * 32), BT, 0, st>>>(
+                    B, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, sval, w->row_sys.p, A->nslices,
+                    V + (size_t)j * ldv, t, j);
+            } else {
+                k_b_spmv<TV><<<bgrid(ctx, total), BT, 0, st>>>(B, A->rp.p, A->ci.p, val,
+                                                               w->row_sys.p, V + (size_t)j * ldv,
+                                                               t, j);
+            }
             SG_CUDA(cudaGetLastError());
             count_launch(ctx);
         }

@@ -71,6 +71,9 @@ int main(int argc, char** argv) {
         hj.apply(v, z, m);
     }, p);
     std::printf("flex_fgmres %d %d %.3e\n", rf.converged ? 1 : 0, rf.iterations, err(xf));
+    std::vector<double> xdf(n, 0.0);
+    GMRESResult rdf = fgmres(A, b, xdf, &gj, p);
+    std::printf("device_fgmres %d %d %.3e\n", rdf.converged ? 1 : 0, rdf.iterations, err(xdf));
     std::vector<double> xn(n, 0.0);
     int sweeps = 0;
     GMRESResult rn = fgmres_flex(A, b, xn, [&](const double* v, double* z, int m) {

@@ -40,7 +40,8 @@ def test_plugin_preconditioner_matches_device_one(results):
 @pytest.mark.gpu
 def test_flexible_apply(results):
     assert results["flex_fgmres"][0] == "1" and float(results["flex_fgmres"][2]) < 1e-6
-    assert abs(int(results["flex_fgmres"][1]) - int(results["plugin_gmres"][1])) <= 3
+    # the FlexApply (host Jacobi) and the GPU Jacobi in FGMRES: same iterations
+    assert abs(int(results["flex_fgmres"][1]) - int(results["device_fgmres"][1])) <= 1
     # a nonlinear apply (the number of inner sweeps varies): FGMRES still converges
     assert results["flex_nonlinear"][0] == "1" and float(results["flex_nonlinear"][2]) < 1e-6
 
