@@ -6,9 +6,13 @@
 // All of it is integer work; the floating-point set-up (value gather,
 // factorisation, coarse operator) runs on the device (schwarz.cu).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <exception>
+#include <mutex>
 #include <numeric>
+#include <thread>
 
 #include "sg_internal.h"
 
@@ -97,6 +101,50 @@ static long long sweep_bank_cost(int n, const int* lrp, const int* lci, const in
     return cost;
 }
 
+// Host threads for the per-subdomain set-up: the hardware threads, at most
+// 32 and at most one per subdomain.
+static int host_threads(int nparts) {
+    unsigned hw = std::thread::hardware_concurrency();
+    int t = hw == 0 ? 4 : (int)hw;
+    t = std::min(t, 32);
+    return std::max(1, std::min(t, nparts));
+}
+
+// f(s, scratch) for s in [0, count): subdomains dealt out dynamically to
+// `threads` threads; each thread keeps one scratch vector across its calls.
+// The first exception thrown by a call is rethrown after all threads end.
+template <class F>
+static void parallel_for(int count, int threads, F&& f) {
+    std::atomic<int> next{0};
+    std::exception_ptr err;
+    std::mutex err_mu;
+    auto work = [&] {
+        std::vector<int> scratch;
+        for (;;) {
+            const int s = next.fetch_add(1);
+            if (s >= count) return;
+            try {
+                f(s, scratch);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(err_mu);
+                if (!err) err = std::current_exception();
+                next.store(count);
+                return;
+            }
+        }
+    };
+    if (threads <= 1) {
+        work();
+    } else {
+        std::vector<std::thread> pool;
+        pool.reserve(threads - 1);
+        for (int i = 0; i < threads - 1; ++i) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+    }
+    if (err) std::rethrow_exception(err);
+}
+
 static void level_order(int n, const int* lev, int nlev, std::vector<int>& perm,
                         std::vector<int>& ptr) {
     ptr.assign(nlev + 1, 0);
@@ -135,16 +183,20 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
         if (pc->owned_ptr[s + 1] == pc->owned_ptr[s])
             fail(SG_ERR_INVALID_ARG, "subdomain %d owns no rows", s);
 
+    // The per-subdomain work below is independent across subdomains: it runs
+    // on host threads (each with its own scratch), every subdomain writes its
+    // results to its own slots, and the concatenation afterwards keeps the
+    // subdomain order -- the output is the same for any thread count.
+    const int nthreads = host_threads(nparts);
+
     // overlap: vertices within `overlap` hops of the owned set, sorted
     // (src/decomp/domain_decomp.h:68-90); owned-local map (ras.h:34-41)
-    pc->sub_ptr.assign(nparts + 1, 0);
-    pc->sub.clear();
-    pc->ownloc_ptr.assign(nparts + 1, 0);
-    pc->ownloc.clear();
-    std::vector<unsigned char> mark(n, 0);
-    std::vector<int> set;
-    set.reserve(1024);
-    for (int s = 0; s < nparts; ++s) {
+    std::vector<std::vector<int>> sub_s(nparts), ownloc_s(nparts);
+    parallel_for(nparts, nthreads, [&](int s, std::vector<int>& scratch) {
+        // scratch: a mark array over the global rows, 0 between subdomains
+        if (scratch.size() != (size_t)n) scratch.assign(n, 0);
+        int* mark = scratch.data();
+        std::vector<int>& set = sub_s[s];
         set.assign(pc->owned.begin() + pc->owned_ptr[s], pc->owned.begin() + pc->owned_ptr[s + 1]);
         for (int v : set) mark[v] = 1;
         size_t lo = 0;
@@ -163,63 +215,76 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
             lo = hi;
         }
         std::sort(set.begin(), set.end());
+        std::vector<int>& ol = ownloc_s[s];
         for (size_t q = 0; q < set.size(); ++q) {
             mark[set[q]] = 0;
-            if (pc->part[set[q]] == s) pc->ownloc.push_back((int)q);
+            if (pc->part[set[q]] == s) ol.push_back((int)q);
         }
-        pc->sub.insert(pc->sub.end(), set.begin(), set.end());
-        pc->sub_ptr[s + 1] = (int)pc->sub.size();
-        pc->ownloc_ptr[s + 1] = (int)pc->ownloc.size();
+    });
+    pc->sub_ptr.assign(nparts + 1, 0);
+    pc->ownloc_ptr.assign(nparts + 1, 0);
+    for (int s = 0; s < nparts; ++s) {
+        pc->sub_ptr[s + 1] = pc->sub_ptr[s] + (int)sub_s[s].size();
+        pc->ownloc_ptr[s + 1] = pc->ownloc_ptr[s] + (int)ownloc_s[s].size();
+    }
+    pc->sub.resize(pc->sub_ptr[nparts]);
+    pc->ownloc.resize(pc->ownloc_ptr[nparts]);
+    for (int s = 0; s < nparts; ++s) {
+        std::copy(sub_s[s].begin(), sub_s[s].end(), pc->sub.begin() + pc->sub_ptr[s]);
+        std::copy(ownloc_s[s].begin(), ownloc_s[s].end(), pc->ownloc.begin() + pc->ownloc_ptr[s]);
+        std::vector<int>().swap(sub_s[s]);
+        std::vector<int>().swap(ownloc_s[s]);
     }
 
     // local CSR A[dofs,dofs] in row order, entries in original order
-    // (src/core/sparse_matrix.h:53-83), plus the global entry of each local one
-    pc->lrp.clear();
-    pc->lci.clear();
-    pc->lmap.clear();
-    pc->ldiag.assign(pc->sub.size(), -1);
-    pc->lev_lo.assign(pc->sub.size(), 0);
-    pc->lev_up.assign(pc->sub.size(), 0);
+    // (src/core/sparse_matrix.h:53-83), the global entry of each local one,
+    // ILU(0) diagonal positions, widths, level schedules and the slot layout
+    const size_t nsub = pc->sub.size();
+    pc->ldiag.assign(nsub, -1);
+    pc->lev_lo.assign(nsub, 0);
+    pc->lev_up.assign(nsub, 0);
     pc->h_info.assign(nparts, SubInfo{});
-    pc->h_lev_ptr_f.clear();
-    pc->h_lev_ptr_b.clear();
-    std::vector<int> perm_f_all(pc->sub.size()), perm_b_all(pc->sub.size());
-    std::vector<int> loc(n, -1);
-    long long fl_total = 0, fu_total = 0;
-    int max_n = 0, t_len = 0;
-    std::vector<int> perm, ptr;
-    for (int s = 0; s < nparts; ++s) {
+    std::vector<int> perm_f_all(nsub), perm_b_all(nsub);
+    struct LocalOut {
+        std::vector<int> lrp, lci, lmap, ptr_f, ptr_b;
+        int missing_diag = -1;  // global row without a diagonal entry (-1: none)
+    };
+    std::vector<LocalOut> lo_s(nparts);
+    parallel_for(nparts, nthreads, [&](int s, std::vector<int>& scratch) {
+        // scratch: global row -> local row (-1 outside the subdomain)
+        if (scratch.size() != (size_t)n) scratch.assign(n, -1);
+        int* loc = scratch.data();
+        LocalOut& L = lo_s[s];
         const int off = pc->sub_ptr[s];
         const int ns = pc->sub_ptr[s + 1] - off;
         const int* dofs = pc->sub.data() + off;
         for (int li = 0; li < ns; ++li) loc[dofs[li]] = li;
-        SubInfo inf{};
+        SubInfo& inf = pc->h_info[s];
         inf.n = ns;
         inf.row_off = off;
-        inf.csr_row_off = (int)pc->lrp.size();
-        inf.csr_nz_off = (long long)pc->lci.size();
-        const size_t rbase = pc->lrp.size();
-        const long long zbase = (long long)pc->lci.size();
+        L.lrp.reserve((size_t)ns + 1);
         for (int li = 0; li < ns; ++li) {
             const int gi = dofs[li];
-            pc->lrp.push_back((int)((long long)pc->lci.size() - zbase));
+            L.lrp.push_back((int)L.lci.size());
             for (int e = rp[gi]; e < rp[gi + 1]; ++e) {
                 const int lj = loc[ci[e]];
                 if (lj >= 0) {
                     if (lj == li && pc->ldiag[off + li] < 0)
-                        pc->ldiag[off + li] = (int)((long long)pc->lci.size() - zbase);
-                    pc->lci.push_back(lj);
-                    pc->lmap.push_back(e);
+                        pc->ldiag[off + li] = (int)L.lci.size();
+                    L.lci.push_back(lj);
+                    L.lmap.push_back(e);
                 }
             }
         }
-        pc->lrp.push_back((int)((long long)pc->lci.size() - zbase));
+        L.lrp.push_back((int)L.lci.size());
         for (int li = 0; li < ns; ++li) loc[dofs[li]] = -1;
-        const int* lrp = pc->lrp.data() + rbase;
-        const int* lci = pc->lci.data() + zbase;
+        const int* lrp = L.lrp.data();
+        const int* lci = L.lci.data();
         for (int li = 0; li < ns; ++li)
-            if (pc->ldiag[off + li] < 0)
-                fail(SG_ERR_SINGULAR, "ILU(0): row %d has no diagonal entry", dofs[li]);
+            if (pc->ldiag[off + li] < 0) {
+                L.missing_diag = dofs[li];
+                return;
+            }
         // widths
         int wl = 0, wu = 0;
         for (int li = 0; li < ns; ++li) {
@@ -236,45 +301,75 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
         const int nlf = levels_lower(ns, lrp, lci, lo);
         const int nlb = levels_upper(ns, lrp, lci, pc->ldiag.data() + off, up);
         inf.nlev_f = nlf;
-        inf.lev_off_f = (int)pc->h_lev_ptr_f.size();
-        level_order(ns, lo, nlf, perm, ptr);
-        std::copy(perm.begin(), perm.end(), perm_f_all.begin() + off);
-        pc->h_lev_ptr_f.insert(pc->h_lev_ptr_f.end(), ptr.begin(), ptr.end());
         inf.nlev_b = nlb;
-        inf.lev_off_b = (int)pc->h_lev_ptr_b.size();
-        level_order(ns, up, nlb, perm, ptr);
+        std::vector<int> perm;
+        level_order(ns, lo, nlf, perm, L.ptr_f);
+        std::copy(perm.begin(), perm.end(), perm_f_all.begin() + off);
+        level_order(ns, up, nlb, perm, L.ptr_b);
         std::copy(perm.begin(), perm.end(), perm_b_all.begin() + off);
-        pc->h_lev_ptr_b.insert(pc->h_lev_ptr_b.end(), ptr.begin(), ptr.end());
         // slot layout of the TMA-fed sweep: the cheapest of none / one pad
         // word per 32 / per 16 rows under the bank model (slots stay 16-bit)
         {
             const int words = pc->opts.sweep_dtype == SG_FP64 ? 2 : 1;
             const int* dgl = pc->ldiag.data() + off;
             const int* pf = perm_f_all.data() + off;
-            const int* pff = pc->h_lev_ptr_f.data() + inf.lev_off_f;
-            const int* pfb = pc->h_lev_ptr_b.data() + inf.lev_off_b;
             inf.tshift = 0;
             long long best = -1;
             for (int p : {0, 5, 4}) {
                 if (tslot(ns, p) > 65535) continue;
-                const long long c = sweep_bank_cost(ns, lrp, lci, dgl, pf, pff, nlf, perm.data(),
-                                                    pfb, nlb, wl, wu, p, words);
+                const long long c = sweep_bank_cost(ns, lrp, lci, dgl, pf, L.ptr_f.data(), nlf,
+                                                    perm.data(), L.ptr_b.data(), nlb, wl, wu, p,
+                                                    words);
                 if (best < 0 || c < best) {
                     best = c;
                     inf.tshift = p;
                 }
             }
         }
-        t_len = std::max(t_len, tslot(ns, inf.tshift) + 1);
+        inf.n_own = pc->ownloc_ptr[s + 1] - pc->ownloc_ptr[s];
+        inf.own_off = pc->ownloc_ptr[s];
+        inf.cscale = 1.0 / std::sqrt((double)(pc->owned_ptr[s + 1] - pc->owned_ptr[s]));
+    });
+    for (int s = 0; s < nparts; ++s)
+        if (lo_s[s].missing_diag >= 0)
+            fail(SG_ERR_SINGULAR, "ILU(0): row %d has no diagonal entry", lo_s[s].missing_diag);
+    // concatenation in subdomain order
+    pc->lrp.clear();
+    pc->lci.clear();
+    pc->lmap.clear();
+    pc->h_lev_ptr_f.clear();
+    pc->h_lev_ptr_b.clear();
+    {
+        size_t nr = 0, nz = 0;
+        for (const auto& L : lo_s) {
+            nr += L.lrp.size();
+            nz += L.lci.size();
+        }
+        pc->lrp.reserve(nr);
+        pc->lci.reserve(nz);
+        pc->lmap.reserve(nz);
+    }
+    long long fl_total = 0, fu_total = 0;
+    int max_n = 0, t_len = 0;
+    for (int s = 0; s < nparts; ++s) {
+        LocalOut& L = lo_s[s];
+        SubInfo& inf = pc->h_info[s];
+        inf.csr_row_off = (int)pc->lrp.size();
+        inf.csr_nz_off = (long long)pc->lci.size();
+        pc->lrp.insert(pc->lrp.end(), L.lrp.begin(), L.lrp.end());
+        pc->lci.insert(pc->lci.end(), L.lci.begin(), L.lci.end());
+        pc->lmap.insert(pc->lmap.end(), L.lmap.begin(), L.lmap.end());
+        inf.lev_off_f = (int)pc->h_lev_ptr_f.size();
+        pc->h_lev_ptr_f.insert(pc->h_lev_ptr_f.end(), L.ptr_f.begin(), L.ptr_f.end());
+        inf.lev_off_b = (int)pc->h_lev_ptr_b.size();
+        pc->h_lev_ptr_b.insert(pc->h_lev_ptr_b.end(), L.ptr_b.begin(), L.ptr_b.end());
+        L = LocalOut();  // release as we go
+        t_len = std::max(t_len, tslot(inf.n, inf.tshift) + 1);
         inf.fl_off = fl_total;
         inf.fu_off = fu_total;
-        fl_total += (long long)wl * ns;
-        fu_total += (long long)wu * ns;
-        inf.own_off = pc->ownloc_ptr[s];
-        inf.n_own = pc->ownloc_ptr[s + 1] - pc->ownloc_ptr[s];
-        inf.cscale = 1.0 / std::sqrt((double)(pc->owned_ptr[s + 1] - pc->owned_ptr[s]));
-        pc->h_info[s] = inf;
-        max_n = std::max(max_n, ns);
+        fl_total += (long long)inf.wl * inf.n;
+        fu_total += (long long)inf.wu * inf.n;
+        max_n = std::max(max_n, inf.n);
     }
     pc->fl_total = fl_total > 0 ? fl_total : 1;
     pc->fu_total = fu_total > 0 ? fu_total : 1;
