@@ -376,7 +376,32 @@ k_dots(const TV* __restrict__ raw, size_t ldv, int n, int k0, int kc, const TV* 
     for (int q = 0; q < KPW; ++q) acc[q] = (TV)0;
     const int nvec = n / VN;
     const int stride = gridDim.x * ngrp * 32;
-    for (int u = (blockIdx.x * ngrp + grp) * 32 + lane; u < nvec; u += stride) {
+    // two tiles per round: all their loads are in flight before the first
+    // product (a step with few vectors has only a few rounds per thread, each
+    // a full memory latency); the tiles are still added in ascending order
+    int u = (blockIdx.x * ngrp + grp) * 32 + lane;
+    for (; u + stride < nvec; u += 2 * stride) {
+        TV w0[VN], w1[VN], v0[KPW][VN], v1[KPW][VN];
+        vload<TV>(w + (size_t)u * VN, w0);
+        vload<TV>(w + (size_t)(u + stride) * VN, w1);
+#pragma unroll
+        for (int q = 0; q < KPW; ++q) {
+            const int k = slot + nwg * q;
+            if (k < kc) {
+                vload<TV>(raw + (size_t)(k0 + k) * ldv + (size_t)u * VN, v0[q]);
+                vload<TV>(raw + (size_t)(k0 + k) * ldv + (size_t)(u + stride) * VN, v1[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < KPW; ++q) {
+            const int k = slot + nwg * q;
+            if (k < kc) {
+                acc[q] += dotv<TV>(v0[q], w0);
+                acc[q] += dotv<TV>(v1[q], w1);
+            }
+        }
+    }
+    if (u < nvec) {
         TV wv[VN];
         vload<TV>(w + (size_t)u * VN, wv);
 #pragma unroll

@@ -289,18 +289,27 @@ __device__ __forceinline__ void rec_load(RowRec<W, TF>& o, uint32_t R, int C, in
     if (BACK) o.d = lds<TF>(vq + vs * (uint32_t)NW);
 }
 
-// t[r] = (t[r] - sum_k v_k t[c_k]) (/ d): the reference row's order
-template <int NW, bool BACK, class TS, bool EXACT, int W, class TF>
-__device__ __forceinline__ void rec_solve(const RowRec<W, TF>& o, uint32_t tb) {
+// t[r] = (t[r] - sum_k v_k t[c_k]) (/ d): the reference row's order.  The
+// gathers of t are issued first; `between` runs before their values are
+// used (the next level's record loads go there, so their latency overlaps
+// the gathers' instead of adding to the level).
+template <int NW, bool BACK, class TS, bool EXACT, int W, class TF, class Between>
+__device__ __forceinline__ void rec_solve(const RowRec<W, TF>& o, uint32_t tb,
+                                          Between&& between) {
     constexpr uint32_t ST = sizeof(TS);
     TS acc = lds<TS>(tb + ST * o.r);
     TS xk[NW];
 #pragma unroll
     for (int k = 0; k < NW; ++k) xk[k] = lds<TS>(tb + ST * o.c[k]);
+    between();
 #pragma unroll
     for (int k = 0; k < NW; ++k) acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(o.v[k]), xk[k]);
     if (BACK) acc = div_diag(acc, Load<TS>::f(o.d));
     sts(tb + ST * o.r, acc);
+}
+template <int NW, bool BACK, class TS, bool EXACT, int W, class TF>
+__device__ __forceinline__ void rec_solve(const RowRec<W, TF>& o, uint32_t tb) {
+    rec_solve<NW, BACK, TS, EXACT>(o, tb, [] {});
 }
 
 // per-level word of the fixed-width loop: rows (16 bits), padded rows (16
@@ -343,6 +352,10 @@ struct RecArgs {
     // (1: no record group 0 is copied; 2: no restriction is counted)
     long long wait_budget;
     int wait_test;
+    // level loop (comparison knob, opts.reserved[3]): 0 the fixed-width loop
+    // with the next record loaded beside the gathers, 1 the generic loop,
+    // 2 the fixed-width loop with the next record loaded before the barrier
+    int level_loop;
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -366,37 +379,49 @@ struct FixedLoop {
 // (bounded) after the barrier, and a failed wait travels in the next level's
 // barrier.  Returns false after a failed wait (error word set, the issued
 // copies drained, y untouched).
-template <int W, class TS, class TF, bool EXACT, class Refill>
+template <bool PIPE, int W, class TS, class TF, bool EXACT, class Refill>
 __device__ __forceinline__ bool fixed_levels(const RecArgs& a, const FixedLoop& L,
                                              Refill&& refill) {
     const int tid = threadIdx.x;
     int q = 0, b = 0, gstart = 0, gend = L.T < L.K ? L.T : L.K;
     uint32_t ph = 0;
-    RowRec<W, TF> pre;
-    auto prefetch = [&](uint64_t m, int g, int buf) {
+    RowRec<W, TF> pre, nxt;
+    auto load_into = [&](RowRec<W, TF>& dst, uint64_t m, int g, int buf) {
         if (tid < meta_rows(m)) {
             const uint32_t R = L.bufs_s + (uint32_t)buf * (uint32_t)L.gbytes + meta_off(m);
-            if (g >= L.nf) rec_load<W, true>(pre, R, meta_pad(m), tid);
-            else rec_load<W, false>(pre, R, meta_pad(m), tid);
+            if (g >= L.nf) rec_load<W, true>(dst, R, meta_pad(m), tid);
+            else rec_load<W, false>(dst, R, meta_pad(m), tid);
         }
     };
     bool ok = L.T == 0 || mbar_wait(smem_u32(&L.bars[0]), 0u, a.wait_budget);
     uint64_t mw = L.T > 0 ? L.meta[0] : 0;
-    if (ok && L.T > 0) prefetch(mw, 0, 0);
+    if (ok && L.T > 0) load_into(pre, mw, 0, 0);
     for (int g = 0; g < L.T; ++g) {
         const uint64_t mwn = g + 1 < L.T ? L.meta[g + 1] : 0;
+        const bool group_end = g + 1 == gend;
+        // PIPE: the next level's record (same buffer) loads while this
+        // level's gathers are in flight; without PIPE it loads after the
+        // level's rows, before the barrier
+        const bool next_here = ok && !group_end && g + 1 < L.T;
+        bool next_done = false;
+        auto between = [&] {
+            if (PIPE && next_here) {
+                load_into(nxt, mwn, g + 1, b);
+                next_done = true;
+            }
+        };
         if (ok) {
             const int c = meta_rows(mw), C = meta_pad(mw);
             const uint32_t R = L.bufs_s + (uint32_t)b * (uint32_t)L.gbytes + meta_off(mw);
             if (g >= L.nf) {
-                if (tid < c) rec_solve<W, true, TS, EXACT>(pre, L.t_s);
+                if (tid < c) rec_solve<W, true, TS, EXACT>(pre, L.t_s, between);
                 for (int qq = tid + L.NC; qq < c; qq += L.NC) {
                     RowRec<W, TF> o;
                     rec_load<W, true>(o, R, C, qq);
                     rec_solve<W, true, TS, EXACT>(o, L.t_s);
                 }
             } else {
-                if (tid < c) rec_solve<W, false, TS, EXACT>(pre, L.t_s);
+                if (tid < c) rec_solve<W, false, TS, EXACT>(pre, L.t_s, between);
                 for (int qq = tid + L.NC; qq < c; qq += L.NC) {
                     RowRec<W, TF> o;
                     rec_load<W, false>(o, R, C, qq);
@@ -404,8 +429,10 @@ __device__ __forceinline__ bool fixed_levels(const RecArgs& a, const FixedLoop& 
                 }
             }
         }
-        const bool group_end = g + 1 == gend;
-        if (ok && !group_end && g + 1 < L.T) prefetch(mwn, g + 1, b);
+        if (next_here) {
+            if (next_done) pre = nxt;
+            else load_into(pre, mwn, g + 1, b);  // no row of this level here
+        }
         if (g == gstart) {
             if (__syncthreads_or(ok ? 0 : 1)) {
                 // a record group did not arrive in time: report, drain the
@@ -446,7 +473,7 @@ __device__ __forceinline__ bool fixed_levels(const RecArgs& a, const FixedLoop& 
             gend = gstart + L.K < L.T ? gstart + L.K : L.T;
             if (g + 1 < L.T) {
                 ok = mbar_wait(smem_u32(&L.bars[b]), ph, a.wait_budget);
-                if (ok) prefetch(mwn, g + 1, b);
+                if (ok) load_into(pre, mwn, g + 1, b);
             }
         }
         mw = mwn;
@@ -567,14 +594,21 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     // whose per-level path is only the gathers of t, the multiply-adds and
     // one barrier -- its first row's record entries load into registers
     // before the previous level's barrier
-    const int wfix = (inf.wl == inf.wu && inf.wl >= 2 && inf.wl <= 4) ? inf.wl : 0;
+    const int wfix = (a.level_loop != 1 && inf.wl == inf.wu && inf.wl >= 2 && inf.wl <= 4)
+                         ? inf.wl : 0;
     if (wfix) {
         FixedLoop L{m_meta, bars, bufs_s, t_s, T, nf, NB, K, ngrp, a.gbytes, NC, producer};
         auto refill = [&](int qq, int bb) { issue(qq, bb); };
         bool done = false;
-        if (wfix == 3) done = fixed_levels<3, TS, TF, EXACT>(a, L, refill);
-        else if (wfix == 2) done = fixed_levels<2, TS, TF, EXACT>(a, L, refill);
-        else done = fixed_levels<4, TS, TF, EXACT>(a, L, refill);
+        if (a.level_loop == 2) {
+            if (wfix == 3) done = fixed_levels<false, 3, TS, TF, EXACT>(a, L, refill);
+            else if (wfix == 2) done = fixed_levels<false, 2, TS, TF, EXACT>(a, L, refill);
+            else done = fixed_levels<false, 4, TS, TF, EXACT>(a, L, refill);
+        } else {
+            if (wfix == 3) done = fixed_levels<true, 3, TS, TF, EXACT>(a, L, refill);
+            else if (wfix == 2) done = fixed_levels<true, 2, TS, TF, EXACT>(a, L, refill);
+            else done = fixed_levels<true, 4, TS, TF, EXACT>(a, L, refill);
+        }
         if (!done) return;  // a record group did not arrive (reported, drained)
         goto levels_done;
     }
@@ -732,6 +766,7 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     a.err = pc->err_d.p;
     a.sub_on = pc->sub_on;
     a.wait_test = pc->wait_test;
+    a.level_loop = pc->opts.reserved[3];
     a.wait_budget = pc->wait_test ? WAIT_TEST_CYCLES : WAIT_CYCLES;
     return a;
 }
