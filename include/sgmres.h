@@ -78,13 +78,7 @@ typedef struct sg_precond_opts {
                          preconditioners compute the coarse restriction
                          inside the TMA-fed sweep when all subdomains' CTAs
                          fit on the GPU at once (0), or in a kernel of its
-                         own (1; same results); reserved[3]: level loop of
-                         the TMA-fed sweep (comparison): 0 a loop specialised
-                         for stencil widths 2-4 whose next level's records
-                         load beside the current level's gathers, 1 the
-                         generic loop, 2 the specialised loop loading the
-                         next records before the level barrier (same
-                         results); other entries must be 0 */
+                         own (1; same results); other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;

@@ -422,8 +422,7 @@ class Preconditioner:
     def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
                  ctx: Context | None = None, generic_sweep: bool = False,
-                 sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True,
-                 level_loop: str = "auto"):
+                 sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True):
         # sweep variant (testing/comparison): "tma" (default: TMA-fed level
         # records), "level" (factors read from global memory), "syncfree"
         if generic_sweep:
@@ -447,10 +446,6 @@ class Preconditioner:
         # two-level: coarse restriction inside the TMA-fed sweep when all the
         # subdomains' CTAs fit at once (False: a kernel of its own; same bits)
         opts.reserved[2] = 0 if fuse_restrict else 1
-        # level loop of the TMA-fed sweep (comparison; same results): "auto"
-        # (the stencil-width loop with pipelined record loads), "generic",
-        # "prefetch" (the stencil-width loop loading records before the barrier)
-        opts.reserved[3] = {"auto": 0, "generic": 1, "prefetch": 2}[level_loop]
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),

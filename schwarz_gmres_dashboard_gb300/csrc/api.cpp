@@ -466,10 +466,6 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             delete pc;
             fail(SG_ERR_INVALID_ARG, "restriction placement (reserved[2]) must be 0 or 1");
         }
-        if (pc->opts.reserved[3] < 0 || pc->opts.reserved[3] > 2) {
-            delete pc;
-            fail(SG_ERR_INVALID_ARG, "level loop (reserved[3]) must be 0, 1 or 2");
-        }
         const int sd = pc->opts.sweep_dtype, fd = pc->opts.factor_dtype;
         const bool ok = (sd == SG_FP64 && fd == SG_FP64) ||
                         (sd == SG_FP32 && (fd == SG_FP32 || fd == SG_BF16));

@@ -262,62 +262,6 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
     }
 }
 
-// ---- fixed-width level loop (the stencils' W = 2, 3, 4 on both triangles).
-// One record row in registers: its slot, columns, values and diagonal.
-template <int W, class TF>
-struct RowRec {
-    uint32_t r;
-    uint32_t c[W];
-    TF v[W];
-    TF d;
-};
-
-// loads row q of the record at shared address R (C padded rows); only the
-// first NW entries are used (NW <= W: the forward or backward width)
-template <int NW, bool BACK, int W, class TF>
-__device__ __forceinline__ void rec_load(RowRec<W, TF>& o, uint32_t R, int C, int q) {
-    constexpr uint32_t SF = sizeof(TF);
-    const uint32_t cs = 2u * (uint32_t)C;
-    const uint32_t rq = R + 2u * (uint32_t)q;
-    o.r = lds_u16(rq);
-#pragma unroll
-    for (int k = 0; k < NW; ++k) o.c[k] = lds_u16(rq + cs * (uint32_t)(k + 1));
-    const uint32_t vq = R + cs * (uint32_t)(1 + NW) + SF * (uint32_t)q;
-    const uint32_t vs = SF * (uint32_t)C;
-#pragma unroll
-    for (int k = 0; k < NW; ++k) o.v[k] = lds<TF>(vq + vs * (uint32_t)k);
-    if (BACK) o.d = lds<TF>(vq + vs * (uint32_t)NW);
-}
-
-// t[r] = (t[r] - sum_k v_k t[c_k]) (/ d): the reference row's order.  The
-// gathers of t are issued first; `between` runs before their values are
-// used (the next level's record loads go there, so their latency overlaps
-// the gathers' instead of adding to the level).
-template <int NW, bool BACK, class TS, bool EXACT, int W, class TF, class Between>
-__device__ __forceinline__ void rec_solve(const RowRec<W, TF>& o, uint32_t tb,
-                                          Between&& between) {
-    constexpr uint32_t ST = sizeof(TS);
-    TS acc = lds<TS>(tb + ST * o.r);
-    TS xk[NW];
-#pragma unroll
-    for (int k = 0; k < NW; ++k) xk[k] = lds<TS>(tb + ST * o.c[k]);
-    between();
-#pragma unroll
-    for (int k = 0; k < NW; ++k) acc = sub_mul<TS, EXACT>(acc, Load<TS>::f(o.v[k]), xk[k]);
-    if (BACK) acc = div_diag(acc, Load<TS>::f(o.d));
-    sts(tb + ST * o.r, acc);
-}
-template <int NW, bool BACK, class TS, bool EXACT, int W, class TF>
-__device__ __forceinline__ void rec_solve(const RowRec<W, TF>& o, uint32_t tb) {
-    rec_solve<NW, BACK, TS, EXACT>(o, tb, [] {});
-}
-
-// per-level word of the fixed-width loop: rows (16 bits), padded rows (16
-// bits), byte offset of the record inside its group's buffer (32 bits)
-__device__ __forceinline__ int meta_rows(uint64_t m) { return (int)(m & 0xffffu); }
-__device__ __forceinline__ int meta_pad(uint64_t m) { return (int)((m >> 16) & 0xffffu); }
-__device__ __forceinline__ uint32_t meta_off(uint64_t m) { return (uint32_t)(m >> 32); }
-
 struct RecArgs {
     const SubInfo* info;
     const int* order;
@@ -352,133 +296,12 @@ struct RecArgs {
     // (1: no record group 0 is copied; 2: no restriction is counted)
     long long wait_budget;
     int wait_test;
-    // level loop (comparison knob, opts.reserved[3]): 0 the fixed-width loop
-    // with the next record loaded beside the gathers, 1 the generic loop,
-    // 2 the fixed-width loop with the next record loaded before the barrier
-    int level_loop;
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
-}
-
-struct FixedLoop {
-    const uint64_t* meta;  // per-level words (meta_rows / meta_pad / meta_off)
-    uint64_t* bars;
-    uint32_t bufs_s, t_s;  // shared addresses of the record buffers and of t
-    int T, nf, NB, K, ngrp, gbytes, NC;
-    bool producer;
-};
-
-// The level loop for stencil width W on both triangles.  Per level: the rows
-// (the thread's first row from registers), the next level's first-row record
-// entries into registers (same buffer), one barrier.  At a group end the
-// producer refills the freed buffer; the next group's mbarrier is waited on
-// (bounded) after the barrier, and a failed wait travels in the next level's
-// barrier.  Returns false after a failed wait (error word set, the issued
-// copies drained, y untouched).
-template <bool PIPE, int W, class TS, class TF, bool EXACT, class Refill>
-__device__ __forceinline__ bool fixed_levels(const RecArgs& a, const FixedLoop& L,
-                                             Refill&& refill) {
-    const int tid = threadIdx.x;
-    int q = 0, b = 0, gstart = 0, gend = L.T < L.K ? L.T : L.K;
-    uint32_t ph = 0;
-    RowRec<W, TF> pre, nxt;
-    auto load_into = [&](RowRec<W, TF>& dst, uint64_t m, int g, int buf) {
-        if (tid < meta_rows(m)) {
-            const uint32_t R = L.bufs_s + (uint32_t)buf * (uint32_t)L.gbytes + meta_off(m);
-            if (g >= L.nf) rec_load<W, true>(dst, R, meta_pad(m), tid);
-            else rec_load<W, false>(dst, R, meta_pad(m), tid);
-        }
-    };
-    bool ok = L.T == 0 || mbar_wait(smem_u32(&L.bars[0]), 0u, a.wait_budget);
-    uint64_t mw = L.T > 0 ? L.meta[0] : 0;
-    if (ok && L.T > 0) load_into(pre, mw, 0, 0);
-    for (int g = 0; g < L.T; ++g) {
-        const uint64_t mwn = g + 1 < L.T ? L.meta[g + 1] : 0;
-        const bool group_end = g + 1 == gend;
-        // PIPE: the next level's record (same buffer) loads while this
-        // level's gathers are in flight; without PIPE it loads after the
-        // level's rows, before the barrier
-        const bool next_here = ok && !group_end && g + 1 < L.T;
-        bool next_done = false;
-        auto between = [&] {
-            if (PIPE && next_here) {
-                load_into(nxt, mwn, g + 1, b);
-                next_done = true;
-            }
-        };
-        if (ok) {
-            const int c = meta_rows(mw), C = meta_pad(mw);
-            const uint32_t R = L.bufs_s + (uint32_t)b * (uint32_t)L.gbytes + meta_off(mw);
-            if (g >= L.nf) {
-                if (tid < c) rec_solve<W, true, TS, EXACT>(pre, L.t_s, between);
-                for (int qq = tid + L.NC; qq < c; qq += L.NC) {
-                    RowRec<W, TF> o;
-                    rec_load<W, true>(o, R, C, qq);
-                    rec_solve<W, true, TS, EXACT>(o, L.t_s);
-                }
-            } else {
-                if (tid < c) rec_solve<W, false, TS, EXACT>(pre, L.t_s, between);
-                for (int qq = tid + L.NC; qq < c; qq += L.NC) {
-                    RowRec<W, TF> o;
-                    rec_load<W, false>(o, R, C, qq);
-                    rec_solve<W, false, TS, EXACT>(o, L.t_s);
-                }
-            }
-        }
-        if (next_here) {
-            if (next_done) pre = nxt;
-            else load_into(pre, mwn, g + 1, b);  // no row of this level here
-        }
-        if (g == gstart) {
-            if (__syncthreads_or(ok ? 0 : 1)) {
-                // a record group did not arrive in time: report, drain the
-                // copies issued (groups q .. q+NB-1), leave y alone; a drain
-                // wait that gives up too leaves with that copy outstanding
-                // (accepted only because it never arrives) and reports 2
-                if (L.producer) {
-                    int code = 1;
-                    int b2 = b;
-                    uint32_t p2 = ph;
-                    for (int h = q; h < L.ngrp && h < q + L.NB; ++h) {
-                        const bool issued = !(a.wait_test == 1 && h == 0);
-                        if (issued && !mbar_wait(smem_u32(&L.bars[b2]), p2, WAIT_CYCLES)) code = 2;
-                        if (++b2 == L.NB) {
-                            b2 = 0;
-                            p2 ^= 1u;
-                        }
-                    }
-                    atomicMax(a.err, code);
-                }
-                return false;
-            }
-        } else {
-            __syncthreads();
-        }
-        if (group_end) {
-            // buffer b is free again: refill it with group q + NB
-            if (L.producer && q + L.NB < L.ngrp) {
-                fence_proxy_async();
-                refill(q + L.NB, b);
-            }
-            ++q;
-            if (++b == L.NB) {
-                b = 0;
-                ph ^= 1u;
-            }
-            gstart = gend;
-            gend = gstart + L.K < L.T ? gstart + L.K : L.T;
-            if (g + 1 < L.T) {
-                ok = mbar_wait(smem_u32(&L.bars[b]), ph, a.wait_budget);
-                if (ok) load_into(pre, mwn, g + 1, b);
-            }
-        }
-        mw = mwn;
-    }
-    return true;
 }
 
 // mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
@@ -506,8 +329,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     // record offset (so the level loop touches global memory only through TMA)
     long long* m_off = reinterpret_cast<long long*>(
         reinterpret_cast<unsigned char*>(t) + (((size_t)a.t_len * sizeof(TS) + 15) & ~(size_t)15));
-    uint64_t* m_meta = reinterpret_cast<uint64_t*>(m_off + a.max_levels);
-    int* m_c = reinterpret_cast<int*>(m_meta + a.max_levels);
+    int* m_c = reinterpret_cast<int*>(m_off + a.max_levels);
     int* m_C = m_c + a.max_levels;
     for (int g = threadIdx.x; g < T; g += blockDim.x) {
         if (g < nf) {
@@ -523,13 +345,6 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
         }
     }
     __syncthreads();
-    // one word per level for the fixed-width loop: rows, padded rows, offset
-    // of its record inside its group's buffer
-    for (int g = threadIdx.x; g < T; g += blockDim.x) {
-        const long long rel = m_off[g] - m_off[(g / K) * K];
-        m_meta[g] = (uint64_t)(uint32_t)m_c[g] | ((uint64_t)(uint32_t)m_C[g] << 16) |
-                    ((uint64_t)rel << 32);
-    }
 
     const uint32_t bytes_f = (uint32_t)(2 + inf.wl * (2 + sf));
     const uint32_t bytes_b = (uint32_t)(2 + inf.wu * (2 + sf) + sf);
@@ -590,29 +405,6 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     // phase advance without divisions; the next level's row counts load while
     // this level computes.
     const uint32_t bufs_s = smem_u32(bufs), t_s = smem_u32(t);
-    // stencil widths (2, 3 or 4 on both triangles): the fixed-width loop,
-    // whose per-level path is only the gathers of t, the multiply-adds and
-    // one barrier -- its first row's record entries load into registers
-    // before the previous level's barrier
-    const int wfix = (a.level_loop != 1 && inf.wl == inf.wu && inf.wl >= 2 && inf.wl <= 4)
-                         ? inf.wl : 0;
-    if (wfix) {
-        FixedLoop L{m_meta, bars, bufs_s, t_s, T, nf, NB, K, ngrp, a.gbytes, NC, producer};
-        auto refill = [&](int qq, int bb) { issue(qq, bb); };
-        bool done = false;
-        if (a.level_loop == 2) {
-            if (wfix == 3) done = fixed_levels<false, 3, TS, TF, EXACT>(a, L, refill);
-            else if (wfix == 2) done = fixed_levels<false, 2, TS, TF, EXACT>(a, L, refill);
-            else done = fixed_levels<false, 4, TS, TF, EXACT>(a, L, refill);
-        } else {
-            if (wfix == 3) done = fixed_levels<true, 3, TS, TF, EXACT>(a, L, refill);
-            else if (wfix == 2) done = fixed_levels<true, 2, TS, TF, EXACT>(a, L, refill);
-            else done = fixed_levels<true, 4, TS, TF, EXACT>(a, L, refill);
-        }
-        if (!done) return;  // a record group did not arrive (reported, drained)
-        goto levels_done;
-    }
-    {
     int q = 0, b = 0, gstart = 0, gend = T < K ? T : K;
     uint32_t ph = 0;
     // level g's rows (c), padded rows (C) and record offset in its buffer
@@ -683,8 +475,6 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
         c = cn;
         C = Cn;
     }
-    }
-levels_done:
 
     if (coarse) {
         if (a.fuse) {
@@ -766,7 +556,6 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     a.err = pc->err_d.p;
     a.sub_on = pc->sub_on;
     a.wait_test = pc->wait_test;
-    a.level_loop = pc->opts.reserved[3];
     a.wait_budget = pc->wait_test ? WAIT_TEST_CYCLES : WAIT_CYCLES;
     return a;
 }
@@ -776,7 +565,7 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
 size_t sweep_smem_for(const sg_precond* pc, int nbuf, long long gbytes) {
     const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
     const size_t tbytes = ((size_t)pc->t_len * ts + 15) & ~(size_t)15;
-    return 128 + (size_t)nbuf * (size_t)gbytes + tbytes + (size_t)pc->max_levels * 24;
+    return 128 + (size_t)nbuf * (size_t)gbytes + tbytes + (size_t)pc->max_levels * 16;
 }
 size_t sweep_smem(const sg_precond* pc) {
     return sweep_smem_for(pc, pc->rec_depth, pc->rec_gbytes);

@@ -28,11 +28,10 @@ def to_sg(sg, A):
     return sg.CSRMatrix(A.nrows, A.ncols, A.row_ptr, A.col_idx, A.vals)
 
 
-def make_pc(sg, kind, nparts, overlap, part, fdt=None, sdt=None, sweep="tma", sweep_threads=0,
-            level_loop="auto"):
+def make_pc(sg, kind, nparts, overlap, part, fdt=None, sdt=None, sweep="tma", sweep_threads=0):
     fdt = sg.FP64 if fdt is None else fdt
     sdt = sg.FP64 if sdt is None else sdt
-    kw = {"sweep": sweep, "sweep_threads": sweep_threads, "level_loop": level_loop}
+    kw = {"sweep": sweep, "sweep_threads": sweep_threads}
     if kind == "jacobi":
         return sg.JacobiPrecond(sweep_dtype=sdt, **kw)
     if kind == "ilu0":
@@ -253,7 +252,7 @@ def test_apply_low_precision(sg, oracle, kind, dt):
 def test_sweep_variants_agree(sg, kind, dt):
     """The sync-free sweep, the level sweep (a barrier per level) and the
     TMA-fed level sweep -- at every block size the set-up autotuner may
-    pick, with each of its level loops -- compute the same thing: bit-exact
+    pick -- compute the same thing: bit-exact
     (same operations in the same order per row, coarse term summed in a
     block-size independent order), up to the atomic order of the ASM sums."""
     A = sg.make_varcoef_3d(20, 22, 18, 1.0, 5.0, 4)
@@ -262,12 +261,9 @@ def test_sweep_variants_agree(sg, kind, dt):
     fdt = {"fp64": sg.FP64, "fp32": sg.FP32, "bf16": sg.BF16}[dt]
     sdt = sg.FP64 if dt == "fp64" else sg.FP32
     ys = []
-    for sweep, threads, loop in (("tma", 0, "auto"), ("tma", 512, "auto"), ("tma", 256, "auto"),
-                                 ("tma", 128, "auto"), ("tma", 256, "generic"),
-                                 ("tma", 128, "prefetch"), ("level", 0, "auto"),
-                                 ("syncfree", 0, "auto")):
-        pc = make_pc(sg, kind, 12, 1, part, fdt, sdt, sweep=sweep, sweep_threads=threads,
-                     level_loop=loop)
+    for sweep, threads in (("tma", 0), ("tma", 512), ("tma", 256), ("tma", 128),
+                           ("level", 0), ("syncfree", 0)):
+        pc = make_pc(sg, kind, 12, 1, part, fdt, sdt, sweep=sweep, sweep_threads=threads)
         pc.setup(A)
         ch = pc.sweep_choice()
         assert ch["sweep"] == sweep
