@@ -73,12 +73,15 @@ typedef struct sg_precond_opts {
                          TMA-fed level sweep, 1 a level sweep reading factors
                          from global memory, 4 the sync-free sweep (per-row
                          ready flags); reserved[1]: threads per CTA of the
-                         TMA-fed sweep (128, 256 or 512; 0 = the fastest,
-                         timed at set-up); reserved[2]: two-level
+                         TMA-fed sweep (128, 256, 384 or 512; 0 = the
+                         fastest, timed at set-up); reserved[2]: two-level
                          preconditioners compute the coarse restriction
                          inside the TMA-fed sweep when all subdomains' CTAs
                          fit on the GPU at once (0), or in a kernel of its
-                         own (1; same results); other entries must be 0 */
+                         own (1; same results); reserved[3]: largest group
+                         of level records the TMA-fed sweep copies at once
+                         (0 = 8192 bytes, else a multiple of 16 in [1024,
+                         65536]; same results); other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;

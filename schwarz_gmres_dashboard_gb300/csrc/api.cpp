@@ -458,9 +458,15 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             pc->opts.sweep_dtype = SG_FP64;
         }
         const int swt = pc->opts.reserved[1];
-        if (!(swt == 0 || swt == 128 || swt == 256 || swt == 512)) {
+        if (!(swt == 0 || swt == 128 || swt == 256 || swt == 384 || swt == 512)) {
             delete pc;
-            fail(SG_ERR_INVALID_ARG, "sweep threads (reserved[1]) must be 0, 128, 256 or 512");
+            fail(SG_ERR_INVALID_ARG, "sweep threads (reserved[1]) must be 0, 128, 256, 384 or 512");
+        }
+        const int grb = pc->opts.reserved[3];
+        if (!(grb == 0 || (grb >= 1024 && grb <= 65536 && grb % 16 == 0))) {
+            delete pc;
+            fail(SG_ERR_INVALID_ARG,
+                 "record group bytes (reserved[3]) must be 0 or a multiple of 16 in [1024, 65536]");
         }
         if (pc->opts.reserved[2] != 0 && pc->opts.reserved[2] != 1) {
             delete pc;

@@ -61,6 +61,14 @@ struct DBuf {
         if (count) SG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
     }
     void upload(const std::vector<T>& v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+    // the same with `pad` zero elements after the data (room for vector loads
+    // that round a range out to 16 bytes)
+    void upload_padded(const std::vector<T>& v, size_t pad, cudaStream_t s) {
+        alloc(v.size() + pad);
+        if (pad) SG_CUDA(cudaMemsetAsync(p + v.size(), 0, pad * sizeof(T), s));
+        if (!v.empty())
+            SG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
     void zero(cudaStream_t s) {
         if (p) SG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
     }
@@ -313,9 +321,13 @@ struct sg_precond {
     // record [rows | columns | values (| diagonal)], rows padded to 8
     bool use_rec = false;
     bool use_sf = false;   // sync-free sweep (per-row ready flags)
-    int rec_depth = 0;               // ring buffers in shared memory (0: no TMA-fed sweep)
-    int rec_glev = 1;                // consecutive levels per buffer (one bulk copy)
-    long long rec_gbytes = 0;        // buffer size: the largest group of rec_glev records
+    int rec_depth = 0;               // 1 when the TMA-fed sweep is set up (0: not used)
+    long long ring_bytes = 0;        // its shared-memory record ring
+    long long ring_gmax = 0;         // largest record group it copies at once
+    // the ring schedule: per subdomain (RingSub, as bytes), per level (int4
+    // as 4 ints), per record group (int2 as 2 ints)
+    std::vector<unsigned char> h_ring_sub;
+    std::vector<int> h_ring_meta, h_ring_grp;
     int sweep_threads = 0;           // threads per CTA of the TMA-fed sweep
     bool fuse_restrict = false;      // two-level: restriction inside the sweep (all CTAs resident)
     sg::DBuf<unsigned> coarse_sync;  // its arrival / departure counters
@@ -342,6 +354,8 @@ struct sg_precond {
     sg::DBuf<long long> rec_off_f_d, rec_off_b_d;
     sg::DBuf<int> rec_rows_f_d, rec_rows_b_d;
     sg::DBuf<unsigned char> rec_d;
+    sg::DBuf<unsigned char> ring_sub_d;
+    sg::DBuf<int> ring_meta_d, ring_grp_d;
     sg::DBuf<int> err_d;  // device error word of the sweeps (bounded waits)
     int wait_test = 0;     // sg_precond_set_wait_test mode (0: normal)
     sg::DBuf<double> gscratch64;

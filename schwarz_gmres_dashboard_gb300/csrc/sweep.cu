@@ -11,17 +11,21 @@
 //   [row slot u16 x C][column slot u16 x C x w][value x C x w](diagonal x C)
 // (C = rows rounded up to 8; a slot is the row's place in the shared-memory
 // vector, tslot, whose per-subdomain padding keeps the rows of a level in
-// distinct banks).  A subdomain's records are contiguous (forward levels,
-// then backward), so the ring holds groups of K consecutive records: the
-// block's last thread copies a whole group into one of NB shared-memory
-// buffers with one cp.async.bulk, tracked by one mbarrier, NB - 1 groups
-// ahead of the group being computed.  So a level costs shared-memory latency
-// plus one barrier instead of a global-memory round trip, and the copy issue
-// and the waits are paid once per K levels.  Every mbarrier wait is bounded
-// (about one second of clock cycles); on expiry the CTA records an error
-// word, waits (bounded again) for the copies it issued, and returns without
-// touching the output.
+// distinct banks).  A subdomain's records form one stream (forward levels,
+// then backward) that flows through a shared-memory byte ring in groups of
+// whole levels: the block's last thread copies a group with one
+// cp.async.bulk tracked by an mbarrier, as far ahead as the ring allows (at
+// 128^3 all CTAs together stream ~120 MB of records per apply, so the copies
+// need tens of KB in flight each).  Where each group lands in the ring and
+// after which level it may be issued is a static schedule computed at
+// set-up, which also checks that no level can wait for a copy not yet
+// issued.  A level costs shared-memory latency plus one barrier; the width
+// of the rows is a template parameter of each sweep direction's loop.  Every
+// mbarrier wait is bounded (about one second of clock cycles); on expiry
+// the CTA records an error word, waits (bounded again) for the copies it
+// issued, and returns without touching the output.
 #include <algorithm>
+#include <type_traits>
 
 #include "dev_common.cuh"
 #include "kernels.h"
@@ -262,25 +266,160 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
     }
 }
 
+// ---- the gather and the restricted scatter of the TMA-fed sweep.  Both
+// read a subdomain's index list (dofs; owned-local and owned-global lists)
+// with 16-byte loads, aligned down to the list's 16-byte line (set-up pads
+// every list by four entries, so the last load stays inside it), and each
+// thread issues all its loads of a round together: a cold gather costs a
+// few round trips instead of one per eight rows.
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+template <class T>
+__device__ __forceinline__ void cp_async_elt(uint32_t dst, const T* src) {
+    if constexpr (sizeof(T) == 8) cp_async8(dst, src);
+    else cp_async4(dst, src);
+}
+
+constexpr int GV = 4;  // 16-byte index loads per thread and round
+
+// t[tslot(li)] = x[dof[li]], li < n, for an input of the sweep's own type:
+// every element is copied global -> shared by cp.async (no register holds a
+// value, so all of a thread's copies are in flight at once).  The caller
+// waits with cp_async_wait_all.
+template <class T>
+__device__ __forceinline__ void gather_async(uint32_t t_s, const T* __restrict__ x,
+                                             const int* __restrict__ dof, int n, int bs, int p) {
+    const int head = (int)((reinterpret_cast<uintptr_t>(dof) >> 2) & 3);
+    const int4* v = reinterpret_cast<const int4*>(dof - head);
+    const int nv = (n + head + 3) >> 2;
+    for (int k0 = threadIdx.x; k0 < nv; k0 += GV * bs) {
+        int4 q[GV];
+#pragma unroll
+        for (int u = 0; u < GV; ++u)
+            if (k0 + u * bs < nv) q[u] = __ldg(v + k0 + u * bs);
+#pragma unroll
+        for (int u = 0; u < GV; ++u) {
+            const int k = k0 + u * bs;
+            if (k >= nv) break;
+            const int e[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int li = 4 * k + j - head;
+                if (li >= 0 && li < n)
+                    cp_async_elt<T>(t_s + (uint32_t)(sizeof(T) * tslot(li, p)), x + e[j]);
+            }
+        }
+    }
+}
+
+// Other input types convert through registers (the index loads as above).
+template <class TS, class TI>
+__device__ __forceinline__ void gather_convert(TS* t, const TI* __restrict__ x,
+                                               const int* __restrict__ dof, int n, int bs, int p) {
+    const int head = (int)((reinterpret_cast<uintptr_t>(dof) >> 2) & 3);
+    const int4* v = reinterpret_cast<const int4*>(dof - head);
+    const int nv = (n + head + 3) >> 2;
+    for (int k0 = threadIdx.x; k0 < nv; k0 += GV * bs) {
+        int4 q[GV];
+#pragma unroll
+        for (int u = 0; u < GV; ++u)
+            if (k0 + u * bs < nv) q[u] = __ldg(v + k0 + u * bs);
+        TI val[GV][4];
+#pragma unroll
+        for (int u = 0; u < GV; ++u) {
+            const int k = k0 + u * bs;
+            const int e[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int li = 4 * k + j - head;
+                val[u][j] = (k < nv && li >= 0 && li < n) ? x[e[j]] : (TI)0;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < GV; ++u)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int li = 4 * (k0 + u * bs) + j - head;
+                if (k0 + u * bs < nv && li >= 0 && li < n) t[tslot(li, p)] = Load<TS>::f(val[u][j]);
+            }
+    }
+}
+
+// y[og[q]] = t[tslot(ol[q])] (+ the coarse term), q < n_own; ol and og share
+// their offset, so one alignment serves both.
+template <class TS, class TO>
+__device__ __forceinline__ void scatter_vec(const TS* t, TO* __restrict__ y,
+                                            const int* __restrict__ ol, const int* __restrict__ og,
+                                            int n_own, int coarse, double zc, int bs, int p) {
+    const CoarseAdd<TO> add(zc);
+    const int head = (int)((reinterpret_cast<uintptr_t>(ol) >> 2) & 3);
+    const int4* vl = reinterpret_cast<const int4*>(ol - head);
+    const int4* vg = reinterpret_cast<const int4*>(og - head);
+    const int nv = (n_own + head + 3) >> 2;
+    for (int k0 = threadIdx.x; k0 < nv; k0 += GV * bs) {
+        int4 ql[GV], qg[GV];
+#pragma unroll
+        for (int u = 0; u < GV; ++u)
+            if (k0 + u * bs < nv) {
+                ql[u] = __ldg(vl + k0 + u * bs);
+                qg[u] = __ldg(vg + k0 + u * bs);
+            }
+#pragma unroll
+        for (int u = 0; u < GV; ++u) {
+            const int k = k0 + u * bs;
+            if (k >= nv) break;
+            const int l[4] = {ql[u].x, ql[u].y, ql[u].z, ql[u].w};
+            const int g[4] = {qg[u].x, qg[u].y, qg[u].z, qg[u].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int q = 4 * k + j - head;
+                if (q >= 0 && q < n_own) {
+                    const TS v = t[tslot(l[j], p)];
+                    y[g[j]] = coarse ? add(v) : Store<TO>::f(v);
+                }
+            }
+        }
+    }
+}
+
+// Static schedule of one subdomain's record stream through the ring: the
+// stream (forward records, then backward, contiguous from `base` in the
+// packed array) is cut into groups of whole levels, each copied by one
+// cp.async.bulk into a fixed ring position and tracked by mbarrier
+// (group % RING_NBAR).  Per level (int4): x = rows | padded rows << 16, y =
+// the record's byte offset in the ring, z = the group whose copy the level
+// waits for (its first level; -1 otherwise), w = the groups that may have
+// been issued once the level is done.  Per group (int2): x = stream offset,
+// y = bytes / 16 | ring position / 16 << 16.
+struct RingSub {
+    long long base;
+    int meta_off, grp_off, ngrp, ninit;
+};
+constexpr int RING_LOG_NBAR = 5;
+constexpr int RING_NBAR = 1 << RING_LOG_NBAR;
+
 struct RecArgs {
     const SubInfo* info;
     const int* order;
     const int* dofs;
-    const int* lev_f;
-    const int* lev_b;
-    const long long* off_f;
-    const long long* off_b;
-    const int* rows_f;
-    const int* rows_b;
+    const RingSub* ring;
+    const int4* meta;
+    const int2* grp;
     const unsigned char* rec;
     const int* ownloc;
     const int* owned;
     const double* a0inv;
     const double* r0;
     int nc;
-    int nbuf;     // record buffers in the ring
-    int glev;     // consecutive levels per buffer
-    int gbytes;   // buffer size
+    int a0pre;       // 1: the coarse row a0inv[s] is prefetched into shared memory
+    int ring_bytes;  // bytes of the record ring
     int t_len;       // elements of the subdomain vector region (largest tslot(n) + 1)
     int max_levels;  // largest nlev_f + nlev_b over the subdomains
     int* err;
@@ -293,7 +432,7 @@ struct RecArgs {
     unsigned* sync;
     // bounded waits: cycle budget of the record and restriction waits, and
     // the test mode that makes one of them run out without any fault
-    // (1: no record group 0 is copied; 2: no restriction is counted)
+    // (1: record group 0 is never copied; 2: no restriction is counted)
     long long wait_budget;
     int wait_test;
 };
@@ -302,6 +441,120 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+
+// The ring side of the level loop.  Set-up has checked that every group is
+// issued (after the level its schedule names) before its first level waits
+// for it, and that a group re-arms an mbarrier or overwrites ring bytes only
+// after every thread has observed, and finished with, the group before it.
+//
+// A wait that gives up marks the thread (bad: it computes no more rows) and
+// the block: the shared word fail takes the failing level + 1.  Every thread
+// reads it when it next opens a group and acts only on a failure at an
+// earlier level -- written before a barrier it has passed, so all threads
+// see it and leave at the same level, while a failure being recorded at the
+// current level by a faster thread is left for the next group -- and once
+// more after the last level.
+struct RecRing {
+    const unsigned char* src;
+    const int2* grp;       // shared memory
+    volatile int* fail;    // shared memory
+    uint32_t bars_s, ring_s;
+    long long budget;
+    int issued;    // producer: groups issued
+    int observed;  // groups this thread has seen complete
+    bool producer, bad;
+    int wait_test;
+
+    __device__ __forceinline__ uint32_t bar(int j) const {
+        return bars_s + 8u * (uint32_t)(j & (RING_NBAR - 1));
+    }
+    __device__ __forceinline__ void issue_to(int limit) {
+        if (issued >= limit) return;
+        fence_proxy_async();  // the ring bytes it overwrites were read by the generic proxy
+        do {
+            const int2 gi = grp[issued];
+            const uint32_t bytes = ((uint32_t)gi.y & 0xffffu) << 4;
+            const uint32_t pos = ((uint32_t)gi.y >> 16) << 4;
+            if (!(wait_test == 1 && issued == 0)) {
+                mbar_expect_tx(bar(issued), bytes);
+                bulk_g2s_stream(ring_s + pos, src + (uint32_t)gi.x, bytes, bar(issued));
+            }
+        } while (++issued < limit);
+    }
+    // the first try costs one mbarrier probe; the bounded loop (which reads
+    // the clock) runs only when the copy has not landed yet
+    __device__ __forceinline__ void wait_group(int j, int level) {
+        const uint32_t par = (uint32_t)(j >> RING_LOG_NBAR) & 1u;
+        if (mbar_try(bar(j), par) || mbar_wait(bar(j), par, budget)) {
+            observed = j + 1;
+        } else {
+            bad = true;
+            *fail = level + 1;
+        }
+    }
+    // the block leaves after a wait gave up: the producer waits (full budget
+    // each) for the copies it issued that it has not seen land, so none
+    // lands after the block has left; if one still does not arrive -- only
+    // possible when a copy never lands at all -- the error word says 2
+    __device__ void drain(int* err) const {
+        if (!producer) return;
+        int code = 1;
+        for (int k = observed; k < issued; ++k) {
+            if (wait_test == 1 && k == 0) continue;
+            if (!mbar_wait(bar(k), (uint32_t)(k >> RING_LOG_NBAR) & 1u, WAIT_CYCLES)) code = 2;
+        }
+        atomicMax(err, code);
+    }
+};
+
+// One sweep direction: levels [g0, g1), rows with W nonzeros per triangle
+// (W = 0: any width w).  Per level: the wait for the level's group when it
+// opens one, the rows, one barrier, then the producer issues the groups the
+// schedule allows.  The next level's metadata loads while this one
+// computes.  Returns false when the block leaves because a group did not
+// arrive within the wait budget.
+template <int W, bool BACK, class TS, class TF, bool EXACT>
+__device__ __forceinline__ bool level_loop(const int4* meta, int g0, int g1, int T, int w,
+                                           RecRing& ring, TS* t, uint32_t t_s,
+                                           unsigned char* ring_g, int NC, int* err) {
+    if (g0 >= g1) return true;
+    int4 md = meta[g0];
+    for (int g = g0; g < g1; ++g) {
+        int4 mn = md;
+        if (g + 1 < T) mn = meta[g + 1];
+        if (md.z >= 0) {
+            const int f = *ring.fail;
+            if (f != 0 && f <= g) {  // a wait at an earlier level gave up
+                ring.drain(err);
+                return false;
+            }
+            ring.wait_group(md.z, g);
+        }
+        if (!ring.bad) {
+            const int c = md.x & 0xffff, C = (int)((unsigned)md.x >> 16);
+            if constexpr (W > 0)
+                level_rows_w<W, BACK, TS, TF, EXACT>(t_s, ring.ring_s + (uint32_t)md.y, C, c, NC);
+            else
+                level_rows_any<TS, TF, EXACT>(t, ring_g + md.y, C, c, w, BACK, NC);
+        }
+        __syncthreads();
+        if (ring.producer) ring.issue_to(md.w);
+        md = mn;
+    }
+    return true;
+}
+
+template <bool BACK, class TS, class TF, bool EXACT>
+__device__ __forceinline__ bool level_loop_w(const int4* meta, int g0, int g1, int T, int w,
+                                             RecRing& ring, TS* t, uint32_t t_s,
+                                             unsigned char* ring_g, int NC, int* err) {
+    switch (w) {
+    case 2: return level_loop<2, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    case 3: return level_loop<3, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    case 4: return level_loop<4, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    default: return level_loop<0, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    }
 }
 
 // mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
@@ -314,68 +567,61 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     __shared__ double s_zc;
     __shared__ double s_red[RC_MAXCH];
     __shared__ int s_ok;
-    const int NB = a.nbuf, K = a.glev;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);              // NB x 8 B
+    __shared__ int s_fail;
+    constexpr uint32_t HDR = RING_NBAR * 8;
     const int NC = (int)blockDim.x;
-    unsigned char* bufs = smraw + 128;                                 // NB x gbytes
-    TS* t = reinterpret_cast<TS*>(bufs + (size_t)NB * a.gbytes);       // t_len
+    unsigned char* ringp = smraw + HDR;                                 // ring_bytes
+    TS* t = reinterpret_cast<TS*>(ringp + a.ring_bytes);                // t_len
+    int4* meta = reinterpret_cast<int4*>(
+        reinterpret_cast<unsigned char*>(t) + (((size_t)a.t_len * sizeof(TS) + 15) & ~(size_t)15));
+    int2* grp = reinterpret_cast<int2*>(meta + a.max_levels);
+    double* a0row = reinterpret_cast<double*>(grp + a.max_levels);  // nc when a0pre
     const int s = a.order[blockIdx.x];
     if (a.sub_on && !a.sub_on[s]) return;  // subdomain not needed by this apply
     const SubInfo inf = a.info[s];
+    const RingSub rs = a.ring[s];
     const int n = inf.n;
     const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
-    const int sf = (int)sizeof(TF);
-    // per-level metadata of both sweeps, staged once: rows, padded rows,
-    // record offset (so the level loop touches global memory only through TMA)
-    long long* m_off = reinterpret_cast<long long*>(
-        reinterpret_cast<unsigned char*>(t) + (((size_t)a.t_len * sizeof(TS) + 15) & ~(size_t)15));
-    int* m_c = reinterpret_cast<int*>(m_off + a.max_levels);
-    int* m_C = m_c + a.max_levels;
-    for (int g = threadIdx.x; g < T; g += blockDim.x) {
-        if (g < nf) {
-            const int i = inf.lev_off_f + g;
-            m_c[g] = a.lev_f[i + 1] - a.lev_f[i];
-            m_C[g] = a.rows_f[i];
-            m_off[g] = a.off_f[i];
-        } else {
-            const int i = inf.lev_off_b + (g - nf);
-            m_c[g] = a.lev_b[i + 1] - a.lev_b[i];
-            m_C[g] = a.rows_b[i];
-            m_off[g] = a.off_b[i];
-        }
+    // the schedule, staged once (the level loop touches global memory only
+    // through the ring)
+    for (int g = threadIdx.x; g < T; g += NC) meta[g] = a.meta[rs.meta_off + g];
+    for (int j = threadIdx.x; j < rs.ngrp; j += NC) grp[j] = a.grp[rs.grp_off + j];
+
+    RecRing ring;
+    ring.src = a.rec + rs.base;
+    ring.grp = grp;
+    ring.bars_s = smem_u32(smraw);
+    ring.ring_s = smem_u32(ringp);
+    ring.budget = a.wait_budget;
+    ring.fail = &s_fail;
+    ring.issued = 0;
+    ring.observed = 0;
+    ring.bad = false;
+    ring.wait_test = a.wait_test;
+    // the producer is the block's last thread: levels rarely have rows for
+    // it, so its copies overlap the other threads' work
+    ring.producer = threadIdx.x == blockDim.x - 1;
+    if (ring.producer) {
+        for (int i = 0; i < RING_NBAR; ++i) mbar_init(ring.bars_s + 8u * (uint32_t)i, 1);
+        fence_mbar_init();
+        s_fail = 0;
     }
     __syncthreads();
-
-    const uint32_t bytes_f = (uint32_t)(2 + inf.wl * (2 + sf));
-    const uint32_t bytes_b = (uint32_t)(2 + inf.wu * (2 + sf) + sf);
-    const int ngrp = (T + K - 1) / K;
-    // copy the records of group q (levels qK .. qK+K-1, contiguous) into
-    // buffer b with one bulk copy
-    auto issue = [&](int q, int b) {
-        const int g0 = q * K, g1 = (g0 + K < T ? g0 + K : T) - 1;
-        const uint32_t bytes = (uint32_t)(m_off[g1] - m_off[g0]) +
-                               (uint32_t)m_C[g1] * (g1 < nf ? bytes_f : bytes_b);
-        const uint32_t bar = smem_u32(&bars[b]);
-        mbar_expect_tx(bar, bytes);
-        bulk_g2s_stream(smem_u32(bufs + (size_t)b * a.gbytes), a.rec + m_off[g0], bytes, bar);
-    };
-
-    // the producer is the block's last thread: levels rarely have rows for
-    // it, so issuing the next copy overlaps the other threads' work (a
-    // separate producer warp, signalled through per-buffer "empty"
-    // mbarriers, measured slower at every block size)
-    const bool producer = threadIdx.x == blockDim.x - 1;
-    if (producer) {
-        for (int i = 0; i < NB; ++i) mbar_init(smem_u32(&bars[i]), 1);
-        fence_mbar_init();
-        fence_proxy_async();
-        for (int q = 0; q < ngrp && q < NB; ++q)
-            if (!(a.wait_test == 1 && q == 0)) issue(q, q);
-    }
-    // gather while the first records are in flight
+    if (ring.producer) ring.issue_to(rs.ninit);
+    // gather while the first records are in flight; with a coarse term the
+    // subdomain's row of the coarse inverse comes into shared memory with it
     const int* dof = a.dofs + inf.row_off;
     const int tp = inf.tshift;
-    gather_rows<TS>(t, x, dof, n, NC, tp);
+    if (coarse && a.a0pre && threadIdx.x < 32) {
+        const double* row = a.a0inv + (size_t)s * a.nc;
+        for (int q = threadIdx.x; q < a.nc; q += 32) cp_async8(smem_u32(a0row + q), row + q);
+    }
+    if constexpr (std::is_same<TI, TS>::value) {
+        gather_async<TS>(smem_u32(t), x, dof, n, NC, tp);
+    } else {
+        gather_convert<TS, TI>(t, x, dof, n, NC, tp);
+    }
+    cp_async_wait_all();
     if (threadIdx.x == 0) t[tslot(n, tp)] = (TS)0;
     if (coarse && a.fuse && (int)blockIdx.x >= (int)gridDim.x / 2) {
         // coarse restrictions (the order of k_restrict), published for the
@@ -397,83 +643,16 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
     __syncthreads();
 
-    // The level loop is the latency chain of the sweep.  Per level: the rows,
-    // then one barrier.  Per group of K levels: every thread observes the
-    // buffer's mbarrier (acquiring the bulk copy) at the first level, a
-    // failed wait travels in that level's barrier, and after the group's last
-    // level the producer refills the buffer with group q + NB.  Buffer and
-    // phase advance without divisions; the next level's row counts load while
-    // this level computes.
-    const uint32_t bufs_s = smem_u32(bufs), t_s = smem_u32(t);
-    int q = 0, b = 0, gstart = 0, gend = T < K ? T : K;
-    uint32_t ph = 0;
-    // level g's rows (c), padded rows (C) and record offset in its buffer
-    // (roff) are in registers; the next level's load during this level and
-    // are used after its barrier, so no shared-memory load heads a level
-    int c = T > 0 ? m_c[0] : 0, C = T > 0 ? m_C[0] : 0;
-    long long base_off = T > 0 ? m_off[0] : 0;
-    uint32_t roff = 0;
-    for (int g = 0; g < T; ++g) {
-        bool ok = true;
-        if (g == gstart) ok = mbar_wait(smem_u32(&bars[b]), ph, a.wait_budget);
-        int cn = 0, Cn = 0;
-        long long on = 0;
-        if (g + 1 < T) {
-            cn = m_c[g + 1];
-            Cn = m_C[g + 1];
-            on = m_off[g + 1];
-        }
-        if (ok) {
-            const bool back = g >= nf;
-            const uint32_t off = (uint32_t)b * (uint32_t)a.gbytes + roff;
-            level_rows<TS, TF, EXACT>(t, t_s, bufs + off, bufs_s + off, C, c,
-                                      back ? inf.wu : inf.wl, back, NC);
-        }
-        if (g == gstart) {
-            if (__syncthreads_or(ok ? 0 : 1)) {
-                // a record group did not arrive in time: report, drain the
-                // copies that were issued (groups q .. q+NB-1; the earlier
-                // ones have landed), leave y alone.  Each drain wait has the
-                // full budget; if one still gives up, the block leaves with
-                // that copy outstanding -- accepted only because such a copy
-                // never arrives at all -- and the error word says 2.
-                if (producer) {
-                    int code = 1;
-                    int b2 = b;
-                    uint32_t p2 = ph;
-                    for (int h = q; h < ngrp && h < q + NB; ++h) {
-                        const bool issued = !(a.wait_test == 1 && h == 0);
-                        if (issued && !mbar_wait(smem_u32(&bars[b2]), p2, WAIT_CYCLES)) code = 2;
-                        if (++b2 == NB) {
-                            b2 = 0;
-                            p2 ^= 1u;
-                        }
-                    }
-                    atomicMax(a.err, code);
-                }
-                return;
-            }
-        } else {
-            __syncthreads();
-        }
-        if (g + 1 == gend) {
-            // buffer b is free again: refill it with group q + NB
-            if (producer && q + NB < ngrp) {
-                fence_proxy_async();
-                issue(q + NB, b);
-            }
-            ++q;
-            if (++b == NB) {
-                b = 0;
-                ph ^= 1u;
-            }
-            gstart = gend;
-            gend = gstart + K < T ? gstart + K : T;
-            base_off = on;  // the next level opens the new group
-        }
-        roff = (uint32_t)(on - base_off);
-        c = cn;
-        C = Cn;
+    // the level loop -- the latency chain of the sweep -- one direction at a
+    // time, specialised on the row width
+    const uint32_t t_s = smem_u32(t);
+    if (!level_loop_w<false, TS, TF, EXACT>(meta, 0, nf, T, inf.wl, ring, t, t_s, ringp, NC, a.err))
+        return;
+    if (!level_loop_w<true, TS, TF, EXACT>(meta, nf, T, T, inf.wu, ring, t, t_s, ringp, NC, a.err))
+        return;
+    if (s_fail) {  // a wait in the last group gave up (read after the last level's barrier)
+        ring.drain(a.err);
+        return;
     }
 
     if (coarse) {
@@ -500,8 +679,9 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             }
         }
         if (threadIdx.x < 32) {
-            const double z = a.fuse ? coarse_dot_warp0<true>(a.a0inv + (size_t)s * a.nc, a.r0, a.nc)
-                                    : coarse_dot_warp0<false>(a.a0inv + (size_t)s * a.nc, a.r0, a.nc);
+            const double* row = a.a0pre ? a0row : a.a0inv + (size_t)s * a.nc;
+            const double z = a.fuse ? coarse_dot_warp0<true>(row, a.r0, a.nc)
+                                    : coarse_dot_warp0<false>(row, a.r0, a.nc);
             if (threadIdx.x == 0) {
                 s_zc = inf.cscale * z;
                 // the last block done with r0 resets the counters
@@ -515,8 +695,8 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
     const double zc = coarse ? s_zc : 0.0;
     if (mode == 0) {
-        scatter_owned<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
-                              coarse, zc, NC, tp);
+        scatter_vec<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
+                            coarse, zc, NC, tp);
     } else {
         for (int li = threadIdx.x; li < n; li += NC)
             atomicAdd(&y[dof[li]], Store<TO>::f(t[tslot(li, tp)]));
@@ -528,6 +708,8 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
 }
 
+bool sweep_a0_prefetch(const sg_precond* pc);
+
 RecArgs rec_args(sg_precond* pc, bool fuse) {
     RecArgs a;
     a.fuse = fuse ? 1 : 0;
@@ -536,21 +718,17 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     a.info = pc->info.p;
     a.order = pc->order.p;
     a.dofs = pc->dofs.p;
-    a.lev_f = pc->lev_ptr_f.p;
-    a.lev_b = pc->lev_ptr_b.p;
-    a.off_f = pc->rec_off_f_d.p;
-    a.off_b = pc->rec_off_b_d.p;
-    a.rows_f = pc->rec_rows_f_d.p;
-    a.rows_b = pc->rec_rows_b_d.p;
+    a.ring = reinterpret_cast<const RingSub*>(pc->ring_sub_d.p);
+    a.meta = reinterpret_cast<const int4*>(pc->ring_meta_d.p);
+    a.grp = reinterpret_cast<const int2*>(pc->ring_grp_d.p);
     a.rec = pc->rec_d.p;
     a.ownloc = pc->ownloc_d.p;
     a.owned = pc->owned_d.p;
     a.a0inv = pc->a0inv.p;
     a.r0 = pc->r0.p;
     a.nc = pc->nc;
-    a.nbuf = pc->rec_depth;
-    a.glev = pc->rec_glev;
-    a.gbytes = (int)pc->rec_gbytes;
+    a.a0pre = sweep_a0_prefetch(pc) ? 1 : 0;
+    a.ring_bytes = (int)pc->ring_bytes;
     a.t_len = pc->t_len;
     a.max_levels = pc->max_levels;
     a.err = pc->err_d.p;
@@ -560,16 +738,22 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     return a;
 }
 
-// dynamic shared memory of the sweep: mbarriers, nbuf record buffers of
-// gbytes, the subdomain vector, per-level metadata
-size_t sweep_smem_for(const sg_precond* pc, int nbuf, long long gbytes) {
+// two-level preconditioners with at most 1024 subdomains keep the
+// subdomain's row of the coarse inverse in shared memory
+bool sweep_a0_prefetch(const sg_precond* pc) {
+    return (pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS) &&
+           pc->nparts <= 1024;
+}
+
+// dynamic shared memory of the sweep: the mbarriers, the record ring, the
+// subdomain vector, per-level and per-group schedule entries, the coarse row
+size_t sweep_smem_for(const sg_precond* pc, long long ring_bytes) {
     const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
     const size_t tbytes = ((size_t)pc->t_len * ts + 15) & ~(size_t)15;
-    return 128 + (size_t)nbuf * (size_t)gbytes + tbytes + (size_t)pc->max_levels * 16;
+    const size_t a0 = sweep_a0_prefetch(pc) ? (size_t)pc->nparts * 8 : 0;
+    return RING_NBAR * 8 + (size_t)ring_bytes + tbytes + (size_t)pc->max_levels * (16 + 8) + a0;
 }
-size_t sweep_smem(const sg_precond* pc) {
-    return sweep_smem_for(pc, pc->rec_depth, pc->rec_gbytes);
-}
+size_t sweep_smem(const sg_precond* pc) { return sweep_smem_for(pc, pc->ring_bytes); }
 
 template <class TI, class TO, class TS, class TF, bool EXACT>
 void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active,
@@ -603,39 +787,122 @@ void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const
 
 }  // namespace
 
-void tune_sweep_threads(sg_precond* pc);
+void tune_sweep(sg_precond* pc, const std::vector<long long>& gmax_list);
 
-// Largest byte span of K consecutive level records of one subdomain (its
-// forward then backward records are contiguous in the packed array).
-static long long rec_group_max(const sg_precond* pc, int K) {
-    const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
-                         : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
-    long long mx = 0;
-    std::vector<long long> offs;
-    for (int s = 0; s < pc->nparts; ++s) {
-        const SubInfo& inf = pc->h_info[s];
-        const int T = inf.nlev_f + inf.nlev_b;
-        if (T == 0) continue;
-        offs.assign((size_t)T + 1, 0);
-        for (int l = 0; l < inf.nlev_f; ++l) offs[l] = pc->h_rec_off_f[inf.lev_off_f + l];
-        for (int l = 0; l < inf.nlev_b; ++l)
-            offs[inf.nlev_f + l] = pc->h_rec_off_b[inf.lev_off_b + l];
-        const long long last_rows = inf.nlev_b > 0
-                                        ? pc->h_rec_rows_b[inf.lev_off_b + inf.nlev_b - 1]
-                                        : pc->h_rec_rows_f[inf.lev_off_f + inf.nlev_f - 1];
-        const long long last_bytes = inf.nlev_b > 0 ? last_rows * (2 + inf.wu * (2 + sf) + sf)
-                                                    : last_rows * (2 + inf.wl * (2 + sf));
-        offs[T] = offs[T - 1] + last_bytes;
-        for (int g0 = 0; g0 < T; g0 += K) {
-            const int g1 = g0 + K < T ? g0 + K : T;
-            mx = std::max(mx, offs[g1] - offs[g0]);
-        }
-    }
-    return mx;
+static void ring_upload(sg_precond* pc) {
+    cudaStream_t st = pc->ctx->stream;
+    pc->ring_sub_d.upload(pc->h_ring_sub, st);
+    pc->ring_meta_d.upload(pc->h_ring_meta, st);
+    pc->ring_grp_d.upload(pc->h_ring_grp, st);
 }
 
-// Packs the level records of the configured factor type and sizes the
-// record ring so that as many subdomains as possible run at once.
+// Builds the static ring schedule of every subdomain (see RingSub) for a ring
+// of ring_bytes and groups of at most gmax bytes (a larger level is a group
+// of its own).  Groups are placed one after another and start over at the
+// ring's beginning when they would cross its end.  Group j may be issued
+// after the last level of every earlier group whose ring bytes it overwrites
+// and of group j - RING_NBAR (its mbarrier's previous user); the schedule is
+// feasible when that is always before group j's first level.  Returns false
+// (nothing kept) when it is not.
+static bool ring_schedule(sg_precond* pc, long long ring_bytes, long long gmax) {
+    const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
+                         : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
+    std::vector<RingSub> subs((size_t)pc->nparts);
+    std::vector<int> meta, grp;  // int4 / int2 entries as ints
+    std::vector<long long> rel, gstart, gbytes, gpos;
+    std::vector<int> B, cnt, padded, gfirst, glast, ia, upto;
+    for (int s = 0; s < pc->nparts; ++s) {
+        const SubInfo& inf = pc->h_info[s];
+        const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
+        rel.resize(T);
+        B.resize(T);
+        cnt.resize(T);
+        padded.resize(T);
+        for (int g = 0; g < T; ++g) {
+            if (g < nf) {
+                const int i = inf.lev_off_f + g;
+                rel[g] = pc->h_rec_off_f[i];
+                padded[g] = pc->h_rec_rows_f[i];
+                cnt[g] = pc->h_lev_ptr_f[i + 1] - pc->h_lev_ptr_f[i];
+                B[g] = (int)(padded[g] * (2 + inf.wl * (2 + sf)));
+            } else {
+                const int i = inf.lev_off_b + (g - nf);
+                rel[g] = pc->h_rec_off_b[i];
+                padded[g] = pc->h_rec_rows_b[i];
+                cnt[g] = pc->h_lev_ptr_b[i + 1] - pc->h_lev_ptr_b[i];
+                B[g] = (int)(padded[g] * (2 + inf.wu * (2 + sf) + sf));
+            }
+        }
+        RingSub& r = subs[s];
+        r.base = T > 0 ? rel[0] : 0;
+        r.meta_off = (int)(meta.size() / 4);
+        r.grp_off = (int)(grp.size() / 2);
+        for (int g = 0; g < T; ++g) rel[g] -= r.base;
+        // groups of whole levels
+        gfirst.clear();
+        glast.clear();
+        gstart.clear();
+        gbytes.clear();
+        for (int g = 0; g < T; ++g) {
+            if (gfirst.empty() || gbytes.back() + B[g] > gmax) {
+                gfirst.push_back(g);
+                glast.push_back(g);
+                gstart.push_back(rel[g]);
+                gbytes.push_back(B[g]);
+            } else {
+                glast.back() = g;
+                gbytes.back() = rel[g] + B[g] - gstart.back();
+            }
+        }
+        const int G = (int)gfirst.size();
+        gpos.assign(G, 0);
+        long long pos = 0;
+        for (int j = 0; j < G; ++j) {
+            if (gbytes[j] > ring_bytes || gbytes[j] >= (1ll << 20)) return false;
+            if (pos + gbytes[j] > ring_bytes) pos = 0;
+            gpos[j] = pos;
+            pos += gbytes[j];
+        }
+        ia.assign(G, -1);
+        int run = -1;
+        for (int j = 0; j < G; ++j) {
+            int v = -1;
+            for (int i = std::max(0, j - RING_NBAR); i < j; ++i)
+                if (gpos[i] < gpos[j] + gbytes[j] && gpos[j] < gpos[i] + gbytes[i])
+                    v = std::max(v, glast[i]);
+            if (j >= RING_NBAR) v = std::max(v, glast[j - RING_NBAR]);
+            run = std::max(run, v);
+            if (run >= gfirst[j]) return false;  // would wait for a copy not yet issued
+            ia[j] = run;
+        }
+        int ninit = 0;
+        while (ninit < G && ia[ninit] < 0) ++ninit;
+        r.ngrp = G;
+        r.ninit = ninit;
+        int jg = 0, ji = 0;
+        for (int g = 0; g < T; ++g) {
+            while (jg + 1 < G && gfirst[jg + 1] <= g) ++jg;
+            while (ji < G && ia[ji] <= g) ++ji;
+            meta.push_back(cnt[g] | (padded[g] << 16));
+            meta.push_back((int)(gpos[jg] + rel[g] - gstart[jg]));
+            meta.push_back(gfirst[jg] == g ? jg : -1);
+            meta.push_back(ji);
+        }
+        for (int j = 0; j < G; ++j) {
+            grp.push_back((int)gstart[j]);
+            grp.push_back((int)((gbytes[j] >> 4) | ((gpos[j] >> 4) << 16)));
+        }
+    }
+    pc->h_ring_sub.assign(reinterpret_cast<const unsigned char*>(subs.data()),
+                          reinterpret_cast<const unsigned char*>(subs.data() + subs.size()));
+    pc->h_ring_meta.swap(meta);
+    pc->h_ring_grp.swap(grp);
+    return true;
+}
+
+// Sizes the record ring (what the shared memory of the CTAs that must share
+// an SM leaves), builds its schedule, packs the level records in the
+// configured factor type and times the block size.
 void rec_setup_device(sg_precond* pc) {
     if (!pc->use_rec) return;
     sg_ctx* ctx = pc->ctx;
@@ -651,39 +918,36 @@ void rec_setup_device(sg_precond* pc) {
     const int static_smem = 1024;  // reduction scratch and the like
     // CTAs per SM needed to keep every subdomain resident at once
     const int want = (pc->nparts + ctx->num_sms - 1) / ctx->num_sms;
-    // ring: nbuf buffers, each holding K consecutive level records (a
-    // subdomain's records are contiguous: forward levels, then backward), so
-    // one bulk copy and one mbarrier serve K levels.  Prefer K*(nbuf-1)
-    // levels of lead (up to 8), then larger K, under the CTAs-per-SM budget.
-    int nbuf = 0, glev = 1;
-    long long gbytes = 0;
-    for (int per_sm = want < 1 ? 1 : want; per_sm >= 1 && nbuf == 0; --per_sm) {
-        const long long budget = (long long)sm_smem / per_sm - static_smem - 1024;
-        int best = -1;
-        for (int K : {8, 6, 4, 3, 2, 1}) {
-            const long long g = (rec_group_max(pc, K) + 127) & ~127ll;
-            for (int nb : {3, 2}) {
-                const long long need = (long long)sweep_smem_for(pc, nb, g);
-                if (need > budget || need > max_smem - static_smem) continue;
-                const int lead = (nb - 1) * K;
-                const int score = (lead < 8 ? lead : 8) * 10 + K;
-                if (score > best) {
-                    best = score;
-                    nbuf = nb;
-                    glev = K;
-                    gbytes = g;
+    // group size: opts.reserved[3] when set, else timed among 8 and 16 KB
+    // (never below the largest record)
+    std::vector<long long> gcand;
+    if (pc->opts.reserved[3] > 0) gcand.push_back(pc->opts.reserved[3]);
+    else gcand = {8192, 16384};
+    long long ring = 0;
+    std::vector<long long> gok;  // feasible group sizes for the chosen ring
+    for (int per_sm = want < 1 ? 1 : want; per_sm >= 1 && gok.empty(); --per_sm) {
+        const long long budget = std::min<long long>((long long)sm_smem / per_sm - static_smem - 1024,
+                                                     (long long)max_smem - static_smem);
+        ring = (budget - (long long)sweep_smem_for(pc, 0)) & ~15ll;
+        if (ring < pc->rec_stage_bytes) continue;
+        for (long long target : gcand) {
+            for (long long gmax : {target, target / 2, target / 4}) {
+                if (gmax < pc->rec_stage_bytes) gmax = pc->rec_stage_bytes;
+                if (ring_schedule(pc, ring, gmax)) {
+                    if (std::find(gok.begin(), gok.end(), gmax) == gok.end()) gok.push_back(gmax);
+                    break;
                 }
             }
         }
     }
-    // an mbarrier transaction count stays below 2^20 bytes
-    if (nbuf == 0 || gbytes >= (1 << 20) || (pc->opts.reserved[0] & 1)) {
+    if (gok.empty() || (pc->opts.reserved[0] & 1)) {
         pc->use_rec = false;
         return;
     }
-    pc->rec_depth = nbuf;
-    pc->rec_glev = glev;
-    pc->rec_gbytes = gbytes;
+    pc->ring_bytes = ring;
+    pc->rec_depth = 1;
+    pc->ring_gmax = gok.back();  // the schedule ring_schedule built last
+    ring_upload(pc);
     pc->rec_off_f_d.upload(pc->h_rec_off_f, st);
     pc->rec_off_b_d.upload(pc->h_rec_off_b, st);
     pc->rec_rows_f_d.upload(pc->h_rec_rows_f, st);
@@ -707,10 +971,10 @@ void rec_setup_device(sg_precond* pc) {
     // 3D subdomain hold ~100+ rows, those of a small 2D one ~20: a 512-thread
     // block then idles at every level barrier, while narrower blocks let more
     // subdomains run at once on an SM.
-    if (pc->opts.reserved[1] > 0) {
+    if (pc->opts.reserved[1] > 0 && gok.size() == 1) {
         pc->sweep_threads = pc->opts.reserved[1];
     } else {
-        tune_sweep_threads(pc);
+        tune_sweep(pc, gok);
     }
     // two-level: the coarse restriction runs inside the sweep when every
     // subdomain's CTA can be resident at once (a cooperative launch)
@@ -743,9 +1007,10 @@ bool sweep_fuses_restrict(const sg_precond* pc) {
     return pc->use_rec && pc->rec_depth > 0 && pc->fuse_restrict && !pc->sub_on;
 }
 
-// Times the sweep (RAS mode, no coarse term, zero input) with 128, 256 and
-// 512 threads per CTA and keeps the fastest.
-void tune_sweep_threads(sg_precond* pc) {
+// Times the sweep (RAS mode, no coarse term, zero input) for every record
+// group size in gmax_list and 128, 256, 384 and 512 threads per CTA (or the
+// forced block size) and keeps the fastest pair.
+void tune_sweep(sg_precond* pc, const std::vector<long long>& gmax_list) {
     sg_ctx* ctx = pc->ctx;
     cudaStream_t st = ctx->stream;
     const size_t n = (size_t)std::max(pc->n, 1);
@@ -770,31 +1035,42 @@ void tune_sweep_threads(sg_precond* pc) {
     cudaEvent_t e0, e1;
     SG_CUDA(cudaEventCreate(&e0));
     SG_CUDA(cudaEventCreate(&e1));
-    float best = 0.f;
+    float best = -1.f;
     int best_nt = SW_T;
-    for (int nt : {512, 256, 128}) {
-        pc->sweep_threads = nt;
-        run();
-        run();
-        cudaEventRecord(e0, st);
-        for (int r = 0; r < 5; ++r) run();
-        cudaEventRecord(e1, st);
-        cudaError_t e = cudaEventSynchronize(e1);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        if (e != cudaSuccess) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            SG_CUDA(e);
-        }
-        if (nt == 512 || ms < best) {
-            best = ms;
-            best_nt = nt;
+    long long best_g = gmax_list.front();
+    std::vector<int> threads = {512, 384, 256, 128};
+    if (pc->opts.reserved[1] > 0) threads = {pc->opts.reserved[1]};
+    for (long long gmax : gmax_list) {
+        if (!ring_schedule(pc, pc->ring_bytes, gmax)) continue;
+        ring_upload(pc);
+        for (int nt : threads) {
+            pc->sweep_threads = nt;
+            run();
+            run();
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < 5; ++r) run();
+            cudaEventRecord(e1, st);
+            cudaError_t e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                SG_CUDA(e);
+            }
+            if (best < 0.f || ms < best) {
+                best = ms;
+                best_nt = nt;
+                best_g = gmax;
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     pc->sweep_threads = best_nt;
+    pc->ring_gmax = best_g;
+    if (!ring_schedule(pc, pc->ring_bytes, best_g)) fail(SG_ERR_INTERNAL, "ring schedule lost");
+    ring_upload(pc);
 }
 
 template <class TI, class TO>
