@@ -183,6 +183,20 @@ sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc);
  * *threads the threads per CTA of the TMA-fed sweep (0 otherwise).  Either
  * pointer may be NULL. */
 sg_status sg_precond_get_sweep(sg_precond* pc, int* sweep, int* threads);
+/* Bytes of the TMA-fed sweep's shared-memory record ring and the largest
+ * group of level records it copies at once (0 and 0 without that sweep;
+ * no counterpart in the reference).  Either pointer may be NULL. */
+sg_status sg_precond_get_sweep_ring(sg_precond* pc, int* ring_bytes, int* group_bytes);
+/* Checked mode of the TMA-fed sweep (no counterpart in the reference, which
+ * has no debug checks): reads the level records back and checks on the host
+ * what bounds asserts in the kernel would -- every row and column slot inside
+ * the subdomain's shared vector, every column computed by an earlier level
+ * of its sweep, every record inside its ring group and the ring, every group
+ * issued before the level that waits for it and never over bytes or an
+ * mbarrier still in use.  *violations = 0 when all hold.  plant = 1 (tests
+ * of the check) first corrupts one column slot of the host copy.  0
+ * violations and SG_OK without that sweep. */
+sg_status sg_precond_check(sg_precond* pc, int plant, long long* violations);
 
 /* A preconditioner that is a caller's host function: FGMRES's flexible apply
  * (FlexApply / fgmres_flex, src/core/fgmres.h:37, src/core/fgmres.cpp:164-172)

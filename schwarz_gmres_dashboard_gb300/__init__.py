@@ -422,7 +422,8 @@ class Preconditioner:
     def __init__(self, nparts: int = 1, overlap: int = 0, partition=None,
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
                  ctx: Context | None = None, generic_sweep: bool = False,
-                 sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True):
+                 sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True,
+                 group_bytes: int = 0):
         # sweep variant (testing/comparison): "tma" (default: TMA-fed level
         # records), "level" (factors read from global memory), "syncfree"
         if generic_sweep:
@@ -446,6 +447,9 @@ class Preconditioner:
         # two-level: coarse restriction inside the TMA-fed sweep when all the
         # subdomains' CTAs fit at once (False: a kernel of its own; same bits)
         opts.reserved[2] = 0 if fuse_restrict else 1
+        # largest group of level records the TMA-fed sweep copies at once
+        # (0: 8 or 16 KB, timed at set-up; same results either way)
+        opts.reserved[3] = int(group_bytes)
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),
@@ -510,7 +514,18 @@ class Preconditioner:
         k, t = C.c_int(0), C.c_int(0)
         _check(_clib.sg_precond_get_sweep(self.handle, C.byref(k), C.byref(t)))
         kinds = {0: "tma", 1: "level", 2: "syncfree", -1: "none"}
-        return {"sweep": kinds[k.value], "threads": t.value}
+        rb, gb = C.c_int(0), C.c_int(0)
+        _check(_clib.sg_precond_get_sweep_ring(self.handle, C.byref(rb), C.byref(gb)))
+        return {"sweep": kinds[k.value], "threads": t.value, "ring_bytes": rb.value,
+                "group_bytes": gb.value}
+
+    def check(self, plant: bool = False) -> int:
+        """Checked mode of the TMA-fed sweep: the number of violated
+        invariants of its level records and ring schedule (0: all hold).
+        plant=True first corrupts one column slot of the host copy."""
+        v = C.c_longlong(-1)
+        _check(_clib.sg_precond_check(self.handle, 1 if plant else 0, C.byref(v)))
+        return v.value
 
     def set_wait_test(self, mode: int) -> None:
         """Test hook of the bounded device waits: 1 makes every sweep CTA's

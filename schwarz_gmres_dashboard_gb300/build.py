@@ -85,7 +85,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
                 if verbose and msg:
                     print(msg, file=sys.stderr)
     if todo or not os.path.exists(LIB):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs]
+        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -298,6 +298,7 @@ sg_status sg_ctx_synchronize(sg_ctx* ctx) {
 sg_status sg_csr_create(sg_ctx* ctx, int nrows, int ncols, int nnz, const int* row_ptr,
                         const int* col_idx, const double* vals, sg_mem mem, sg_csr** out) {
     return guard([&] {
+        sg::TraceRange trace("sg_csr_create");
         SG_CHECK_ARG(ctx && out, "NULL argument");
         *out = nullptr;
         SG_CHECK_ARG(nrows >= 0 && ncols >= 0 && nnz >= 0, "negative size");
@@ -506,6 +507,7 @@ uint64_t structure_key(const sg_precond* pc, const sg_csr* A, const int* part, i
 
 sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
     return guard([&] {
+        sg::TraceRange trace("sg_precond_setup");
         SG_CHECK_ARG(pc && A, "NULL argument");
         SG_CHECK_ARG(A->ctx == pc->ctx, "matrix and preconditioner belong to different contexts");
         use_device(pc->ctx);
@@ -562,6 +564,7 @@ sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
 
 sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg_mem mem) {
     return guard([&] {
+        sg::TraceRange trace("sg_precond_apply");
         SG_CHECK_ARG(pc && x && y, "NULL argument");
         if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
         SG_CHECK_ARG(n == pc->n, "n (%d) does not match the set-up size (%d)", n, pc->n);
@@ -704,6 +707,25 @@ sg_status sg_precond_get_coarse(sg_precond* pc, double* a0, int cap, int* nc) {
     });
 }
 
+sg_status sg_precond_get_sweep_ring(sg_precond* pc, int* ring_bytes, int* group_bytes) {
+    return guard([&] {
+        SG_CHECK_ARG(pc, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        const bool tma = pc->use_rec && pc->rec_depth > 0;
+        if (ring_bytes) *ring_bytes = tma ? (int)pc->ring_bytes : 0;
+        if (group_bytes) *group_bytes = tma ? (int)pc->ring_gmax : 0;
+    });
+}
+
+sg_status sg_precond_check(sg_precond* pc, int plant, long long* violations) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && violations, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        use_device(pc->ctx);
+        *violations = sg::sweep_check(pc, plant);
+    });
+}
+
 sg_status sg_precond_get_sweep(sg_precond* pc, int* sweep, int* threads) {
     return guard([&] {
         SG_CHECK_ARG(pc, "NULL argument");
@@ -720,6 +742,7 @@ sg_status sg_solve(sg_ctx* ctx, sg_solver solver, const sg_csr* A, sg_precond* p
                    const double* b, double* x, int n, sg_mem mem, const sg_solve_params* params,
                    sg_solve_result* result) {
     return guard([&] {
+        sg::TraceRange trace("sg_solve");
         SG_CHECK_ARG(ctx && A && b && x, "NULL argument");
         SG_CHECK_ARG(A->ctx == ctx, "matrix belongs to a different context");
         SG_CHECK_ARG(A->nrows == A->ncols, "the solvers need a square matrix");
@@ -777,6 +800,7 @@ sg_status sg_solve_batched(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsy
                            sg_mem mem, const sg_solve_params* params, sg_batch_result* results,
                            double* time_s) {
     return guard([&] {
+        sg::TraceRange trace("sg_solve_batched");
         SG_CHECK_ARG(ctx && A && b && x && sys_row_ptr, "NULL argument");
         SG_CHECK_ARG(A->ctx == ctx, "matrix belongs to a different context");
         SG_CHECK_ARG(A->nrows == A->ncols, "the solvers need a square matrix");
@@ -846,6 +870,7 @@ void check_analysis_args(sg_ctx* ctx, const sg_csr* A, sg_precond* pc) {
 sg_status sg_estimate_condition(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int k,
                                 unsigned seed, sg_condition_estimate* out) {
     return guard([&] {
+        sg::TraceRange trace("sg_estimate_condition");
         check_analysis_args(ctx, A, pc);
         SG_CHECK_ARG(out, "NULL argument");
         use_device(ctx);
@@ -857,6 +882,7 @@ sg_status sg_estimate_spectral_radius(sg_ctx* ctx, const sg_csr* A, sg_precond* 
                                       double tol, unsigned seed, double* eigenvector,
                                       sg_spectral_result* out) {
     return guard([&] {
+        sg::TraceRange trace("sg_estimate_spectral_radius");
         check_analysis_args(ctx, A, pc);
         SG_CHECK_ARG(out, "NULL argument");
         use_device(ctx);

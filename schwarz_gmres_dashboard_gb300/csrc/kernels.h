@@ -97,6 +97,7 @@ bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool e
                const int* active);
 // reads the sweeps' error word (0: none) and clears it
 int sweep_error(sg_precond* pc);
+long long sweep_check(sg_precond* pc, int plant);
 // whether sg_precond_set_wait_test's mode applies to this set-up
 bool sweep_wait_test_supported(const sg_precond* pc, int mode);
 // the TMA sweep computes the coarse restriction itself (no k_restrict launch)

@@ -777,16 +777,16 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
     // ---- batched ILU(0): host structures -> device
     pc->info.upload(pc->h_info, st);
     pc->order.upload(pc->h_order, st);
-    pc->dofs.upload_padded(pc->sub, 4, st);
+    pc->dofs.upload(pc->sub, st);
     pc->lev_ptr_f.upload(pc->h_lev_ptr_f, st);
     pc->lev_ptr_b.upload(pc->h_lev_ptr_b, st);
     pc->lrp_d.upload(pc->lrp, st);
     pc->lci_d.upload(pc->lci, st);
     pc->ldiag_d.upload(pc->ldiag, st);
     pc->lmap_d.upload(pc->lmap, st);
-    pc->ownloc_d.upload_padded(pc->ownloc, 4, st);
+    pc->ownloc_d.upload(pc->ownloc, st);
     pc->owned_ptr_d.upload(pc->owned_ptr, st);
-    pc->owned_d.upload_padded(pc->owned, 4, st);
+    pc->owned_d.upload(pc->owned, st);
     
     if (pc->wide_cols) {
         pc->perm_f.upload(reinterpret_cast<const uint16_t*>(pc->h_perm_f32.data()),

@@ -11,6 +11,8 @@
 
 #include "sgmres.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace sg {
 
 // --------------------------------------------------------------- errors
@@ -35,6 +37,16 @@ void set_last_error(const char* msg);
     do {                                                                               \
         if (!(cond)) ::sg::fail(SG_ERR_INVALID_ARG, __VA_ARGS__);                      \
     } while (0)
+
+// NVTX range for the life of a scope (entry points, restart cycles): a
+// profiler or tracer attached to the process shows set-up, applies, solves
+// and cycles by name; without one the calls return at once.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // --------------------------------------------------------------- device buffers
 template <class T>
@@ -61,14 +73,6 @@ struct DBuf {
         if (count) SG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
     }
     void upload(const std::vector<T>& v, cudaStream_t s) { upload(v.data(), v.size(), s); }
-    // the same with `pad` zero elements after the data (room for vector loads
-    // that round a range out to 16 bytes)
-    void upload_padded(const std::vector<T>& v, size_t pad, cudaStream_t s) {
-        alloc(v.size() + pad);
-        if (pad) SG_CUDA(cudaMemsetAsync(p + v.size(), 0, pad * sizeof(T), s));
-        if (!v.empty())
-            SG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-    }
     void zero(cudaStream_t s) {
         if (p) SG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
     }

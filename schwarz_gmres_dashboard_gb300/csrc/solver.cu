@@ -303,6 +303,7 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     int cycles = 0;
     try {
         while (!done_at_start && cycles < prm.max_iter) {
+            TraceRange trace_cycle(use_graph ? "restart cycle (graph)" : "restart cycle");
             if (use_graph) {
                 SG_CUDA(cudaGraphLaunch(exec, ctx->stream));
                 ctx->launches += w->graph_nodes;

@@ -266,12 +266,11 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
     }
 }
 
-// ---- the gather and the restricted scatter of the TMA-fed sweep.  Both
-// read a subdomain's index list (dofs; owned-local and owned-global lists)
-// with 16-byte loads, aligned down to the list's 16-byte line (set-up pads
-// every list by four entries, so the last load stays inside it), and each
-// thread issues all its loads of a round together: a cold gather costs a
-// few round trips instead of one per eight rows.
+// ---- the gather and the restricted scatter of the TMA-fed sweep.  Rows are
+// spread over the threads (consecutive rows on consecutive lanes, so index
+// loads, element copies and stores stay coalesced) and each thread keeps
+// SW_ILP index loads in flight: a cold gather or scatter of ~9,000 rows
+// costs two or three memory round trips.
 __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -287,105 +286,46 @@ __device__ __forceinline__ void cp_async_elt(uint32_t dst, const T* src) {
     else cp_async4(dst, src);
 }
 
-constexpr int GV = 4;  // 16-byte index loads per thread and round
+constexpr int SW_ILP = 16;
 
 // t[tslot(li)] = x[dof[li]], li < n, for an input of the sweep's own type:
-// every element is copied global -> shared by cp.async (no register holds a
-// value, so all of a thread's copies are in flight at once).  The caller
-// waits with cp_async_wait_all.
+// every element is copied global -> shared by cp.async, so no register holds
+// a value and a thread's copies all stay in flight.  The caller waits with
+// cp_async_wait_all.
 template <class T>
 __device__ __forceinline__ void gather_async(uint32_t t_s, const T* __restrict__ x,
                                              const int* __restrict__ dof, int n, int bs, int p) {
-    const int head = (int)((reinterpret_cast<uintptr_t>(dof) >> 2) & 3);
-    const int4* v = reinterpret_cast<const int4*>(dof - head);
-    const int nv = (n + head + 3) >> 2;
-    for (int k0 = threadIdx.x; k0 < nv; k0 += GV * bs) {
-        int4 q[GV];
+    for (int li = threadIdx.x; li < n; li += SW_ILP * bs) {
+        int d[SW_ILP];
 #pragma unroll
-        for (int u = 0; u < GV; ++u)
-            if (k0 + u * bs < nv) q[u] = __ldg(v + k0 + u * bs);
+        for (int u = 0; u < SW_ILP; ++u) d[u] = li + u * bs < n ? __ldg(dof + li + u * bs) : -1;
 #pragma unroll
-        for (int u = 0; u < GV; ++u) {
-            const int k = k0 + u * bs;
-            if (k >= nv) break;
-            const int e[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int li = 4 * k + j - head;
-                if (li >= 0 && li < n)
-                    cp_async_elt<T>(t_s + (uint32_t)(sizeof(T) * tslot(li, p)), x + e[j]);
-            }
-        }
+        for (int u = 0; u < SW_ILP; ++u)
+            if (d[u] >= 0)
+                cp_async_elt<T>(t_s + (uint32_t)(sizeof(T) * tslot(li + u * bs, p)), x + d[u]);
     }
 }
 
-// Other input types convert through registers (the index loads as above).
-template <class TS, class TI>
-__device__ __forceinline__ void gather_convert(TS* t, const TI* __restrict__ x,
-                                               const int* __restrict__ dof, int n, int bs, int p) {
-    const int head = (int)((reinterpret_cast<uintptr_t>(dof) >> 2) & 3);
-    const int4* v = reinterpret_cast<const int4*>(dof - head);
-    const int nv = (n + head + 3) >> 2;
-    for (int k0 = threadIdx.x; k0 < nv; k0 += GV * bs) {
-        int4 q[GV];
-#pragma unroll
-        for (int u = 0; u < GV; ++u)
-            if (k0 + u * bs < nv) q[u] = __ldg(v + k0 + u * bs);
-        TI val[GV][4];
-#pragma unroll
-        for (int u = 0; u < GV; ++u) {
-            const int k = k0 + u * bs;
-            const int e[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int li = 4 * k + j - head;
-                val[u][j] = (k < nv && li >= 0 && li < n) ? x[e[j]] : (TI)0;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < GV; ++u)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int li = 4 * (k0 + u * bs) + j - head;
-                if (k0 + u * bs < nv && li >= 0 && li < n) t[tslot(li, p)] = Load<TS>::f(val[u][j]);
-            }
-    }
-}
-
-// y[og[q]] = t[tslot(ol[q])] (+ the coarse term), q < n_own; ol and og share
-// their offset, so one alignment serves both.
+// y[og[q]] = t[tslot(ol[q])] (+ the coarse term), q < n_own.
 template <class TS, class TO>
-__device__ __forceinline__ void scatter_vec(const TS* t, TO* __restrict__ y,
+__device__ __forceinline__ void scatter_ilp(const TS* t, TO* __restrict__ y,
                                             const int* __restrict__ ol, const int* __restrict__ og,
                                             int n_own, int coarse, double zc, int bs, int p) {
     const CoarseAdd<TO> add(zc);
-    const int head = (int)((reinterpret_cast<uintptr_t>(ol) >> 2) & 3);
-    const int4* vl = reinterpret_cast<const int4*>(ol - head);
-    const int4* vg = reinterpret_cast<const int4*>(og - head);
-    const int nv = (n_own + head + 3) >> 2;
-    for (int k0 = threadIdx.x; k0 < nv; k0 += GV * bs) {
-        int4 ql[GV], qg[GV];
+    for (int q = threadIdx.x; q < n_own; q += SW_ILP * bs) {
+        int l[SW_ILP], g[SW_ILP];
 #pragma unroll
-        for (int u = 0; u < GV; ++u)
-            if (k0 + u * bs < nv) {
-                ql[u] = __ldg(vl + k0 + u * bs);
-                qg[u] = __ldg(vg + k0 + u * bs);
-            }
-#pragma unroll
-        for (int u = 0; u < GV; ++u) {
-            const int k = k0 + u * bs;
-            if (k >= nv) break;
-            const int l[4] = {ql[u].x, ql[u].y, ql[u].z, ql[u].w};
-            const int g[4] = {qg[u].x, qg[u].y, qg[u].z, qg[u].w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int q = 4 * k + j - head;
-                if (q >= 0 && q < n_own) {
-                    const TS v = t[tslot(l[j], p)];
-                    y[g[j]] = coarse ? add(v) : Store<TO>::f(v);
-                }
-            }
+        for (int u = 0; u < SW_ILP; ++u) {
+            const bool in = q + u * bs < n_own;
+            l[u] = in ? __ldg(ol + q + u * bs) : -1;
+            g[u] = in ? __ldg(og + q + u * bs) : 0;
         }
+#pragma unroll
+        for (int u = 0; u < SW_ILP; ++u)
+            if (l[u] >= 0) {
+                const TS v = t[tslot(l[u], p)];
+                y[g[u]] = coarse ? add(v) : Store<TO>::f(v);
+            }
     }
 }
 
@@ -619,7 +559,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     if constexpr (std::is_same<TI, TS>::value) {
         gather_async<TS>(smem_u32(t), x, dof, n, NC, tp);
     } else {
-        gather_convert<TS, TI>(t, x, dof, n, NC, tp);
+        gather_rows<TS>(t, x, dof, n, NC, tp);
     }
     cp_async_wait_all();
     if (threadIdx.x == 0) t[tslot(n, tp)] = (TS)0;
@@ -695,7 +635,7 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
     const double zc = coarse ? s_zc : 0.0;
     if (mode == 0) {
-        scatter_vec<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
+        scatter_ilp<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
                             coarse, zc, NC, tp);
     } else {
         for (int li = threadIdx.x; li < n; li += NC)
@@ -1118,5 +1058,146 @@ template bool sweep_tma<double, float>(sg_precond*, const double*, float*, int, 
                                        const int*);
 template bool sweep_tma<float, float>(sg_precond*, const float*, float*, int, bool, bool,
                                       const int*);
+
+}  // namespace sg
+
+namespace sg {
+
+// Host check of the TMA-fed sweep's data -- what a debug build's bounds
+// asserts in the kernel would test, done on the host so that no check can
+// fault a GPU: the level records are read back and
+//  * every row slot of a level is a real row of the subdomain and every
+//    column slot a real row or the zero slot (all inside the shared vector);
+//  * every column a row reads was computed by an earlier level of the same
+//    sweep (forward: the lower triangle; backward: the upper), i.e. the level
+//    schedule respects the factor's dependences;
+//  * every level's record lies inside its group's ring bytes and inside the
+//    ring, each group is issued before the level that waits for it, and no
+//    group overwrites ring bytes or re-arms an mbarrier of a group that a
+//    later level still reads; each group's stream bytes match its records'
+//    packed offsets.
+// plant = 1 (testing) first corrupts one column slot of the host copy.
+// Returns the number of violations found (0: all hold).
+long long sweep_check(sg_precond* pc, int plant) {
+    if (!pc->use_rec || pc->rec_depth == 0) return 0;
+    cudaStream_t st = pc->ctx->stream;
+    std::vector<unsigned char> rec((size_t)pc->rec_total);
+    SG_CUDA(cudaMemcpyAsync(rec.data(), pc->rec_d.p, rec.size(), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
+                         : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
+    const RingSub* subs = reinterpret_cast<const RingSub*>(pc->h_ring_sub.data());
+    const int* meta = pc->h_ring_meta.data();
+    const int* grp = pc->h_ring_grp.data();
+    long long bad = 0;
+    bool planted = false;
+    std::vector<char> done;
+    std::vector<int> last_level, first_level;
+    for (int s = 0; s < pc->nparts; ++s) {
+        const SubInfo& inf = pc->h_info[s];
+        const RingSub& r = subs[s];
+        const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b, n = inf.n, p = inf.tshift;
+        const int zero_slot = tslot(n, p);
+        // slot -> is it a real row
+        std::vector<char> real((size_t)zero_slot + 1, 0);
+        for (int li = 0; li < n; ++li) real[tslot(li, p)] = 1;
+        // ---- records: bounds and dependences
+        for (int dir = 0; dir < 2; ++dir) {
+            done.assign((size_t)zero_slot + 1, 0);
+            const int w = dir == 0 ? inf.wl : inf.wu;
+            const int nl = dir == 0 ? inf.nlev_f : inf.nlev_b;
+            for (int l = 0; l < nl; ++l) {
+                const int i = (dir == 0 ? inf.lev_off_f : inf.lev_off_b) + l;
+                const int c = dir == 0 ? pc->h_lev_ptr_f[i + 1] - pc->h_lev_ptr_f[i]
+                                       : pc->h_lev_ptr_b[i + 1] - pc->h_lev_ptr_b[i];
+                const int C = dir == 0 ? pc->h_rec_rows_f[i] : pc->h_rec_rows_b[i];
+                const long long off = dir == 0 ? pc->h_rec_off_f[i] : pc->h_rec_off_b[i];
+                const long long bytes = (long long)C * (2 + w * (2 + sf) + (dir ? sf : 0));
+                if (C % 8 || c > C || off < 0 || off + bytes > pc->rec_total) {
+                    ++bad;
+                    continue;
+                }
+                uint16_t* rows = reinterpret_cast<uint16_t*>(rec.data() + off);
+                uint16_t* cols = rows + C;
+                if (plant && !planted && l > 0 && c > 0 && w > 0) {
+                    cols[0] = (uint16_t)rows[0];  // a row reading itself: not yet computed
+                    planted = true;
+                }
+                for (int q = 0; q < c; ++q) {
+                    const int rs = rows[q];
+                    if (rs >= zero_slot || !real[rs]) {
+                        ++bad;
+                        continue;
+                    }
+                    for (int k = 0; k < w; ++k) {
+                        const int cs = cols[(size_t)k * C + q];
+                        if (cs > zero_slot) ++bad;
+                        else if (cs != zero_slot && (!real[cs] || !done[cs])) ++bad;
+                    }
+                }
+                for (int q = 0; q < c; ++q)
+                    if (rows[q] < zero_slot) done[rows[q]] = 1;
+            }
+        }
+        // ---- ring schedule: simulate the producer and the level loop
+        const int G = r.ngrp;
+        last_level.assign(G, -1);
+        first_level.assign(G, -1);
+        int cur = -1;
+        for (int g = 0; g < T; ++g) {
+            const int* m = meta + 4 * ((size_t)r.meta_off + g);
+            if (m[2] >= 0) {
+                if (m[2] != cur + 1) ++bad;  // groups open in order
+                cur = m[2];
+                first_level[cur] = g;
+            }
+            if (cur < 0 || cur >= G) {
+                ++bad;
+                break;
+            }
+            last_level[cur] = g;
+        }
+        int issued = r.ninit;
+        if (issued > G) ++bad;
+        for (int g = 0; g < T && cur >= 0; ++g) {
+            const int* m = meta + 4 * ((size_t)r.meta_off + g);
+            int j = 0;
+            while (j + 1 < G && first_level[j + 1] >= 0 && first_level[j + 1] <= g) ++j;
+            const int c = m[0] & 0xffff, C = (int)((unsigned)m[0] >> 16);
+            const bool back = g >= nf;
+            const int i = back ? inf.lev_off_b + (g - nf) : inf.lev_off_f + g;
+            const long long B = (long long)C * (back ? 2 + inf.wu * (2 + sf) + sf : 2 + inf.wl * (2 + sf));
+            const long long rel = (back ? pc->h_rec_off_b[i] : pc->h_rec_off_f[i]) - r.base;
+            const int* gj = grp + 2 * ((size_t)r.grp_off + j);
+            const long long gstart = (unsigned)gj[0];
+            const long long gbytes = (long long)(((unsigned)gj[1] & 0xffffu) << 4);
+            const long long gpos = (long long)(((unsigned)gj[1] >> 16) << 4);
+            if (c != (back ? pc->h_lev_ptr_b[i + 1] - pc->h_lev_ptr_b[i]
+                           : pc->h_lev_ptr_f[i + 1] - pc->h_lev_ptr_f[i]))
+                ++bad;
+            if (m[1] < gpos || m[1] + B > gpos + gbytes || m[1] + B > pc->ring_bytes) ++bad;
+            if (rel - gstart != m[1] - gpos) ++bad;  // the ring copy holds this record
+            if (m[2] >= 0 && m[2] >= issued) ++bad;  // waits for a copy not yet issued
+            // issue after the level: what the new groups overwrite must be done
+            for (int k = issued; k < m[3] && k < G; ++k) {
+                const int* gk = grp + 2 * ((size_t)r.grp_off + k);
+                const long long kb = (long long)(((unsigned)gk[1] & 0xffffu) << 4);
+                const long long kp = (long long)(((unsigned)gk[1] >> 16) << 4);
+                for (int q = 0; q < k; ++q) {
+                    if (last_level[q] <= g) continue;  // finished: its bytes are free
+                    const int* gq = grp + 2 * ((size_t)r.grp_off + q);
+                    const long long qb = (long long)(((unsigned)gq[1] & 0xffffu) << 4);
+                    const long long qp = (long long)(((unsigned)gq[1] >> 16) << 4);
+                    if (kp < qp + qb && qp < kp + kb) ++bad;
+                }
+                if (k >= RING_NBAR && last_level[k - RING_NBAR] > g) ++bad;
+            }
+            if (m[3] > issued) issued = m[3];
+        }
+        if (issued != G && T > 0) ++bad;  // every group issued by the end
+    }
+    if (plant && !planted) ++bad;  // nothing to corrupt: report it as found
+    return bad;
+}
 
 }  // namespace sg
