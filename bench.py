@@ -961,7 +961,7 @@ def main():
     ap.add_argument("--fields", type=int, default=200, help="learned: training fields")
     ap.add_argument("--held-out", type=int, default=20, help="learned: held-out test fields")
     ap.add_argument("--epochs", type=int, default=20, help="learned: training epochs")
-    ap.add_argument("--sweep-threads", type=int, default=0, choices=[0, 128, 256, 512],
+    ap.add_argument("--sweep-threads", type=int, default=0, choices=[0, 128, 256, 384, 512],
                     help="cfg3: threads per CTA of the TMA-fed sweep (0: timed at set-up); "
                          "fixes the choice for profiler runs, where the timing is distorted")
     args = ap.parse_args()

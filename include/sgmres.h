@@ -80,8 +80,13 @@ typedef struct sg_precond_opts {
                          fit on the GPU at once (0), or in a kernel of its
                          own (1; same results); reserved[3]: largest group
                          of level records the TMA-fed sweep copies at once
-                         (0 = 8192 bytes, else a multiple of 16 in [1024,
-                         65536]; same results); other entries must be 0 */
+                         (0 = 8 or 16 KB, timed at set-up, else a multiple
+                         of 16 in [1024, 65536]; same results); reserved[4]:
+                         launch shape of the TMA-fed sweep (0 = timed, 1 one
+                         CTA per subdomain, 2 persistent: resident CTAs take
+                         subdomains largest first from a work counter, k > 2
+                         persistent with k CTAs at most; same results);
+                         other entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;

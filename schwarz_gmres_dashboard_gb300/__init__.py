@@ -423,7 +423,7 @@ class Preconditioner:
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
                  ctx: Context | None = None, generic_sweep: bool = False,
                  sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True,
-                 group_bytes: int = 0):
+                 group_bytes: int = 0, sweep_launch: str = "auto"):
         # sweep variant (testing/comparison): "tma" (default: TMA-fed level
         # records), "level" (factors read from global memory), "syncfree"
         if generic_sweep:
@@ -450,6 +450,11 @@ class Preconditioner:
         # largest group of level records the TMA-fed sweep copies at once
         # (0: 8 or 16 KB, timed at set-up; same results either way)
         opts.reserved[3] = int(group_bytes)
+        # launch shape of the TMA-fed sweep: "auto" (timed), "per_subdomain"
+        # (one CTA each), "persistent" (resident CTAs loop over subdomains)
+        # or an int k > 2 (persistent with at most k CTAs)
+        opts.reserved[4] = (int(sweep_launch) if isinstance(sweep_launch, int) else
+                            {"auto": 0, "per_subdomain": 1, "persistent": 2}[sweep_launch])
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),

@@ -463,6 +463,10 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             delete pc;
             fail(SG_ERR_INVALID_ARG, "sweep threads (reserved[1]) must be 0, 128, 256, 384 or 512");
         }
+        if (pc->opts.reserved[4] < 0) {
+            delete pc;
+            fail(SG_ERR_INVALID_ARG, "sweep launch shape (reserved[4]) must be >= 0");
+        }
         const int grb = pc->opts.reserved[3];
         if (!(grb == 0 || (grb >= 1024 && grb <= 65536 && grb % 16 == 0))) {
             delete pc;
@@ -712,8 +716,8 @@ sg_status sg_precond_get_sweep_ring(sg_precond* pc, int* ring_bytes, int* group_
         SG_CHECK_ARG(pc, "NULL argument");
         if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
         const bool tma = pc->use_rec && pc->rec_depth > 0;
-        if (ring_bytes) *ring_bytes = tma ? (int)pc->ring_bytes : 0;
-        if (group_bytes) *group_bytes = tma ? (int)pc->ring_gmax : 0;
+        if (ring_bytes) *ring_bytes = tma ? (int)pc->ring1.ring_bytes : 0;
+        if (group_bytes) *group_bytes = tma ? (int)pc->ring1.gmax : 0;
     });
 }
 

@@ -22,6 +22,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "dev_common.cuh"
@@ -676,6 +677,20 @@ void apply_pc_batched(sg_ctx* ctx, sg_precond* pc, const BatchDev& B, BatchWork*
         }
     } reset{pc};
     for (int rr = 0; rr < B.R; ++rr) {
+        // four right-hand sides through one sweep that reads each level
+        // record once for all of them (RAS with FP32 sweeps)
+        if constexpr (std::is_same<TV, float>::value) {
+            if (pc && rr + 4 <= B.R && pc->kind == SG_PC_RAS) {
+                const int* gsw = gate ? w->sub_on.p + (size_t)rr * pc->nparts : nullptr;
+                pc->sub_on = nullptr;
+                const bool done4 = first ? sweep_tma4<double, float>(pc, r64 + rr * N, out + rr * N, N, gsw)
+                                         : sweep_tma4<float, float>(pc, tin + rr * N, out + rr * N, N, gsw);
+                if (done4) {
+                    rr += 3;
+                    continue;
+                }
+            }
+        }
         if (gate) pc->sub_on = w->sub_on.p + (size_t)rr * pc->nparts;
         if (first) {
             if (pc && pc->kind != SG_PC_NONE)
@@ -904,6 +919,8 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
     B.notdone = w->notdone.p;
     B.m = m; B.I = I; B.S = S; B.R = R; B.N = N;
     B.tol = prm.tol; B.tol_kind = prm.tol_kind; B.max_iter = prm.max_iter;
+    // four right-hand sides per sweep: planned once per set-up, before any capture
+    if (fp32 && pc && R >= 4) sweep_plan4(pc);
     const auto t0 = std::chrono::high_resolution_clock::now();
     // b and x (device copies in the batch layout)
     if (w->b64.n < tot) w->b64.alloc(tot);

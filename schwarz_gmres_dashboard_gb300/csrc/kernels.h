@@ -97,6 +97,11 @@ bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool e
                const int* active);
 // reads the sweeps' error word (0: none) and clears it
 int sweep_error(sg_precond* pc);
+// four right-hand sides ld apart at once (RAS, FP32 sweeps); false: use four
+// single applies
+template <class TI, class TO>
+bool sweep_tma4(sg_precond* pc, const TI* x, TO* y, long long ld, const int* sub_on);
+bool sweep_plan4(sg_precond* pc);  // plans that sweep (outside stream capture)
 long long sweep_check(sg_precond* pc, int plant);
 // whether sg_precond_set_wait_test's mode applies to this set-up
 bool sweep_wait_test_supported(const sg_precond* pc, int mode);

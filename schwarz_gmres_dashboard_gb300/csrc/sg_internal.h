@@ -293,6 +293,26 @@ struct SubInfo {
 // level -- a fixed stride apart in a box subdomain -- fall in distinct banks.
 __host__ __device__ __forceinline__ int tslot(int r, int p) { return p ? r + (r >> p) : r; }
 
+// One way of streaming the level records through the TMA-fed sweep's
+// shared-memory ring: its size, the largest group of records copied at once,
+// the block size, whether CTAs loop over subdomains (persistent: grid CTAs
+// take subdomains from a work counter, largest first) and the static
+// schedule -- per subdomain (sub: RingSub records as bytes), per level (meta:
+// int4 as four ints), per record group (grp: int2 as two ints).
+struct RingPlan {
+    int R = 1;                 // right-hand sides interleaved in the shared vector
+    bool ready = false;
+    long long ring_bytes = 0;
+    long long gmax = 0;
+    int threads = 0;
+    int grid = 0;              // CTAs of a persistent launch (0: one CTA per subdomain)
+    std::vector<unsigned char> sub;
+    std::vector<int> meta, grp;
+    DBuf<unsigned char> sub_d;
+    DBuf<int> meta_d, grp_d;
+    DBuf<unsigned> work;       // persistent launches: next subdomain, CTAs done
+};
+
 }  // namespace sg
 
 struct sg_precond {
@@ -326,12 +346,10 @@ struct sg_precond {
     bool use_rec = false;
     bool use_sf = false;   // sync-free sweep (per-row ready flags)
     int rec_depth = 0;               // 1 when the TMA-fed sweep is set up (0: not used)
-    long long ring_bytes = 0;        // its shared-memory record ring
-    long long ring_gmax = 0;         // largest record group it copies at once
-    // the ring schedule: per subdomain (RingSub, as bytes), per level (int4
-    // as 4 ints), per record group (int2 as 2 ints)
-    std::vector<unsigned char> h_ring_sub;
-    std::vector<int> h_ring_meta, h_ring_grp;
+    // how the level records stream through the sweep's shared-memory ring,
+    // for one right-hand side at a time (ring1) and for four interleaved ones
+    // (ring4, planned when a batched solve first asks for it)
+    sg::RingPlan ring1, ring4;
     int sweep_threads = 0;           // threads per CTA of the TMA-fed sweep
     bool fuse_restrict = false;      // two-level: restriction inside the sweep (all CTAs resident)
     sg::DBuf<unsigned> coarse_sync;  // its arrival / departure counters
@@ -358,8 +376,6 @@ struct sg_precond {
     sg::DBuf<long long> rec_off_f_d, rec_off_b_d;
     sg::DBuf<int> rec_rows_f_d, rec_rows_b_d;
     sg::DBuf<unsigned char> rec_d;
-    sg::DBuf<unsigned char> ring_sub_d;
-    sg::DBuf<int> ring_meta_d, ring_grp_d;
     sg::DBuf<int> err_d;  // device error word of the sweeps (bounded waits)
     int wait_test = 0;     // sg_precond_set_wait_test mode (0: normal)
     sg::DBuf<double> gscratch64;

@@ -266,11 +266,91 @@ k_pack_rec(const SubInfo* __restrict__ info, const int* __restrict__ lrp,
     }
 }
 
+// ---- R right-hand sides at once (FP32 sweeps): the shared vector holds R
+// interleaved floats per slot, so every level record is read once for all of
+// them; the row arithmetic per right-hand side is the single-vector code's.
+template <int R>
+struct FVec;
+template <>
+struct FVec<2> {
+    __device__ __forceinline__ static void ld(uint32_t a, float (&v)[2]) {
+        asm volatile("ld.shared.v2.f32 {%0,%1}, [%2];" : "=f"(v[0]), "=f"(v[1]) : "r"(a) : "memory");
+    }
+    __device__ __forceinline__ static void st(uint32_t a, const float (&v)[2]) {
+        asm volatile("st.shared.v2.f32 [%0], {%1,%2};" ::"r"(a), "f"(v[0]), "f"(v[1]) : "memory");
+    }
+};
+template <>
+struct FVec<4> {
+    __device__ __forceinline__ static void ld(uint32_t a, float (&v)[4]) {
+        asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+                     : "r"(a)
+                     : "memory");
+    }
+    __device__ __forceinline__ static void st(uint32_t a, const float (&v)[4]) {
+        asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(a), "f"(v[0]), "f"(v[1]),
+                     "f"(v[2]), "f"(v[3])
+                     : "memory");
+    }
+};
+
+// W > 0: rows with W nonzeros per triangle; W = 0: any width w
+template <int W, bool BACK, class TF, int R>
+__device__ __forceinline__ void level_rows_mr(uint32_t tb, uint32_t Rr, int C, int c, int w,
+                                              int nthreads) {
+    constexpr uint32_t SF = sizeof(TF), ST = 4u * R;
+    const int ww = W > 0 ? W : w;
+    const uint32_t cstride = 2u * (uint32_t)C;
+    const uint32_t vbase = Rr + cstride * (uint32_t)(1 + ww);
+    const uint32_t vstride = SF * (uint32_t)C;
+    for (int q = threadIdx.x; q < c; q += nthreads) {
+        const uint32_t rq = Rr + 2u * (uint32_t)q;
+        const uint32_t vq = vbase + SF * (uint32_t)q;
+        const uint32_t r = lds_u16(rq);
+        float acc[R];
+        FVec<R>::ld(tb + ST * r, acc);
+        if constexpr (W > 0) {
+            uint32_t ck[W];
+            TF vk[W];
+#pragma unroll
+            for (int k = 0; k < W; ++k) ck[k] = lds_u16(rq + cstride * (uint32_t)(k + 1));
+#pragma unroll
+            for (int k = 0; k < W; ++k) vk[k] = lds<TF>(vq + vstride * (uint32_t)k);
+            float xk[W][R];
+#pragma unroll
+            for (int k = 0; k < W; ++k) FVec<R>::ld(tb + ST * ck[k], xk[k]);
+#pragma unroll
+            for (int k = 0; k < W; ++k) {
+                const float v = Load<float>::f(vk[k]);
+#pragma unroll
+                for (int i = 0; i < R; ++i) acc[i] = fmaf(-v, xk[k][i], acc[i]);
+            }
+        } else {
+            for (int k = 0; k < ww; ++k) {
+                const uint32_t ci = lds_u16(rq + cstride * (uint32_t)(k + 1));
+                const float v = Load<float>::f(lds<TF>(vq + vstride * (uint32_t)k));
+                float xv[R];
+                FVec<R>::ld(tb + ST * ci, xv);
+#pragma unroll
+                for (int i = 0; i < R; ++i) acc[i] = fmaf(-v, xv[i], acc[i]);
+            }
+        }
+        if (BACK) {
+            const float rd = 1.0f / Load<float>::f(lds<TF>(vq + vstride * (uint32_t)ww));
+#pragma unroll
+            for (int i = 0; i < R; ++i) acc[i] = acc[i] * rd;
+        }
+        FVec<R>::st(tb + ST * r, acc);
+    }
+}
+
 // ---- the gather and the restricted scatter of the TMA-fed sweep.  Rows are
 // spread over the threads (consecutive rows on consecutive lanes, so index
 // loads, element copies and stores stay coalesced) and each thread keeps
 // SW_ILP index loads in flight: a cold gather or scatter of ~9,000 rows
-// costs two or three memory round trips.
+// costs two or three memory round trips.  With R right-hand sides, element
+// i of row li sits at x[i * ldx + dof[li]] and in slot component i.
 __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -288,43 +368,76 @@ __device__ __forceinline__ void cp_async_elt(uint32_t dst, const T* src) {
 
 constexpr int SW_ILP = 16;
 
-// t[tslot(li)] = x[dof[li]], li < n, for an input of the sweep's own type:
-// every element is copied global -> shared by cp.async, so no register holds
-// a value and a thread's copies all stay in flight.  The caller waits with
-// cp_async_wait_all.
-template <class T>
+// input of the sweep's own type: every element copied global -> shared by
+// cp.async (no register holds a value, so all of a thread's copies stay in
+// flight); the caller waits with cp_async_wait_all
+template <class T, int R>
 __device__ __forceinline__ void gather_async(uint32_t t_s, const T* __restrict__ x,
-                                             const int* __restrict__ dof, int n, int bs, int p) {
-    for (int li = threadIdx.x; li < n; li += SW_ILP * bs) {
-        int d[SW_ILP];
+                                             long long ldx, const int* __restrict__ dof, int n,
+                                             int bs, int p) {
+    constexpr int U = sizeof(T) == 8 ? SW_ILP / 2 : SW_ILP;
+    for (int li = threadIdx.x; li < n; li += U * bs) {
+        int d[U];
 #pragma unroll
-        for (int u = 0; u < SW_ILP; ++u) d[u] = li + u * bs < n ? __ldg(dof + li + u * bs) : -1;
+        for (int u = 0; u < U; ++u) d[u] = li + u * bs < n ? __ldg(dof + li + u * bs) : -1;
 #pragma unroll
-        for (int u = 0; u < SW_ILP; ++u)
-            if (d[u] >= 0)
-                cp_async_elt<T>(t_s + (uint32_t)(sizeof(T) * tslot(li + u * bs, p)), x + d[u]);
+        for (int u = 0; u < U; ++u)
+            if (d[u] >= 0) {
+                const uint32_t slot = t_s + (uint32_t)(sizeof(T) * R * tslot(li + u * bs, p));
+#pragma unroll
+                for (int i = 0; i < R; ++i)
+                    cp_async_elt<T>(slot + (uint32_t)(sizeof(T) * i), x + i * ldx + d[u]);
+            }
     }
 }
 
-// y[og[q]] = t[tslot(ol[q])] (+ the coarse term), q < n_own.
-template <class TS, class TO>
-__device__ __forceinline__ void scatter_ilp(const TS* t, TO* __restrict__ y,
+// other input types convert through registers
+template <class TS, class TI, int R>
+__device__ __forceinline__ void gather_convert(TS* t, const TI* __restrict__ x, long long ldx,
+                                               const int* __restrict__ dof, int n, int bs, int p) {
+    // values in flight per thread (U x R inputs held in registers)
+    constexpr int U = R > 1 ? 2 : (sizeof(TI) == 8 ? 4 : 8);
+    for (int li = threadIdx.x; li < n; li += U * bs) {
+        int d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) d[u] = li + u * bs < n ? __ldg(dof + li + u * bs) : -1;
+        TI v[U][R];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int i = 0; i < R; ++i) v[u][i] = d[u] >= 0 ? x[i * ldx + d[u]] : (TI)0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (d[u] >= 0)
+#pragma unroll
+                for (int i = 0; i < R; ++i)
+                    t[(size_t)R * tslot(li + u * bs, p) + i] = Load<TS>::f(v[u][i]);
+    }
+}
+
+// y[i * ldy + og[q]] = t[tslot(ol[q])][i] (+ the coarse term), q < n_own
+template <class TS, class TO, int R>
+__device__ __forceinline__ void scatter_ilp(const TS* t, TO* __restrict__ y, long long ldy,
                                             const int* __restrict__ ol, const int* __restrict__ og,
                                             int n_own, int coarse, double zc, int bs, int p) {
     const CoarseAdd<TO> add(zc);
-    for (int q = threadIdx.x; q < n_own; q += SW_ILP * bs) {
-        int l[SW_ILP], g[SW_ILP];
+    constexpr int U = sizeof(TO) == 8 ? SW_ILP / 2 : SW_ILP;
+    for (int q = threadIdx.x; q < n_own; q += U * bs) {
+        int l[U], g[U];
 #pragma unroll
-        for (int u = 0; u < SW_ILP; ++u) {
+        for (int u = 0; u < U; ++u) {
             const bool in = q + u * bs < n_own;
             l[u] = in ? __ldg(ol + q + u * bs) : -1;
             g[u] = in ? __ldg(og + q + u * bs) : 0;
         }
 #pragma unroll
-        for (int u = 0; u < SW_ILP; ++u)
+        for (int u = 0; u < U; ++u)
             if (l[u] >= 0) {
-                const TS v = t[tslot(l[u], p)];
-                y[g[u]] = coarse ? add(v) : Store<TO>::f(v);
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const TS v = t[(size_t)R * tslot(l[u], p) + i];
+                    y[i * ldy + g[u]] = coarse ? add(v) : Store<TO>::f(v);
+                }
             }
     }
 }
@@ -357,13 +470,21 @@ struct RecArgs {
     const int* owned;
     const double* a0inv;
     const double* r0;
+    int nparts;
     int nc;
     int a0pre;       // 1: the coarse row a0inv[s] is prefetched into shared memory
     int ring_bytes;  // bytes of the record ring
-    int t_len;       // elements of the subdomain vector region (largest tslot(n) + 1)
+    int t_len;       // slots of the subdomain vector region (largest tslot(n) + 1)
     int max_levels;  // largest nlev_f + nlev_b over the subdomains
+    long long ldx, ldy;  // distance between right-hand sides (R > 1)
     int* err;
-    const int* sub_on;  // optional per-subdomain switch (0: the subdomain is skipped)
+    // optional per-subdomain switches, one array of nparts per right-hand
+    // side (0: skipped; a subdomain runs when any of its R switches is on)
+    const int* sub_on;
+    // persistent launch: CTAs take subdomains (in `order`) from work[0];
+    // work[1] counts the CTAs that are done, and the last one resets both
+    int persist;
+    unsigned* work;
     // coarse restriction fused into the sweep (cooperative launch, all blocks
     // resident): each block writes r0[s] and counts itself in sync[0]; sync[1]
     // counts the blocks done with r0 (the last one resets both)
@@ -401,13 +522,19 @@ struct RecRing {
     volatile int* fail;    // shared memory
     uint32_t bars_s, ring_s;
     long long budget;
+    int gbase;     // groups this CTA streamed for earlier subdomains: group j
+                   // of this one uses mbarrier (gbase + j) % RING_NBAR with
+                   // phase parity ((gbase + j) / RING_NBAR) & 1
     int issued;    // producer: groups issued
     int observed;  // groups this thread has seen complete
     bool producer, bad;
     int wait_test;
 
     __device__ __forceinline__ uint32_t bar(int j) const {
-        return bars_s + 8u * (uint32_t)(j & (RING_NBAR - 1));
+        return bars_s + 8u * (uint32_t)((gbase + j) & (RING_NBAR - 1));
+    }
+    __device__ __forceinline__ uint32_t parity(int j) const {
+        return (uint32_t)((gbase + j) >> RING_LOG_NBAR) & 1u;
     }
     __device__ __forceinline__ void issue_to(int limit) {
         if (issued >= limit) return;
@@ -425,7 +552,7 @@ struct RecRing {
     // the first try costs one mbarrier probe; the bounded loop (which reads
     // the clock) runs only when the copy has not landed yet
     __device__ __forceinline__ void wait_group(int j, int level) {
-        const uint32_t par = (uint32_t)(j >> RING_LOG_NBAR) & 1u;
+        const uint32_t par = parity(j);
         if (mbar_try(bar(j), par) || mbar_wait(bar(j), par, budget)) {
             observed = j + 1;
         } else {
@@ -442,7 +569,7 @@ struct RecRing {
         int code = 1;
         for (int k = observed; k < issued; ++k) {
             if (wait_test == 1 && k == 0) continue;
-            if (!mbar_wait(bar(k), (uint32_t)(k >> RING_LOG_NBAR) & 1u, WAIT_CYCLES)) code = 2;
+            if (!mbar_wait(bar(k), parity(k), WAIT_CYCLES)) code = 2;
         }
         atomicMax(err, code);
     }
@@ -454,7 +581,7 @@ struct RecRing {
 // schedule allows.  The next level's metadata loads while this one
 // computes.  Returns false when the block leaves because a group did not
 // arrive within the wait budget.
-template <int W, bool BACK, class TS, class TF, bool EXACT>
+template <int W, bool BACK, class TS, class TF, bool EXACT, int R>
 __device__ __forceinline__ bool level_loop(const int4* meta, int g0, int g1, int T, int w,
                                            RecRing& ring, TS* t, uint32_t t_s,
                                            unsigned char* ring_g, int NC, int* err) {
@@ -473,7 +600,9 @@ __device__ __forceinline__ bool level_loop(const int4* meta, int g0, int g1, int
         }
         if (!ring.bad) {
             const int c = md.x & 0xffff, C = (int)((unsigned)md.x >> 16);
-            if constexpr (W > 0)
+            if constexpr (R > 1)
+                level_rows_mr<W, BACK, TF, R>(t_s, ring.ring_s + (uint32_t)md.y, C, c, w, NC);
+            else if constexpr (W > 0)
                 level_rows_w<W, BACK, TS, TF, EXACT>(t_s, ring.ring_s + (uint32_t)md.y, C, c, NC);
             else
                 level_rows_any<TS, TF, EXACT>(t, ring_g + md.y, C, c, w, BACK, NC);
@@ -485,67 +614,76 @@ __device__ __forceinline__ bool level_loop(const int4* meta, int g0, int g1, int
     return true;
 }
 
-template <bool BACK, class TS, class TF, bool EXACT>
+template <bool BACK, class TS, class TF, bool EXACT, int R>
 __device__ __forceinline__ bool level_loop_w(const int4* meta, int g0, int g1, int T, int w,
                                              RecRing& ring, TS* t, uint32_t t_s,
                                              unsigned char* ring_g, int NC, int* err) {
     switch (w) {
-    case 2: return level_loop<2, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
-    case 3: return level_loop<3, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
-    case 4: return level_loop<4, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
-    default: return level_loop<0, BACK, TS, TF, EXACT>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    case 2: return level_loop<2, BACK, TS, TF, EXACT, R>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    case 3: return level_loop<3, BACK, TS, TF, EXACT, R>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    case 4: return level_loop<4, BACK, TS, TF, EXACT, R>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
+    default: return level_loop<0, BACK, TS, TF, EXACT, R>(meta, g0, g1, T, w, ring, t, t_s, ring_g, NC, err);
     }
 }
 
-// mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).
-template <class TI, class TO, class TS, class TF, bool EXACT>
-__global__ void __launch_bounds__(SW_T, 2)
-k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, int coarse,
-            const int* __restrict__ active) {
-    if (active && *active == 0) return;
-    extern __shared__ __align__(128) unsigned char smraw[];
+// The shared memory of one CTA of the sweep.
+struct SweepSmem {
+    unsigned char* raw;   // RING_NBAR mbarriers, then the ring
+    unsigned char* ring;  // ring_bytes
+    void* t;              // t_len slots of R elements
+    int4* meta;           // max_levels
+    int2* grp;            // max_levels
+    double* a0row;        // nc (a0pre)
+};
+
+// One subdomain: stage its schedule, start its record stream, gather its
+// right-hand side(s) (and, in the fused two-level mode, the coarse
+// restrictions this block owes), run both sweeps, add the coarse term and
+// write the owned rows.  Returns false when the block must leave (a bounded
+// wait gave up; the error word is set).
+template <class TI, class TO, class TS, class TF, bool EXACT, int R>
+__device__ __forceinline__ bool sweep_one(const RecArgs& a, int s, const TI* __restrict__ x,
+                                          TO* __restrict__ y, int mode, int coarse,
+                                          const SweepSmem& sm, int& gbase, bool first) {
     __shared__ double s_zc;
     __shared__ double s_red[RC_MAXCH];
     __shared__ int s_ok;
     __shared__ int s_fail;
-    constexpr uint32_t HDR = RING_NBAR * 8;
     const int NC = (int)blockDim.x;
-    unsigned char* ringp = smraw + HDR;                                 // ring_bytes
-    TS* t = reinterpret_cast<TS*>(ringp + a.ring_bytes);                // t_len
-    int4* meta = reinterpret_cast<int4*>(
-        reinterpret_cast<unsigned char*>(t) + (((size_t)a.t_len * sizeof(TS) + 15) & ~(size_t)15));
-    int2* grp = reinterpret_cast<int2*>(meta + a.max_levels);
-    double* a0row = reinterpret_cast<double*>(grp + a.max_levels);  // nc when a0pre
-    const int s = a.order[blockIdx.x];
-    if (a.sub_on && !a.sub_on[s]) return;  // subdomain not needed by this apply
+    TS* t = reinterpret_cast<TS*>(sm.t);
     const SubInfo inf = a.info[s];
     const RingSub rs = a.ring[s];
     const int n = inf.n;
     const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
     // the schedule, staged once (the level loop touches global memory only
     // through the ring)
-    for (int g = threadIdx.x; g < T; g += NC) meta[g] = a.meta[rs.meta_off + g];
-    for (int j = threadIdx.x; j < rs.ngrp; j += NC) grp[j] = a.grp[rs.grp_off + j];
+    for (int g = threadIdx.x; g < T; g += NC) sm.meta[g] = a.meta[rs.meta_off + g];
+    for (int j = threadIdx.x; j < rs.ngrp; j += NC) sm.grp[j] = a.grp[rs.grp_off + j];
 
     RecRing ring;
     ring.src = a.rec + rs.base;
-    ring.grp = grp;
-    ring.bars_s = smem_u32(smraw);
-    ring.ring_s = smem_u32(ringp);
+    ring.grp = sm.grp;
+    ring.bars_s = smem_u32(sm.raw);
+    ring.ring_s = smem_u32(sm.ring);
     ring.budget = a.wait_budget;
     ring.fail = &s_fail;
+    ring.gbase = gbase;
     ring.issued = 0;
     ring.observed = 0;
     ring.bad = false;
     ring.wait_test = a.wait_test;
     // the producer is the block's last thread: levels rarely have rows for
-    // it, so its copies overlap the other threads' work
+    // it, so its copies overlap the other threads' work.  The mbarriers are
+    // initialised with the CTA's first subdomain; later ones continue their
+    // phases (every group of the previous subdomain was issued and observed).
     ring.producer = threadIdx.x == blockDim.x - 1;
     if (ring.producer) {
-        for (int i = 0; i < RING_NBAR; ++i) mbar_init(ring.bars_s + 8u * (uint32_t)i, 1);
+        if (first)
+            for (int i = 0; i < RING_NBAR; ++i) mbar_init(ring.bars_s + 8u * (uint32_t)i, 1);
         fence_mbar_init();
         s_fail = 0;
     }
+    gbase += rs.ngrp;
     __syncthreads();
     if (ring.producer) ring.issue_to(rs.ninit);
     // gather while the first records are in flight; with a coarse term the
@@ -554,15 +692,15 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     const int tp = inf.tshift;
     if (coarse && a.a0pre && threadIdx.x < 32) {
         const double* row = a.a0inv + (size_t)s * a.nc;
-        for (int q = threadIdx.x; q < a.nc; q += 32) cp_async8(smem_u32(a0row + q), row + q);
+        for (int q = threadIdx.x; q < a.nc; q += 32) cp_async8(smem_u32(sm.a0row + q), row + q);
     }
     if constexpr (std::is_same<TI, TS>::value) {
-        gather_async<TS>(smem_u32(t), x, dof, n, NC, tp);
+        gather_async<TS, R>(smem_u32(t), x, a.ldx, dof, n, NC, tp);
     } else {
-        gather_rows<TS>(t, x, dof, n, NC, tp);
+        gather_convert<TS, TI, R>(t, x, a.ldx, dof, n, NC, tp);
     }
     cp_async_wait_all();
-    if (threadIdx.x == 0) t[tslot(n, tp)] = (TS)0;
+    if (threadIdx.x < R) t[(size_t)R * tslot(n, tp) + threadIdx.x] = (TS)0;
     if (coarse && a.fuse && (int)blockIdx.x >= (int)gridDim.x / 2) {
         // coarse restrictions (the order of k_restrict), published for the
         // other blocks before the level loop.  Blocks run largest subdomain
@@ -586,13 +724,15 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     // the level loop -- the latency chain of the sweep -- one direction at a
     // time, specialised on the row width
     const uint32_t t_s = smem_u32(t);
-    if (!level_loop_w<false, TS, TF, EXACT>(meta, 0, nf, T, inf.wl, ring, t, t_s, ringp, NC, a.err))
-        return;
-    if (!level_loop_w<true, TS, TF, EXACT>(meta, nf, T, T, inf.wu, ring, t, t_s, ringp, NC, a.err))
-        return;
+    if (!level_loop_w<false, TS, TF, EXACT, R>(sm.meta, 0, nf, T, inf.wl, ring, t, t_s, sm.ring,
+                                               NC, a.err))
+        return false;
+    if (!level_loop_w<true, TS, TF, EXACT, R>(sm.meta, nf, T, T, inf.wu, ring, t, t_s, sm.ring,
+                                              NC, a.err))
+        return false;
     if (s_fail) {  // a wait in the last group gave up (read after the last level's barrier)
         ring.drain(a.err);
-        return;
+        return false;
     }
 
     if (coarse) {
@@ -615,11 +755,11 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
             __syncthreads();
             if (!s_ok) {
                 if (threadIdx.x == 0) atomicMax(a.err, 1);
-                return;
+                return false;
             }
         }
         if (threadIdx.x < 32) {
-            const double* row = a.a0pre ? a0row : a.a0inv + (size_t)s * a.nc;
+            const double* row = a.a0pre ? sm.a0row : a.a0inv + (size_t)s * a.nc;
             const double z = a.fuse ? coarse_dot_warp0<true>(row, a.r0, a.nc)
                                     : coarse_dot_warp0<false>(row, a.r0, a.nc);
             if (threadIdx.x == 0) {
@@ -635,22 +775,77 @@ k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, i
     }
     const double zc = coarse ? s_zc : 0.0;
     if (mode == 0) {
-        scatter_ilp<TS, TO>(t, y, a.ownloc + inf.own_off, a.owned + inf.own_off, inf.n_own,
-                            coarse, zc, NC, tp);
+        scatter_ilp<TS, TO, R>(t, y, a.ldy, a.ownloc + inf.own_off, a.owned + inf.own_off,
+                               inf.n_own, coarse, zc, NC, tp);
     } else {
         for (int li = threadIdx.x; li < n; li += NC)
-            atomicAdd(&y[dof[li]], Store<TO>::f(t[tslot(li, tp)]));
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+                atomicAdd(&y[i * a.ldy + dof[li]], Store<TO>::f(t[(size_t)R * tslot(li, tp) + i]));
         if (coarse) {
             const int* og = a.owned + inf.own_off;
             for (int q = threadIdx.x; q < inf.n_own; q += NC)
                 atomicAdd(&y[og[q]], Store<TO>::f(zc));
         }
     }
+    return true;
+}
+
+// mode 0: RAS (owned rows written), 1: ASM (all rows added atomically).  One
+// subdomain per CTA, or (PERSIST) CTAs looping over subdomains taken largest
+// first from a work counter.
+template <class TI, class TO, class TS, class TF, bool EXACT, int R, bool PERSIST>
+__global__ void __launch_bounds__(SW_T, 2)
+k_sweep_tma(RecArgs a, const TI* __restrict__ x, TO* __restrict__ y, int mode, int coarse,
+            const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    constexpr uint32_t HDR = RING_NBAR * 8;
+    SweepSmem sm;
+    sm.raw = smraw;
+    sm.ring = smraw + HDR;
+    sm.t = sm.ring + a.ring_bytes;
+    sm.meta = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(sm.t) +
+                                      (((size_t)a.t_len * R * sizeof(TS) + 15) & ~(size_t)15));
+    sm.grp = reinterpret_cast<int2*>(sm.meta + a.max_levels);
+    sm.a0row = reinterpret_cast<double*>(sm.grp + a.max_levels);
+    auto on = [&](int s) {
+        if (!a.sub_on) return true;
+        bool v = false;
+#pragma unroll
+        for (int i = 0; i < R; ++i) v = v || a.sub_on[(size_t)i * a.nparts + s] != 0;
+        return v;
+    };
+    int gbase = 0;  // record groups this CTA has streamed (mbarrier phases)
+    if constexpr (!PERSIST) {
+        const int s = a.order[blockIdx.x];
+        if (!on(s)) return;  // subdomain not needed by this apply
+        sweep_one<TI, TO, TS, TF, EXACT, R>(a, s, x, y, mode, coarse, sm, gbase, true);
+    } else {
+        __shared__ int s_next;
+        bool first = true;
+        for (;;) {
+            __syncthreads();  // every thread has read the previous index
+            if (threadIdx.x == 0) s_next = (int)atomicAdd(&a.work[0], 1u);
+            __syncthreads();
+            const int idx = s_next;
+            if (idx >= a.nparts) break;
+            const int s = a.order[idx];
+            if (!on(s)) continue;
+            if (!sweep_one<TI, TO, TS, TF, EXACT, R>(a, s, x, y, mode, coarse, sm, gbase, first))
+                return;
+            first = false;
+        }
+        if (threadIdx.x == 0 && atomicAdd(&a.work[1], 1u) == gridDim.x - 1) {
+            a.work[0] = 0u;  // every CTA has taken its last index: the counters restart
+            a.work[1] = 0u;
+        }
+    }
 }
 
 bool sweep_a0_prefetch(const sg_precond* pc);
 
-RecArgs rec_args(sg_precond* pc, bool fuse) {
+RecArgs rec_args(sg_precond* pc, const RingPlan& plan, bool fuse) {
     RecArgs a;
     a.fuse = fuse ? 1 : 0;
     a.r0w = pc->r0.p;
@@ -658,21 +853,26 @@ RecArgs rec_args(sg_precond* pc, bool fuse) {
     a.info = pc->info.p;
     a.order = pc->order.p;
     a.dofs = pc->dofs.p;
-    a.ring = reinterpret_cast<const RingSub*>(pc->ring_sub_d.p);
-    a.meta = reinterpret_cast<const int4*>(pc->ring_meta_d.p);
-    a.grp = reinterpret_cast<const int2*>(pc->ring_grp_d.p);
+    a.ring = reinterpret_cast<const RingSub*>(plan.sub_d.p);
+    a.meta = reinterpret_cast<const int4*>(plan.meta_d.p);
+    a.grp = reinterpret_cast<const int2*>(plan.grp_d.p);
     a.rec = pc->rec_d.p;
     a.ownloc = pc->ownloc_d.p;
     a.owned = pc->owned_d.p;
     a.a0inv = pc->a0inv.p;
     a.r0 = pc->r0.p;
+    a.nparts = pc->nparts;
     a.nc = pc->nc;
     a.a0pre = sweep_a0_prefetch(pc) ? 1 : 0;
-    a.ring_bytes = (int)pc->ring_bytes;
+    a.ring_bytes = (int)plan.ring_bytes;
     a.t_len = pc->t_len;
     a.max_levels = pc->max_levels;
+    a.ldx = 0;
+    a.ldy = 0;
     a.err = pc->err_d.p;
     a.sub_on = pc->sub_on;
+    a.persist = (plan.grid > 0 && !fuse) ? 1 : 0;
+    a.work = plan.work.p;
     a.wait_test = pc->wait_test;
     a.wait_budget = pc->wait_test ? WAIT_TEST_CYCLES : WAIT_CYCLES;
     return a;
@@ -686,23 +886,34 @@ bool sweep_a0_prefetch(const sg_precond* pc) {
 }
 
 // dynamic shared memory of the sweep: the mbarriers, the record ring, the
-// subdomain vector, per-level and per-group schedule entries, the coarse row
-size_t sweep_smem_for(const sg_precond* pc, long long ring_bytes) {
+// subdomain vector (R elements per slot), per-level and per-group schedule
+// entries, the coarse row
+size_t sweep_smem_for(const sg_precond* pc, long long ring_bytes, int R) {
     const size_t ts = pc->opts.sweep_dtype == SG_FP64 ? 8 : 4;
-    const size_t tbytes = ((size_t)pc->t_len * ts + 15) & ~(size_t)15;
+    const size_t tbytes = ((size_t)pc->t_len * ts * R + 15) & ~(size_t)15;
     const size_t a0 = sweep_a0_prefetch(pc) ? (size_t)pc->nparts * 8 : 0;
     return RING_NBAR * 8 + (size_t)ring_bytes + tbytes + (size_t)pc->max_levels * (16 + 8) + a0;
 }
-size_t sweep_smem(const sg_precond* pc) { return sweep_smem_for(pc, pc->ring_bytes); }
+size_t sweep_smem(const sg_precond* pc, const RingPlan& plan) {
+    return sweep_smem_for(pc, plan.ring_bytes, plan.R);
+}
 
-template <class TI, class TO, class TS, class TF, bool EXACT>
-void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const int* active,
-                bool fuse = false) {
-    const size_t smem = sweep_smem(pc);
-    const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
-    auto kern = k_sweep_tma<TI, TO, TS, TF, EXACT>;
+template <class TI, class TO, class TS, class TF, bool EXACT, int R>
+void launch_tma(sg_precond* pc, const RingPlan& plan, const TI* x, TO* y, int mode, bool coarse,
+                const int* active, bool fuse = false, long long ldx = 0, long long ldy = 0) {
+    const size_t smem = sweep_smem(pc, plan);
+    const int nt = plan.threads > 0 ? plan.threads : SW_T;
+    RecArgs a = rec_args(pc, plan, fuse);
+    // persistent CTAs only for FP32 sweeps (the FP64 ones keep their
+    // registers for the level loop)
+    if (sizeof(TS) == 8) a.persist = 0;
+    auto kern = k_sweep_tma<TI, TO, TS, TF, EXACT, R, false>;
+    if constexpr (sizeof(TS) == 4) {
+        if (a.persist) kern = k_sweep_tma<TI, TO, TS, TF, EXACT, R, true>;
+    }
     SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    RecArgs a = rec_args(pc, fuse);
+    a.ldx = ldx;
+    a.ldy = ldy;
     const int coarse_i = coarse ? 1 : 0;
     if (fuse) {
         // the blocks wait for one another's restriction: co-residency is
@@ -719,7 +930,8 @@ void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const
         cfg.numAttrs = 1;
         SG_CUDA(cudaLaunchKernelEx(&cfg, kern, a, x, y, mode, coarse_i, active));
     } else {
-        kern<<<pc->nparts, nt, smem, pc->ctx->stream>>>(a, x, y, mode, coarse_i, active);
+        const int grid = a.persist ? plan.grid : pc->nparts;
+        kern<<<grid, nt, smem, pc->ctx->stream>>>(a, x, y, mode, coarse_i, active);
     }
     SG_CUDA(cudaGetLastError());
     count_launch(pc->ctx);
@@ -727,30 +939,22 @@ void launch_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, const
 
 }  // namespace
 
-void tune_sweep(sg_precond* pc, const std::vector<long long>& gmax_list);
-
-static void ring_upload(sg_precond* pc) {
-    cudaStream_t st = pc->ctx->stream;
-    pc->ring_sub_d.upload(pc->h_ring_sub, st);
-    pc->ring_meta_d.upload(pc->h_ring_meta, st);
-    pc->ring_grp_d.upload(pc->h_ring_grp, st);
-}
-
-// Builds the static ring schedule of every subdomain (see RingSub) for a ring
-// of ring_bytes and groups of at most gmax bytes (a larger level is a group
-// of its own).  Groups are placed one after another and start over at the
-// ring's beginning when they would cross its end.  Group j may be issued
-// after the last level of every earlier group whose ring bytes it overwrites
-// and of group j - RING_NBAR (its mbarrier's previous user); the schedule is
-// feasible when that is always before group j's first level.  Returns false
-// (nothing kept) when it is not.
-static bool ring_schedule(sg_precond* pc, long long ring_bytes, long long gmax) {
+// Builds the static ring schedule of every subdomain (see RingSub) into
+// `plan` for a ring of ring_bytes and groups of at most gmax bytes (a larger
+// level is a group of its own).  Groups are placed one after another and
+// start over at the ring's beginning when they would cross its end.  Group
+// j may be issued after the last level of every earlier group whose ring
+// bytes it overwrites and of group j - RING_NBAR (its mbarrier's previous
+// user); the schedule is feasible when that is always before group j's
+// first level.  Returns false (plan unchanged) when it is not.
+static bool ring_schedule(const sg_precond* pc, RingPlan& plan, long long ring_bytes,
+                          long long gmax) {
     const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
                          : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
     std::vector<RingSub> subs((size_t)pc->nparts);
     std::vector<int> meta, grp;  // int4 / int2 entries as ints
     std::vector<long long> rel, gstart, gbytes, gpos;
-    std::vector<int> B, cnt, padded, gfirst, glast, ia, upto;
+    std::vector<int> B, cnt, padded, gfirst, glast, ia;
     for (int s = 0; s < pc->nparts; ++s) {
         const SubInfo& inf = pc->h_info[s];
         const int nf = inf.nlev_f, T = inf.nlev_f + inf.nlev_b;
@@ -833,61 +1037,95 @@ static bool ring_schedule(sg_precond* pc, long long ring_bytes, long long gmax) 
             grp.push_back((int)((gbytes[j] >> 4) | ((gpos[j] >> 4) << 16)));
         }
     }
-    pc->h_ring_sub.assign(reinterpret_cast<const unsigned char*>(subs.data()),
-                          reinterpret_cast<const unsigned char*>(subs.data() + subs.size()));
-    pc->h_ring_meta.swap(meta);
-    pc->h_ring_grp.swap(grp);
+    plan.sub.assign(reinterpret_cast<const unsigned char*>(subs.data()),
+                    reinterpret_cast<const unsigned char*>(subs.data() + subs.size()));
+    plan.meta.swap(meta);
+    plan.grp.swap(grp);
+    plan.ring_bytes = ring_bytes;
+    plan.gmax = gmax;
     return true;
 }
 
-// Sizes the record ring (what the shared memory of the CTAs that must share
-// an SM leaves), builds its schedule, packs the level records in the
-// configured factor type and times the block size.
-void rec_setup_device(sg_precond* pc) {
-    if (!pc->use_rec) return;
+static void ring_upload(sg_precond* pc, RingPlan& plan) {
+    cudaStream_t st = pc->ctx->stream;
+    plan.sub_d.upload(plan.sub, st);
+    plan.meta_d.upload(plan.meta, st);
+    plan.grp_d.upload(plan.grp, st);
+}
+
+// Resident CTAs per SM of the sweep kernel for the plan's shared memory and
+// block size.
+template <class K>
+static int sweep_occupancy(sg_precond* pc, const RingPlan& plan, K kern) {
+    const size_t smem = sweep_smem(pc, plan);
+    const int nt = plan.threads > 0 ? plan.threads : SW_T;
+    int per_sm = 0;
+    SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
+    return per_sm;
+}
+
+// Sizes a plan's ring (what the shared memory of the CTAs that must share an
+// SM leaves) and lists the record-group sizes whose schedule is feasible
+// for it (the schedule of the last one is left in `plan`).
+static std::vector<long long> ring_size(sg_precond* pc, RingPlan& plan) {
     sg_ctx* ctx = pc->ctx;
-    cudaStream_t st = ctx->stream;
-    if (pc->rec_stage_bytes % 16 != 0 || pc->rec_total % 16 != 0)
-        fail(SG_ERR_INTERNAL, "level records are not 16-byte multiples");
-    int max_smem = 0;
+    int max_smem = 0, sm_smem = 0;
     SG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin,
                                    ctx->device));
-    int sm_smem = 0;
     SG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
                                    ctx->device));
     const int static_smem = 1024;  // reduction scratch and the like
-    // CTAs per SM needed to keep every subdomain resident at once
-    const int want = (pc->nparts + ctx->num_sms - 1) / ctx->num_sms;
+    // CTAs per SM needed to keep every subdomain resident at once (more
+    // subdomains than that run persistent or in waves)
+    int want = (pc->nparts + ctx->num_sms - 1) / ctx->num_sms;
+    if (want > 4) want = 4;
     // group size: opts.reserved[3] when set, else timed among 8 and 16 KB
     // (never below the largest record)
     std::vector<long long> gcand;
     if (pc->opts.reserved[3] > 0) gcand.push_back(pc->opts.reserved[3]);
     else gcand = {8192, 16384};
-    long long ring = 0;
-    std::vector<long long> gok;  // feasible group sizes for the chosen ring
+    std::vector<long long> gok;
     for (int per_sm = want < 1 ? 1 : want; per_sm >= 1 && gok.empty(); --per_sm) {
         const long long budget = std::min<long long>((long long)sm_smem / per_sm - static_smem - 1024,
                                                      (long long)max_smem - static_smem);
-        ring = (budget - (long long)sweep_smem_for(pc, 0)) & ~15ll;
+        const long long ring = (budget - (long long)sweep_smem_for(pc, 0, plan.R)) & ~15ll;
         if (ring < pc->rec_stage_bytes) continue;
         for (long long target : gcand) {
             for (long long gmax : {target, target / 2, target / 4}) {
                 if (gmax < pc->rec_stage_bytes) gmax = pc->rec_stage_bytes;
-                if (ring_schedule(pc, ring, gmax)) {
+                if (ring_schedule(pc, plan, ring, gmax)) {
                     if (std::find(gok.begin(), gok.end(), gmax) == gok.end()) gok.push_back(gmax);
                     break;
                 }
             }
         }
     }
+    return gok;
+}
+
+void tune_plan(sg_precond* pc, RingPlan& plan, const std::vector<long long>& gmax_list);
+
+// Packs the level records in the configured factor type, plans the
+// one-vector ring and times its block size, record-group size and launch
+// shape.
+void rec_setup_device(sg_precond* pc) {
+    if (!pc->use_rec) return;
+    sg_ctx* ctx = pc->ctx;
+    cudaStream_t st = ctx->stream;
+    if (pc->rec_stage_bytes % 16 != 0 || pc->rec_total % 16 != 0)
+        fail(SG_ERR_INTERNAL, "level records are not 16-byte multiples");
+    RingPlan& plan = pc->ring1;
+    plan.R = 1;
+    plan.ready = false;
+    pc->ring4.ready = false;  // a new set-up plans the four-vector ring again when asked
+    const std::vector<long long> gok = ring_size(pc, plan);
     if (gok.empty() || (pc->opts.reserved[0] & 1)) {
         pc->use_rec = false;
         return;
     }
-    pc->ring_bytes = ring;
     pc->rec_depth = 1;
-    pc->ring_gmax = gok.back();  // the schedule ring_schedule built last
-    ring_upload(pc);
+    ring_upload(pc, plan);
     pc->rec_off_f_d.upload(pc->h_rec_off_f, st);
     pc->rec_off_b_d.upload(pc->h_rec_off_b, st);
     pc->rec_rows_f_d.upload(pc->h_rec_rows_f, st);
@@ -907,34 +1145,24 @@ void rec_setup_device(sg_precond* pc) {
     else SG_PACK(float);
 #undef SG_PACK
     SG_CUDA(cudaGetLastError());
-    // threads per CTA: forced by opts.reserved[1], else timed.  Levels of a
-    // 3D subdomain hold ~100+ rows, those of a small 2D one ~20: a 512-thread
-    // block then idles at every level barrier, while narrower blocks let more
-    // subdomains run at once on an SM.
-    if (pc->opts.reserved[1] > 0 && gok.size() == 1) {
-        pc->sweep_threads = pc->opts.reserved[1];
-    } else {
-        tune_sweep(pc, gok);
-    }
+    // block size (forced by opts.reserved[1], else timed), record-group size
+    // and launch shape.  Levels of a 3D subdomain hold ~100+ rows, those of a
+    // small 2D one ~20: a 512-thread block then idles at every level
+    // barrier, while narrower blocks let more subdomains run at once.
+    tune_plan(pc, plan, gok);
+    pc->sweep_threads = plan.threads;
     // two-level: the coarse restriction runs inside the sweep when every
     // subdomain's CTA can be resident at once (a cooperative launch)
     pc->fuse_restrict = false;
     if (pc->kind == SG_PC_TWOLEVEL_ASM || pc->kind == SG_PC_TWOLEVEL_RAS) {
-        const size_t smem = sweep_smem(pc);
-        const int nt = pc->sweep_threads > 0 ? pc->sweep_threads : SW_T;
         int coop = 0, per_sm = 0;
         SG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
-        auto occupancy = [&](auto kern) {
-            SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem));
-            SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
-        };
         if (pc->opts.sweep_dtype == SG_FP64)
-            occupancy(k_sweep_tma<double, double, double, double, false>);
+            per_sm = sweep_occupancy(pc, plan, k_sweep_tma<double, double, double, double, false, 1, false>);
         else if (pc->opts.factor_dtype == SG_BF16)
-            occupancy(k_sweep_tma<float, float, float, uint16_t, false>);
+            per_sm = sweep_occupancy(pc, plan, k_sweep_tma<float, float, float, uint16_t, false, 1, false>);
         else
-            occupancy(k_sweep_tma<float, float, float, float, false>);
+            per_sm = sweep_occupancy(pc, plan, k_sweep_tma<float, float, float, float, false, 1, false>);
         if (coop && (long long)per_sm * ctx->num_sms >= pc->nparts && pc->opts.reserved[2] == 0) {
             pc->coarse_sync.alloc(2);
             pc->coarse_sync.zero(st);
@@ -947,13 +1175,16 @@ bool sweep_fuses_restrict(const sg_precond* pc) {
     return pc->use_rec && pc->rec_depth > 0 && pc->fuse_restrict && !pc->sub_on;
 }
 
-// Times the sweep (RAS mode, no coarse term, zero input) for every record
-// group size in gmax_list and 128, 256, 384 and 512 threads per CTA (or the
-// forced block size) and keeps the fastest pair.
-void tune_sweep(sg_precond* pc, const std::vector<long long>& gmax_list) {
+// Times the sweep (RAS mode, no coarse term, zero input; R interleaved
+// vectors) for every record-group size in gmax_list, 128, 256, 384 and 512
+// threads per CTA (or the forced block size) and, when there are more
+// subdomains than resident CTAs, one CTA per subdomain against a persistent
+// grid; keeps the fastest.
+void tune_plan(sg_precond* pc, RingPlan& plan, const std::vector<long long>& gmax_list) {
     sg_ctx* ctx = pc->ctx;
     cudaStream_t st = ctx->stream;
-    const size_t n = (size_t)std::max(pc->n, 1);
+    const int R = plan.R;
+    const size_t n = (size_t)std::max(pc->n, 1) * R;
     const bool f64 = pc->opts.sweep_dtype == SG_FP64;
     const bool bf16 = pc->opts.factor_dtype == SG_BF16;
     DBuf<double> x64, y64;
@@ -967,65 +1198,142 @@ void tune_sweep(sg_precond* pc, const std::vector<long long>& gmax_list) {
         y32.alloc(n);
         x32.zero(st);
     }
+    if (!plan.work.p) {
+        plan.work.alloc(2);
+        plan.work.zero(st);
+    }
+    const long long ld = pc->n;
     auto run = [&] {
-        if (f64) launch_tma<double, double, double, double, false>(pc, x64.p, y64.p, 0, false, nullptr);
-        else if (bf16) launch_tma<float, float, float, uint16_t, false>(pc, x32.p, y32.p, 0, false, nullptr);
-        else launch_tma<float, float, float, float, false>(pc, x32.p, y32.p, 0, false, nullptr);
+        if (f64) launch_tma<double, double, double, double, false, 1>(pc, plan, x64.p, y64.p, 0, false, nullptr);
+        else if (R == 4 && bf16) launch_tma<float, float, float, uint16_t, false, 4>(pc, plan, x32.p, y32.p, 0, false, nullptr, false, ld, ld);
+        else if (R == 4) launch_tma<float, float, float, float, false, 4>(pc, plan, x32.p, y32.p, 0, false, nullptr, false, ld, ld);
+        else if (bf16) launch_tma<float, float, float, uint16_t, false, 1>(pc, plan, x32.p, y32.p, 0, false, nullptr);
+        else launch_tma<float, float, float, float, false, 1>(pc, plan, x32.p, y32.p, 0, false, nullptr);
+    };
+    auto occupancy = [&]() -> int {
+        if (f64) return sweep_occupancy(pc, plan, k_sweep_tma<double, double, double, double, false, 1, false>);
+        if (R == 4 && bf16) return sweep_occupancy(pc, plan, k_sweep_tma<float, float, float, uint16_t, false, 4, false>);
+        if (R == 4) return sweep_occupancy(pc, plan, k_sweep_tma<float, float, float, float, false, 4, false>);
+        if (bf16) return sweep_occupancy(pc, plan, k_sweep_tma<float, float, float, uint16_t, false, 1, false>);
+        return sweep_occupancy(pc, plan, k_sweep_tma<float, float, float, float, false, 1, false>);
     };
     cudaEvent_t e0, e1;
     SG_CUDA(cudaEventCreate(&e0));
     SG_CUDA(cudaEventCreate(&e1));
     float best = -1.f;
-    int best_nt = SW_T;
+    int best_nt = SW_T, best_grid = 0;
     long long best_g = gmax_list.front();
     std::vector<int> threads = {512, 384, 256, 128};
     if (pc->opts.reserved[1] > 0) threads = {pc->opts.reserved[1]};
     for (long long gmax : gmax_list) {
-        if (!ring_schedule(pc, pc->ring_bytes, gmax)) continue;
-        ring_upload(pc);
+        if (!ring_schedule(pc, plan, plan.ring_bytes, gmax)) continue;
+        ring_upload(pc, plan);
         for (int nt : threads) {
-            pc->sweep_threads = nt;
-            run();
-            run();
-            cudaEventRecord(e0, st);
-            for (int r = 0; r < 5; ++r) run();
-            cudaEventRecord(e1, st);
-            cudaError_t e = cudaEventSynchronize(e1);
-            float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            if (e != cudaSuccess) {
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                SG_CUDA(e);
-            }
-            if (best < 0.f || ms < best) {
-                best = ms;
-                best_nt = nt;
-                best_g = gmax;
+            plan.threads = nt;
+            plan.grid = 0;
+            const int per_sm = occupancy();
+            if (per_sm < 1) continue;
+            const long long cap = (long long)per_sm * ctx->num_sms;
+            // launch shape: opts.reserved[4] 1 forces one CTA per subdomain,
+            // 2 a persistent grid of the resident CTAs, k > 2 a persistent
+            // grid of k CTAs (at most the resident ones); 0 times one CTA per
+            // subdomain against the persistent grid when there are more
+            // subdomains than resident CTAs
+            std::vector<int> grids = {0};
+            const int shape = pc->opts.reserved[4];
+            if (shape == 2) grids = {(int)std::min<long long>(cap, pc->nparts)};
+            else if (shape > 2) grids = {(int)std::min<long long>(std::min<long long>(cap, shape), pc->nparts)};
+            else if (shape == 0 && cap < pc->nparts) grids.push_back((int)cap);
+            if (f64) grids = {0};  // FP64 sweeps run one CTA per subdomain
+            for (int grid : grids) {
+                plan.grid = grid;
+                run();
+                run();
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < 5; ++r) run();
+                cudaEventRecord(e1, st);
+                cudaError_t e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    SG_CUDA(e);
+                }
+                if (best < 0.f || ms < best) {
+                    best = ms;
+                    best_nt = nt;
+                    best_g = gmax;
+                    best_grid = grid;
+                }
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    pc->sweep_threads = best_nt;
-    pc->ring_gmax = best_g;
-    if (!ring_schedule(pc, pc->ring_bytes, best_g)) fail(SG_ERR_INTERNAL, "ring schedule lost");
-    ring_upload(pc);
+    if (best < 0.f) fail(SG_ERR_INTERNAL, "no sweep configuration fits the GPU");
+    plan.threads = best_nt;
+    plan.grid = best_grid;
+    if (!ring_schedule(pc, plan, plan.ring_bytes, best_g)) fail(SG_ERR_INTERNAL, "ring schedule lost");
+    ring_upload(pc, plan);
+    plan.ready = true;
 }
 
 template <class TI, class TO>
 bool sweep_tma(sg_precond* pc, const TI* x, TO* y, int mode, bool coarse, bool exact,
                const int* active) {
     if (!pc->use_rec || pc->rec_depth == 0) return false;
+    const RingPlan& plan = pc->ring1;
     const bool fuse = coarse && sweep_fuses_restrict(pc);
     if (pc->opts.sweep_dtype == SG_FP64) {
-        if (exact) launch_tma<TI, TO, double, double, true>(pc, x, y, mode, coarse, active, fuse);
-        else launch_tma<TI, TO, double, double, false>(pc, x, y, mode, coarse, active, fuse);
+        if (exact) launch_tma<TI, TO, double, double, true, 1>(pc, plan, x, y, mode, coarse, active, fuse);
+        else launch_tma<TI, TO, double, double, false, 1>(pc, plan, x, y, mode, coarse, active, fuse);
     } else if (pc->opts.factor_dtype == SG_BF16) {
-        launch_tma<TI, TO, float, uint16_t, false>(pc, x, y, mode, coarse, active, fuse);
+        launch_tma<TI, TO, float, uint16_t, false, 1>(pc, plan, x, y, mode, coarse, active, fuse);
     } else {
-        launch_tma<TI, TO, float, float, false>(pc, x, y, mode, coarse, active, fuse);
+        launch_tma<TI, TO, float, float, false, 1>(pc, plan, x, y, mode, coarse, active, fuse);
     }
+    return true;
+}
+
+// Plans (and times) the four-vector ring of a RAS preconditioner with FP32
+// sweeps, once per set-up; call it outside stream capture.  False when the
+// preconditioner has no such sweep.
+bool sweep_plan4(sg_precond* pc) {
+    if (!pc->use_rec || pc->rec_depth == 0 || pc->opts.sweep_dtype == SG_FP64) return false;
+    if (pc->kind != SG_PC_RAS) return false;
+    RingPlan& plan = pc->ring4;
+    if (plan.ready) return true;
+    plan.R = 4;
+    const std::vector<long long> gok = ring_size(pc, plan);
+    if (gok.empty()) return false;
+    const int* keep = pc->sub_on;
+    pc->sub_on = nullptr;
+    tune_plan(pc, plan, gok);
+    pc->sub_on = keep;
+    return true;
+}
+
+// Four right-hand sides at once (RAS without a coarse term, FP32 sweeps): x
+// and y hold them ld apart; sub_on (NULL or 4 x nparts switches) gates the
+// subdomains.  Returns false, launching nothing, when the four-vector ring
+// has not been planned (sweep_plan4).
+template <class TI, class TO>
+bool sweep_tma4(sg_precond* pc, const TI* x, TO* y, long long ld, const int* sub_on) {
+    if (!pc->use_rec || pc->rec_depth == 0 || pc->opts.sweep_dtype == SG_FP64) return false;
+    if (pc->kind != SG_PC_RAS || !pc->ring4.ready) return false;
+    const RingPlan& plan = pc->ring4;
+    const int* keep = pc->sub_on;
+    pc->sub_on = sub_on;
+    struct Restore {
+        sg_precond* pc;
+        const int* v;
+        ~Restore() { pc->sub_on = v; }
+    } restore{pc, keep};
+    if (pc->opts.factor_dtype == SG_BF16)
+        launch_tma<TI, TO, float, uint16_t, false, 4>(pc, plan, x, y, 0, false, nullptr, false, ld, ld);
+    else
+        launch_tma<TI, TO, float, float, false, 4>(pc, plan, x, y, 0, false, nullptr, false, ld, ld);
     return true;
 }
 
@@ -1034,12 +1342,14 @@ int sweep_error(sg_precond* pc) {
     int e = 0;
     SG_CUDA(cudaMemcpyAsync(&e, pc->err_d.p, sizeof(int), cudaMemcpyDeviceToHost, pc->ctx->stream));
     SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
-    // reported once: clear the error word, and the fused restriction's
-    // counters, which a sweep that gave up may have left mid-count, so the
-    // next apply starts clean
+    // reported once: clear the error word, the fused restriction's counters
+    // and the persistent launches' work counters, which a sweep that gave up
+    // may have left mid-count, so the next apply starts clean
     if (e) {
         pc->err_d.zero(pc->ctx->stream);
         if (pc->coarse_sync.p) pc->coarse_sync.zero(pc->ctx->stream);
+        if (pc->ring1.work.p) pc->ring1.work.zero(pc->ctx->stream);
+        if (pc->ring4.work.p) pc->ring4.work.zero(pc->ctx->stream);
         SG_CUDA(cudaStreamSynchronize(pc->ctx->stream));
     }
     return e;
@@ -1058,6 +1368,8 @@ template bool sweep_tma<double, float>(sg_precond*, const double*, float*, int, 
                                        const int*);
 template bool sweep_tma<float, float>(sg_precond*, const float*, float*, int, bool, bool,
                                       const int*);
+template bool sweep_tma4<double, float>(sg_precond*, const double*, float*, long long, const int*);
+template bool sweep_tma4<float, float>(sg_precond*, const float*, float*, long long, const int*);
 
 }  // namespace sg
 
@@ -1078,17 +1390,25 @@ namespace sg {
 //    packed offsets.
 // plant = 1 (testing) first corrupts one column slot of the host copy.
 // Returns the number of violations found (0: all hold).
+static long long plan_check(sg_precond* pc, const RingPlan& plan, int plant);
+
 long long sweep_check(sg_precond* pc, int plant) {
     if (!pc->use_rec || pc->rec_depth == 0) return 0;
+    long long bad = plan_check(pc, pc->ring1, plant);
+    if (pc->ring4.ready) bad += plan_check(pc, pc->ring4, 0);
+    return bad;
+}
+
+static long long plan_check(sg_precond* pc, const RingPlan& plan, int plant) {
     cudaStream_t st = pc->ctx->stream;
     std::vector<unsigned char> rec((size_t)pc->rec_total);
     SG_CUDA(cudaMemcpyAsync(rec.data(), pc->rec_d.p, rec.size(), cudaMemcpyDeviceToHost, st));
     SG_CUDA(cudaStreamSynchronize(st));
     const long long sf = pc->opts.sweep_dtype == SG_FP64 ? 8
                          : (pc->opts.factor_dtype == SG_BF16 ? 2 : 4);
-    const RingSub* subs = reinterpret_cast<const RingSub*>(pc->h_ring_sub.data());
-    const int* meta = pc->h_ring_meta.data();
-    const int* grp = pc->h_ring_grp.data();
+    const RingSub* subs = reinterpret_cast<const RingSub*>(plan.sub.data());
+    const int* meta = plan.meta.data();
+    const int* grp = plan.grp.data();
     long long bad = 0;
     bool planted = false;
     std::vector<char> done;
@@ -1175,7 +1495,7 @@ long long sweep_check(sg_precond* pc, int plant) {
             if (c != (back ? pc->h_lev_ptr_b[i + 1] - pc->h_lev_ptr_b[i]
                            : pc->h_lev_ptr_f[i + 1] - pc->h_lev_ptr_f[i]))
                 ++bad;
-            if (m[1] < gpos || m[1] + B > gpos + gbytes || m[1] + B > pc->ring_bytes) ++bad;
+            if (m[1] < gpos || m[1] + B > gpos + gbytes || m[1] + B > plan.ring_bytes) ++bad;
             if (rel - gstart != m[1] - gpos) ++bad;  // the ring copy holds this record
             if (m[2] >= 0 && m[2] >= issued) ++bad;  // waits for a copy not yet issued
             // issue after the level: what the new groups overwrite must be done
