@@ -86,7 +86,11 @@ typedef struct sg_precond_opts {
                          CTA per subdomain, 2 persistent: resident CTAs take
                          subdomains largest first from a work counter, k > 2
                          persistent with k CTAs at most; same results);
-                         other entries must be 0 */
+                         reserved[5]: integer set-up (decomposition,
+                         overlap, local matrices, level schedules) on the
+                         device (0; host threads when its bitmaps would not
+                         fit) or on host threads (1); same results; other
+                         entries must be 0 */
 } sg_precond_opts;
 
 typedef struct sg_ctx sg_ctx;
@@ -202,6 +206,21 @@ sg_status sg_precond_get_sweep_ring(sg_precond* pc, int* ring_bytes, int* group_
  * of the check) first corrupts one column slot of the host copy.  0
  * violations and SG_OK without that sweep. */
 sg_status sg_precond_check(sg_precond* pc, int plant, long long* violations);
+/* Where the integer set-up of the last sg_precond_setup ran (no
+ * counterpart in the reference, which sets up on the host): *on_device 1
+ * for the device kernels, 0 for host threads. */
+sg_status sg_precond_get_setup_path(sg_precond* pc, int* on_device);
+/* Read-back of the subdomain schedule the set-up built (no counterpart in
+ * the reference; for tests and inspection): which 0/1 level pointers of the
+ * forward/backward sweeps (per subdomain nlev + 1 entries, concatenated),
+ * 2/3 rows in level order, 4 slot-layout shift per subdomain, 5 global entry
+ * of every local entry, 6 local row pointers (n_s + 1 per subdomain), 7
+ * diagonal entry per local row, 8 local columns, 9/10 forward/backward level
+ * per local row, 11 per subdomain (lower width, upper width, forward levels,
+ * backward levels), 12 launch order of the subdomains.  out may be NULL to
+ * query *len. */
+sg_status sg_precond_get_schedule(sg_precond* pc, int which, int* out, long long cap,
+                                  long long* len);
 
 /* A preconditioner that is a caller's host function: FGMRES's flexible apply
  * (FlexApply / fgmres_flex, src/core/fgmres.h:37, src/core/fgmres.cpp:164-172)

@@ -423,7 +423,7 @@ class Preconditioner:
                  factor_dtype: int = FP64, sweep_dtype: int = FP64,
                  ctx: Context | None = None, generic_sweep: bool = False,
                  sweep: str = "tma", sweep_threads: int = 0, fuse_restrict: bool = True,
-                 group_bytes: int = 0, sweep_launch: str = "auto"):
+                 group_bytes: int = 0, sweep_launch: str = "auto", setup: str = "device"):
         # sweep variant (testing/comparison): "tma" (default: TMA-fed level
         # records), "level" (factors read from global memory), "syncfree"
         if generic_sweep:
@@ -455,6 +455,9 @@ class Preconditioner:
         # or an int k > 2 (persistent with at most k CTAs)
         opts.reserved[4] = (int(sweep_launch) if isinstance(sweep_launch, int) else
                             {"auto": 0, "per_subdomain": 1, "persistent": 2}[sweep_launch])
+        # integer set-up: "device" (kernels; host threads when its bitmaps
+        # would not fit) or "host" (threads); same results
+        opts.reserved[5] = {"device": 0, "host": 1}[setup]
         self._opts = opts
         h = C.c_void_p()
         _check(_clib.sg_precond_create(self.ctx.handle, L.PC_KINDS[self.kind], C.byref(opts),
@@ -523,6 +526,21 @@ class Preconditioner:
         _check(_clib.sg_precond_get_sweep_ring(self.handle, C.byref(rb), C.byref(gb)))
         return {"sweep": kinds[k.value], "threads": t.value, "ring_bytes": rb.value,
                 "group_bytes": gb.value}
+
+    def setup_on_device(self) -> bool:
+        """True when the last set-up's integer part ran on the device."""
+        v = C.c_int(0)
+        _check(_clib.sg_precond_get_setup_path(self.handle, C.byref(v)))
+        return bool(v.value)
+
+    def schedule(self, which: int) -> np.ndarray:
+        """Read-back of a subdomain schedule array (sg_precond_get_schedule)."""
+        ln = C.c_longlong(0)
+        _check(_clib.sg_precond_get_schedule(self.handle, int(which), None, 0, C.byref(ln)))
+        out = np.empty(ln.value, np.int32)
+        _check(_clib.sg_precond_get_schedule(self.handle, int(which), out.ctypes.data, out.size,
+                                             C.byref(ln)))
+        return out
 
     def check(self, plant: bool = False) -> int:
         """Checked mode of the TMA-fed sweep: the number of violated

@@ -116,6 +116,9 @@ PROTOTYPES = {
     "sg_precond_get_sweep": (C.c_int, [_vp, _ip, _ip]),
     "sg_precond_get_sweep_ring": (C.c_int, [_vp, _ip, _ip]),
     "sg_precond_check": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_longlong)]),
+    "sg_precond_get_setup_path": (C.c_int, [_vp, _ip]),
+    "sg_precond_get_schedule": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_longlong,
+                                          C.POINTER(C.c_longlong)]),
     "sg_precond_set_wait_test": (C.c_int, [_vp, C.c_int]),
     "sg_precond_create_host": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
     "sg_estimate_condition": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_uint,

@@ -38,6 +38,8 @@ void fail(sg_status st, const char* fmt, ...) {
 
 // defined in setup.cpp / solver.cu
 void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part, int nparts, int overlap);
+bool build_schwarz_device(sg_precond* pc, const sg_csr* A, const int* part, int nparts,
+                          int overlap);
 void partition_graph(int n, const int* rp, const int* ci, int nparts, int* part);
 void partition_boxes(int nx, int ny, int nz, int nparts, double spread, uint64_t seed, int* part);
 int gen_poisson2d(int nx, int ny, int* rp, int* ci, double* v);
@@ -467,6 +469,10 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             delete pc;
             fail(SG_ERR_INVALID_ARG, "sweep launch shape (reserved[4]) must be >= 0");
         }
+        if (pc->opts.reserved[5] != 0 && pc->opts.reserved[5] != 1) {
+            delete pc;
+            fail(SG_ERR_INVALID_ARG, "set-up path (reserved[5]) must be 0 or 1");
+        }
         const int grb = pc->opts.reserved[3];
         if (!(grb == 0 || (grb >= 1024 && grb <= 65536 && grb % 16 == 0))) {
             delete pc;
@@ -557,7 +563,11 @@ sg_status sg_precond_setup(sg_precond* pc, const sg_csr* A) {
         const uint64_t key = structure_key(pc, A, part.data(), nparts, overlap);
         if (!(pc->has_structure && pc->structure_key == key)) {
             pc->has_structure = false;
-            build_schwarz_host(pc, A, part.data(), nparts, overlap);
+            // the integer set-up on the device (opts.reserved[5] = 0), unless
+            // its bitmaps would not fit; else, or when asked (1), on host threads
+            pc->setup_on_device = pc->opts.reserved[5] == 0 &&
+                                  build_schwarz_device(pc, A, part.data(), nparts, overlap);
+            if (!pc->setup_on_device) build_schwarz_host(pc, A, part.data(), nparts, overlap);
             pc->structure_key = key;
             pc->has_structure = true;
         }
@@ -727,6 +737,63 @@ sg_status sg_precond_check(sg_precond* pc, int plant, long long* violations) {
         if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
         use_device(pc->ctx);
         *violations = sg::sweep_check(pc, plant);
+    });
+}
+
+sg_status sg_precond_get_setup_path(sg_precond* pc, int* on_device) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && on_device, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        *on_device = pc->setup_on_device ? 1 : 0;
+    });
+}
+
+sg_status sg_precond_get_schedule(sg_precond* pc, int which, int* out, long long cap,
+                                  long long* len) {
+    return guard([&] {
+        SG_CHECK_ARG(pc && len, "NULL argument");
+        if (!pc->is_setup) fail(SG_ERR_NOT_SETUP, "preconditioner used before setup");
+        SG_CHECK_ARG(pc->kind >= SG_PC_ILU0 && pc->kind != SG_PC_HOST,
+                     "no subdomain schedule for this preconditioner kind");
+        std::vector<int> tmp;
+        const std::vector<int>* v = &tmp;
+        switch (which) {
+        case 0: v = &pc->h_lev_ptr_f; break;
+        case 1: v = &pc->h_lev_ptr_b; break;
+        case 2:
+            if (pc->wide_cols) v = &pc->h_perm_f32;
+            else tmp.assign(pc->h_perm_f16.begin(), pc->h_perm_f16.end());
+            break;
+        case 3:
+            if (pc->wide_cols) v = &pc->h_perm_b32;
+            else tmp.assign(pc->h_perm_b16.begin(), pc->h_perm_b16.end());
+            break;
+        case 4:
+            for (const auto& inf : pc->h_info) tmp.push_back(inf.tshift);
+            break;
+        case 5: v = &pc->lmap; break;
+        case 6: v = &pc->lrp; break;
+        case 7: v = &pc->ldiag; break;
+        case 8: v = &pc->lci; break;
+        case 9: v = &pc->lev_lo; break;
+        case 10: v = &pc->lev_up; break;
+        case 11:
+            for (const auto& inf : pc->h_info) {
+                tmp.push_back(inf.wl);
+                tmp.push_back(inf.wu);
+                tmp.push_back(inf.nlev_f);
+                tmp.push_back(inf.nlev_b);
+            }
+            break;
+        case 12: tmp.assign(pc->h_order.begin(), pc->h_order.end()); break;
+        default: fail(SG_ERR_INVALID_ARG, "unknown schedule array %d", which);
+        }
+        *len = (long long)v->size();
+        if (out) {
+            SG_CHECK_ARG(cap >= (long long)v->size(), "cap %lld < length %lld", cap,
+                         (long long)v->size());
+            std::copy(v->begin(), v->end(), out);
+        }
     });
 }
 

@@ -18,6 +18,9 @@
 
 namespace sg {
 
+void schwarz_finish(sg_precond* pc, const std::vector<int>& perm_f_all,
+                    const std::vector<int>& perm_b_all);
+
 // Level of every row of one local CSR for the forward sweep (reads columns
 // before the first column >= row, src/precond/ilu0.h:62-67) and for the
 // backward sweep (reads the entries after the diagonal, :70-76).
@@ -349,8 +352,6 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
         pc->lci.reserve(nz);
         pc->lmap.reserve(nz);
     }
-    long long fl_total = 0, fu_total = 0;
-    int max_n = 0, t_len = 0;
     for (int s = 0; s < nparts; ++s) {
         LocalOut& L = lo_s[s];
         SubInfo& inf = pc->h_info[s];
@@ -364,6 +365,23 @@ void build_schwarz_host(sg_precond* pc, const sg_csr* A, const int* part_in, int
         inf.lev_off_b = (int)pc->h_lev_ptr_b.size();
         pc->h_lev_ptr_b.insert(pc->h_lev_ptr_b.end(), L.ptr_b.begin(), L.ptr_b.end());
         L = LocalOut();  // release as we go
+    }
+    schwarz_finish(pc, perm_f_all, perm_b_all);
+}
+
+// What both set-up paths (host threads, or the device kernels of
+// setup_gpu.cu) finish on the host once every subdomain's local structure,
+// level schedules and slot layout are in pc (concatenated in subdomain
+// order) and perm_f_all / perm_b_all hold the level orders: factor offsets,
+// vector sizes, 16-bit level orders, the level records' layout and the
+// launch order.
+void schwarz_finish(sg_precond* pc, const std::vector<int>& perm_f_all,
+                    const std::vector<int>& perm_b_all) {
+    const int nparts = pc->nparts;
+    long long fl_total = 0, fu_total = 0;
+    int max_n = 0, t_len = 0;
+    for (int s = 0; s < nparts; ++s) {
+        SubInfo& inf = pc->h_info[s];
         t_len = std::max(t_len, tslot(inf.n, inf.tshift) + 1);
         inf.fl_off = fl_total;
         inf.fu_off = fu_total;

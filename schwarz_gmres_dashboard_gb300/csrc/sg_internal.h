@@ -321,7 +321,8 @@ struct sg_precond {
     int kind = SG_PC_NONE;
     sg_precond_opts opts{};
     bool is_setup = false;
-    bool has_structure = false;   // host integer set-up done for structure_key
+    bool has_structure = false;   // integer set-up done for structure_key
+    bool setup_on_device = false; // ... by the device kernels (false: host threads)
     uint64_t structure_key = 0;
     int n = 0;
     int nparts = 0;
