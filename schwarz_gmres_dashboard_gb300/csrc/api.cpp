@@ -500,10 +500,26 @@ namespace {
 // FNV-1a over everything the host set-up of a Schwarz preconditioner reads
 uint64_t structure_key(const sg_precond* pc, const sg_csr* A, const int* part, int nparts,
                        int overlap) {
-    uint64_t h = 1469598103934665603ull;
+    // four independent 64-bit lanes (multiply, xor-shift) over 8-byte words,
+    // so the hash runs at memory speed; each array is hashed with its length
+    uint64_t h[4] = {0x243f6a8885a308d3ull, 0x13198a2e03707344ull, 0xa4093822299f31d0ull,
+                     0x082efa98ec4e6c89ull};
+    auto step = [](uint64_t x, uint64_t w) {
+        x ^= w * 0x9e3779b97f4a7c15ull;
+        x *= 0xbf58476d1ce4e5b9ull;
+        return x ^ (x >> 31);
+    };
     auto mix = [&](const void* p, size_t bytes) {
         const unsigned char* c = static_cast<const unsigned char*>(p);
-        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
+        size_t i = 0;
+        for (; i + 32 <= bytes; i += 32) {
+            uint64_t w[4];
+            std::memcpy(w, c + i, 32);
+            for (int l = 0; l < 4; ++l) h[l] = step(h[l], w[l]);
+        }
+        uint64_t tail[4] = {0, 0, 0, 0};
+        std::memcpy(tail, c + i, bytes - i);
+        for (int l = 0; l < 4; ++l) h[l] = step(h[l], tail[l] ^ ((uint64_t)bytes << (8 * l)));
     };
     const int head[6] = {pc->kind, A->nrows, A->ncols, A->nnz, nparts, overlap};
     mix(head, sizeof(head));
@@ -511,7 +527,9 @@ uint64_t structure_key(const sg_precond* pc, const sg_csr* A, const int* part, i
     mix(A->h_rp.data(), sizeof(int) * A->h_rp.size());
     mix(A->h_ci.data(), sizeof(int) * A->h_ci.size());
     mix(part, sizeof(int) * (size_t)A->nrows);
-    return h;
+    uint64_t r = 0;
+    for (int l = 0; l < 4; ++l) r = step(r ^ (uint64_t)l, h[l]);
+    return r;
 }
 }  // namespace
 

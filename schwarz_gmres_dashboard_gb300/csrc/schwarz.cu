@@ -458,46 +458,61 @@ k_sweep_sf(const SubInfo* __restrict__ info, const int* __restrict__ order,
 
 // ---------------------------------------------------------------- coarse space
 // A0[i][j] in the reference's summation order (see oracle notes): for every
-// owned row k of part i ascending, the part-j sum of row k in entry order,
-// then accumulated into row i.  One thread per part keeps the order.
-__global__ void k_a0_build(int nc, const int* __restrict__ owned_ptr,
-                           const int* __restrict__ owned, const int* __restrict__ rp,
-                           const int* __restrict__ ci, const double* __restrict__ v,
-                           const int* __restrict__ part, const double* __restrict__ cscale,
-                           double* a0) {
+// owned row k of part i ascending, the part-j sum of row k in entry order
+// (from 0.0), then c_i times it accumulated into A0[i][j] (from 0.0), all
+// rounded op by op.  Every (i, j) is its own fold over k, so one block per
+// part i lists the parts j its rows touch and gives each j a thread; the
+// threads of a warp walk the same rows and entries in lockstep (the loads
+// are broadcasts) and each keeps only its own j's terms.
+__global__ void __launch_bounds__(256)
+k_a0_build(int nc, const int* __restrict__ owned_ptr, const int* __restrict__ owned,
+           const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ v,
+           const int* __restrict__ part, const double* __restrict__ cscale, double* a0) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    double* acc = reinterpret_cast<double*>(smraw);
-    double* row = acc + nc;
-    int* seen = reinterpret_cast<int*>(row + nc);
-    int* list = seen + nc;
+    int* flag = reinterpret_cast<int*>(smraw);  // nc
+    int* list = flag + nc;                      // nc
+    __shared__ int s_nl;
     const int i = blockIdx.x;
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
-        row[t] = 0.0;
-        seen[t] = -1;
+    const int q0 = owned_ptr[i], q1 = owned_ptr[i + 1];
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) flag[t] = 0;
+    __syncthreads();
+    for (int q = q0 + (int)threadIdx.x; q < q1; q += blockDim.x) {
+        const int k = owned[q];
+        for (int e = rp[k]; e < rp[k + 1]; ++e) flag[part[ci[e]]] = 1;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        const double c_i = cscale[i];
-        for (int q = owned_ptr[i]; q < owned_ptr[i + 1]; ++q) {
-            const int k = owned[q];
-            int nl = 0;
-            for (int e = rp[k]; e < rp[k + 1]; ++e) {
-                const int j = part[ci[e]];
-                if (seen[j] != k) {
-                    seen[j] = k;
-                    acc[j] = 0.0;
-                    list[nl++] = j;
-                }
-                acc[j] = __dadd_rn(acc[j], __dmul_rn(v[e], cscale[j]));
-            }
-            for (int t = 0; t < nl; ++t) {
-                const int j = list[t];
-                row[j] = __dadd_rn(row[j], __dmul_rn(c_i, acc[j]));
-            }
+    if (threadIdx.x < 32) {  // the touched parts, ascending
+        const int lane = threadIdx.x;
+        int base = 0;
+        for (int t0 = 0; t0 < nc; t0 += 32) {
+            const bool on = t0 + lane < nc && flag[t0 + lane];
+            const unsigned m = __ballot_sync(0xffffffffu, on);
+            if (on) list[base + __popc(m & ((1u << lane) - 1u))] = t0 + lane;
+            base += __popc(m);
         }
+        if (lane == 0) s_nl = base;
     }
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) a0[(size_t)i * nc + t] = 0.0;
     __syncthreads();
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) a0[(size_t)i * nc + t] = row[t];
+    const int nl = s_nl;
+    const double c_i = cscale[i];
+    for (int x = threadIdx.x; x < nl; x += blockDim.x) {
+        const int jj = list[x];
+        const double c_j = cscale[jj];
+        double row = 0.0;
+        for (int q = q0; q < q1; ++q) {
+            const int k = owned[q];
+            double acc = 0.0;
+            bool any = false;
+            for (int e = rp[k]; e < rp[k + 1]; ++e) {
+                if (part[ci[e]] != jj) continue;
+                acc = __dadd_rn(acc, __dmul_rn(v[e], c_j));
+                any = true;
+            }
+            if (any) row = __dadd_rn(row, __dmul_rn(c_i, acc));
+        }
+        a0[(size_t)i * nc + jj] = row;
+    }
 }
 
 // Dense LU with partial pivoting, one CTA (src/precond/coarse_solve.h:15-47:
@@ -821,10 +836,10 @@ void precond_setup_device(sg_precond* pc, const sg_csr* A) {
         pc->r0.alloc(nc);
         pc->status_d.alloc(1);
         pc->status_d.zero(st);
-        const size_t smem = (size_t)nc * (8 + 8 + 4 + 4);
+        const size_t smem = (size_t)nc * (4 + 4);
         SG_CUDA(cudaFuncSetAttribute(k_a0_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
-        k_a0_build<<<nc, 32, smem, st>>>(nc, pc->owned_ptr_d.p, pc->owned_d.p, A->rp.p, A->ci.p,
+        k_a0_build<<<nc, 256, smem, st>>>(nc, pc->owned_ptr_d.p, pc->owned_d.p, A->rp.p, A->ci.p,
                                          A->val.p, pc->part_d.p, pc->cscale_d.p, pc->a0.p);
         SG_CUDA(cudaGetLastError());
         SG_CUDA(cudaMemcpyAsync(pc->lu0.p, pc->a0.p, sizeof(double) * nc * nc,

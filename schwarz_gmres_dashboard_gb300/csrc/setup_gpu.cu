@@ -16,8 +16,9 @@
 //  3. local CSR: per local row the entries whose column is in the bitmap,
 //     local column = its rank, in the original (sorted) order, plus the
 //     global entry index, the diagonal position and the row's widths;
-//  4. level schedules: one thread per subdomain walks its rows in order
-//     (forward) and in reverse (backward), then places the rows by level;
+//  4. level schedules: one block per subdomain relaxes the level recurrence
+//     to its (unique) fixed point in shared memory, then one warp places the
+//     rows by level, stably;
 //  5. slot layout: per candidate shift the warp-exact bank-conflict cost of
 //     the sweep's shared-memory loads (distinct slots per bank, as the host
 //     counts them).
@@ -409,48 +410,102 @@ struct LevArgs {
     int* lev_up;
     int* nlev;          // [2P]: forward, backward level counts
     int P;
+    int* bad;           // set when a relaxation did not settle (never, for a valid CSR)
 };
 
-// one thread per subdomain: the forward levels in row order, the backward
-// levels in reverse (levels_lower / levels_upper of setup.cpp)
-__global__ void k_levels(LevArgs a) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.P) return;
+// One block per subdomain: the forward and backward levels (levels_lower /
+// levels_upper of setup.cpp) as the fixed point of
+//   lev(i) = max(lev(c) + 1 over the row's lower (upper) columns c), 0 if none,
+// relaxed in place by all threads until a pass changes nothing.  The fixed
+// point of this recurrence over a DAG is unique (the longest path into the
+// row), so the result is the serial loop's whatever the update order; a pass
+// propagates at least one more level, and in natural order usually many.
+// Levels live in shared memory when the subdomain fits (else in global).
+constexpr int LV_T = 256;
+
+__device__ __forceinline__ int lev_pass(const int* rp, const int* ci, const int* dg, int ns,
+                                        int* lev, bool back) {
+    int changed = 0;
+    for (int i = threadIdx.x; i < ns; i += LV_T) {
+        const int r = back ? ns - 1 - i : i;
+        int l = 0;
+        if (!back) {
+            for (int e = rp[r]; e < rp[r + 1]; ++e) {
+                const int c = ci[e];
+                if (c >= r) break;
+                l = max(l, ((volatile int*)lev)[c] + 1);
+            }
+        } else {
+            // a repeated diagonal entry (c == r) counts as level 0 + 1: the
+            // serial loop reads the row's own level before writing it
+            for (int e = dg[r] + 1; e < rp[r + 1]; ++e) {
+                const int c = ci[e];
+                l = max(l, c == r ? 1 : ((volatile int*)lev)[c] + 1);
+            }
+        }
+        if (l != ((volatile int*)lev)[r]) {
+            ((volatile int*)lev)[r] = l;
+            changed = 1;
+        }
+    }
+    return __syncthreads_or(changed);
+}
+
+__global__ void __launch_bounds__(LV_T) k_levels(LevArgs a, int smem_rows) {
+    extern __shared__ int slev[];
+    const int s = blockIdx.x;
     const int r0 = a.sub_ptr[s], ns = a.sub_ptr[s + 1] - r0;
     const int* rp = a.lrp + r0 + s;
     const int* ci = a.lci + a.nz0[s];
     const int* dg = a.ldiag + r0;
-    int* lo = a.lev_lo + r0;
-    int* up = a.lev_up + r0;
-    int nl = 0;
-    for (int i = 0; i < ns; ++i) {
-        int l = 0;
-        for (int e = rp[i]; e < rp[i + 1]; ++e) {
-            const int c = ci[e];
-            if (c >= i) break;
-            l = max(l, lo[c] + 1);
+    for (int dir = 0; dir < 2; ++dir) {
+        int* out = (dir ? a.lev_up : a.lev_lo) + r0;
+        int* lev = ns <= smem_rows ? slev : out;  // out is zero on entry
+        if (lev == slev)
+            for (int i = threadIdx.x; i < ns; i += LV_T) slev[i] = 0;
+        __syncthreads();
+        // the fixed point needs at most (longest path + 1) <= ns + 1 passes;
+        // the bound makes any error in the recurrence end with a status
+        // instead of a loop that never ends
+        int pass = 0;
+        while (lev_pass(rp, ci, dg, ns, lev, dir == 1)) {
+            if (++pass > ns + 1) {
+                if (threadIdx.x == 0) atomicExch(a.bad, 1);
+                break;
+            }
         }
-        lo[i] = l;
-        nl = max(nl, l + 1);
+        int nl = 0;
+        for (int i = threadIdx.x; i < ns; i += LV_T) {
+            const int l = lev[i];
+            nl = max(nl, l + 1);
+            if (lev == slev) out[i] = l;
+        }
+        nl = __reduce_max_sync(0xffffffffu, nl);
+        __shared__ int s_nl[LV_T / 32];
+        if ((threadIdx.x & 31) == 0) s_nl[threadIdx.x >> 5] = nl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int m = 0;
+            for (int w = 0; w < LV_T / 32; ++w) m = max(m, s_nl[w]);
+            a.nlev[dir * a.P + s] = m;
+        }
+        __syncthreads();
     }
-    a.nlev[s] = nl;
-    nl = 0;
-    for (int i = ns - 1; i >= 0; --i) {
-        int l = 0;
-        for (int e = dg[i] + 1; e < rp[i + 1]; ++e) l = max(l, up[ci[e]] + 1);
-        up[i] = l;
-        nl = max(nl, l + 1);
-    }
-    a.nlev[a.P + s] = nl;
 }
 
-// one thread per subdomain and direction: rows placed by level, stable
-// (level_order of setup.cpp); ptr (nlev + 1 entries) is zero on entry
-__global__ void k_level_order(const int* sub_ptr, const int* lev_lo, const int* lev_up,
-                              const int* lev_off_f, const int* lev_off_b, const int* nlev, int P,
-                              int* ptr_f, int* ptr_b, int* perm_f, int* perm_b) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 2 * P) return;
+// One block per subdomain and direction: rows placed by level, stable
+// (level_order of setup.cpp).  All threads count per level; warp 0 places
+// the rows 32 at a time in row order (equal levels ranked by
+// __match_any_sync), advancing per-level cursors.  ptr (nlev + 1 entries,
+// zero on entry) is in global memory; the cursors in shared memory when
+// they fit.
+__global__ void __launch_bounds__(LV_T) k_level_order(const int* sub_ptr, const int* lev_lo,
+                                                      const int* lev_up, const int* lev_off_f,
+                                                      const int* lev_off_b, const int* nlev,
+                                                      int P, int* ptr_f, int* ptr_b, int* perm_f,
+                                                      int* perm_b, int smem_levels) {
+    extern __shared__ int scur[];
+    const int t = blockIdx.x;
     const int s = t % P;
     const bool back = t >= P;
     const int r0 = sub_ptr[s], ns = sub_ptr[s + 1] - r0;
@@ -458,12 +513,44 @@ __global__ void k_level_order(const int* sub_ptr, const int* lev_lo, const int* 
     int* ptr = back ? ptr_b + lev_off_b[s] : ptr_f + lev_off_f[s];
     int* perm = (back ? perm_b : perm_f) + r0;
     const int nl = nlev[t];
-    for (int i = 0; i < ns; ++i) ptr[lev[i] + 1]++;
-    for (int l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
-    // place in row order; ptr[l] advances to ptr[l + 1] and is restored after
-    for (int i = 0; i < ns; ++i) perm[ptr[lev[i]]++] = i;
-    for (int l = nl; l > 0; --l) ptr[l] = ptr[l - 1];
-    ptr[0] = 0;
+    for (int i = threadIdx.x; i < ns; i += LV_T) atomicAdd(&ptr[lev[i] + 1], 1);
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
+    __syncthreads();
+    int* cur = nl <= smem_levels ? scur : nullptr;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        if (cur)
+            for (int l = lane; l < nl; l += 32) cur[l] = ptr[l];
+        __syncwarp();
+        const unsigned lt = (1u << lane) - 1u;
+        for (int i0 = 0; i0 < ns; i0 += 32) {
+            const int i = i0 + lane;
+            const bool valid = i < ns;
+            const int l = valid ? lev[i] : -1 - lane;
+            const unsigned peers = __match_any_sync(0xffffffffu, l);
+            int base = 0;
+            if (valid) base = cur ? cur[l] : ptr[l];
+            __syncwarp();
+            if (valid) {
+                perm[base + __popc(peers & lt)] = i;
+                if (lane == __ffs(peers) - 1) {
+                    if (cur) cur[l] = base + __popc(peers);
+                    else ptr[l] = base + __popc(peers);
+                }
+            }
+            __syncwarp();
+        }
+        if (!cur) {
+            // the cursors ran in ptr: each advanced to the next level's start
+            __syncwarp();
+            if (lane == 0) {
+                for (int l = nl; l > 0; --l) ptr[l] = ptr[l - 1];
+                ptr[0] = 0;
+            }
+        }
+    }
 }
 
 // ------------------------------------------------------------ slot layout
@@ -768,12 +855,21 @@ bool build_schwarz_device(sg_precond* pc, const sg_csr* A, const int* part_in, i
     d_lev_lo.zero(st);  // as the host's level arrays: a repeated diagonal entry reads 0
     d_lev_up.zero(st);
     d_nlev.alloc((size_t)2 * P);
-    LevArgs la{d_sptr.p, d_lrp.p, d_lci.p, d_ldiag.p, d_nz0.p, d_lev_lo.p, d_lev_up.p, d_nlev.p, P};
-    k_levels<<<(P + 63) / 64, 64, 0, st>>>(la);
+    d_bad.zero(st);
+    LevArgs la{d_sptr.p, d_lrp.p, d_lci.p, d_ldiag.p, d_nz0.p, d_lev_lo.p, d_lev_up.p, d_nlev.p, P,
+               d_bad.p};
+    const int lv_smem_rows = 24 * 1024;  // 96 KB of shared levels per block at most
+    int max_ns = 0;
+    for (int s = 0; s < P; ++s) max_ns = std::max(max_ns, sptr[s + 1] - sptr[s]);
+    const size_t lv_smem = sizeof(int) * (size_t)std::min(max_ns, lv_smem_rows);
+    SG_CUDA(cudaFuncSetAttribute(k_levels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lv_smem));
+    k_levels<<<P, LV_T, lv_smem, st>>>(la, lv_smem_rows);
     SG_CUDA(cudaGetLastError());
     std::vector<int> nlev;
     download(nlev, d_nlev.p, (size_t)2 * P, st);
+    download(bad, d_bad.p, 1, st);
     SG_CUDA(cudaStreamSynchronize(st));
+    if (bad[0]) fail(SG_ERR_INTERNAL, "device set-up: a level schedule did not settle");
     std::vector<int> loff_f((size_t)P), loff_b((size_t)P);
     long long tf = 0, tb = 0;
     for (int s = 0; s < P; ++s) {
@@ -791,9 +887,15 @@ bool build_schwarz_device(sg_precond* pc, const sg_csr* A, const int* part_in, i
     d_ptr_b.zero(st);
     d_perm_f.alloc((size_t)nsub);
     d_perm_b.alloc((size_t)nsub);
-    k_level_order<<<(2 * P + 63) / 64, 64, 0, st>>>(d_sptr.p, d_lev_lo.p, d_lev_up.p, d_loff_f.p,
-                                                    d_loff_b.p, d_nlev.p, P, d_ptr_f.p, d_ptr_b.p,
-                                                    d_perm_f.p, d_perm_b.p);
+    int max_nl = 0;
+    for (int t = 0; t < 2 * P; ++t) max_nl = std::max(max_nl, nlev[t]);
+    const int lo_smem_levels = 16 * 1024;
+    const size_t lo_smem = sizeof(int) * (size_t)std::min(max_nl, lo_smem_levels);
+    SG_CUDA(cudaFuncSetAttribute(k_level_order, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)std::max<size_t>(lo_smem, 4)));
+    k_level_order<<<2 * P, LV_T, std::max<size_t>(lo_smem, 4), st>>>(
+        d_sptr.p, d_lev_lo.p, d_lev_up.p, d_loff_f.p, d_loff_b.p, d_nlev.p, P, d_ptr_f.p,
+        d_ptr_b.p, d_perm_f.p, d_perm_b.p, lo_smem_levels);
     SG_CUDA(cudaGetLastError());
     // ---- slot layout
     DBuf<long long> d_cost;
