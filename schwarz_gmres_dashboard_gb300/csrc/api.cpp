@@ -23,9 +23,24 @@ uint64_t next_object_gen() {
 
 namespace sg {
 
-static thread_local std::string g_last_error;
+// The last error message of this thread.  A fixed buffer rather than a
+// std::string: thread_local objects with destructors are destroyed before
+// static ones at exit, and a caller that releases its objects from a static
+// destructor (a context kept in a static smart pointer, say) would otherwise
+// write into the freed string.
+struct LastError {
+    char msg[1024];
+    void set(const char* m) {
+        size_t k = 0;
+        if (m)
+            for (; m[k] && k + 1 < sizeof(msg); ++k) msg[k] = m[k];
+        msg[k] = '\0';
+    }
+    void clear() { msg[0] = '\0'; }
+};
+static thread_local LastError g_last_error{};
 
-void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+void set_last_error(const char* msg) { g_last_error.set(msg); }
 
 void fail(sg_status st, const char* fmt, ...) {
     char buf[1024];
@@ -60,16 +75,16 @@ static sg_status guard(F&& f) {
         g_last_error.clear();
         return SG_OK;
     } catch (const Error& e) {
-        g_last_error = e.msg;
+        g_last_error.set(e.msg.c_str());
         return e.status;
     } catch (const std::bad_alloc&) {
-        g_last_error = "host allocation failed";
+        g_last_error.set("host allocation failed");
         return SG_ERR_OOM;
     } catch (const std::exception& e) {
-        g_last_error = e.what();
+        g_last_error.set(e.what());
         return SG_ERR_INTERNAL;
     } catch (...) {
-        g_last_error = "unknown internal error";
+        g_last_error.set("unknown internal error");
         return SG_ERR_INTERNAL;
     }
 }
@@ -167,7 +182,7 @@ extern "C" {
 
 int sg_abi_version(void) { return SG_ABI_VERSION; }
 
-const char* sg_last_error(void) { return g_last_error.c_str(); }
+const char* sg_last_error(void) { return g_last_error.msg; }
 
 const char* sg_status_string(sg_status st) {
     switch (st) {

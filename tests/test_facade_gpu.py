@@ -23,8 +23,13 @@ def results(sg, tmp_path_factory):
     subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "facade_plugins.cpp"), "-o", exe,
                     "-L", BUILD, "-lsgmres", f"-Wl,-rpath,{BUILD}"], check=True)
-    out = subprocess.run([exe, os.path.join(ROOT, "tests", "golden", "mtx", "symmetric.mtx")],
-                         capture_output=True, text=True, timeout=300, check=True).stdout
+    # three runs: the program releases its context from a static destructor
+    # at exit, after the library's thread-local storage is gone -- a path
+    # that once wrote into freed memory and aborted one run in four
+    outs = [subprocess.run([exe, os.path.join(ROOT, "tests", "golden", "mtx", "symmetric.mtx")],
+                           capture_output=True, text=True, timeout=300, check=True).stdout
+            for _ in range(3)]
+    out = outs[0]
     return {ln.split(" ", 1)[0]: ln.split(" ", 1)[1].split() for ln in out.splitlines() if ln}
 
 
