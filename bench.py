@@ -593,7 +593,7 @@ def run_learned(args):
     if lrn:
         fl = learned_flops(nc)
         ach = fl / (lrn["us_per_launch"] / 1e6) / 1e12
-        roofline = {"kernel": "learned stage (FP32 residual+restrict, 4 x k_conv3d mma.sync "
+        roofline = {"kernel": "learned stage (FP32 residual+restrict, 4 x k_conv3d_tc tcgen05 "
                               "BF16, prolong)", "bound": "tensor", "achieved": ach,
                     "peak": bf16_peak, "unit": "TFLOP/s", "frac": ach / bf16_peak,
                     "traffic": None, "flops_per_apply": fl,

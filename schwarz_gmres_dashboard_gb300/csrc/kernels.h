@@ -117,6 +117,7 @@ void learned_begin(sg_learned* L, SolveState* st);
 void learned_monitor(sg_learned* L, SolveState* st);
 void learned_detach(sg_learned* L);
 uint64_t learned_gen(const sg_learned* L);  // changes when the stage's matrix changes
+int learned_error(sg_learned* L);  // a convolution's bounded wait ran out (read and cleared)
 
 // ---------------------------------------------------------------- batched.cu
 // nsys independent systems (block-diagonal A, rows of system s at

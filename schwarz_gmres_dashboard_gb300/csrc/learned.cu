@@ -24,16 +24,20 @@
 // the solve when the cycle reduced the FP64 true residual by less than the
 // stagnation ratio -- the plain preconditioner is the fallback.
 //
-// Every layer is an implicit GEMM on the tensor cores (mma.sync m16n8k16,
-// BF16 x BF16 -> FP32): a CTA owns an 8x8x8 block of output voxels, stages
-// the 10x10x10 input halo (16 channels, channel-last) and the layer's weights
-// in shared memory, and each warp accumulates one z-plane of 64 voxels over
-// the 27 taps (K = 16 channels per tap).  The input gradient is the same
-// kernel with flipped, transposed weights and the ReLU mask of the layer
-// input in the epilogue; the weight gradient is a second mma kernel (M =
-// input channel, N = output channel, K = the tile's voxels) whose per-CTA
-// partials a reduction kernel adds in a fixed order.  Channels are padded to
-// 16 everywhere (layer 1 reads 2, layer 4 writes 1); padded weights stay 0.
+// Every layer is an implicit GEMM on the tensor cores.  The forward layers
+// and the input gradient run on tcgen05.mma (BF16 x BF16 -> FP32 in tensor
+// memory): a CTA owns an 8 x 16 x 4 block of output voxels, TMA stages its
+// 10 x 18 x 6 input halo (16 channels as two 8-channel planes) and a bulk copy
+// the layer's weights, and one thread issues one 128 x 16 x 16 MMA per tap
+// and z-plane straight from the shifted halo (k_conv3d_tc).  The input
+// gradient is the same kernel with flipped, transposed weights and the ReLU
+// mask of the layer input in the epilogue.  The weight gradient (M = 16 input
+// channels, below the 64 rows a tcgen05.mma needs; N = output channel, K =
+// the tile's voxels) is an mma.sync kernel whose per-CTA partials a reduction
+// kernel adds in a fixed order.  Channels are padded to 16 everywhere (layer
+// 1 reads 2, layer 4 writes 1); padded weights stay 0.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -43,6 +47,7 @@
 
 #include "dev_common.cuh"
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace sg {
 
@@ -69,12 +74,11 @@ struct LearnedCtl {
 
 namespace {
 
-constexpr int CT = 256;  // threads of the conv kernels (8 warps)
+constexpr int CT = 256;  // threads of the weight-gradient kernel (8 warps)
 constexpr int TB = 8;    // output tile edge
 constexpr int HB = TB + 2;
 constexpr int HALO_U32 = HB * HB * HB * 8;
 constexpr int TILE_U32 = TB * TB * TB * 8;
-constexpr int W_U32 = LTAPS * LC * 8;
 constexpr int WGRAD_SMEM = (HALO_U32 + TILE_U32) * 4 + CT * 4;
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -114,89 +118,216 @@ __device__ __forceinline__ void load_halo(uint32_t* halo, const uint32_t* __rest
     }
 }
 
-// conv3d 3x3x3, 16 -> 16 channels, one 8^3 output tile per CTA, grid =
-// tiles x batch.  w: BF16 [27][co][ci] (ci contiguous).  Epilogues:
+// ---- the convolution layers on the 5th-generation tensor cores
+//
+// One CTA computes an output tile of 8 (x) x 16 (y) x 4 (z) voxels as four
+// GEMMs of M = 128 rows (the (y, x) positions of one z-plane), N = 16 output
+// channels and K = 27 taps x 16 input channels, accumulated in tensor memory
+// (four 128-lane x 16-column FP32 accumulators).  TMA copies the tile's
+// 10 x 18 x 6 input halo into shared memory as two 8-channel planes (16 B
+// per voxel each; the tensor map fills the voxels outside the volume with 0)
+// and a bulk copy brings the layer's weights, already in the operand layout.
+// With that layout every tap is one tcgen05.mma: the A operand of tap
+// (dz, dy, dx) is the halo plane shifted by that voxel offset -- eight
+// consecutive x positions are one 8-row x 16-byte core matrix, the 16 rows
+// of y are 8-row groups 18 x 16 B apart, the second channel half is the other
+// plane -- so no operand is ever copied or re-laid out in shared memory.
+// One thread issues the 108 MMAs and commits them to an mbarrier; each warp
+// then reads its 32 accumulator lanes (tcgen05.ld) and runs the epilogue.
+constexpr int TC_TY = 16, TC_TZ = 4;
+constexpr int TC_HX = TB + 2, TC_HY = TC_TY + 2, TC_HZ = TC_TZ + 2;
+constexpr int TC_PLANE = TC_HX * TC_HY * TC_HZ * 16;  // one 8-channel half of the halo
+constexpr int TC_WBYTES = LTAPS * LC * LC * 2;        // one layer's BF16 weights
+constexpr int TC_OFF_W = 2 * TC_PLANE;
+constexpr int TC_OFF_BAR = TC_OFF_W + TC_WBYTES;
+constexpr int TC_SMEM = TC_OFF_BAR + 32 + 128;        // + barriers and words, + alignment slack
+constexpr int TC_THREADS = 128;                       // warp w reads accumulator lanes 32w..32w+31
+constexpr int TC_COLS = TC_TZ * LC;                   // tensor-memory columns (a power of 2, >= 32)
+static_assert(TC_PLANE % 128 == 0 && TC_OFF_W % 128 == 0 && TC_OFF_BAR % 16 == 0,
+              "TMA destinations and mbarriers must stay aligned");
+static_assert(TC_COLS == 64, "tensor-memory allocation must be a power of two >= 32");
+
+// instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits
+// 4-5 = 1), BF16 A and B (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 =
+// 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28
+constexpr uint32_t tc_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+constexpr uint32_t TC_IDESC = tc_idesc(128, LC);
+
+// shared-memory operand descriptor, no swizzle, K-major: start address,
+// byte offset between the two K-adjacent core matrices (lbo) and between
+// M/N-adjacent 8-row groups (sbo), all in 16-byte units; bit 46 is the
+// descriptor version of this architecture
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// whole warp: allocate `cols` tensor-memory columns, address into smem slot
+__device__ __forceinline__ void tc_alloc(uint32_t slot, uint32_t cols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+                 "r"(cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t cols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols)
+                 : "memory");
+}
+// D[taddr] (+)= A * B^T, one thread
+__device__ __forceinline__ void tc_mma(uint32_t taddr, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(taddr),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// arrive on the mbarrier once every MMA this thread issued has completed
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+        : "memory");
+}
+// whole warp: 16 consecutive FP32 columns of this thread's accumulator lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// conv3d 3x3x3, 16 -> 16 channels.  in_map: the BF16 [batch][D][D][D][16]
+// input as a 5D tensor map (box 8 ch x 10 x 18 x 6 x 1).  w: the layer's
+// weights in operand layout ([tap][ci / 8][co][ci % 8], 512 B per tap).
+// Grid: (D/8) x ceil(D/16) x (D/4) tiles x batch.  Epilogues:
 //  RELU        out = relu(acc + bias) as BF16 [V][16]
 //  LINEAR_F32  outf[v] = acc[ch 0] + bias[0] (FP32, one channel)
 //  MASK        out = acc * (mask[v][ch] > 0) as BF16 (input gradient; no bias)
-__global__ void __launch_bounds__(CT)
-k_conv3d(const uint32_t* __restrict__ in, const uint32_t* __restrict__ w,
-         const float* __restrict__ bias, int D, int epi, uint32_t* __restrict__ out,
-         float* __restrict__ outf, const uint32_t* __restrict__ mask, const int* enabled,
-         const int* active) {
+// A wait that runs out of its budget sets *err, drains what is in flight and
+// leaves the tile's output unwritten.
+__global__ void __launch_bounds__(TC_THREADS)
+k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restrict__ w,
+            const float* __restrict__ bias, int D, int epi, uint32_t* __restrict__ out,
+            float* __restrict__ outf, const uint32_t* __restrict__ mask, const int* enabled,
+            const int* active, int* err) {
     if (skip(enabled, active)) return;
-    __shared__ __align__(16) uint32_t halo[HALO_U32];
-    __shared__ __align__(16) uint32_t ws[W_U32];
-    const int tiles = D / TB;
-    const int nt3 = tiles * tiles * tiles;
-    const int b = blockIdx.x / nt3;
-    const int t = blockIdx.x % nt3;
-    const int z0 = (t / (tiles * tiles)) * TB, y0 = ((t / tiles) % tiles) * TB, x0 = (t % tiles) * TB;
-    const size_t V = (size_t)D * D * D;
-    load_halo(halo, in + (size_t)b * V * 8, D, z0, y0, x0);
-    for (int q = threadIdx.x; q < W_U32 / 4; q += blockDim.x)
-        reinterpret_cast<uint4*>(ws)[q] = reinterpret_cast<const uint4*>(w)[q];
+    extern __shared__ uint8_t tc_raw[];
+    const uint32_t raw = smem_u32(tc_raw);
+    const uint32_t base = (raw + 127u) & ~127u;
+    uint8_t* sm = tc_raw + (base - raw);
+    const uint32_t plane0 = base, wsm = base + TC_OFF_W;
+    const uint32_t bar_in = base + TC_OFF_BAR, bar_mma = bar_in + 8;
+    uint32_t* s_taddr = reinterpret_cast<uint32_t*>(sm + TC_OFF_BAR + 16);
+    volatile int* s_bad = reinterpret_cast<volatile int*>(sm + TC_OFF_BAR + 20);
+
+    const int ntx = D / TB, nty = (D + TC_TY - 1) / TC_TY, ntz = D / TC_TZ;
+    int t = blockIdx.x;
+    const int tx = t % ntx;
+    t /= ntx;
+    const int ty = t % nty;
+    t /= nty;
+    const int tz = t % ntz, b = t / ntz;
+    const int x0 = tx * TB, y0 = ty * TC_TY, z0 = tz * TC_TZ;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        *s_bad = 0;
+        mbar_init(bar_in, 1);
+        mbar_init(bar_mma, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tc_alloc(smem_u32(s_taddr), TC_COLS);
+    tc_fence_before();
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, tg = lane & 3;
-    const int z = warp;  // this warp's z-plane of the tile
-    float acc[4][2][4];
-#pragma unroll
-    for (int mt = 0; mt < 4; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[mt][nt][e] = 0.f;
-    for (int tap = 0; tap < LTAPS; ++tap) {
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        uint32_t bf[2][2];
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt) {
-            const uint32_t* wr = ws + (tap * LC + nt * 8 + g) * 8;
-            bf[nt][0] = wr[tg];
-            bf[nt][1] = wr[tg + 4];
+    tc_fence_after();
+    const uint32_t taddr = *s_taddr;
+
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(bar_in, 2 * TC_PLANE + TC_WBYTES);
+        tma_load_5d(plane0, &in_map, 0, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
+        tma_load_5d(plane0 + TC_PLANE, &in_map, 8, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
+        bulk_g2s(wsm, w, TC_WBYTES, bar_in);
+        int bad = 0;
+        if (mbar_wait(bar_in, 0, WAIT_CYCLES)) {
+            tc_fence_after();
+            for (int mt = 0; mt < TC_TZ; ++mt)
+                for (int tap = 0; tap < LTAPS; ++tap) {
+                    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+                    const uint32_t a =
+                        plane0 + (((mt + 1 + dz) * TC_HY + 1 + dy) * TC_HX + 1 + dx) * 16;
+                    tc_mma(taddr + mt * LC, tc_sdesc(a, TC_PLANE, TC_HX * 16),
+                           tc_sdesc(wsm + tap * 512, 256, 128), TC_IDESC, tap > 0);
+                }
+            tc_commit(bar_mma);
+            if (!mbar_wait(bar_mma, 0, WAIT_CYCLES)) {
+                bad = 2;
+                mbar_wait(bar_mma, 0, WAIT_CYCLES);  // let the MMAs finish before TMEM is freed
+            }
+        } else {
+            bad = 1;
+            mbar_wait(bar_in, 0, WAIT_CYCLES);  // the copies may still land: wait once more
         }
-        // M-tile mt covers rows y = 2mt, 2mt+1 of the plane: row r -> (y = 2mt + r/8, x = r%8)
-        const int hbase = (z + 1 + dz) * HB * HB + (1 + dy) * HB + (1 + dx);
-#pragma unroll
-        for (int mt = 0; mt < 4; ++mt) {
-            const int h0 = hbase + (2 * mt) * HB + g;
-            const int h1 = h0 + HB;
-            uint32_t af[4];
-            af[0] = halo[h0 * 8 + tg];
-            af[1] = halo[h1 * 8 + tg];
-            af[2] = halo[h0 * 8 + tg + 4];
-            af[3] = halo[h1 * 8 + tg + 4];
-#pragma unroll
-            for (int nt = 0; nt < 2; ++nt) mma_bf16(acc[mt][nt], af, bf[nt]);
+        if (bad) {
+            *s_bad = bad;
+            atomicExch(err, bad);
         }
     }
-    // C fragment: rows g / g+8 of the M-tile (y = 2mt / 2mt+1, x = g),
-    // columns nt*8 + 2tg, +1
-#pragma unroll
-    for (int mt = 0; mt < 4; ++mt) {
-#pragma unroll
-        for (int hr = 0; hr < 2; ++hr) {
-            const int yy = y0 + 2 * mt + hr, xx = x0 + g, zz = z0 + z;
-            const size_t v = (size_t)b * V + ((size_t)zz * D + yy) * D + xx;
-#pragma unroll
-            for (int nt = 0; nt < 2; ++nt) {
-                const int ch = nt * 8 + 2 * tg;
-                float a0 = acc[mt][nt][2 * hr], a1 = acc[mt][nt][2 * hr + 1];
-                if (epi == EPI_RELU) {
-                    a0 = fmaxf(a0 + bias[ch], 0.f);
-                    a1 = fmaxf(a1 + bias[ch + 1], 0.f);
-                    out[v * 8 + ch / 2] = pack_bf16(a0, a1);
-                } else if (epi == EPI_MASK) {
-                    const uint32_t mk = mask[v * 8 + ch / 2];
-                    a0 = bf_lo(mk) > 0.f ? a0 : 0.f;
-                    a1 = bf_hi(mk) > 0.f ? a1 : 0.f;
-                    out[v * 8 + ch / 2] = pack_bf16(a0, a1);
-                } else if (ch == 0) {
-                    outf[v] = a0 + bias[0];
-                }
+    __syncthreads();
+    tc_fence_after();
+    if (*s_bad == 0) {
+        const int m = warp * 32 + lane;  // accumulator lane = GEMM row = (y, x) in the z-plane
+        const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
+        const size_t V = (size_t)D * D * D;
+#pragma unroll 1
+        for (int mt = 0; mt < TC_TZ; ++mt) {
+            float acc[16];
+            tc_ld16(taddr + ((uint32_t)(warp * 32) << 16) + mt * LC, acc);
+            if (yy >= D) continue;
+            const size_t v = (size_t)b * V + ((size_t)(z0 + mt) * D + yy) * D + xx;
+            if (epi == EPI_LINEAR_F32) {
+                outf[v] = acc[0] + bias[0];
+                continue;
             }
+            uint32_t pk[8];
+            if (epi == EPI_RELU) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    pk[c] = pack_bf16(fmaxf(acc[2 * c] + bias[2 * c], 0.f),
+                                      fmaxf(acc[2 * c + 1] + bias[2 * c + 1], 0.f));
+            } else {
+                const uint4 m0 = reinterpret_cast<const uint4*>(mask + v * 8)[0];
+                const uint4 m1 = reinterpret_cast<const uint4*>(mask + v * 8)[1];
+                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    pk[c] = pack_bf16(bf_lo(mw[c]) > 0.f ? acc[2 * c] : 0.f,
+                                      bf_hi(mw[c]) > 0.f ? acc[2 * c + 1] : 0.f);
+            }
+            uint4* o = reinterpret_cast<uint4*>(out + v * 8);
+            o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
         }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tc_dealloc(taddr, TC_COLS);
     }
 }
 
@@ -292,9 +423,11 @@ __global__ void k_wgrad_reduce(const float* __restrict__ part, int nblk,
     grad[i] = s * pmask[i];
 }
 
-// master FP32 [layer][tap][ci][co] -> forward BF16 [layer][tap][co][ci] and
-// the flipped, transposed BF16 weights of the input gradient
-// [layer][26 - tap][ci][co]
+// master FP32 [layer][tap][ci][co] -> the BF16 weights of the forward layers
+// and the flipped, transposed weights of the input gradient (tap 26 - t,
+// input and output channels swapped), both in the operand layout of
+// k_conv3d_tc: per tap the 16 x 16 (output x input channel) block as two
+// 8-input-channel halves, each 16 rows of 8 channels ([tap][k / 8][n][k % 8])
 __global__ void k_prep_weights(const float* __restrict__ master, __nv_bfloat16* __restrict__ wf,
                                __nv_bfloat16* __restrict__ wt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -302,8 +435,9 @@ __global__ void k_prep_weights(const float* __restrict__ master, __nv_bfloat16* 
     const int l = i / LAYER_W, r = i % LAYER_W;
     const int tap = r / (LC * LC), ci = (r / LC) % LC, co = r % LC;
     const __nv_bfloat16 v = __float2bfloat16_rn(master[(size_t)l * LAYER_P + r]);
-    wf[(size_t)l * LAYER_W + (tap * LC + co) * LC + ci] = v;
-    wt[(size_t)l * LAYER_W + ((LTAPS - 1 - tap) * LC + ci) * LC + co] = v;
+    const size_t lb = (size_t)l * LAYER_W;
+    wf[lb + tap * LC * LC + (ci / 8) * 8 * LC + co * 8 + ci % 8] = v;
+    wt[lb + (LTAPS - 1 - tap) * LC * LC + (co / 8) * 8 * LC + ci * 8 + co % 8] = v;
 }
 
 // Adam (Kingma & Ba 2015) on the network parameters; padded entries stay 0
@@ -647,6 +781,7 @@ struct LearnedImpl {
     DBuf<float> feat;                        // coefficient feature of A
     DBuf<double> partials;
     DBuf<unsigned> counter;
+    DBuf<int> cerr;  // set by a convolution whose bounded wait ran out
     // inference scratch (one sample)
     DBuf<float> rc, ec, yout;
     DBuf<uint32_t> act[4];
@@ -693,13 +828,48 @@ void prep_weights(sg_learned* L) {
     count_launch(L->ctx);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link the driver API)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    if (!fn) fail(SG_ERR_CUDA, "the driver provides no cuTensorMapEncodeTiled");
+    return fn;
+}
+
+// the 5D tensor map of a BF16 [batch][D][D][D][16] activation volume whose
+// box is one 8-channel half of a k_conv3d_tc halo
+CUtensorMap halo_map(const uint32_t* in, int D, int batch) {
+    CUtensorMap m;
+    const cuuint64_t d = (cuuint64_t)D;
+    const cuuint64_t dims[5] = {LC, d, d, d, (cuuint64_t)batch};
+    const cuuint64_t strides[4] = {LC * 2, LC * 2 * d, LC * 2 * d * d, LC * 2 * d * d * d};
+    const cuuint32_t box[5] = {8, TC_HX, TC_HY, TC_HZ, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const CUresult r = tensor_map_encoder()(
+        &m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<uint32_t*>(in), dims, strides, box, estr,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(SG_ERR_CUDA, "tensor map encoding failed (CUresult %d)", (int)r);
+    return m;
+}
+
 void conv(sg_learned* L, const uint32_t* in, int l, bool transposed, int epi, int batch,
           uint32_t* out, float* outf, const uint32_t* mask, const int* enabled, const int* active) {
-    const int tiles = L->cx / TB;
+    const int D = L->cx;
+    const int tiles = (D / TB) * ((D + TC_TY - 1) / TC_TY) * (D / TC_TZ);
     const __nv_bfloat16* w = (transposed ? L->wt.p : L->wf.p) + (size_t)l * LAYER_W;
-    k_conv3d<<<tiles * tiles * tiles * batch, CT, 0, L->ctx->stream>>>(
-        in, reinterpret_cast<const uint32_t*>(w), L->master.p + (size_t)l * LAYER_P + LAYER_W,
-        L->cx, epi, out, outf, mask, enabled, active);
+    k_conv3d_tc<<<tiles * batch, TC_THREADS, TC_SMEM, L->ctx->stream>>>(
+        halo_map(in, D, batch), reinterpret_cast<const uint8_t*>(w),
+        L->master.p + (size_t)l * LAYER_P + LAYER_W, D, epi, out, outf, mask, enabled, active,
+        L->cerr.p);
     SG_CUDA(cudaGetLastError());
     count_launch(L->ctx);
 }
@@ -901,9 +1071,26 @@ void check_ready(const sg_learned* L) {
     if (!L->A) fail(SG_ERR_NOT_SETUP, "learned stage has no matrix (sg_learned_set_matrix)");
 }
 
+void check_conv(sg_learned* L) {
+    if (learned_error(L))
+        fail(SG_ERR_DEVICE_TIMEOUT, "a learned-stage convolution gave up waiting for its tile");
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- hooks
+int learned_error(sg_learned* L) {
+    if (!L || !L->cerr.p) return 0;
+    int e = 0;
+    SG_CUDA(cudaMemcpyAsync(&e, L->cerr.p, sizeof(int), cudaMemcpyDeviceToHost, L->ctx->stream));
+    SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    if (e) {  // reported once
+        L->cerr.zero(L->ctx->stream);
+        SG_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    }
+    return e;
+}
+
 template <class TI, class TO>
 void learned_apply(sg_learned* L, const TI* x, TO* y, int n, const int* active) {
     check_ready(L);
@@ -1052,6 +1239,10 @@ sg_status sg_learned_create(sg_ctx* ctx, int nx, int ny, int nz, sg_learned** ou
             L->partials.alloc(4096);
             L->counter.alloc(1);
             L->counter.zero(ctx->stream);
+            L->cerr.alloc(1);
+            L->cerr.zero(ctx->stream);
+            SG_CUDA(cudaFuncSetAttribute(k_conv3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         TC_SMEM));
             L->rc.alloc(L->nc);
             L->ec.alloc(L->nc);
             L->yout.alloc(L->nc);
@@ -1316,6 +1507,7 @@ sg_status sg_learned_sample_gradient(sg_learned* L, int first, int count, float*
         SG_CUDA(cudaMemcpyAsync(grad, L->grad.p, sizeof(float) * NET_PARAMS, cudaMemcpyDeviceToHost,
                                 ctx->stream));
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_conv(L);
         *loss = l;
     });
 }
@@ -1385,6 +1577,7 @@ sg_status sg_learned_train(sg_learned* L, int first, int count, int epochs, int 
                                     ctx->stream));
             SG_CUDA(cudaStreamSynchronize(ctx->stream));
             if (epoch_loss) epoch_loss[ep] = (double)lsum / nb;
+            check_conv(L);
             if (!std::isfinite(lsum)) fail(SG_ERR_NONFINITE, "training loss is not finite");
         }
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1421,6 +1614,7 @@ sg_status sg_learned_eval(sg_learned* L, int first, int count, double* loss) {
             SG_CUDA(cudaStreamSynchronize(ctx->stream));
             total += (double)l * bs;
         }
+        check_conv(L);
         *loss = total / count;
     });
 }
@@ -1446,6 +1640,7 @@ sg_status sg_learned_forward(sg_learned* L, const float* x, int batch, float* y)
                 nullptr);
         SG_CUDA(cudaMemcpyAsync(y, L->ty.p, sizeof(float) * V, cudaMemcpyDeviceToHost, ctx->stream));
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_conv(L);
     });
 }
 
@@ -1475,6 +1670,7 @@ sg_status sg_learned_gradient(sg_learned* L, const float* x, const float* t, int
         SG_CUDA(cudaMemcpyAsync(grad, L->grad.p, sizeof(float) * NET_PARAMS, cudaMemcpyDeviceToHost,
                                 ctx->stream));
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_conv(L);
         *loss = l;
     });
 }

@@ -349,6 +349,8 @@ void solve_device(sg_ctx* ctx, int solver, const sg_csr* A, sg_precond* pc, cons
     }
     if (pc && sweep_error(pc))
         fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+    if (pc && pc->learned && learned_error(pc->learned))
+        fail(SG_ERR_DEVICE_TIMEOUT, "a learned-stage convolution gave up waiting for its tile");
     if (pc) {
         const int hst = host_precond_status(pc);
         if (hst) fail(SG_ERR_CALLBACK, "the host preconditioner function returned %d", hst);

@@ -47,6 +47,16 @@ __device__ __forceinline__ void bulk_g2s_stream(uint32_t dst, const void* src, u
         "l"(src), "r"(bytes), "r"(bar)
         : "memory");
 }
+// tiled 5D tensor copy global -> shared (box and element type from the
+// tensor map; coordinates innermost first, out-of-range elements read 0)
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const void* map, int c0, int c1, int c2,
+                                            int c3, int c4, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+        : "memory");
+}
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
