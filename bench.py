@@ -775,7 +775,7 @@ def run_batched(args):
                  float((it_e * (nnz_sys * 8 + 4 * (rows + 1) + 2 * rows * 4)).sum())),
         "residual": ("batched residual_fp64 (k_b_residual)",
                      float(((cy_e + 1) * (nnz_sys * 12 + 4 * (rows + 1) + 4 * rows * 8)).sum())),
-        "ortho": ("batched cgs2 passes (k_b_dots, k_b_upd_dots, k_b_upd_norm)",
+        "ortho": ("batched lagged two-pass cgs2 (k_b_lag_a, k_b_lag_b)",
                   float(sum(cgs2_bytes(int(rows[s]), 4, int(it_e[r, s]), B_RESTART)
                             for r in range(B_RHS) for s in range(prob.nsys)))),
     }

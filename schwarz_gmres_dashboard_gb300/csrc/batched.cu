@@ -74,6 +74,12 @@ struct BatchDev {
     unsigned* ticket;
     double* part;    // [chunks][BLD]
     int* notdone;
+    // lagged CGS2 (ortho 0): the basis is V = S T over the stored vectors S
+    double* lagT;    // [I][BLD * BLD] T(l, i) at l + i * BLD (upper triangle)
+    double* lagH;    // [I][BLD * BMMAX] unrotated Hessenberg H(i, k) at i + k * BLD
+    double* lagc;    // [I][BLD] v_j = T(j,j) raw_j - sum_{k<j} lagc[k] v_k
+    double* cfu;     // [I][BLD] update coefficients on the stored vectors
+    int lagged;
     int m, I, S, R;
     long long N;
     double tol;
@@ -235,6 +241,7 @@ k_b_cycle_init(BatchDev B, const TV* __restrict__ raw0) {
         return;
     }
     B.vscale[(size_t)inst * ld] = 1.0 / beta;
+    if (B.lagged) B.lagT[(size_t)inst * BLD * BLD] = 1.0 / beta;  // v_0 = raw_0 / beta
     B.g[(size_t)inst * ld] = beta;
     B.est[inst] = B.rnorm[inst] / beta;
 }
@@ -440,6 +447,57 @@ k_b_upd_dots(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
     }
 }
 
+// End of Arnoldi step j of one instance (one thread), as the single-system
+// solver: the Hessenberg column (h_{0..j} from hs, h_{j+1} = nrm), the
+// Givens rotations, the residual estimate and the stopping tests.  Returns
+// true while the instance continues with step j + 1 (vscale_{j+1} = 1/nrm).
+__device__ bool b_arnoldi_end(const BatchDev& B, int inst, int j, double nrm) {
+    const int m = B.m, ld = m + 1;
+    double* Hc = B.H + (size_t)inst * ld * m + (size_t)j * ld;
+    double* g = B.g + (size_t)inst * ld;
+    double* cs = B.cs + (size_t)inst * m;
+    double* sn = B.sn + (size_t)inst * m;
+    for (int i = 0; i <= j; ++i) Hc[i] = B.hs[(size_t)inst * ld + i];
+    Hc[j + 1] = nrm;
+    if (!(nrm >= 1e-30)) {
+        if (!isfinite(nrm)) {
+            B.flags[inst] |= 1;
+            B.done[inst] = 1;
+        }
+        B.flags[inst] |= 2;
+        B.kcount[inst] = j + 1;
+        B.active[inst] = 0;
+        return false;
+    }
+    B.vscale[(size_t)inst * ld + j + 1] = 1.0 / nrm;
+    for (int i = 0; i < j; ++i) b_rot_apply(cs[i], sn[i], Hc[i], Hc[i + 1]);
+    b_rot_compute(cs[j], sn[j], Hc[j], Hc[j + 1]);
+    b_rot_apply(cs[j], sn[j], Hc[j], Hc[j + 1]);
+    b_rot_apply(cs[j], sn[j], g[j], g[j + 1]);
+    const double res = fabs(g[j + 1]);
+    B.lastres[inst] = res;
+    B.iters[inst] += 1;
+    B.kcount[inst] = j + 1;
+    bool stop = false;
+    if (B.tol_kind == SG_TOL_REF_ABS) {
+        if (res < B.tol) {
+            B.conv[inst] = 1;
+            B.done[inst] = 1;
+            stop = true;
+        }
+    } else if (B.tol_kind == SG_TOL_TRUE_REL) {
+        if (res * B.est[inst] <= 0.5 * B.tol * B.bnorm[inst]) stop = true;
+    }
+    if (!isfinite(res)) {
+        B.flags[inst] |= 1;
+        B.done[inst] = 1;
+        stop = true;
+    }
+    if (j + 1 >= m) stop = true;
+    if (stop) B.active[inst] = 0;
+    return !stop;
+}
+
 // ---- CGS2 pass C: w'' = w' - sum_k h2_k v_k, ||w''||, then the instance's
 // Hessenberg column, Givens rotations and stopping test
 template <class TV>
@@ -478,50 +536,144 @@ k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][0] = ss;
     __syncthreads();
     if (!seg_reduce(B, c, inst, red, 1, bsum, tot) || threadIdx.x != 0) return;
-    // Arnoldi step j of this instance (as the single-system solver)
-    const double nrm = sqrt(tot[0]);
-    double* Hc = B.H + (size_t)inst * ld * m + (size_t)j * ld;
-    double* g = B.g + (size_t)inst * ld;
-    double* cs = B.cs + (size_t)inst * m;
-    double* sn = B.sn + (size_t)inst * m;
-    for (int i = 0; i <= j; ++i) Hc[i] = B.hs[(size_t)inst * ld + i];
-    Hc[j + 1] = nrm;
-    if (!(nrm >= 1e-30)) {
-        if (!isfinite(nrm)) {
-            B.flags[inst] |= 1;
-            B.done[inst] = 1;
+    b_arnoldi_end(B, inst, j, sqrt(tot[0]));
+}
+
+// ---- lagged CGS2 (ortho 0, restart < 32), as the single-system solver.
+// Step j orthogonalises z = B (vscale_j raw_j), where the stored raw_j still
+// lacks its second projection: v_j = T(j,j) raw_j - sum_{k<j} c_k v_k, so
+// B v_j = z - V g with g = H(0..j, 0..j-1) c (Arnoldi relation), and two
+// passes over the stored vectors S (V = S T) do the work of three:
+//   A  d = S^T z; p = T^T d; hs = p - g; update coefficients u = T p
+//   B  w' = z - S u; r = S^T w'; ||w'||^2; h2 = T^T r; the column is hs +
+//      h2, ||w''||^2 = ||w'||^2 - ||h2||^2, and w' is stored as raw_{j+1}
+//      with its pending correction c = h2 / ||w''||.
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_lag_a(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (!B.active[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[BLD], tot[BLD];
+    __shared__ double Ts[BLD][BLD + 1];
+    __shared__ double ps[BLD], csh[BLD];
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    const TV* w = V + (size_t)(j + 1) * ldv + off;
+    TV wv[BRPT];
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
+    }
+    chunk_dots<TV>(V, ldv, off, len, j, wv, red);
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, j + 1, bsum, tot)) return;
+    const int ld = B.m + 1, n1 = j + 1;
+    const double* T = B.lagT + (size_t)inst * BLD * BLD;
+    const double* Hn = B.lagH + (size_t)inst * BLD * BMMAX;
+    for (int idx = threadIdx.x; idx < n1 * n1; idx += BT) {
+        const int l = idx % n1, i = idx / n1;
+        Ts[l][i] = l <= i ? T[l + i * BLD] : 0.0;
+    }
+    for (int k = threadIdx.x; k < j; k += BT) csh[k] = B.lagc[(size_t)inst * BLD + k];
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j; i += BT) {
+        double sp = 0.0;
+        for (int l = 0; l <= i; ++l) sp += Ts[l][i] * tot[l];
+        ps[i] = sp;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j; i += BT) {
+        double g = 0.0;
+        for (int k = (i > 0 ? i - 1 : 0); k < j; ++k) g += Hn[i + k * BLD] * csh[k];
+        B.hs[(size_t)inst * ld + i] = ps[i] - g;
+        double u = 0.0;
+        for (int k = i; k <= j; ++k) u += Ts[i][k] * ps[k];
+        B.cfu[(size_t)inst * BLD + i] = u;
+    }
+}
+
+template <class TV>
+__global__ void __launch_bounds__(BT)
+k_b_lag_b(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
+    const int c = blockIdx.x;
+    const int inst = B.cinst[c];
+    if (!B.active[inst]) return;
+    __shared__ double red[BT / 32][BLD];
+    __shared__ double bsum[BLD], tot[BLD];
+    __shared__ TV cf[BLD];
+    __shared__ double Ts[BLD][BLD + 1];
+    __shared__ double h2s[BLD], csn[BLD];
+    __shared__ double s_vs;
+    for (int k = threadIdx.x; k <= j; k += BT) cf[k] = (TV)B.cfu[(size_t)inst * BLD + k];
+    __syncthreads();
+    const long long off = B.coff[c];
+    const int len = B.clen[c];
+    TV* w = V + (size_t)(j + 1) * ldv + off;
+    TV wv[BRPT];
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        wv[q] = row < len ? ld_stream(&w[row]) : (TV)0;
+    }
+    chunk_update<TV>(V, ldv, off, len, j, cf, wv);
+    TV ssv = (TV)0;
+#pragma unroll
+    for (int q = 0; q < BRPT; ++q) {
+        const int row = threadIdx.x + q * BT;
+        if (row < len) {
+            w[row] = wv[q];
+            ssv += wv[q] * wv[q];
         }
-        B.flags[inst] |= 2;
-        B.kcount[inst] = j + 1;
-        B.active[inst] = 0;
-        return;
     }
-    B.vscale[(size_t)inst * ld + j + 1] = 1.0 / nrm;
-    for (int i = 0; i < j; ++i) b_rot_apply(cs[i], sn[i], Hc[i], Hc[i + 1]);
-    b_rot_compute(cs[j], sn[j], Hc[j], Hc[j + 1]);
-    b_rot_apply(cs[j], sn[j], Hc[j], Hc[j + 1]);
-    b_rot_apply(cs[j], sn[j], g[j], g[j + 1]);
-    const double res = fabs(g[j + 1]);
-    B.lastres[inst] = res;
-    B.iters[inst] += 1;
-    B.kcount[inst] = j + 1;
-    bool stop = false;
-    if (B.tol_kind == SG_TOL_REF_ABS) {
-        if (res < B.tol) {
-            B.conv[inst] = 1;
-            B.done[inst] = 1;
-            stop = true;
-        }
-    } else if (B.tol_kind == SG_TOL_TRUE_REL) {
-        if (res * B.est[inst] <= 0.5 * B.tol * B.bnorm[inst]) stop = true;
+    chunk_dots<TV>(V, ldv, off, len, j, wv, red);
+    const double ss = warp_sum((double)ssv);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][j + 1] = ss;
+    __syncthreads();
+    if (!seg_reduce(B, c, inst, red, j + 2, bsum, tot)) return;
+    const int ld = B.m + 1, n1 = j + 1;
+    double* T = B.lagT + (size_t)inst * BLD * BLD;
+    double* Hn = B.lagH + (size_t)inst * BLD * BMMAX;
+    for (int idx = threadIdx.x; idx < n1 * n1; idx += BT) {
+        const int l = idx % n1, i = idx / n1;
+        Ts[l][i] = l <= i ? T[l + i * BLD] : 0.0;
     }
-    if (!isfinite(res)) {
-        B.flags[inst] |= 1;
-        B.done[inst] = 1;
-        stop = true;
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j; i += BT) {
+        double h2 = 0.0;
+        for (int l = 0; l <= i; ++l) h2 += Ts[l][i] * tot[l];
+        h2s[i] = h2;
+        const double hc = B.hs[(size_t)inst * ld + i] + h2;  // the Hessenberg column
+        B.hs[(size_t)inst * ld + i] = hc;
+        Hn[i + j * BLD] = hc;
     }
-    if (j + 1 >= m) stop = true;
-    if (stop) B.active[inst] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double nrm2 = tot[j + 1];
+        for (int i = 0; i <= j; ++i) nrm2 -= h2s[i] * h2s[i];
+        if (!(nrm2 > 0.0)) nrm2 = isfinite(nrm2) ? 0.0 : nrm2;
+        const double nrm = sqrt(nrm2);
+        Hn[j + 1 + j * BLD] = nrm;
+        s_vs = b_arnoldi_end(B, inst, j, nrm) ? 1.0 / nrm : 0.0;
+    }
+    __syncthreads();
+    const double vs = s_vs;
+    if (vs == 0.0) return;
+    // the pending correction of the new stored vector and its column of T:
+    // T(:, j+1) = T(j+1, j+1) e_{j+1} - T(:, 0..j) c
+    for (int k = threadIdx.x; k <= j; k += BT) {
+        csn[k] = h2s[k] * vs;
+        B.lagc[(size_t)inst * BLD + k] = csn[k];
+    }
+    if (threadIdx.x == 0) T[(j + 1) + (j + 1) * BLD] = vs;
+    __syncthreads();
+    for (int l = threadIdx.x; l <= j; l += BT) {
+        double sc = 0.0;
+        for (int k = l; k <= j; ++k) sc += Ts[l][k] * csn[k];
+        T[l + (j + 1) * BLD] = -sc;
+    }
 }
 
 // ---- y = H^{-1} g per instance (src/core/gmres.cpp:131-137)
@@ -538,10 +690,17 @@ __global__ void k_b_backsolve(BatchDev B) {
         for (int l = i + 1; l < k; ++l) yi -= H[i + l * ld] * y[l];
         y[i] = yi / H[i + i * ld];
     }
-    // coefficients of the update x += sum_k (y_k vscale_k) raw_k
+    // coefficients of the update x += sum_k (y_k vscale_k) raw_k; lagged
+    // CGS2: V y = S (T y)
     const double* vs = B.vscale + (size_t)inst * ld;
+    const double* T = B.lagged ? B.lagT + (size_t)inst * BLD * BLD : nullptr;
     for (int i = 0; i < k; ++i) {
-        const double c = y[i] * vs[i];
+        double c = 0.0;
+        if (T) {
+            for (int l = i; l < k; ++l) c += T[i + l * BLD] * y[l];
+        } else {
+            c = y[i] * vs[i];
+        }
         B.yd[(size_t)inst * m + i] = c;
         B.yf[(size_t)inst * m + i] = (float)c;
     }
@@ -614,6 +773,7 @@ struct BatchWork {
     DBuf<int> in, ich0, inch, cinst, clen, row_sys;
     DBuf<int> active, done, conv, iters, cycles, kcount, ran, flags, notdone;
     DBuf<double> bnorm, rnorm, est, lastres, g, cs, sn, H, vscale, y, yd, h, hs, part;
+    DBuf<double> lagT, lagH, lagc, cfu;
     DBuf<float> yf;
     DBuf<unsigned> ticket;
     DBuf<double> b64, x64, r64;
@@ -746,6 +906,15 @@ void enqueue_batch_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const Bat
             apply_pc_batched<TV>(ctx, pc, B, w, nullptr, V + (size_t)(j + 1) * ldv, false, t);
         }
         ClassTimer tm(ctx, TK_ORTHO);
+        if (B.lagged) {
+            k_b_lag_a<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
+            SG_CUDA(cudaGetLastError());
+            k_b_lag_b<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
+            SG_CUDA(cudaGetLastError());
+            count_launch(ctx);
+            count_launch(ctx);
+            continue;
+        }
         k_b_dots<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
         SG_CUDA(cudaGetLastError());
         k_b_upd_dots<TV><<<nchunks, BT, 0, st>>>(B, V, ldv, j);
@@ -882,6 +1051,13 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
     dalloc(w->h, I * ld);
     dalloc(w->hs, I * ld);
     dalloc(w->part, (size_t)nchunks * BLD);
+    const bool lagged = prm.ortho == 0 && m < SG_LAGM;
+    if (lagged) {
+        dalloc(w->lagT, (size_t)I * BLD * BLD);
+        dalloc(w->lagH, (size_t)I * BLD * BMMAX);
+        dalloc(w->lagc, (size_t)I * BLD);
+        dalloc(w->cfu, (size_t)I * BLD);
+    }
     dalloc(w->ticket, (size_t)I);
     w->ticket.zero(st);
     const size_t tot = (size_t)N * R;
@@ -917,6 +1093,8 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
     B.g = w->g.p; B.cs = w->cs.p; B.sn = w->sn.p; B.H = w->H.p; B.vscale = w->vscale.p;
     B.y = w->y.p; B.yd = w->yd.p; B.yf = w->yf.p; B.h = w->h.p; B.hs = w->hs.p; B.ticket = w->ticket.p; B.part = w->part.p;
     B.notdone = w->notdone.p;
+    B.lagT = w->lagT.p; B.lagH = w->lagH.p; B.lagc = w->lagc.p; B.cfu = w->cfu.p;
+    B.lagged = lagged ? 1 : 0;
     B.m = m; B.I = I; B.S = S; B.R = R; B.N = N;
     B.tol = prm.tol; B.tol_kind = prm.tol_kind; B.max_iter = prm.max_iter;
     // four right-hand sides per sweep: planned once per set-up, before any capture

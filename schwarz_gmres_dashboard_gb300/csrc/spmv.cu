@@ -581,5 +581,8 @@ template void launch_spmv_a<double, double, double>(sg_ctx*, const sg_csr*, cons
                                                     double*, const double*, const int*);
 template void launch_spmv_a<float, float, float>(sg_ctx*, const sg_csr*, const float*, float*,
                                                  const double*, const int*);
+// FP32 values, FP64 input (the learned stage's residual inside an FP64 cycle)
+template void launch_spmv_a<float, double, float>(sg_ctx*, const sg_csr*, const double*, float*,
+                                                  const double*, const int*);
 
 }  // namespace sg

@@ -57,8 +57,11 @@ def test_block_diagonal_ras_equals_per_system_ras(sg, fp64):
         assert np.array_equal(Ms.apply(v[lo:hi]), y[lo:hi]), s
 
 
+@pytest.mark.parametrize("ortho", [0, 1])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_batched_solve_matches_single_solves(sg, precision):
+def test_batched_solve_matches_single_solves(sg, precision, ortho):
+    """ortho 0: the lagged two-pass CGS2 (restart < 32), ortho 1: three
+    passes; the single-system solver runs the same form."""
     prob = _small_batch(sg)
     prec = sg.FP64 if precision == "fp64" else sg.FP32
     M = _precond(sg, prob, precision == "fp64")
@@ -67,7 +70,7 @@ def test_batched_solve_matches_single_solves(sg, precision):
     B = sg.uniform(R * prob.n, 21).reshape(R, prob.n)
     X = np.zeros_like(B)
     prm = sg.GMRESParams(restart=30, max_iter=2000, tol=1e-8, tol_kind=sg.TOL_TRUE_REL,
-                         precision=prec)
+                         precision=prec, ortho=ortho)
     res, t = sg.solve_batched(prob.A, M, prob.sys_row_ptr, R, B, X, prm)
     assert t > 0 and len(res) == R * prob.nsys
     assert np.all(res["converged"] == 1) and np.all(res["status"] == 0)
