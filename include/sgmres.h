@@ -73,8 +73,9 @@ typedef struct sg_precond_opts {
                          TMA-fed level sweep, 1 a level sweep reading factors
                          from global memory, 4 the sync-free sweep (per-row
                          ready flags); reserved[1]: threads per CTA of the
-                         TMA-fed sweep (128, 256, 384 or 512; 0 = the
-                         fastest, timed at set-up); reserved[2]: two-level
+                         TMA-fed sweep (32, 64, 128, 256, 384 or 512; 0 =
+                         the fastest of 128-512, timed at set-up);
+                         reserved[2]: two-level
                          preconditioners compute the coarse restriction
                          inside the TMA-fed sweep when all subdomains' CTAs
                          fit on the GPU at once (0), or in a kernel of its

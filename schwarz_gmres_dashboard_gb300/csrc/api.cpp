@@ -476,9 +476,11 @@ sg_status sg_precond_create(sg_ctx* ctx, sg_precond_kind kind, const sg_precond_
             pc->opts.sweep_dtype = SG_FP64;
         }
         const int swt = pc->opts.reserved[1];
-        if (!(swt == 0 || swt == 128 || swt == 256 || swt == 384 || swt == 512)) {
+        if (!(swt == 0 || swt == 32 || swt == 64 || swt == 128 || swt == 256 || swt == 384 ||
+              swt == 512)) {
             delete pc;
-            fail(SG_ERR_INVALID_ARG, "sweep threads (reserved[1]) must be 0, 128, 256, 384 or 512");
+            fail(SG_ERR_INVALID_ARG,
+                 "sweep threads (reserved[1]) must be 0, 32, 64, 128, 256, 384 or 512");
         }
         if (pc->opts.reserved[4] < 0) {
             delete pc;

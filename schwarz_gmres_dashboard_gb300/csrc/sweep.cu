@@ -1223,6 +1223,10 @@ void tune_plan(sg_precond* pc, RingPlan& plan, const std::vector<long long>& gma
     float best = -1.f;
     int best_nt = SW_T, best_grid = 0;
     long long best_g = gmax_list.front();
+    // one- and two-warp CTAs (reserved[1] = 32 or 64) are not timed: on the
+    // 2D subdomains of the batched workload (~20 rows per level) they
+    // measured slower than 128 threads (the gather, scatter and record
+    // stream lose more than the cheaper barrier gains)
     std::vector<int> threads = {512, 384, 256, 128};
     if (pc->opts.reserved[1] > 0) threads = {pc->opts.reserved[1]};
     for (long long gmax : gmax_list) {

@@ -261,8 +261,8 @@ def test_sweep_variants_agree(sg, kind, dt):
     fdt = {"fp64": sg.FP64, "fp32": sg.FP32, "bf16": sg.BF16}[dt]
     sdt = sg.FP64 if dt == "fp64" else sg.FP32
     ys = []
-    for sweep, threads in (("tma", 0), ("tma", 512), ("tma", 256), ("tma", 128),
-                           ("level", 0), ("syncfree", 0)):
+    for sweep, threads in (("tma", 0), ("tma", 512), ("tma", 256), ("tma", 128), ("tma", 64),
+                           ("tma", 32), ("level", 0), ("syncfree", 0)):
         pc = make_pc(sg, kind, 12, 1, part, fdt, sdt, sweep=sweep, sweep_threads=threads)
         pc.setup(A)
         ch = pc.sweep_choice()
