@@ -471,6 +471,11 @@ sg_status sg_learned_gradient(sg_learned* L, const float* x, const float* t, int
                               float* grad, double* loss);
 /* Switch the stage on/off for later applies and solves. */
 sg_status sg_learned_set_enabled(sg_learned* L, int on);
+/* Testing of the bounded device waits: mode 1 (2) makes every convolution's
+ * wait for its halo copies (for its tensor-core MMAs) impossible to satisfy
+ * with a ~1 ms budget; the kernel drains what is in flight, leaves its tile
+ * unwritten and the call returns SG_ERR_DEVICE_TIMEOUT.  0: normal waits. */
+sg_status sg_learned_set_wait_test(sg_learned* L, int mode);
 /* enabled: 1 while on; fallback_cycle: restart cycle after which the monitor
  * switched it off in the last solve (-1: never); applies: stage applies so far. */
 sg_status sg_learned_get_state(sg_learned* L, int* enabled, int* fallback_cycle,

@@ -169,6 +169,7 @@ PROTOTYPES = {
     "sg_learned_forward": (C.c_int, [_vp, _vp, C.c_int, _vp]),
     "sg_learned_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _dp]),
     "sg_learned_set_enabled": (C.c_int, [_vp, C.c_int]),
+    "sg_learned_set_wait_test": (C.c_int, [_vp, C.c_int]),
     "sg_learned_get_state": (C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_longlong)]),
     "sg_precond_set_learned": (C.c_int, [_vp, _vp, C.c_double]),
 }

@@ -228,8 +228,13 @@ __global__ void __launch_bounds__(TC_THREADS)
 k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restrict__ w,
             const float* __restrict__ bias, int D, int epi, uint32_t* __restrict__ out,
             float* __restrict__ outf, const uint32_t* __restrict__ mask, const int* enabled,
-            const int* active, int* err) {
+            const int* active, int* err, int wait_test) {
     if (skip(enabled, active)) return;
+    // wait_test 1 / 2 (testing of the give-up path): the copy barrier expects
+    // 16 bytes nobody sends / the MMA barrier one arrival nobody makes, so
+    // its wait runs out (short budget); the block then supplies what it
+    // withheld and drains the real copies / MMAs with the full budget
+    const bool t1 = wait_test == 1, t2 = wait_test == 2;
     extern __shared__ uint8_t tc_raw[];
     const uint32_t raw = smem_u32(tc_raw);
     const uint32_t base = (raw + 127u) & ~127u;
@@ -254,9 +259,9 @@ k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restric
     if (threadIdx.x == 0) {
         *s_bad = 0;
         mbar_init(bar_in, 1);
-        mbar_init(bar_mma, 1);
+        mbar_init(bar_mma, t2 ? 2 : 1);
         fence_mbar_init();
-        mbar_expect_tx(bar_in, 2 * TC_PLANE + TC_WBYTES);
+        mbar_expect_tx(bar_in, 2 * TC_PLANE + TC_WBYTES + (t1 ? 16 : 0));
         tma_load_5d(plane0, &in_map, 0, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
         tma_load_5d(plane0 + TC_PLANE, &in_map, 8, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
         bulk_g2s(wsm, w, TC_WBYTES, bar_in);
@@ -272,7 +277,7 @@ k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restric
 
     if (threadIdx.x == 0) {
         int bad = 0;
-        if (mbar_wait(bar_in, 0, WAIT_CYCLES)) {
+        if (mbar_wait(bar_in, 0, t1 ? WAIT_TEST_CYCLES : WAIT_CYCLES)) {
             tc_fence_after();
             for (int mt = 0; mt < TC_TZ; ++mt)
                 for (int tap = 0; tap < LTAPS; ++tap) {
@@ -283,12 +288,14 @@ k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restric
                            tc_sdesc(wsm + tap * 512, 256, 128), TC_IDESC, tap > 0);
                 }
             tc_commit(bar_mma);
-            if (!mbar_wait(bar_mma, 0, WAIT_CYCLES)) {
+            if (!mbar_wait(bar_mma, 0, t2 ? WAIT_TEST_CYCLES : WAIT_CYCLES)) {
                 bad = 2;
+                if (t2) mbar_arrive(bar_mma);
                 mbar_wait(bar_mma, 0, WAIT_CYCLES);  // let the MMAs finish before TMEM is freed
             }
         } else {
             bad = 1;
+            if (t1) mbar_complete_tx(bar_in, 16);
             mbar_wait(bar_in, 0, WAIT_CYCLES);  // the copies may still land: wait once more
         }
         if (bad) {
@@ -788,6 +795,7 @@ struct LearnedImpl {
     DBuf<double> partials;
     DBuf<unsigned> counter;
     DBuf<int> cerr;  // set by a convolution whose bounded wait ran out
+    int wait_test = 0;  // testing: 1 / 2 make the convolutions' copy / MMA waits give up
     DBuf<float> az32;   // A z of the stage's residual (FP32 values)
     DBuf<double> az64;  // the same for the FP64 training pairs
     // inference scratch (one sample)
@@ -877,7 +885,7 @@ void conv(sg_learned* L, const uint32_t* in, int l, bool transposed, int epi, in
     k_conv3d_tc<<<tiles * batch, TC_THREADS, TC_SMEM, L->ctx->stream>>>(
         halo_map(in, D, batch), reinterpret_cast<const uint8_t*>(w),
         L->master.p + (size_t)l * LAYER_P + LAYER_W, D, epi, out, outf, mask, enabled, active,
-        L->cerr.p);
+        L->cerr.p, L->wait_test);
     SG_CUDA(cudaGetLastError());
     count_launch(L->ctx);
 }
@@ -1707,6 +1715,14 @@ sg_status sg_learned_set_enabled(sg_learned* L, int on) {
         LearnedCtl c = read_ctl(L);
         c.enabled = L->on ? 1 : 0;
         write_ctl(L, c);
+    });
+}
+
+sg_status sg_learned_set_wait_test(sg_learned* L, int mode) {
+    return lguard([&] {
+        SG_CHECK_ARG(L, "NULL argument");
+        SG_CHECK_ARG(mode >= 0 && mode <= 2, "wait test mode must be 0, 1 or 2 (got %d)", mode);
+        L->wait_test = mode;
     });
 }
 

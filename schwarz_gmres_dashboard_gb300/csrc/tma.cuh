@@ -67,6 +67,14 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// one arrival / `bytes` of transaction count on the barrier's current phase
+// from this thread (the wait tests withhold one and supply it afterwards)
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_complete_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
 // bounded wait: false when the phase did not complete within the budget
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long budget) {
     const long long t0 = clock64();

@@ -193,6 +193,12 @@ class LearnedCorrection:
     def enabled(self, on: bool) -> None:
         _check(_clib.sg_learned_set_enabled(self.handle, 1 if on else 0))
 
+    def set_wait_test(self, mode: int) -> None:
+        """Testing: 1 / 2 make the convolutions' copy / MMA waits give up at
+        once (the next call raises SgError with SG_ERR_DEVICE_TIMEOUT); 0
+        restores the normal budget."""
+        _check(_clib.sg_learned_set_wait_test(self.handle, int(mode)))
+
     def state(self) -> dict:
         en, fb, ap = C.c_int(0), C.c_int(0), C.c_longlong(0)
         _check(_clib.sg_learned_get_state(self.handle, C.byref(en), C.byref(fb), C.byref(ap)))

@@ -86,3 +86,30 @@ def test_wait_test_needs_the_wait(sg):
     with pytest.raises(sg.SgError) as ei:
         R.set_wait_test(2)  # one-level: no coarse restriction to wait for
     assert ei.value.status == 8
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_learned_convolution_wait_runs_out_then_recovers(sg, mode):
+    """The tcgen05 convolution waits on one mbarrier for its TMA halo and
+    weight copies and on another for its MMAs.  Mode 1 (2) makes the first
+    (second) barrier expect 16 bytes (one arrival) that nothing supplies, with
+    a ~1 ms budget: every CTA's wait runs out, the CTA supplies what was
+    withheld, drains its real copies (MMAs), frees its tensor memory and
+    leaves its tile unwritten; the call reports SG_ERR_DEVICE_TIMEOUT, and
+    the next call with the normal waits returns the normal network output."""
+    st = sg.LearnedCorrection(32)
+    try:
+        rng = np.random.default_rng(40 + mode)
+        p = (rng.uniform(-1, 1, sg.learned.NUM_PARAMS) * 0.2).astype(np.float32)
+        p[-1] = 1.0
+        st.weights = p
+        x2 = rng.standard_normal((2, st.nc, 2)).astype(np.float32)
+        want = st.forward(x2)
+        st.set_wait_test(mode)
+        with pytest.raises(sg.SgError) as ei:
+            st.forward(x2)
+        assert ei.value.status == TIMEOUT
+        st.set_wait_test(0)
+        np.testing.assert_array_equal(st.forward(x2), want)
+    finally:
+        st.close()
