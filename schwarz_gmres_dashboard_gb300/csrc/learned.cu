@@ -28,8 +28,8 @@
 // and the input gradient run on tcgen05.mma (BF16 x BF16 -> FP32 in tensor
 // memory): a CTA owns an 8 x 16 x 2 block of output voxels, TMA stages its
 // 10 x 18 x 4 input halo (16 channels as two 8-channel planes) and a bulk copy
-// the layer's weights, and one thread issues one 128 x 16 x 16 MMA per tap
-// and z-plane straight from the shifted halo (k_conv3d_tc).  The input
+// the layer's weights, and one thread issues the MMAs straight from the
+// shifted halo, one per (dy, dx) tap pair and halo slice (k_conv3d_tc).  The input
 // gradient is the same kernel with flipped, transposed weights and the ReLU
 // mask of the layer input in the epilogue.  The weight gradient (M = 16 input
 // channels, below the 64 rows a tcgen05.mma needs; N = output channel, K =
@@ -128,13 +128,15 @@ __device__ __forceinline__ void load_halo(uint32_t* halo, const uint32_t* __rest
 // 10 x 18 x 4 input halo into shared memory as two 8-channel planes (16 B
 // per voxel each; the tensor map fills the voxels outside the volume with 0)
 // and a bulk copy brings the layer's weights, already in the operand layout.
-// With that layout every tap is one tcgen05.mma: the A operand of tap
-// (dz, dy, dx) is the halo plane shifted by that voxel offset -- eight
-// consecutive x positions are one 8-row x 16-byte core matrix, the 16 rows
-// of y are 8-row groups 18 x 16 B apart, the second channel half is the other
-// plane -- so no operand is ever copied or re-laid out in shared memory.
-// One thread issues the 54 MMAs and commits them to an mbarrier; each warp
-// then reads its 32 accumulator lanes (tcgen05.ld) and runs the epilogue.
+// With that layout the A operand of tap (dz, dy, dx) is the halo slice of
+// its dz shifted by (dy, dx) -- eight consecutive x positions are one 8-row x
+// 16-byte core matrix, the 16 rows of y are 8-row groups 18 x 16 B apart,
+// the second channel half is the other plane -- so no operand is ever copied
+// or re-laid out in shared memory, and one A tile serves every dz tap whose
+// output plane lies in the tile: one tcgen05.mma of N = 16 or 32 per (dy,
+// dx) pair and halo slice, 36 in all, each reading its 4 KB A tile once.
+// One thread issues them and commits them to an mbarrier; each warp then
+// reads its 32 accumulator lanes (tcgen05.ld) and runs the epilogue.
 // (Two z-planes per CTA rather than four: 2.8 CTAs per SM at 48^3 instead
 // of 1.4 balance the SMs better, measured 0.7 us faster per layer.)
 constexpr int TC_TY = 16, TC_TZ = 2;
@@ -158,7 +160,11 @@ constexpr uint32_t tc_idesc(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
            ((uint32_t)(M >> 4) << 24);
 }
-constexpr uint32_t TC_IDESC = tc_idesc(128, LC);
+// one MMA per (dy, dx) tap pair and halo slice covers the dz taps whose
+// output planes lie in the tile: N = 16 output channels per tap (16 or 32)
+constexpr uint32_t TC_IDESC16 = tc_idesc(128, LC);
+constexpr uint32_t TC_IDESC32 = tc_idesc(128, 2 * LC);
+static_assert(TC_TZ == 2, "the MMA order below initialises both planes' accumulators first");
 
 // shared-memory operand descriptor, no swizzle, K-major: start address,
 // byte offset between the two K-adjacent core matrices (lbo) and between
@@ -217,7 +223,8 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
 
 // conv3d 3x3x3, 16 -> 16 channels.  in_map: the BF16 [batch][D][D][D][16]
 // input as a 5D tensor map (box 8 ch x 10 x 18 x 4 x 1).  w: the layer's
-// weights in operand layout ([tap][ci / 8][co][ci % 8], 512 B per tap).
+// weights in operand layout ([(dy, dx)][ci / 8][dz * 16 + co][ci % 8],
+// 1,536 B per (dy, dx) pair).
 // Grid: (D/8) x ceil(D/16) x (D/2) tiles x batch.  Epilogues:
 //  RELU        out = relu(acc + bias) as BF16 [V][16]
 //  LINEAR_F32  outf[v] = acc[ch 0] + bias[0] (FP32, one channel)
@@ -279,14 +286,26 @@ k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restric
         int bad = 0;
         if (mbar_wait(bar_in, 0, t1 ? WAIT_TEST_CYCLES : WAIT_CYCLES)) {
             tc_fence_after();
-            for (int mt = 0; mt < TC_TZ; ++mt)
-                for (int tap = 0; tap < LTAPS; ++tap) {
-                    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-                    const uint32_t a =
-                        plane0 + (((mt + 1 + dz) * TC_HY + 1 + dy) * TC_HX + 1 + dx) * 16;
-                    tc_mma(taddr + mt * LC, tc_sdesc(a, TC_PLANE, TC_HX * 16),
-                           tc_sdesc(wsm + tap * 512, 256, 128), TC_IDESC, tap > 0);
+            // halo slice h feeds output plane z = h - 1 - dz: the taps dz of
+            // one (dy, dx) that land in the tile are adjacent rows of the
+            // weight block and, with the planes' accumulators in descending
+            // order (plane z at columns (TZ - 1 - z) * 16), adjacent columns
+            // of tensor memory -- one MMA of N = 16 per tap.  Slice 1 goes
+            // first: it writes both planes, so later MMAs all accumulate.
+            constexpr int order[TC_TZ + 2] = {1, 0, 2, 3};
+            for (int c = 0; c < 9; ++c) {
+                const int dy = c / 3 - 1, dx = c % 3 - 1;
+#pragma unroll
+                for (int q = 0; q < TC_TZ + 2; ++q) {
+                    const int h = order[q];
+                    const int lo = h - TC_TZ + 1 > 0 ? h - TC_TZ + 1 : 0, hi = h < 2 ? h : 2;
+                    const uint32_t a = plane0 + ((h * TC_HY + 1 + dy) * TC_HX + 1 + dx) * 16;
+                    tc_mma(taddr + (uint32_t)((TC_TZ - 1 - (h - lo)) * LC),
+                           tc_sdesc(a, TC_PLANE, TC_HX * 16),
+                           tc_sdesc(wsm + c * 1536 + lo * 256, 768, 128),
+                           hi > lo ? TC_IDESC32 : TC_IDESC16, (c > 0 || q > 0) ? 1u : 0u);
                 }
+            }
             tc_commit(bar_mma);
             if (!mbar_wait(bar_mma, 0, t2 ? WAIT_TEST_CYCLES : WAIT_CYCLES)) {
                 bad = 2;
@@ -312,7 +331,7 @@ k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restric
 #pragma unroll 1
         for (int mt = 0; mt < TC_TZ; ++mt) {
             float acc[16];
-            tc_ld16(taddr + ((uint32_t)(warp * 32) << 16) + mt * LC, acc);
+            tc_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)((TC_TZ - 1 - mt) * LC), acc);
             if (yy >= D) continue;
             const size_t v = (size_t)b * V + ((size_t)(z0 + mt) * D + yy) * D + xx;
             if (epi == EPI_LINEAR_F32) {
@@ -442,8 +461,9 @@ __global__ void k_wgrad_reduce(const float* __restrict__ part, int nblk,
 // master FP32 [layer][tap][ci][co] -> the BF16 weights of the forward layers
 // and the flipped, transposed weights of the input gradient (tap 26 - t,
 // input and output channels swapped), both in the operand layout of
-// k_conv3d_tc: per tap the 16 x 16 (output x input channel) block as two
-// 8-input-channel halves, each 16 rows of 8 channels ([tap][k / 8][n][k % 8])
+// k_conv3d_tc: per (dy, dx) pair c a 48 x 16 block -- rows dz-tap x output
+// channel, columns input channel -- as two 8-input-channel halves of 48 rows
+// of 8 channels ([c][k / 8][dz * 16 + n][k % 8], 1,536 bytes per pair)
 __global__ void k_prep_weights(const float* __restrict__ master, __nv_bfloat16* __restrict__ wf,
                                __nv_bfloat16* __restrict__ wt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -452,8 +472,9 @@ __global__ void k_prep_weights(const float* __restrict__ master, __nv_bfloat16* 
     const int tap = r / (LC * LC), ci = (r / LC) % LC, co = r % LC;
     const __nv_bfloat16 v = __float2bfloat16_rn(master[(size_t)l * LAYER_P + r]);
     const size_t lb = (size_t)l * LAYER_W;
-    wf[lb + tap * LC * LC + (ci / 8) * 8 * LC + co * 8 + ci % 8] = v;
-    wt[lb + (LTAPS - 1 - tap) * LC * LC + (co / 8) * 8 * LC + ci * 8 + co % 8] = v;
+    const int tt = LTAPS - 1 - tap;
+    wf[lb + (tap % 9) * 768 + (ci / 8) * 384 + ((tap / 9) * LC + co) * 8 + ci % 8] = v;
+    wt[lb + (tt % 9) * 768 + (co / 8) * 384 + ((tt / 9) * LC + ci) * 8 + co % 8] = v;
 }
 
 // Adam (Kingma & Ba 2015) on the network parameters; padded entries stay 0

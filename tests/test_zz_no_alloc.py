@@ -84,3 +84,33 @@ def test_dot_noalloc_rejects_sizes_beyond_its_scratch(sg):
                             C.c_void_p(out.data_ptr()), None)
     assert st == 1  # SG_ERR_INVALID_ARG, nothing launched
     assert b"exceeds" in lib.sg_last_error()
+
+
+def test_dot_noalloc_inside_a_cuda_graph(sg):
+    """The reason the entry point exists: a call captured into a CUDA graph
+    (after a first call outside capture has looked up the scratch array) is
+    replayed on new contents of x and gives the same sum as sg_dot."""
+    torch = pytest.importorskip("torch")
+    from schwarz_gmres_dashboard_gb300 import _lib
+
+    lib = _lib.load()
+    n = 1_000_003
+    xd = torch.from_numpy(sg.uniform(n, seed=21)).cuda()
+    yd = torch.from_numpy(sg.uniform(n, seed=22)).cuda()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    args = (C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr()), n, C.c_void_p(out.data_ptr()))
+    assert lib.sg_dot_noalloc(*args, None) == 0  # first call, outside capture
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        st = lib.sg_dot_noalloc(*args, C.c_void_p(s.cuda_stream))
+    assert st == 0, lib.sg_last_error().decode()
+    for scale in (2.0, -0.5):
+        xd.mul_(scale)
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        ref = sg.dot(xd, yd)
+        bound = 1e-14 * float((xd * yd).abs().sum().item())
+        assert abs(float(out.item()) - ref) <= bound, (float(out.item()), ref)
