@@ -80,11 +80,22 @@ struct BatchDev {
     double* lagc;    // [I][BLD] v_j = T(j,j) raw_j - sum_{k<j} lagc[k] v_k
     double* cfu;     // [I][BLD] update coefficients on the stored vectors
     int lagged;
+    // compacted launches (late cycles): the chunks of the instances still
+    // running and the SELL slices of their systems; null = all
+    const int* clist;
+    const int* slist;
+    int nslist;
     int m, I, S, R;
     long long N;
     double tol;
     int tol_kind, max_iter;
 };
+
+// the chunk of this block: block b of a compacted launch takes the b-th
+// chunk of the list, otherwise chunk b
+__device__ __forceinline__ int chunk_of(const BatchDev& B) {
+    return B.clist ? B.clist[blockIdx.x] : (int)blockIdx.x;
+}
 
 __device__ void b_rot_compute(double& c, double& s, double a, double b) {
     // src/core/gmres.cpp:9-30
@@ -147,7 +158,7 @@ __global__ void __launch_bounds__(BT)
 k_b_residual(BatchDev B, const int* __restrict__ rp, const int* __restrict__ ci,
              const double* __restrict__ val, const double* __restrict__ b,
              const double* __restrict__ x, double* __restrict__ r) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (MODE == 1 && B.done[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -198,7 +209,7 @@ k_b_residual(BatchDev B, const int* __restrict__ rp, const int* __restrict__ ci,
 template <class TV>
 __global__ void __launch_bounds__(BT)
 k_b_cycle_init(BatchDev B, const TV* __restrict__ raw0) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (!B.active[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -282,7 +293,9 @@ k_b_spmv_sell(BatchDev B, const long long* __restrict__ sl_ptr, const int* __res
     const int lane = threadIdx.x & 31;
     const int ld = B.m + 1;
     const int wstride = (gridDim.x * blockDim.x) >> 5;
-    for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < nslices; sl += wstride) {
+    const int nsl = B.slist ? B.nslist : nslices;
+    for (int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < nsl; li += wstride) {
+        const int sl = B.slist ? B.slist[li] : li;
         const long long row = (long long)sl * 32 + lane;
         const bool in = row < B.N;
         const int sys = in ? row_sys[row] : 0;
@@ -382,7 +395,7 @@ __device__ __forceinline__ void chunk_update(const TV* V, size_t ldv, long long 
 template <class TV>
 __global__ void __launch_bounds__(BT)
 k_b_dots(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (!B.active[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -412,7 +425,7 @@ k_b_dots(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
 template <class TV>
 __global__ void __launch_bounds__(BT)
 k_b_upd_dots(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (!B.active[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -503,7 +516,7 @@ __device__ bool b_arnoldi_end(const BatchDev& B, int inst, int j, double nrm) {
 template <class TV>
 __global__ void __launch_bounds__(BT)
 k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (!B.active[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -551,7 +564,7 @@ k_b_upd_norm(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
 template <class TV>
 __global__ void __launch_bounds__(BT)
 k_b_lag_a(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (!B.active[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -598,7 +611,7 @@ k_b_lag_a(BatchDev B, const TV* __restrict__ V, size_t ldv, int j) {
 template <class TV>
 __global__ void __launch_bounds__(BT)
 k_b_lag_b(BatchDev B, TV* __restrict__ V, size_t ldv, int j) {
-    const int c = blockIdx.x;
+    const int c = chunk_of(B);
     const int inst = B.cinst[c];
     if (!B.active[inst]) return;
     __shared__ double red[BT / 32][BLD];
@@ -774,6 +787,10 @@ struct BatchWork {
     DBuf<int> active, done, conv, iters, cycles, kcount, ran, flags, notdone;
     DBuf<double> bnorm, rnorm, est, lastres, g, cs, sn, H, vscale, y, yd, h, hs, part;
     DBuf<double> lagT, lagH, lagc, cfu;
+    // compacted launches: chunk and SELL-slice lists, host copies of the
+    // instances' chunk ranges
+    DBuf<int> clist, slist;
+    std::vector<int> h_ich0, h_inch;
     DBuf<float> yf;
     DBuf<unsigned> ticket;
     DBuf<double> b64, x64, r64;
@@ -890,7 +907,7 @@ void enqueue_batch_cycle(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, const Bat
             ClassTimer tm(ctx, TK_SPMV);
             const TV* sval = BBasis<TV>::sell_vals(A);
             if (A->sell_ok && sval) {
-                k_b_spmv_sell<TV><<<bgrid(ctx, (long long)A->nslices * 32), BT, 0, st>>>(
+                k_b_spmv_sell<TV><<<bgrid(ctx, (long long)(B.slist ? B.nslist : A->nslices) * 32), BT, 0, st>>>(
                     B, A->sl_ptr.p, A->sl_w.p, A->sl_col.p, sval, w->row_sys.p, A->nslices,
                     V + (size_t)j * ldv, t, j);
             } else {
@@ -1008,6 +1025,8 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
         w->row_sys.upload(row_sys, st);
         SG_CUDA(cudaStreamSynchronize(st));
         w->nchunks = (int)cinst.size();
+        w->h_ich0 = ich0;
+        w->h_inch = inch;
         w->key_A = A;
         w->key_nnz = A->nnz;
         w->key_nrhs = R;
@@ -1095,6 +1114,9 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
     B.notdone = w->notdone.p;
     B.lagT = w->lagT.p; B.lagH = w->lagH.p; B.lagc = w->lagc.p; B.cfu = w->cfu.p;
     B.lagged = lagged ? 1 : 0;
+    B.clist = nullptr;
+    B.slist = nullptr;
+    B.nslist = 0;
     B.m = m; B.I = I; B.S = S; B.R = R; B.N = N;
     B.tol = prm.tol; B.tol_kind = prm.tol_kind; B.max_iter = prm.max_iter;
     // four right-hand sides per sweep: planned once per set-up, before any capture
@@ -1115,14 +1137,57 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
     count_launch(ctx);
     const bool use_graph = prm.use_graph != 0 && prm.max_iter > 0;
     cudaGraphExec_t exec = nullptr;
-    if (use_graph) {
+    // The cycle's launches cover `covered` instances: all at first; once at
+    // most a quarter of them are still running, the chunk kernels are launched
+    // over the chunks of the running instances only and the SELL SpMV over
+    // their systems' slices (each block still takes one chunk, so the
+    // reductions and their order are unchanged), and the graph is captured
+    // again for the new grids.  Instances only ever finish, so a list stays
+    // a superset of the running instances until the next rebuild.
+    BatchDev Bc = B;
+    int ncl = nchunks, covered = I;
+    auto rebuild = [&](int left) {
+        std::vector<int> done(I);
+        SG_CUDA(cudaMemcpyAsync(done.data(), w->done.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+        SG_CUDA(cudaStreamSynchronize(st));
+        std::vector<int> cl;
+        std::vector<char> mark(A->sell_ok ? A->nslices : 0, 0);
+        for (int i = 0; i < I; ++i) {
+            if (done[i]) continue;
+            for (int c = w->h_ich0[i]; c < w->h_ich0[i] + w->h_inch[i]; ++c) cl.push_back(c);
+            const int sy = i % S;
+            if (A->sell_ok && rows[sy + 1] > rows[sy])
+                for (int q = rows[sy] / 32; q <= (rows[sy + 1] - 1) / 32; ++q) mark[q] = 1;
+        }
+        std::vector<int> sl;
+        for (int q = 0; q < (int)mark.size(); ++q)
+            if (mark[q]) sl.push_back(q);
+        if (cl.empty()) return;
+        dalloc(w->clist, cl.size());
+        w->clist.upload(cl, st);
+        Bc.clist = w->clist.p;
+        if (!sl.empty()) {
+            dalloc(w->slist, sl.size());
+            w->slist.upload(sl, st);
+            Bc.slist = w->slist.p;
+            Bc.nslist = (int)sl.size();
+        }
+        SG_CUDA(cudaStreamSynchronize(st));
+        ncl = (int)cl.size();
+        covered = left;
+    };
+    auto capture = [&]() {
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
         cudaGraph_t gph = nullptr;
         SG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
         ctx->capturing = true;
         ctx->captured = 0;
         try {
-            if (fp32) enqueue_batch_cycle<float>(ctx, A, pc, B, w, nchunks, ldv);
-            else enqueue_batch_cycle<double>(ctx, A, pc, B, w, nchunks, ldv);
+            if (fp32) enqueue_batch_cycle<float>(ctx, A, pc, Bc, w, ncl, ldv);
+            else enqueue_batch_cycle<double>(ctx, A, pc, Bc, w, ncl, ldv);
         } catch (...) {
             ctx->capturing = false;
             cudaStreamEndCapture(st, &gph);
@@ -1134,23 +1199,29 @@ void solve_batched_device(sg_ctx* ctx, const sg_csr* A, sg_precond* pc, int nsys
         const cudaError_t e = cudaGraphInstantiate(&exec, gph, 0);
         cudaGraphDestroy(gph);
         SG_CUDA(e);
-    }
+    };
     const int max_cycles = prm.max_iter > 0 ? (prm.max_iter + m - 1) / m + 1 : 0;
     try {
+        if (use_graph) capture();
         for (int cyc = 0; cyc < max_cycles; ++cyc) {
             if (use_graph) {
                 SG_CUDA(cudaGraphLaunch(exec, st));
                 ctx->launches += ctx->captured;
             } else if (fp32) {
-                enqueue_batch_cycle<float>(ctx, A, pc, B, w, nchunks, ldv);
+                enqueue_batch_cycle<float>(ctx, A, pc, Bc, w, ncl, ldv);
             } else {
-                enqueue_batch_cycle<double>(ctx, A, pc, B, w, nchunks, ldv);
+                enqueue_batch_cycle<double>(ctx, A, pc, Bc, w, ncl, ldv);
             }
             SG_CUDA(cudaMemcpyAsync(w->h_notdone, w->notdone.p, sizeof(int),
                                     cudaMemcpyDeviceToHost, st));
             SG_CUDA(cudaStreamSynchronize(st));
             if (ctx->timing) collect_timers(ctx);
-            if (*w->h_notdone == 0) break;
+            const int left = *w->h_notdone;
+            if (left == 0) break;
+            if (4 * left <= covered && cyc + 1 < max_cycles) {
+                rebuild(left);
+                if (use_graph) capture();
+            }
         }
     } catch (...) {
         if (exec) cudaGraphExecDestroy(exec);
