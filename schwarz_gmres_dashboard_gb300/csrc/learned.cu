@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(TC_THREADS)
 k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restrict__ w,
             const float* __restrict__ bias, int D, int epi, uint32_t* __restrict__ out,
             float* __restrict__ outf, const uint32_t* __restrict__ mask, const int* enabled,
-            const int* active, int* err, int wait_test) {
+            const int* active, int* err, int wait_test, const float* __restrict__ fin_rc,
+            const float* __restrict__ fin_feat, const float* __restrict__ fin_s) {
     if (skip(enabled, active)) return;
     // wait_test 1 / 2 (testing of the give-up path): the copy barrier expects
     // 16 bytes nobody sends / the MMA barrier one arrival nobody makes, so
@@ -263,15 +264,38 @@ k_conv3d_tc(const __grid_constant__ CUtensorMap in_map, const uint8_t* __restric
 
     // the copies go out first; the tensor-memory allocation and the block
     // barrier overlap their latency
+    const bool fields = fin_rc != nullptr;
     if (threadIdx.x == 0) {
         *s_bad = 0;
         mbar_init(bar_in, 1);
         mbar_init(bar_mma, t2 ? 2 : 1);
         fence_mbar_init();
-        mbar_expect_tx(bar_in, 2 * TC_PLANE + TC_WBYTES + (t1 ? 16 : 0));
-        tma_load_5d(plane0, &in_map, 0, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
-        tma_load_5d(plane0 + TC_PLANE, &in_map, 8, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
+        mbar_expect_tx(bar_in, (fields ? 0 : 2 * TC_PLANE) + TC_WBYTES + (t1 ? 16 : 0));
+        if (!fields) {
+            tma_load_5d(plane0, &in_map, 0, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
+            tma_load_5d(plane0 + TC_PLANE, &in_map, 8, x0 - 1, y0 - 1, z0 - 1, b, bar_in);
+        }
         bulk_g2s(wsm, w, TC_WBYTES, bar_in);
+    }
+    if (fields) {
+        // the first layer of an apply packs its own input into the halo
+        // planes: channel 0 = rc / s, channel 1 = the coefficient feature,
+        // the rest 0 (one sample, read straight from rc and f), written by
+        // the threads and fenced for the tensor cores' (async proxy) reads
+        const float sv = *fin_s;
+        const float inv = sv > 0.f ? 1.f / sv : 0.f;
+        for (int q = threadIdx.x; q < TC_HX * TC_HY * TC_HZ; q += blockDim.x) {
+            const int hx = q % TC_HX, hy = (q / TC_HX) % TC_HY, hz = q / (TC_HX * TC_HY);
+            const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+            uint32_t c01 = 0u;
+            if (x >= 0 && x < D && y >= 0 && y < D && z >= 0 && z < D) {
+                const size_t v = ((size_t)z * D + y) * D + x;
+                c01 = pack_bf16(fin_rc[v] * inv, fin_feat[v]);
+            }
+            *reinterpret_cast<uint4*>(sm + (size_t)q * 16) = make_uint4(c01, 0u, 0u, 0u);
+            *reinterpret_cast<uint4*>(sm + TC_PLANE + (size_t)q * 16) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        fence_proxy_async();
     }
     if (warp == 0) {
         __syncwarp();
@@ -553,20 +577,6 @@ k_resid_restrict(const TI* __restrict__ v, const TZ* __restrict__ az, int nx, in
     block_sum_multi<1>(v1, 1, red, bs);
     if (last_block_reduce(partials, counter, bs, 1, tot) && threadIdx.x == 0)
         *s_out = (float)sqrt(tot[0] / (double)nc);
-}
-
-// network input of one sample: channel 0 = rc / s, channel 1 = f, 2..15 = 0
-__global__ void k_pack_input(const float* __restrict__ rc, const float* __restrict__ feat, int nc,
-                             const float* __restrict__ snorm, const int* enabled,
-                             const int* active, uint32_t* __restrict__ X) {
-    if (skip(enabled, active)) return;
-    const float s = *snorm;
-    const float inv = s > 0.f ? 1.f / s : 0.f;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        uint4* x4 = reinterpret_cast<uint4*>(X + (size_t)c * 8);
-        x4[0] = make_uint4(pack_bf16(rc[c] * inv, feat[c]), 0u, 0u, 0u);
-        x4[1] = make_uint4(0u, 0u, 0u, 0u);
-    }
 }
 
 // packed inputs of a batch of stored samples (idx[b] = sample of batch entry
@@ -898,15 +908,19 @@ CUtensorMap halo_map(const uint32_t* in, int D, int batch) {
     return m;
 }
 
+// fin_*: the first layer of an inference apply reads its input from rc, f
+// and s directly (one sample; `in` then only names a buffer for the map)
 void conv(sg_learned* L, const uint32_t* in, int l, bool transposed, int epi, int batch,
-          uint32_t* out, float* outf, const uint32_t* mask, const int* enabled, const int* active) {
+          uint32_t* out, float* outf, const uint32_t* mask, const int* enabled, const int* active,
+          const float* fin_rc = nullptr, const float* fin_feat = nullptr,
+          const float* fin_s = nullptr) {
     const int D = L->cx;
     const int tiles = (D / TB) * ((D + TC_TY - 1) / TC_TY) * (D / TC_TZ);
     const __nv_bfloat16* w = (transposed ? L->wt.p : L->wf.p) + (size_t)l * LAYER_W;
     k_conv3d_tc<<<tiles * batch, TC_THREADS, TC_SMEM, L->ctx->stream>>>(
         halo_map(in, D, batch), reinterpret_cast<const uint8_t*>(w),
         L->master.p + (size_t)l * LAYER_P + LAYER_W, D, epi, out, outf, mask, enabled, active,
-        L->cerr.p, L->wait_test);
+        L->cerr.p, L->wait_test, fin_rc, fin_feat, fin_s);
     SG_CUDA(cudaGetLastError());
     count_launch(L->ctx);
 }
@@ -1152,11 +1166,12 @@ void learned_apply(sg_learned* L, const TI* x, TO* y, int n, const int* active) 
     LearnedCtl* c = L->ctl.p;
     const int* en = &c->enabled;
     resid_restrict<float, TI, TO, float>(L, x, y, L->rc.p, &c->snorm, en, active);
-    k_pack_input<<<kblocks(L->ctx, (size_t)L->nc), 256, 0, L->ctx->stream>>>(
-        L->rc.p, L->feat.p, L->nc, &c->snorm, en, active, L->act[0].p);
-    SG_CUDA(cudaGetLastError());
-    count_launch(L->ctx);
-    forward(L, L->act[0].p, L->act[1].p, L->act[2].p, L->act[3].p, L->yout.p, 1, en, active);
+    // the first layer packs its input from rc, f and s itself
+    conv(L, L->act[0].p, 0, false, EPI_RELU, 1, L->act[1].p, nullptr, nullptr, en, active, L->rc.p,
+         L->feat.p, &c->snorm);
+    conv(L, L->act[1].p, 1, false, EPI_RELU, 1, L->act[2].p, nullptr, nullptr, en, active);
+    conv(L, L->act[2].p, 2, false, EPI_RELU, 1, L->act[3].p, nullptr, nullptr, en, active);
+    conv(L, L->act[3].p, 3, false, EPI_LINEAR_F32, 1, nullptr, L->yout.p, nullptr, en, active);
     // one fine cell per thread: each thread's eight loads of Y in flight at once
     k_prolong_add<TO><<<(n + 255) / 256, 256, 0, L->ctx->stream>>>(L->yout.p, L->nx, L->ny, L->nz,
                                                                    c, active, y);
