@@ -639,6 +639,8 @@ sg_status sg_precond_apply(sg_precond* pc, const double* x, double* y, int n, sg
         SG_CUDA(cudaStreamSynchronize(ctx->stream));
         if (sweep_error(pc))
             fail(SG_ERR_DEVICE_TIMEOUT, "a subdomain sweep gave up waiting for its factor records");
+        if (pc->learned && learned_error(pc->learned))
+            fail(SG_ERR_DEVICE_TIMEOUT, "a learned-stage convolution gave up waiting for its tile");
         if (const int hst = host_precond_status(pc))
             fail(SG_ERR_CALLBACK, "the host preconditioner function returned %d", hst);
     });

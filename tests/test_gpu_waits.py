@@ -113,3 +113,44 @@ def test_learned_convolution_wait_runs_out_then_recovers(sg, mode):
         np.testing.assert_array_equal(st.forward(x2), want)
     finally:
         st.close()
+
+
+def test_learned_wait_runs_out_inside_an_apply_and_a_solve(sg):
+    """The same give-up path reached through the preconditioner the stage is
+    attached to: an apply and an FGMRES solve report SG_ERR_DEVICE_TIMEOUT,
+    and both succeed again once the normal waits are back."""
+    N = 32
+    A = sg.make_varcoef_3d(N, N, N, 1.0, 8.0 * N / 96, 3)
+    part = sg.partition_boxes(N, N, N, 8, 0.08, 7)
+    M = sg.TwoLevelSchwarzPrecond(8, 1, sg.FineLevelType.RAS, partition=part,
+                                  factor_dtype=sg.FP32, sweep_dtype=sg.FP32)
+    M.setup(A)
+    st = sg.LearnedCorrection(N)
+    try:
+        st.set_matrix(A)
+        rng = np.random.default_rng(43)
+        p = (rng.uniform(-1, 1, sg.learned.NUM_PARAMS) * 0.1).astype(np.float32)
+        p[-1] = 0.5
+        st.weights = p
+        st.attach(M, stagnation=0.0)
+        v = rng.standard_normal(A.nrows)
+        want = M.apply(v)
+        b = rng.standard_normal(A.nrows)
+        prm = sg.GMRESParams(restart=30, max_iter=300, tol=1e-8, tol_kind=sg.TOL_TRUE_REL,
+                             precision=sg.FP32)
+        st.set_wait_test(1)
+        with pytest.raises(sg.SgError) as ei:
+            M.apply(v)
+        assert ei.value.status == TIMEOUT
+        short = sg.GMRESParams(restart=30, max_iter=5, tol=1e-8, tol_kind=sg.TOL_TRUE_REL,
+                               precision=sg.FP32)  # every wait that runs out costs ~1 ms
+        with pytest.raises(sg.SgError) as ei:
+            sg.fgmres(A, b, np.zeros(A.nrows), M, short)
+        assert ei.value.status == TIMEOUT
+        st.set_wait_test(0)
+        np.testing.assert_array_equal(M.apply(v), want)
+        res = sg.fgmres(A, b, np.zeros(A.nrows), M, prm)
+        assert res.converged
+        st.detach()
+    finally:
+        st.close()
